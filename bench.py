@@ -1,0 +1,284 @@
+"""DDGI probe-update benchmark.
+
+A step is one probe update (trace + shade of every probe ray, atlas blend with
+hysteresis, border copy) of the 32x16x32-probe, 256-ray grid over the seeded
+terrain + box-cluster scene (4097 instances, ~1M unique triangles).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is primary probe rays per second (Grays/s) with the scene and atlas
+resident in HBM, from CUDA events on the launching stream around each
+update; L2 is flushed (a 256 MB write) before every timed update.  `e2e` is
+the same metric through the public C-ABI calls a host program makes per
+update: host->device upload of the step's inputs (rotation-derived ray
+table) and device->host read of both atlases into pinned host memory.
+
+--impl reference times the CPU restatement of the reference's probe update
+(the reference itself is Vulkan/GLSL and cannot run here) on the host cores,
+on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DDGI update Grays/s & ms/update (32x16x32, 256 rays) vs plain FP32; bwd/fwd ratio"
+UNIT = "Grays/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.proc:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return out
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, n in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(n)
+        out.update(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
+                   reasons=sorted(reasons), samples=len(rows))
+        return out
+
+
+def cpu_baseline(w, sample_probes, threads=None):
+    """Times the CPU oracle on a bounded sample of probes of the workload."""
+    from oracle.oracle import Oracle, zero_atlas
+
+    threads = threads or os.cpu_count()
+    t0 = time.perf_counter()
+    o = Oracle(w.scene, threads=threads)
+    build_s = time.perf_counter() - t0
+    rng = np.random.default_rng(5)
+    plist = np.sort(rng.permutation(w.grid.probe_count())[:sample_probes]).astype(np.uint32)
+    c, d = zero_atlas(w.grid)
+    st = np.ones(w.grid.probe_count(), np.uint32)
+    t0 = time.perf_counter()
+    o.update(w.grid, w.light, w.orientation(0), c, d, st, plist)
+    dt = time.perf_counter() - t0
+    rays = len(plist) * w.grid.rays_per_probe
+    o.close()
+    return {"value": rays / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of %d probes x %d rays, 1 update from a zero atlas (%.1f s; BVH build %.1f s untimed)"
+                      % (len(plist), w.grid.probe_count(), w.grid.rays_per_probe, dt, build_s),
+            "ms_per_update_extrapolated": dt * 1e3 * w.grid.probe_count() / len(plist)}
+
+
+def run_reference(args, w):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    probes = args.cpu_probes
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(w, probes)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(w, probes))
+    wall = time.perf_counter() - t0
+    v = statistics.median(x["value"] for x in vals)
+    cb = dict(vals[0])
+    cb["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": config_dict(w, args), "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference is Vulkan/GLSL (no graphics stack on this box); timed here is the C++ restatement "
+                    "of its probe-update shaders on the host cores"}
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(w, args):
+    g = w.grid
+    return {"workload": w.name, "probes": g.probe_count(), "grid": list(g.resolution), "rays_per_probe":
+            g.rays_per_probe, "triangles": w.scene.triangle_count, "unique_triangles": w.scene.unique_triangle_count,
+            "instances": int(len(w.scene.instances)), "color_res": g.color_res, "depth_res": g.depth_res,
+            "precision": "fp32" if g.precision == 0 else "bf16", "l2": "flushed (256 MB write) before each timed update",
+            "seed": w.seed}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--cpu-probes", type=int, default=1024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank, world, local = dist_env()
+    from vulkanexp_gb300 import scenes
+
+    w = scenes.workload(args.config)
+    if args.impl == "reference":
+        run_reference(args, w)
+        return
+
+    import torch
+
+    from vulkanexp_gb300 import abi, build
+    from vulkanexp_gb300.ddgi import Context
+
+    build.build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+    ctx = Context(w.grid)
+    t0 = time.perf_counter()
+    ctx.build_scene(w.scene, stream)
+    build_s = time.perf_counter() - t0
+    ctx.set_light(w.light)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    P, R = w.grid.probe_count(), w.grid.rays_per_probe
+
+    # measurement pass (untimed): algorithmic fetch bytes of one trace launch
+    fetches = ctx.count_fetches(w.orientation(0), stream=stream)
+
+    for k in range(args.warmup):
+        ctx.update(w.orientation(k), stream=stream)
+    ctx.synchronize(stream)
+    ctx.enable_timing(True)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    trace_ms, blend_ms = [], []
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(k & 255)
+        ev[k][0].record(stream)
+        ctx.update(w.orientation(args.warmup + k), stream=stream)
+        ev[k][1].record(stream)
+        t = ctx.timings()  # synchronises on the update's last event
+        trace_ms.append(t["trace_ms"])
+        blend_ms.append(t["blend_ms"])
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    clocks = sampler.stop()
+    ms = float(np.mean(step_ms))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * P * R / (ms * 1e-3) / 1e9
+
+    # e2e through the host-buffer API: inputs up, both atlases down (pinned)
+    ch, cw, cc = ctx.atlas_shape(abi.ATLAS_COLOR)
+    dh, dw, dc = ctx.atlas_shape(abi.ATLAS_DEPTH)
+    host_c = torch.empty((ch, cw, cc), dtype=torch.float32, pin_memory=True).numpy()
+    host_d = torch.empty((dh, dw, dc), dtype=torch.float32, pin_memory=True).numpy()
+    ctx.enable_timing(False)
+    e2e_ms = []
+    for k in range(max(args.steps, 1)):
+        flush.fill_(k & 255)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.update(w.orientation(k), stream=stream)
+        ctx.get_atlas(abi.ATLAS_COLOR, host_c, stream)
+        ctx.get_atlas(abi.ATLAS_DEPTH, host_d, stream)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_val = world * P * R / (np.mean(e2e_ms) * 1e-3) / 1e9
+
+    hbm, _, peak_kind = load_peaks()
+    trace_avg = float(np.mean(trace_ms))
+    alg_bytes = fetches["nodes"] * 64 + fetches["tris"] * 48 + fetches["instances"] * 64 + fetches["shade_bytes"]
+    achieved = alg_bytes / (trace_avg * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_trace_shade", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": trace_avg,
+                "fetches_per_launch": fetches}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config_dict(w, args),
+            "impl": "ours", "form": "plain FP32 (trace+shade kernel, SIMT blend + fused border)",
+            "stage_ms": {"trace_shade": trace_avg, "blend_border": float(np.mean(blend_ms))},
+            "gpu_launches": 2 * args.steps, "clocks": clocks, "roofline": roofline,
+            "e2e": {"value": e2e_val, "unit": UNIT, "ms_per_step": float(np.mean(e2e_ms)),
+                    "h2d_bytes_per_step": R * 20, "d2h_bytes_per_step": int(host_c.nbytes + host_d.nbytes)},
+            "scene_build_s": build_s, "wall_s_timed": wall}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_probes)
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,270 @@
+/*
+ * ddgi.h — C ABI of the GB300 DDGI irradiance-probe update.
+ *
+ * This library replaces the probe-update pass of VulkanExp's
+ * `IrradianceProbes` class (src/IrradianceProbes.hpp:16-129,
+ * src/IrradianceProbes.cpp:12-594) and the GPU programs it drives
+ * (src/shaders/traceProbes.rgen, closesthit.glsl with NO_REFLECTION,
+ * miss.rmiss, shadow.rmiss, probesUpdate.glsl, probesCopyBorders.comp,
+ * probesInit.rgen).  The driver-built Vulkan BLAS/TLAS
+ * (src/Renderer.cpp:240-642) is replaced by an LBVH built on the GPU.
+ *
+ * Conventions
+ *  - Every entry point returns a ddgi_status and never throws.
+ *  - The context owns its device memory; callers own host arrays and streams.
+ *  - A context is not thread-safe; separate contexts are independent.
+ *  - Streams are passed as `ddgi_stream` (a cudaStream_t); NULL is the legacy
+ *    default stream.
+ *  - Host arrays are read during the call only and may be freed afterwards.
+ */
+#ifndef DDGI_H
+#define DDGI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* ddgi_stream; /* == cudaStream_t */
+typedef struct ddgi_ctx ddgi_ctx;
+
+typedef enum ddgi_status {
+    DDGI_OK = 0,
+    DDGI_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size or grid parameter */
+    DDGI_ERR_CUDA = 2,             /* a CUDA runtime call failed (see ddgi_last_error) */
+    DDGI_ERR_OUT_OF_MEMORY = 3,
+    DDGI_ERR_NO_SCENE = 4,         /* update/init before ddgi_scene_build */
+    DDGI_ERR_TIMEOUT = 5,          /* ddgi_synchronize gave up waiting */
+    DDGI_ERR_DEVICE = 6,           /* a kernel raised its error word (stack overflow, bad index) */
+    DDGI_ERR_UNSUPPORTED = 7       /* valid request this build does not implement */
+} ddgi_status;
+
+/* Blend precision of ddgi_update. */
+typedef enum ddgi_precision {
+    DDGI_PRECISION_FP32 = 0, /* plain form: FP32 SIMT blend, FP32 atlas */
+    DDGI_PRECISION_BF16 = 1  /* tcgen05 BF16 contraction, FP32 accumulate, FP16 atlas */
+} ddgi_precision;
+
+/*
+ * Grid parameters.  Mirrors IrradianceProbes::GridInfo
+ * (src/IrradianceProbes.hpp:49-60; std140 layout in
+ * src/shaders/ProbeGrid.glsl:4-15).  colorRes/depthRes are runtime values here
+ * (the reference bakes 8/16 into its shaders); the last word selects the blend
+ * precision where the reference has padding.
+ */
+typedef struct ddgi_grid_desc {
+    float extent_min[3];
+    float depth_sharpness;   /* exponent of the depth blend weight */
+    float extent_max[3];
+    float hysteresis;        /* weight of the previous atlas value */
+    int32_t resolution[3];   /* probes along x, y, z (each >= 2) */
+    uint32_t rays_per_probe; /* 1 .. DDGI_MAX_RAYS_PER_PROBE */
+    uint32_t color_res;      /* colour tile side incl. 1-texel border (>= 3) */
+    uint32_t depth_res;      /* depth tile side incl. 1-texel border (>= 3) */
+    float shadow_bias;
+    uint32_t precision;      /* ddgi_precision */
+} ddgi_grid_desc;
+
+#define DDGI_MAX_RAYS_PER_PROBE 1024u
+
+/* Vertex record, 64 bytes.  Same layout as src/vulkan/Vertex.hpp:8-15. */
+typedef struct ddgi_vertex {
+    float pos[3];
+    float color[3];
+    float normal[3];
+    float tangent[4];
+    float uv[2];
+    uint32_t padding;
+} ddgi_vertex;
+
+/* Material::Properties, 12 words (src/vulkan/Material.hpp:16-25).
+ * Texture ids are accepted but textures are not sampled. */
+typedef struct ddgi_material {
+    float metallic;
+    float roughness;
+    float base_color[3];
+    float emissive[3];
+    uint32_t albedo_texture;
+    uint32_t normal_texture;
+    uint32_t metallic_roughness_texture;
+    uint32_t emissive_texture;
+} ddgi_material;
+
+/* Renderer::OffsetEntry (src/Renderer.hpp:21-25), indexed by an instance's
+ * custom index at shading time (src/shaders/closesthit.glsl:147-155). */
+typedef struct ddgi_offset_entry {
+    uint32_t material_index;
+    uint32_t vertex_offset; /* in vertices */
+    uint32_t index_offset;  /* in indices */
+} ddgi_offset_entry;
+
+/* One bottom-level structure is built per mesh over its index range
+ * (src/Renderer.cpp:272-449).  Indices are relative to vertex_offset. */
+typedef struct ddgi_mesh {
+    uint32_t vertex_offset;
+    uint32_t vertex_count;
+    uint32_t index_offset;
+    uint32_t index_count; /* multiple of 3 */
+} ddgi_mesh;
+
+/* Like VkAccelerationStructureInstanceKHR (src/Renderer.cpp:538-550):
+ * object-to-world transform, row-major 3x4; 24-bit custom index (an
+ * offset-table entry) and 8-bit visibility mask; the mesh it instances. */
+typedef struct ddgi_instance {
+    float transform[12];
+    uint32_t custom_index; /* low 24 bits used */
+    uint32_t mask;         /* low 8 bits used */
+    uint32_t mesh_index;
+    uint32_t padding;
+} ddgi_instance;
+
+/* LightBuffer (src/Light.hpp:6-9): direction points TOWARDS the sun,
+ * color.rgb is the sun radiance.  sky.rgb is the constant radiance returned on
+ * a miss (replacing the atmospheric sky of src/shaders/sky.glsl). */
+typedef struct ddgi_light {
+    float direction[4];
+    float color[4];
+    float sky[4];
+} ddgi_light;
+
+typedef struct ddgi_scene_desc {
+    const ddgi_vertex* vertices;
+    uint32_t vertex_count;
+    const uint32_t* indices;
+    uint32_t index_count;
+    const ddgi_mesh* meshes;
+    uint32_t mesh_count;
+    const ddgi_instance* instances;
+    uint32_t instance_count;
+    const ddgi_offset_entry* offsets;
+    uint32_t offset_count;
+    const ddgi_material* materials;
+    uint32_t material_count;
+} ddgi_scene_desc;
+
+/* Closest-hit record of one probe ray (for parity checks).
+ * instance == 0xFFFFFFFF marks a miss. */
+typedef struct ddgi_hit {
+    uint32_t instance;
+    uint32_t primitive;
+    float t;
+    uint32_t backface;
+} ddgi_hit;
+
+typedef enum ddgi_atlas_kind {
+    DDGI_ATLAS_COLOR = 0, /* RGBA per texel, A = 1 */
+    DDGI_ATLAS_DEPTH = 1  /* (mean distance, mean squared distance) per texel */
+} ddgi_atlas_kind;
+
+/* Per-stage device times of the last update, in milliseconds, in the order of
+ * the reference's five timestamps (src/IrradianceProbes.cpp:441-452):
+ * total, trace+shade, blend, border copy, atlas publish. */
+typedef struct ddgi_timings {
+    float total_ms;
+    float trace_ms;
+    float blend_ms;
+    float border_ms;
+    float copy_ms;
+} ddgi_timings;
+
+const char* ddgi_status_string(ddgi_status status);
+/* Message of the last failing call on this context (never NULL). */
+const char* ddgi_last_error(const ddgi_ctx* ctx);
+
+/* IrradianceProbes::init (src/IrradianceProbes.cpp:12-104): validates the
+ * grid and allocates the atlases and per-ray buffers on the current device.
+ * The atlas starts at zero; probe states start at 1 (ON). */
+ddgi_status ddgi_create(const ddgi_grid_desc* grid, ddgi_ctx** out);
+ddgi_status ddgi_destroy(ddgi_ctx* ctx);
+
+/* IrradianceProbes::updateUniforms (src/IrradianceProbes.cpp:106-108):
+ * replace hysteresis, depth sharpness, shadow bias, rays per probe, extent
+ * and precision.  Resolution, colorRes and depthRes must not change. */
+ddgi_status ddgi_set_grid(ddgi_ctx* ctx, const ddgi_grid_desc* grid);
+ddgi_status ddgi_get_grid(const ddgi_ctx* ctx, ddgi_grid_desc* out);
+uint32_t ddgi_probe_count(const ddgi_ctx* ctx);
+
+/* Builds the bottom-level LBVHs (one per mesh) and the top-level LBVH over
+ * the instances on `stream`, replacing the Vulkan BLAS/TLAS build
+ * (src/Renderer.cpp:272-449, 525-642).  Returns after the build completes. */
+ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* scene, ddgi_stream stream);
+
+/* IrradianceProbes::setLightBuffer / writeLightDescriptor
+ * (src/IrradianceProbes.cpp:323-336). */
+ddgi_status ddgi_set_light(ddgi_ctx* ctx, const ddgi_light* light);
+
+/* IrradianceProbes::update (src/IrradianceProbes.cpp:426-594).
+ * `orientation` is the row-major 3x3 rotation applied to the spherical
+ * Fibonacci ray set (the push constant of src/shaders/traceProbes.rgen:36).
+ * `probe_list` lists linear probe indices to update; NULL updates all probes
+ * in index order.  Work is enqueued on `stream`; the call does not wait. */
+ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
+                        uint32_t probe_count, ddgi_stream stream);
+
+/* Copies an atlas to host memory as FP32 (RGBA for colour, RG for depth),
+ * row-major, width = res*resolution.x*resolution.y, height = res*resolution.z.
+ * `bytes` must equal width*height*channels*4.  Synchronous on `stream`. */
+ddgi_status ddgi_get_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, float* dst, size_t bytes,
+                           ddgi_stream stream);
+/* Replaces an atlas from host FP32 data of the same shape (checkpoint load). */
+ddgi_status ddgi_set_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, const float* src, size_t bytes,
+                           ddgi_stream stream);
+ddgi_status ddgi_atlas_dims(const ddgi_ctx* ctx, ddgi_atlas_kind kind, uint32_t* width,
+                            uint32_t* height, uint32_t* channels);
+
+/* Ray records of the last update: (r, g, b, depth) per (probe slot, ray),
+ * slot-major, as written by src/shaders/traceProbes.rgen:45.  `count` is
+ * probe_count * rays_per_probe of that update. */
+ddgi_status ddgi_get_ray_records(ddgi_ctx* ctx, float* dst, size_t count, ddgi_stream stream);
+/* Closest-hit records of the last update, same order as the ray records.
+ * Recorded only when hit recording is on (ddgi_record_hits). */
+ddgi_status ddgi_record_hits(ddgi_ctx* ctx, int enable);
+ddgi_status ddgi_get_hits(ddgi_ctx* ctx, ddgi_hit* dst, size_t count, ddgi_stream stream);
+/* Ray directions of the last update (x, y, z, 1) per ray
+ * (src/shaders/traceProbes.rgen:46-47). */
+ddgi_status ddgi_get_ray_directions(ddgi_ctx* ctx, float* dst, size_t count);
+
+/* Probe states (0 OFF, 1..8 refresh period) as in ProbeInfo
+ * (src/IrradianceProbes.hpp:64-66). */
+ddgi_status ddgi_get_probe_states(ddgi_ctx* ctx, uint32_t* dst, size_t count, ddgi_stream stream);
+ddgi_status ddgi_set_probe_states(ddgi_ctx* ctx, const uint32_t* src, size_t count,
+                                  ddgi_stream stream);
+
+/* Device pointers of the current atlases (FP32 form: float4 colour and
+ * float2 depth; BF16 form: half4 colour and half2 depth), for zero-copy
+ * consumers.  Valid until the next ddgi_update, ddgi_set_grid or destroy. */
+ddgi_status ddgi_atlas_device_ptr(const ddgi_ctx* ctx, ddgi_atlas_kind kind, void** ptr);
+
+/* Closest-hit (any_hit = 0) or any-hit (any_hit = 1) queries of n world-space
+ * rays against the built scene, with t in [tmin, tmax] and an instance mask:
+ * the traceRayEXT calls of src/shaders/traceProbes.rgen:43 and
+ * src/shaders/closesthit.glsl:270-281, exposed for parity checks.  Host
+ * arrays: origins/dirs 3*n floats, hits n records, barycentrics 2*n floats
+ * (may be NULL).  Synchronous on `stream`. */
+ddgi_status ddgi_trace_rays(ddgi_ctx* ctx, const float* origins, const float* dirs, uint32_t n, float tmin,
+                            float tmax, uint32_t mask, int any_hit, ddgi_hit* hits, float* barycentrics,
+                            ddgi_stream stream);
+
+/* Measurement: runs the trace + shade of one update (no blend; atlas and
+ * probe states untouched) with fetch counters, and returns
+ * out[0] inner-node fetches (64 B each), out[1] triangle tests (48 B each),
+ * out[2] instance entries (64 B each), out[3] rays traced (primary + shadow),
+ * out[4] shading bytes (hit data, atlas texels of the bounce lookups, ray
+ * record).  Synchronous on `stream`. */
+ddgi_status ddgi_count_fetches(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
+                               uint32_t probe_count, uint64_t out[5], ddgi_stream stream);
+
+/* Waits for `stream` with a timeout (poll), then checks the device error word.
+ * timeout_ms < 0 waits forever. */
+ddgi_status ddgi_synchronize(ddgi_ctx* ctx, ddgi_stream stream, int timeout_ms);
+ddgi_status ddgi_get_timings(const ddgi_ctx* ctx, ddgi_timings* out);
+/* Enables per-stage CUDA-event timing of updates (off by default). */
+ddgi_status ddgi_enable_timing(ddgi_ctx* ctx, int enable);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* DDGI_H */

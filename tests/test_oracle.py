@@ -1,0 +1,199 @@
+"""CPU checks of the oracle: pins against the reference's own tables and
+known-answer tests derived from the shader math (no GPU)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle, zero_atlas
+from vulkanexp_gb300 import abi, scenes
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_border_tables_match_reference():
+    """The generalised border copy reproduces probesCopyBorders.comp's
+    tables (8x8 colour, 16x16 depth) entry for entry, in order."""
+    ref = json.load(open(os.path.join(GOLDEN, "border_tables.json")))
+    for n, dst, src in ((8, "irradianceCopiesDst", "irradianceCopiesSrc"), (16, "depthCopiesDst", "depthCopiesSrc")):
+        t = Oracle.border_table(n)
+        ref_pairs = sorted(zip(map(tuple, ref[dst]), map(tuple, ref[src])))
+        ours = sorted((tuple(r[:2]), tuple(r[2:])) for r in t)
+        assert ours == ref_pairs
+        # every border texel written exactly once, every source interior
+        dsts = [tuple(r[:2]) for r in t]
+        assert len(set(dsts)) == len(dsts) == 4 * (n - 1)
+        assert all(1 <= r[2] <= n - 2 and 1 <= r[3] <= n - 2 for r in t)
+
+
+def test_truncated_texel_constants():
+    # probesUpdate.glsl:37,40 use 0.33333 and 0.142857, not 1/3 and 1/7
+    assert Oracle.texel_scale(6) == np.float32(0.33333)
+    assert Oracle.texel_scale(14) == np.float32(0.142857)
+    assert Oracle.texel_scale(4) == np.float32(0.5)
+
+
+def test_oct_decode_unit_and_roundtrip():
+    for n in (6, 14):
+        s = Oracle.texel_scale(n)
+        for ty in range(n):
+            for tx in range(n):
+                x, y = s * (tx - 0.5 * (n - 1)), s * (ty - 0.5 * (n - 1))
+                d = Oracle.oct_decode(x, y)
+                assert abs(np.linalg.norm(d) - 1.0) < 1e-6
+                u, v = Oracle.sphere_to_oct_uv(d)
+                # spherePointToOctohedralUV o octDecode is the identity on texel centres
+                assert abs((2 * u - 1) - x) < 2e-5 and abs((2 * v - 1) - y) < 2e-5
+
+
+def test_spherical_fibonacci_table():
+    """Unrotated table: z_i = 1 - (2i+1)/N, unit length, the golden-angle
+    spiral (irradiance.glsl:52-64); a rotation keeps lengths and dots."""
+    n = 128
+    t = Oracle.direction_table(np.eye(3, dtype=np.float32).reshape(9), n)
+    i = np.arange(n)
+    z = 1.0 - (2 * i + 1) / n
+    phi = 2 * np.pi * np.mod(i * 0.6180339887498949, 1.0)
+    s = np.sqrt(np.clip(1 - z * z, 0, 1))
+    v = np.stack([np.cos(phi) * s, np.sin(phi) * s, z], 1)
+    np.testing.assert_allclose(t[:, :3], v, atol=1e-6)
+    assert (t[:, 3] == 1.0).all()
+    M = scenes.random_orientation(4, 2).reshape(3, 3)
+    np.testing.assert_allclose(M @ M.T, np.eye(3), atol=1e-6)
+    tr = Oracle.direction_table(M.reshape(9), n)
+    np.testing.assert_allclose(tr[:, :3], v @ M.T.astype(np.float64), atol=2e-6)
+
+
+def _empty_scene():
+    sc = scenes.room_with_boxes(5, n_boxes=0)
+    sc.instances = sc.instances[:0]
+    sc.offsets = sc.offsets[:1]
+    return sc
+
+
+def test_empty_scene_known_answer():
+    """No geometry: every ray misses, so after one update from zero every
+    interior colour texel is (1-h)*sky and every depth texel (1-h)*(c, c^2)
+    with c = |cell| (misses count as depth c, probesUpdate.glsl:78-79)."""
+    sc = _empty_scene()
+    g = abi.make_grid((0, 0, 0), (4, 3, 5), (3, 3, 3), 64, hysteresis=0.9)
+    L = scenes.default_light()
+    o = Oracle(sc, threads=2)
+    c, d = zero_atlas(g)
+    st = np.ones(g.probe_count(), np.uint32)
+    o.update(g, L, scenes.random_orientation(3, 0), c, d, st)
+    sky = np.array(L.sky[:3], np.float32)
+    h = 0.9
+    cell = np.linalg.norm(np.array([4 / 2, 3 / 2, 5 / 2]))
+    for p in range(g.probe_count()):
+        x, y, z = p % 3, (p // 3) % 3, p // 9
+        tile = y * 3 + x
+        col = c[8 * z + 1:8 * z + 7, 8 * tile + 1:8 * tile + 7, :3]
+        np.testing.assert_allclose(col, np.broadcast_to((1 - h) * sky, col.shape), rtol=2e-6)
+        dep = d[16 * z + 1:16 * z + 15, 16 * tile + 1:16 * tile + 15]
+        np.testing.assert_allclose(dep[..., 0], (1 - h) * cell, rtol=2e-6)
+        np.testing.assert_allclose(dep[..., 1], (1 - h) * cell * cell, rtol=2e-6)
+    # all rays out of range -> state 8 (probesUpdate.glsl:111-112)
+    assert (st == 8).all()
+
+
+def test_hysteresis_recurrence():
+    """K updates of a constant scene from zero give (1 - h^K) * x."""
+    sc = _empty_scene()
+    g = abi.make_grid((0, 0, 0), (2, 2, 2), (2, 2, 2), 32, hysteresis=0.8)
+    L = scenes.default_light()
+    o = Oracle(sc, threads=2)
+    c, d = zero_atlas(g)
+    st = np.ones(g.probe_count(), np.uint32)
+    K = 5
+    for k in range(K):
+        o.update(g, L, scenes.random_orientation(9, k), c, d, st)
+    sky = np.array(L.sky[:3])
+    np.testing.assert_allclose(c[1:7, 1:7, :3], np.broadcast_to((1 - 0.8 ** K) * sky, (6, 6, 3)), rtol=1e-5)
+
+
+def test_single_triangle_exact_t_and_facing():
+    """A triangle in the plane z = 2 seen along +z from the origin: t = 2;
+    front-facing exactly when its normal points back at the ray."""
+    from vulkanexp_gb300.abi import INSTANCE_DTYPE, MATERIAL_DTYPE, MESH_DTYPE, OFFSET_DTYPE
+
+    for flip in (False, True):
+        pos = np.array([[-1, -1, 2], [2, -1, 2], [-1, 2, 2]], np.float64)
+        tri = np.array([0, 2, 1] if flip else [0, 1, 2], np.uint32)
+        verts = scenes.make_vertices(pos, np.tile([0, 0, -1.0], (3, 1)))
+        meshes = np.array([(0, 3, 0, 3)], MESH_DTYPE)
+        inst = np.zeros(1, INSTANCE_DTYPE)
+        inst[0]["transform"] = scenes.affine_3x4(np.eye(3), np.zeros(3))
+        inst[0]["mask"] = 1
+        sc = scenes.Scene(verts, tri, meshes, inst, np.zeros(1, OFFSET_DTYPE), np.zeros(1, MATERIAL_DTYPE))
+        o = Oracle(sc, threads=1)
+        hits, bary = o.trace(np.zeros((1, 3)), np.array([[0, 0, 1.0]]), 0.01, 100.0)
+        assert hits[0]["instance"] == 0 and hits[0]["t"] == np.float32(2.0)
+        n = np.cross(pos[tri[1]] - pos[tri[0]], pos[tri[2]] - pos[tri[0]])
+        front = np.dot([0, 0, 1.0], n) < 0
+        assert bool(hits[0]["backface"]) == (not front)
+        # tmin/tmax are inclusive; beyond tmax is a miss
+        assert o.trace(np.zeros((1, 3)), np.array([[0, 0, 1.0]]), 0.01, 2.0)[0][0]["t"] == np.float32(2.0)
+        assert o.trace(np.zeros((1, 3)), np.array([[0, 0, 1.0]]), 0.01, 1.999)[0][0]["instance"] == abi.MISS
+
+
+def test_tie_breaks_to_lowest_instance_and_primitive():
+    """Two coincident instances of a box, hit through the centre of a face
+    (on the diagonal shared by its two triangles): equal t everywhere, so the
+    hit goes to the lowest instance, then the lowest primitive."""
+    sc = scenes.room_with_boxes(11, n_boxes=2)
+    sc.instances = sc.instances[1:3].copy()
+    sc.instances[1]["transform"] = sc.instances[0]["transform"]
+    o = Oracle(sc, threads=1)
+    M = sc.instances[0]["transform"].reshape(3, 4).astype(np.float64)
+    centre = M[:, 3]
+    # face centre of the local +x face, approached along the face normal
+    face = centre + M[:, 0] * 0.5
+    normal = M[:, 0] / np.linalg.norm(M[:, 0])
+    origin = face + 2.0 * normal
+    hits, _ = o.trace(origin[None].astype(np.float32), (-normal)[None].astype(np.float32), 0.01, 100.0)
+    assert hits[0]["instance"] == 0
+    assert hits[0]["primitive"] == 0  # +x face = triangles 0, 1
+    assert hits[0]["backface"] == 0
+
+
+def test_fp32_matches_fp64_room():
+    """The FP32 restatement stays within 1e-4 of the FP64 one on the small
+    room workload (one update from zero)."""
+    w = scenes.workload(0)
+    o = Oracle(w.scene)
+    c, d = zero_atlas(w.grid)
+    st = np.ones(w.grid.probe_count(), np.uint32)
+    o.update(w.grid, w.light, w.orientation(0), c, d, st)
+    c64, d64 = zero_atlas(w.grid, fp64=True)
+    st64 = np.ones(w.grid.probe_count(), np.uint32)
+    o.update(w.grid, w.light, w.orientation(0), c64, d64, st64, fp64=True)
+    from conftest import rel_err
+
+    assert rel_err(c, c64, 1e-3).max() < 1e-4
+    assert rel_err(d, d64, 1e-3).max() < 1e-4
+    assert (st == st64).all()
+
+
+def test_scene_generators_sizes():
+    sc = scenes.room_with_boxes(1234)
+    assert sc.triangle_count == 2412
+    big = scenes.terrain_with_clusters(1235, n_instances=64, boxes_per_cluster=100, cells=64)
+    assert big.unique_triangle_count == 64 * 64 * 2 + 8 * 100 * 12
+    assert len(big.instances) == 65
+
+
+@pytest.mark.parametrize("res", [(8, 16), (6, 14)])
+def test_blend_entry_point_normalises(res):
+    """Equal-radiance rays blend to that radiance times (1-h)."""
+    g = abi.make_grid((0, 0, 0), (1, 1, 1), (2, 2, 2), 64, color_res=res[0], depth_res=res[1], hysteresis=0.5)
+    rays = np.zeros((8, 64, 4), np.float32)
+    rays[..., :3] = (0.25, 0.5, 1.0)
+    rays[..., 3] = 0.1
+    c, d = zero_atlas(g)
+    st = np.ones(8, np.uint32)
+    Oracle.blend(g, scenes.random_orientation(1, 0), rays, c, d, st)
+    n = res[0]
+    np.testing.assert_allclose(c[1:n - 1, 1:n - 1, :3], np.broadcast_to([0.125, 0.25, 0.5], (n - 2, n - 2, 3)),
+                               rtol=1e-5)

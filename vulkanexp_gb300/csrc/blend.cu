@@ -1,0 +1,167 @@
+// blend.cu — plain FP32 atlas blend with the border copy fused in.
+//
+// One block per updated probe, one thread per interior texel of both atlases
+// (36 colour + 196 depth for 8/16 tiles), as the reference's two dispatches
+// do (src/shaders/probesUpdate.glsl:49-121: WG 1x6x6 and 1x14x14, one
+// workgroup per probe).  The probe's ray records and the shared direction
+// table are staged in shared memory; each texel sums its cosine (colour) or
+// cosine^sharpness (depth) weighted rays in ray order, normalises, applies
+// hysteresis against the previous texel in place, and the block then copies
+// the octahedral border (src/shaders/probesCopyBorders.comp:21-245,
+// generalised to any tile side) and updates the probe state
+// (probesUpdate.glsl:104-120, with the max-change taken over all texels).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace ddgi {
+
+namespace {
+
+// Border entry e of a tile of side n: (dst x, dst y, src x, src y).
+__device__ __forceinline__ int4 border_entry(int e, int n) {
+    int m = n - 2;
+    if (e == 0) return make_int4(0, 0, n - 2, n - 2);
+    if (e == 1) return make_int4(0, n - 1, n - 2, 1);
+    if (e == 2) return make_int4(n - 1, 0, 1, n - 2);
+    if (e == 3) return make_int4(n - 1, n - 1, 1, 1);
+    e -= 4;
+    int side = e / m, j = e % m + 1;
+    if (side == 0) return make_int4(0, j, 1, n - 1 - j);
+    if (side == 1) return make_int4(n - 1, j, n - 2, n - 1 - j);
+    if (side == 2) return make_int4(j, 0, n - 1 - j, 1);
+    return make_int4(j, n - 1, n - 1 - j, n - 2);
+}
+
+__global__ void __launch_bounds__(256) k_blend_fp32(DeviceGrid g, const uint32_t* __restrict__ probe_list,
+                                                    const float4* __restrict__ rays, const float4* __restrict__ dirs,
+                                                    uint32_t* states, float4* color, float2* depth) {
+    extern __shared__ float4 smem[];
+    const uint32_t R = g.rays;
+    float4* s_rays = smem;
+    float4* s_dirs = smem + R;
+    __shared__ uint32_t s_max_change;
+    __shared__ uint32_t s_out_of_range;
+
+    const uint32_t slot = blockIdx.x;
+    const uint32_t probe = probe_list ? probe_list[slot] : slot;
+    const float4* pr = rays + (size_t)slot * R;
+    if (threadIdx.x == 0) {
+        s_max_change = 0u;
+        s_out_of_range = 0u;
+    }
+    __syncthreads();
+    uint32_t oor = 0;
+    for (uint32_t r = threadIdx.x; r < R; r += blockDim.x) {
+        float4 v = pr[r];
+        s_rays[r] = v;
+        s_dirs[r] = dirs[r];
+        if (v.w < 0.0f || v.w > g.cell_len) ++oor;
+    }
+    if (oor) atomicAdd(&s_out_of_range, oor);
+    __syncthreads();
+
+    const uint32_t rx = (uint32_t)g.res[0], rxy = (uint32_t)(g.res[0] * g.res[1]);
+    const int ix = (int)(probe % rx), iy = (int)((probe % rxy) / rx), iz = (int)(probe / rxy);
+    const int tile = iy * g.res[0] + ix;
+    const int nc = (int)g.color_res - 2, nd = (int)g.depth_res - 2;
+    const int ncol = nc * nc, ntex = ncol + nd * nd;
+    const float hy = g.hyst;
+
+    for (int t = threadIdx.x; t < ntex; t += blockDim.x) {
+        if (t < ncol) {
+            int tx = t % nc, ty = t / nc;
+            float sc = texel_scale((uint32_t)nc), ce = 0.5f * (float)(nc - 1);
+            float3 td = oct_decode(sc * ((float)tx - ce), sc * ((float)ty - ce));
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, aw = 0.f;
+            for (uint32_t r = 0; r < R; ++r) {
+                float4 d = s_dirs[r];
+                float4 v = s_rays[r];
+                float w = fmaxf(0.0f, td.x * d.x + td.y * d.y + td.z * d.z);
+                a0 += w * v.x;
+                a1 += w * v.y;
+                a2 += w * v.z;
+                aw += w;
+            }
+            if (aw > 1e-3f) {
+                a0 /= aw;
+                a1 /= aw;
+                a2 /= aw;
+            }
+            size_t px = (size_t)((int)g.color_res * tile + 1 + tx), py = (size_t)((int)g.color_res * iz + 1 + ty);
+            float4* texel = color + py * g.color_w + px;
+            float4 prev = *texel;
+            float mc = fmaxf(fmaxf(fabsf(a0 - prev.x), fabsf(a1 - prev.y)), fabsf(a2 - prev.z));
+            atomicMax(&s_max_change, __float_as_uint(mc));
+            *texel = make_float4(a0 * (1.0f - hy) + prev.x * hy, a1 * (1.0f - hy) + prev.y * hy,
+                                 a2 * (1.0f - hy) + prev.z * hy, 1.0f);
+        } else {
+            int u = t - ncol;
+            int tx = u % nd, ty = u / nd;
+            float sc = texel_scale((uint32_t)nd), ce = 0.5f * (float)(nd - 1);
+            float3 td = oct_decode(sc * ((float)tx - ce), sc * ((float)ty - ce));
+            float a0 = 0.f, a1 = 0.f, aw = 0.f;
+            const float cl = g.cell_len;
+            for (uint32_t r = 0; r < R; ++r) {
+                float4 d = s_dirs[r];
+                float dep = fminf(cl, s_rays[r].w);
+                if (dep < 0.0f) dep = cl;
+                float w = powf(fmaxf(0.0f, td.x * d.x + td.y * d.y + td.z * d.z), g.sharp);
+                a0 += w * dep;
+                a1 += w * dep * dep;
+                aw += w;
+            }
+            if (aw > 1e-3f) {
+                a0 /= aw;
+                a1 /= aw;
+            }
+            size_t px = (size_t)((int)g.depth_res * tile + 1 + tx), py = (size_t)((int)g.depth_res * iz + 1 + ty);
+            float2* texel = depth + py * g.depth_w + px;
+            float2 prev = *texel;
+            *texel = make_float2(a0 * (1.0f - hy) + prev.x * hy, a1 * (1.0f - hy) + prev.y * hy);
+        }
+    }
+    __syncthreads();
+
+    // border copy (probesCopyBorders.comp), generalised
+    const int nbc = 4 + 4 * nc, nbd = 4 + 4 * nd;
+    for (int e = threadIdx.x; e < nbc + nbd; e += blockDim.x) {
+        if (e < nbc) {
+            int4 b = border_entry(e, (int)g.color_res);
+            size_t ox = (size_t)g.color_res * tile, oy = (size_t)g.color_res * iz;
+            color[(oy + b.y) * g.color_w + ox + b.x] = color[(oy + b.w) * g.color_w + ox + b.z];
+        } else {
+            int4 b = border_entry(e - nbc, (int)g.depth_res);
+            size_t ox = (size_t)g.depth_res * tile, oy = (size_t)g.depth_res * iz;
+            depth[(oy + b.y) * g.depth_w + ox + b.x] = depth[(oy + b.w) * g.depth_w + ox + b.z];
+        }
+    }
+
+    if (threadIdx.x == 0) {  // probesUpdate.glsl:110-119
+        uint32_t s = states[probe];
+        if (s_out_of_range >= R) {
+            s = 8;
+        } else {
+            float mc = __uint_as_float(s_max_change);
+            float sf = (float)s;
+            if (mc < 0.02f / sf) s = min(s + 1u, 8u);
+            else if (mc > 0.04f / sf) s = max(s - 1u, 1u);
+            else if (mc > 0.25f) s = 1;
+        }
+        states[probe] = s;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_blend_fp32(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
+                              const float4* dirs, uint32_t* states, float4* color, float2* depth, cudaStream_t st) {
+    if (nprobes == 0) return cudaSuccess;
+    size_t smem = sizeof(float4) * 2 * g.rays;
+    k_blend_fp32<<<nprobes, 256, smem, st>>>(g, probe_list, rays, dirs, states, color, depth);
+    return cudaGetLastError();
+}
+
+}  // namespace ddgi

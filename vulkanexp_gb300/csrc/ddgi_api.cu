@@ -1,0 +1,880 @@
+// ddgi_api.cu — the C ABI (include/ddgi.h): context, scene build, update.
+//
+// Mirrors the host orchestration of IrradianceProbes
+// (src/IrradianceProbes.cpp:12-594): init allocates the atlases and per-ray
+// buffers, update records trace -> blend (+border) on the caller's stream.
+// Differences by design: the atlas is updated in place (the reference's
+// work -> final image copy, :532-577, is not needed because nothing samples
+// the atlas while a blend runs), the direction table is computed on the host
+// once per update, and every call returns a status instead of throwing.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "../../include/ddgi.h"
+#include "../../include/ddgi_exact.h"
+#include "common.cuh"
+#include "kernels.h"
+#include "lbvh.h"
+
+using namespace ddgi;
+
+namespace {
+
+constexpr int kBlasLeafMax = 4;
+constexpr int kTlasLeafMax = 1;
+
+struct SceneBuffers {
+    BvhNode* nodes = nullptr;
+    BvhTri* tris = nullptr;
+    GpuInstance* inst_leaf = nullptr;
+    GpuInstance* inst_id = nullptr;
+    float4* normals = nullptr;
+    uint32_t* indices = nullptr;
+    ddgi_offset_entry* offsets = nullptr;
+    ddgi_material* materials = nullptr;
+    int32_t tlas_root = -1;
+    uint32_t vertex_count = 0, index_count = 0, offset_count = 0, material_count = 0, instance_count = 0;
+    uint64_t node_count = 0, tri_count = 0;
+    bool built = false;
+};
+
+}  // namespace
+
+struct ddgi_ctx {
+    ddgi_grid_desc grid{};
+    DeviceGrid dg{};
+    DeviceLight dl{};
+    int device = 0;
+    bool fp16 = false;
+    void* color = nullptr;
+    void* depth = nullptr;
+    uint32_t* states = nullptr;
+    float4* rays = nullptr;
+    size_t rays_cap = 0;  // in records
+    ddgi_hit* hits = nullptr;
+    size_t hits_cap = 0;
+    bool record_hits = false;
+    float4* dirs = nullptr;
+    uint32_t* ray_order = nullptr;
+    uint32_t* probe_list = nullptr;
+    uint32_t* err = nullptr;
+    uint32_t last_count = 0;
+    uint32_t last_rays = 0;
+    std::vector<float> host_dirs;
+    std::vector<uint32_t> host_order;
+    SceneBuffers scene;
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool timing_pending = false;
+    ddgi_timings timings{};
+    char msg[512] = "";
+};
+
+namespace {
+
+ddgi_status fail(ddgi_ctx* c, ddgi_status s, const char* fmt, ...) {
+    if (c) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(c->msg, sizeof(c->msg), fmt, ap);
+        va_end(ap);
+    }
+    return s;
+}
+
+ddgi_status cuda_fail(ddgi_ctx* c, cudaError_t e, const char* what) {
+    cudaGetLastError();  // clear a sticky-free error
+    if (e == cudaErrorMemoryAllocation) return fail(c, DDGI_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+    return fail(c, DDGI_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                  \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+    } while (0)
+
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+void dfree_v(void*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+bool grid_valid(const ddgi_grid_desc* g, char* why, size_t n) {
+    for (int k = 0; k < 3; ++k) {
+        if (g->resolution[k] < 2) return snprintf(why, n, "resolution[%d] = %d < 2", k, g->resolution[k]), false;
+        if (!std::isfinite(g->extent_min[k]) || !std::isfinite(g->extent_max[k]) || !(g->extent_max[k] > g->extent_min[k]))
+            return snprintf(why, n, "extent axis %d is empty or not finite", k), false;
+    }
+    if (g->rays_per_probe < 1 || g->rays_per_probe > DDGI_MAX_RAYS_PER_PROBE)
+        return snprintf(why, n, "rays_per_probe = %u outside [1, %u]", g->rays_per_probe, DDGI_MAX_RAYS_PER_PROBE), false;
+    if (g->color_res < 3 || g->color_res > 64) return snprintf(why, n, "color_res = %u outside [3, 64]", g->color_res), false;
+    if (g->depth_res < 3 || g->depth_res > 64) return snprintf(why, n, "depth_res = %u outside [3, 64]", g->depth_res), false;
+    if (!std::isfinite(g->hysteresis) || !std::isfinite(g->depth_sharpness) || !std::isfinite(g->shadow_bias))
+        return snprintf(why, n, "non-finite hysteresis/sharpness/bias"), false;
+    if (g->precision != DDGI_PRECISION_FP32 && g->precision != DDGI_PRECISION_BF16)
+        return snprintf(why, n, "unknown precision %u", g->precision), false;
+    uint64_t probes = (uint64_t)g->resolution[0] * g->resolution[1] * g->resolution[2];
+    if (probes > (1u << 24)) return snprintf(why, n, "too many probes (%llu)", (unsigned long long)probes), false;
+    uint64_t w = (uint64_t)g->depth_res * g->resolution[0] * g->resolution[1];
+    if (w > (1u << 30)) return snprintf(why, n, "atlas too wide"), false;
+    return true;
+}
+
+DeviceGrid make_device_grid(const ddgi_grid_desc& g) {
+    DeviceGrid d{};
+    for (int k = 0; k < 3; ++k) {
+        d.mn[k] = g.extent_min[k];
+        d.mx[k] = g.extent_max[k];
+        d.res[k] = g.resolution[k];
+        volatile float diff = g.extent_max[k] - g.extent_min[k];
+        d.cell[k] = diff / (float)(g.resolution[k] - 1);
+    }
+    {
+        volatile float a = d.cell[0] * d.cell[0];
+        volatile float b = d.cell[1] * d.cell[1];
+        volatile float c = d.cell[2] * d.cell[2];
+        volatile float s = a + b;
+        s = s + c;
+        d.cell_len = std::sqrt((float)s);
+    }
+    {
+        volatile float dx = g.extent_max[0] - g.extent_min[0];
+        volatile float dy = g.extent_max[1] - g.extent_min[1];
+        volatile float dz = g.extent_max[2] - g.extent_min[2];
+        volatile float a = dx * dx, b = dy * dy, c = dz * dz;
+        volatile float s = a + b;
+        s = s + c;
+        d.tmax = std::sqrt((float)s);
+    }
+    d.rays = g.rays_per_probe;
+    d.color_res = g.color_res;
+    d.depth_res = g.depth_res;
+    d.sharp = g.depth_sharpness;
+    d.hyst = g.hysteresis;
+    d.bias = g.shadow_bias;
+    d.color_w = g.color_res * g.resolution[0] * g.resolution[1];
+    d.color_h = g.color_res * g.resolution[2];
+    d.depth_w = g.depth_res * g.resolution[0] * g.resolution[1];
+    d.depth_h = g.depth_res * g.resolution[2];
+    return d;
+}
+
+uint32_t probe_count_of(const ddgi_grid_desc& g) {
+    return (uint32_t)g.resolution[0] * (uint32_t)g.resolution[1] * (uint32_t)g.resolution[2];
+}
+
+size_t atlas_bytes(const DeviceGrid& d, ddgi_atlas_kind k, bool fp16) {
+    size_t texels = k == DDGI_ATLAS_COLOR ? (size_t)d.color_w * d.color_h : (size_t)d.depth_w * d.depth_h;
+    size_t per = k == DDGI_ATLAS_COLOR ? (fp16 ? 8 : 16) : (fp16 ? 4 : 8);
+    return texels * per;
+}
+
+DeviceScene device_scene(const ddgi_ctx* c) {
+    DeviceScene s{};
+    s.nodes = c->scene.nodes;
+    s.tris = c->scene.tris;
+    s.instances = c->scene.inst_leaf;
+    s.instances_by_id = c->scene.inst_id;
+    s.normals = c->scene.normals;
+    s.indices = c->scene.indices;
+    s.offsets = c->scene.offsets;
+    s.materials = c->scene.materials;
+    s.tlas_root = c->scene.tlas_root;
+    s.vertex_count = c->scene.vertex_count;
+    s.index_count = c->scene.index_count;
+    s.offset_count = c->scene.offset_count;
+    s.material_count = c->scene.material_count;
+    return s;
+}
+
+void free_scene(SceneBuffers& s) {
+    dfree(s.nodes);
+    dfree(s.tris);
+    dfree(s.inst_leaf);
+    dfree(s.inst_id);
+    dfree(s.normals);
+    dfree(s.indices);
+    dfree(s.offsets);
+    dfree(s.materials);
+    s = SceneBuffers{};
+}
+
+ddgi_status ensure_ray_capacity(ddgi_ctx* ctx, size_t records) {
+    if (records > ctx->rays_cap) {
+        dfree(ctx->rays);
+        CK(cudaMalloc(&ctx->rays, records * sizeof(float4)), "cudaMalloc ray records");
+        ctx->rays_cap = records;
+    }
+    if (ctx->record_hits && records > ctx->hits_cap) {
+        dfree(ctx->hits);
+        CK(cudaMalloc(&ctx->hits, records * sizeof(ddgi_hit)), "cudaMalloc hit records");
+        ctx->hits_cap = records;
+    }
+    return DDGI_OK;
+}
+
+ddgi_status check_device_error(ddgi_ctx* ctx) {
+    uint32_t e = 0;
+    CK(cudaMemcpy(&e, ctx->err, sizeof(e), cudaMemcpyDeviceToHost), "read device error word");
+    if (e != 0) {
+        cudaMemset(ctx->err, 0, sizeof(uint32_t));
+        const char* what = e == DEV_STACK_OVERFLOW ? "traversal stack overflow"
+                           : e == DEV_BAD_INDEX    ? "index out of range in scene data"
+                           : e == DEV_WAIT_TIMEOUT ? "device wait timed out"
+                                                   : "unknown device error";
+        return fail(ctx, DDGI_ERR_DEVICE, "device error %u: %s", e, what);
+    }
+    return DDGI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ddgi_status_string(ddgi_status s) {
+    switch (s) {
+        case DDGI_OK: return "DDGI_OK";
+        case DDGI_ERR_INVALID_ARGUMENT: return "DDGI_ERR_INVALID_ARGUMENT";
+        case DDGI_ERR_CUDA: return "DDGI_ERR_CUDA";
+        case DDGI_ERR_OUT_OF_MEMORY: return "DDGI_ERR_OUT_OF_MEMORY";
+        case DDGI_ERR_NO_SCENE: return "DDGI_ERR_NO_SCENE";
+        case DDGI_ERR_TIMEOUT: return "DDGI_ERR_TIMEOUT";
+        case DDGI_ERR_DEVICE: return "DDGI_ERR_DEVICE";
+        case DDGI_ERR_UNSUPPORTED: return "DDGI_ERR_UNSUPPORTED";
+    }
+    return "DDGI_ERR_UNKNOWN";
+}
+
+const char* ddgi_last_error(const ddgi_ctx* ctx) { return ctx ? ctx->msg : "null context"; }
+
+ddgi_status ddgi_create(const ddgi_grid_desc* grid, ddgi_ctx** out) {
+    if (!out) return DDGI_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (!grid) return DDGI_ERR_INVALID_ARGUMENT;
+    char why[256];
+    if (!grid_valid(grid, why, sizeof(why))) return DDGI_ERR_INVALID_ARGUMENT;
+    ddgi_ctx* ctx = new (std::nothrow) ddgi_ctx();
+    if (!ctx) return DDGI_ERR_OUT_OF_MEMORY;
+    ctx->grid = *grid;
+    ctx->dg = make_device_grid(*grid);
+    ctx->fp16 = grid->precision == DDGI_PRECISION_BF16;
+    // default light: LightBuffer defaults (src/Light.hpp:6-9), black sky
+    {
+        float d[3] = {0.2f, 2.0f, 0.2f};
+        float l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (int k = 0; k < 3; ++k) {
+            ctx->dl.dir[k] = d[k] / l;
+            ctx->dl.color[k] = 10.0f;
+            ctx->dl.sky[k] = 0.0f;
+        }
+    }
+    cudaError_t e = cudaGetDevice(&ctx->device);
+    ddgi_status st = DDGI_OK;
+    const uint32_t P = probe_count_of(*grid);
+    auto bail = [&](ddgi_status s) {
+        ddgi_destroy(ctx);
+        return s;
+    };
+    if (e != cudaSuccess) return bail(DDGI_ERR_CUDA);
+    if (cudaMalloc(&ctx->color, atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, ctx->fp16)) != cudaSuccess ||
+        cudaMalloc(&ctx->depth, atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, ctx->fp16)) != cudaSuccess ||
+        cudaMalloc(&ctx->states, sizeof(uint32_t) * P) != cudaSuccess ||
+        cudaMalloc(&ctx->dirs, sizeof(float4) * DDGI_MAX_RAYS_PER_PROBE) != cudaSuccess ||
+        cudaMalloc(&ctx->ray_order, sizeof(uint32_t) * DDGI_MAX_RAYS_PER_PROBE) != cudaSuccess ||
+        cudaMalloc(&ctx->probe_list, sizeof(uint32_t) * P) != cudaSuccess ||
+        cudaMalloc(&ctx->err, sizeof(uint32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(DDGI_ERR_OUT_OF_MEMORY);
+    }
+    st = ensure_ray_capacity(ctx, (size_t)P * grid->rays_per_probe);
+    if (st != DDGI_OK) return bail(st);
+    cudaMemset(ctx->color, 0, atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, ctx->fp16));
+    cudaMemset(ctx->depth, 0, atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, ctx->fp16));
+    cudaMemset(ctx->err, 0, sizeof(uint32_t));
+    std::vector<uint32_t> ones(P, 1u);
+    cudaMemcpy(ctx->states, ones.data(), sizeof(uint32_t) * P, cudaMemcpyHostToDevice);
+    for (int i = 0; i < 4; ++i)
+        if (cudaEventCreate(&ctx->ev[i]) != cudaSuccess) return bail(DDGI_ERR_CUDA);
+    if (cudaDeviceSynchronize() != cudaSuccess) return bail(DDGI_ERR_CUDA);
+    *out = ctx;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_destroy(ddgi_ctx* ctx) {
+    if (!ctx) return DDGI_OK;
+    cudaDeviceSynchronize();
+    free_scene(ctx->scene);
+    dfree_v(ctx->color);
+    dfree_v(ctx->depth);
+    dfree(ctx->states);
+    dfree(ctx->rays);
+    dfree(ctx->hits);
+    dfree(ctx->dirs);
+    dfree(ctx->ray_order);
+    dfree(ctx->probe_list);
+    dfree(ctx->err);
+    for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    delete ctx;
+    return DDGI_OK;
+}
+
+uint32_t ddgi_probe_count(const ddgi_ctx* ctx) { return ctx ? probe_count_of(ctx->grid) : 0u; }
+
+ddgi_status ddgi_get_grid(const ddgi_ctx* ctx, ddgi_grid_desc* out) {
+    if (!ctx || !out) return DDGI_ERR_INVALID_ARGUMENT;
+    *out = ctx->grid;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_set_grid(ddgi_ctx* ctx, const ddgi_grid_desc* g) {
+    if (!ctx || !g) return DDGI_ERR_INVALID_ARGUMENT;
+    char why[256];
+    if (!grid_valid(g, why, sizeof(why))) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "%s", why);
+    for (int k = 0; k < 3; ++k)
+        if (g->resolution[k] != ctx->grid.resolution[k])
+            return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "resolution cannot change (recreate the context)");
+    if (g->color_res != ctx->grid.color_res || g->depth_res != ctx->grid.depth_res)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "color_res/depth_res cannot change (recreate the context)");
+    if (g->precision != ctx->grid.precision)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "precision cannot change (recreate the context)");
+    ddgi_status st = ensure_ray_capacity(ctx, (size_t)probe_count_of(*g) * g->rays_per_probe);
+    if (st != DDGI_OK) return st;
+    ctx->grid = *g;
+    ctx->dg = make_device_grid(*g);
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_set_light(ddgi_ctx* ctx, const ddgi_light* l) {
+    if (!ctx || !l) return DDGI_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < 3; ++k) {
+        if (!std::isfinite(l->direction[k]) || !std::isfinite(l->color[k]) || !std::isfinite(l->sky[k]))
+            return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "non-finite light");
+        ctx->dl.dir[k] = l->direction[k];
+        ctx->dl.color[k] = l->color[k];
+        ctx->dl.sky[k] = l->sky[k];
+    }
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_record_hits(ddgi_ctx* ctx, int enable) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    ctx->record_hits = enable != 0;
+    if (ctx->record_hits) return ensure_ray_capacity(ctx, ctx->rays_cap);
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_enable_timing(ddgi_ctx* ctx, int enable) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    ctx->timing = enable != 0;
+    return DDGI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Scene build (replaces the BLAS/TLAS build of src/Renderer.cpp:272-642)
+// ---------------------------------------------------------------------------
+ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_stream stream) {
+    if (!ctx || !d) return DDGI_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    // ---- validation (the reference would fault on any of these) ----
+    if ((d->vertex_count && !d->vertices) || (d->index_count && !d->indices) || (d->mesh_count && !d->meshes) ||
+        (d->instance_count && !d->instances) || (d->offset_count && !d->offsets) ||
+        (d->material_count && !d->materials))
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "null array with a non-zero count");
+    for (uint32_t m = 0; m < d->mesh_count; ++m) {
+        const ddgi_mesh& me = d->meshes[m];
+        if (me.index_count % 3) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "mesh %u: index_count not a multiple of 3", m);
+        if ((uint64_t)me.index_offset + me.index_count > d->index_count ||
+            (uint64_t)me.vertex_offset + me.vertex_count > d->vertex_count)
+            return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "mesh %u: range outside the vertex/index arrays", m);
+        for (uint32_t i = 0; i < me.index_count; ++i)
+            if (d->indices[me.index_offset + i] >= me.vertex_count)
+                return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "mesh %u: index %u out of range", m, i);
+        if ((uint64_t)me.index_count / 3 >= (1ull << 28))
+            return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "mesh %u: too many triangles", m);
+    }
+    for (uint32_t o = 0; o < d->offset_count; ++o) {
+        const ddgi_offset_entry& oe = d->offsets[o];
+        if (oe.material_index >= d->material_count)
+            return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "offset entry %u: material out of range", o);
+        if (oe.index_offset > d->index_count || oe.vertex_offset > d->vertex_count)
+            return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "offset entry %u: offsets out of range", o);
+    }
+    std::vector<float> w2o((size_t)d->instance_count * 12);
+    // (vertex_offset, index_offset, index_count) ranges already checked
+    std::vector<std::array<uint32_t, 3>> checked;
+    for (uint32_t i = 0; i < d->instance_count; ++i) {
+        const ddgi_instance& in = d->instances[i];
+        if (in.mesh_index >= d->mesh_count)
+            return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "instance %u: mesh_index out of range", i);
+        if ((in.custom_index & 0xFFFFFFu) >= d->offset_count)
+            return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "instance %u: custom_index out of range", i);
+        for (int k = 0; k < 12; ++k)
+            if (!std::isfinite(in.transform[k]))
+                return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "instance %u: non-finite transform", i);
+        if (!ddgi_affine_inverse(in.transform, &w2o[(size_t)i * 12]))
+            return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "instance %u: singular transform", i);
+        // an instance's shading reads must stay inside the arrays
+        const ddgi_offset_entry& oe = d->offsets[in.custom_index & 0xFFFFFFu];
+        const ddgi_mesh& me = d->meshes[in.mesh_index];
+        if ((uint64_t)oe.index_offset + me.index_count > d->index_count)
+            return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "instance %u: offset entry index range too short", i);
+        std::array<uint32_t, 3> key = {oe.vertex_offset, oe.index_offset, me.index_count};
+        if (std::find(checked.begin(), checked.end(), key) == checked.end()) {
+            for (uint32_t q = 0; q < me.index_count; ++q)
+                if ((uint64_t)oe.vertex_offset + d->indices[oe.index_offset + q] >= d->vertex_count)
+                    return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "instance %u: shading vertex out of range", i);
+            checked.push_back(key);
+        }
+    }
+
+    CK(cudaStreamSynchronize(st), "sync before scene build");
+    free_scene(ctx->scene);
+    SceneBuffers& S = ctx->scene;
+
+    // ---- upload shading data ----
+    std::vector<float4> pos(d->vertex_count), nrm(d->vertex_count);
+    for (uint32_t v = 0; v < d->vertex_count; ++v) {
+        const ddgi_vertex& vx = d->vertices[v];
+        pos[v] = make_float4(vx.pos[0], vx.pos[1], vx.pos[2], 1.0f);
+        nrm[v] = make_float4(vx.normal[0], vx.normal[1], vx.normal[2], 0.0f);
+    }
+    float4* dpos = nullptr;
+    uint64_t total_tris = 0, total_nodes = 0;
+    uint32_t max_tris = 0;
+    for (uint32_t m = 0; m < d->mesh_count; ++m) {
+        uint32_t nt = d->meshes[m].index_count / 3;
+        total_tris += nt;
+        total_nodes += nt > 1 ? nt - 1 : (nt == 1 ? 1 : 0);
+        max_tris = std::max(max_tris, nt);
+    }
+    uint32_t ni = d->instance_count;
+    uint64_t tlas_nodes = ni > 1 ? ni - 1 : (ni == 1 ? 1 : 0);
+    uint32_t max_prims = std::max(max_tris, ni);
+    void* scratch = nullptr;
+    float4* box_lo = nullptr;
+    float4* box_hi = nullptr;
+    uint32_t* sorted = nullptr;
+    auto cleanup = [&]() {
+        if (dpos) cudaFree(dpos);
+        if (scratch) cudaFree(scratch);
+        if (box_lo) cudaFree(box_lo);
+        if (box_hi) cudaFree(box_hi);
+        if (sorted) cudaFree(sorted);
+    };
+#define CKB(call, what)                               \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) {                      \
+            cleanup();                                \
+            free_scene(ctx->scene);                   \
+            return cuda_fail(ctx, e_, what);          \
+        }                                             \
+    } while (0)
+    size_t vbytes = sizeof(float4) * std::max<uint32_t>(d->vertex_count, 1);
+    CKB(cudaMalloc(&dpos, vbytes), "alloc positions");
+    CKB(cudaMalloc(&S.normals, vbytes), "alloc normals");
+    CKB(cudaMalloc(&S.indices, sizeof(uint32_t) * std::max<uint32_t>(d->index_count, 1)), "alloc indices");
+    CKB(cudaMalloc(&S.offsets, sizeof(ddgi_offset_entry) * std::max<uint32_t>(d->offset_count, 1)), "alloc offsets");
+    CKB(cudaMalloc(&S.materials, sizeof(ddgi_material) * std::max<uint32_t>(d->material_count, 1)), "alloc materials");
+    CKB(cudaMalloc(&S.nodes, sizeof(BvhNode) * std::max<uint64_t>(total_nodes + tlas_nodes, 1)), "alloc nodes");
+    CKB(cudaMalloc(&S.tris, sizeof(BvhTri) * std::max<uint64_t>(total_tris, 1)), "alloc triangles");
+    CKB(cudaMalloc(&S.inst_leaf, sizeof(GpuInstance) * std::max<uint32_t>(ni, 1)), "alloc instances");
+    CKB(cudaMalloc(&S.inst_id, sizeof(GpuInstance) * std::max<uint32_t>(ni, 1)), "alloc instances");
+    CKB(cudaMalloc(&scratch, lbvh_scratch_bytes(std::max<uint32_t>(max_prims, 1))), "alloc build scratch");
+    CKB(cudaMalloc(&box_lo, sizeof(float4) * std::max<uint32_t>(max_prims, 1)), "alloc build boxes");
+    CKB(cudaMalloc(&box_hi, sizeof(float4) * std::max<uint32_t>(max_prims, 1)), "alloc build boxes");
+    CKB(cudaMalloc(&sorted, sizeof(uint32_t) * std::max<uint32_t>(max_prims, 1)), "alloc build order");
+    if (d->vertex_count) {
+        CKB(cudaMemcpyAsync(dpos, pos.data(), sizeof(float4) * d->vertex_count, cudaMemcpyHostToDevice, st), "upload");
+        CKB(cudaMemcpyAsync(S.normals, nrm.data(), sizeof(float4) * d->vertex_count, cudaMemcpyHostToDevice, st), "upload");
+    }
+    if (d->index_count)
+        CKB(cudaMemcpyAsync(S.indices, d->indices, sizeof(uint32_t) * d->index_count, cudaMemcpyHostToDevice, st), "upload");
+    if (d->offset_count)
+        CKB(cudaMemcpyAsync(S.offsets, d->offsets, sizeof(ddgi_offset_entry) * d->offset_count, cudaMemcpyHostToDevice, st),
+            "upload");
+    if (d->material_count)
+        CKB(cudaMemcpyAsync(S.materials, d->materials, sizeof(ddgi_material) * d->material_count, cudaMemcpyHostToDevice,
+                            st),
+            "upload");
+
+    // ---- bottom level: one LBVH per mesh ----
+    std::vector<int32_t> mesh_root(d->mesh_count, -1);
+    std::vector<float> mesh_lo((size_t)d->mesh_count * 3, INFINITY), mesh_hi((size_t)d->mesh_count * 3, -INFINITY);
+    uint64_t node_base = 0, tri_base = 0;
+    for (uint32_t m = 0; m < d->mesh_count; ++m) {
+        const ddgi_mesh& me = d->meshes[m];
+        uint32_t nt = me.index_count / 3;
+        if (nt == 0) continue;
+        for (uint32_t q = 0; q < me.index_count; ++q) {
+            const float4& p = pos[me.vertex_offset + d->indices[me.index_offset + q]];
+            float pp[3] = {p.x, p.y, p.z};
+            for (int k = 0; k < 3; ++k) {
+                if (pp[k] == pp[k]) {
+                    mesh_lo[m * 3 + k] = std::min(mesh_lo[m * 3 + k], pp[k]);
+                    mesh_hi[m * 3 + k] = std::max(mesh_hi[m * 3 + k], pp[k]);
+                }
+            }
+        }
+        CKB(build_mesh_blas(dpos, S.indices, me.vertex_offset, me.vertex_count, me.index_offset, nt, kBlasLeafMax,
+                            S.nodes, (int)node_base, S.tris, (int)tri_base, box_lo, box_hi, sorted, scratch, ctx->err,
+                            st),
+            "bottom-level build");
+        mesh_root[m] = (int32_t)node_base;
+        node_base += nt > 1 ? nt - 1 : 1;
+        tri_base += nt;
+    }
+
+    // ---- top level over instance world boxes ----
+    std::vector<float4> ilo(ni), ihi(ni);
+    std::vector<GpuInstance> recs(ni);
+    for (uint32_t i = 0; i < ni; ++i) {
+        const ddgi_instance& in = d->instances[i];
+        GpuInstance& r = recs[i];
+        const float* w = &w2o[(size_t)i * 12];
+        for (int k = 0; k < 3; ++k) r.w2o[k] = make_float4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+        r.blas_root = mesh_root[in.mesh_index];
+        r.custom = in.custom_index & 0xFFFFFFu;
+        r.mask = in.mask & 0xFFu;
+        r.id = i;
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        const float* ml = &mesh_lo[(size_t)in.mesh_index * 3];
+        const float* mh = &mesh_hi[(size_t)in.mesh_index * 3];
+        if (r.blas_root >= 0 && ml[0] <= mh[0]) {
+            for (int c = 0; c < 8; ++c) {
+                double p[3] = {(c & 1) ? mh[0] : ml[0], (c & 2) ? mh[1] : ml[1], (c & 4) ? mh[2] : ml[2]};
+                for (int k = 0; k < 3; ++k) {
+                    float q = (float)(in.transform[4 * k] * p[0] + in.transform[4 * k + 1] * p[1] +
+                                      in.transform[4 * k + 2] * p[2] + in.transform[4 * k + 3]);
+                    lo[k] = std::min(lo[k], q);
+                    hi[k] = std::max(hi[k], q);
+                }
+            }
+            for (int k = 0; k < 3; ++k) {
+                float e = (hi[k] - lo[k]) * 1e-5f + (std::fabs(lo[k]) + std::fabs(hi[k])) * 1e-6f + 1e-7f;
+                lo[k] -= e;
+                hi[k] += e;
+            }
+        }
+        ilo[i] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+        ihi[i] = make_float4(hi[0], hi[1], hi[2], 0.0f);
+    }
+    if (ni > 0) {
+        CKB(cudaMemcpyAsync(box_lo, ilo.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
+        CKB(cudaMemcpyAsync(box_hi, ihi.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
+        CKB(lbvh_build(box_lo, box_hi, ni, kTlasLeafMax, S.nodes, (int)node_base, 0, sorted, scratch, st), "top-level build");
+        std::vector<uint32_t> order(ni);
+        CKB(cudaMemcpyAsync(order.data(), sorted, sizeof(uint32_t) * ni, cudaMemcpyDeviceToHost, st), "read order");
+        CKB(cudaStreamSynchronize(st), "top-level build");
+        std::vector<GpuInstance> leaf(ni);
+        for (uint32_t s = 0; s < ni; ++s) leaf[s] = recs[order[s]];
+        CKB(cudaMemcpyAsync(S.inst_leaf, leaf.data(), sizeof(GpuInstance) * ni, cudaMemcpyHostToDevice, st), "upload");
+        CKB(cudaMemcpyAsync(S.inst_id, recs.data(), sizeof(GpuInstance) * ni, cudaMemcpyHostToDevice, st), "upload");
+        S.tlas_root = (int32_t)node_base;
+    }
+    CKB(cudaStreamSynchronize(st), "scene build");
+    cleanup();
+#undef CKB
+    S.vertex_count = d->vertex_count;
+    S.index_count = d->index_count;
+    S.offset_count = d->offset_count;
+    S.material_count = d->material_count;
+    S.instance_count = ni;
+    S.node_count = total_nodes + tlas_nodes;
+    S.tri_count = total_tris;
+    S.built = true;
+    return check_device_error(ctx);
+}
+
+// ---------------------------------------------------------------------------
+// Update (IrradianceProbes::update, src/IrradianceProbes.cpp:426-594)
+// ---------------------------------------------------------------------------
+namespace {
+
+// Validates the request, uploads the direction table, the octant-binned ray
+// order and the probe list; returns the device probe list (NULL = all).
+ddgi_status prepare_update(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
+                           uint32_t probe_count, cudaStream_t st, const uint32_t** dlist, uint32_t* n_out) {
+    if (!ctx->scene.built) return fail(ctx, DDGI_ERR_NO_SCENE, "ddgi_update before ddgi_scene_build");
+    for (int k = 0; k < 9; ++k)
+        if (!std::isfinite(orientation[k])) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "non-finite orientation");
+    const uint32_t P = probe_count_of(ctx->grid);
+    const uint32_t R = ctx->grid.rays_per_probe;
+    uint32_t n = probe_list ? probe_count : P;
+    if (probe_list) {
+        if (probe_count > P) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "probe list longer than the grid");
+        std::vector<uint8_t> seen(P, 0);
+        for (uint32_t i = 0; i < probe_count; ++i) {
+            if (probe_list[i] >= P) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "probe %u out of range", probe_list[i]);
+            if (seen[probe_list[i]]++) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "probe %u listed twice", probe_list[i]);
+        }
+    }
+    // direction table (exact host definition) and octant-binned ray order
+    ctx->host_dirs.resize(4 * (size_t)R);
+    ddgi_ray_direction_table(orientation, R, ctx->host_dirs.data());
+    ctx->host_order.resize(R);
+    {
+        uint32_t counts[9] = {0};
+        std::vector<uint8_t> oct(R);
+        for (uint32_t r = 0; r < R; ++r) {
+            const float* dd = &ctx->host_dirs[4 * (size_t)r];
+            oct[r] = (uint8_t)((dd[0] < 0.0f ? 1 : 0) | (dd[1] < 0.0f ? 2 : 0) | (dd[2] < 0.0f ? 4 : 0));
+            counts[oct[r] + 1]++;
+        }
+        for (int k = 0; k < 8; ++k) counts[k + 1] += counts[k];
+        for (uint32_t r = 0; r < R; ++r) ctx->host_order[counts[oct[r]]++] = r;
+    }
+    CK(cudaMemcpyAsync(ctx->dirs, ctx->host_dirs.data(), sizeof(float4) * R, cudaMemcpyHostToDevice, st), "upload dirs");
+    CK(cudaMemcpyAsync(ctx->ray_order, ctx->host_order.data(), sizeof(uint32_t) * R, cudaMemcpyHostToDevice, st),
+       "upload order");
+    *dlist = nullptr;
+    if (probe_list && n > 0) {
+        CK(cudaMemcpyAsync(ctx->probe_list, probe_list, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st), "upload list");
+        *dlist = ctx->probe_list;
+    }
+    ddgi_status s = ensure_ray_capacity(ctx, (size_t)n * R);
+    if (s != DDGI_OK) return s;
+    *n_out = n;
+    return DDGI_OK;
+}
+
+}  // namespace
+
+ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list, uint32_t probe_count,
+                        ddgi_stream stream) {
+    if (!ctx || !orientation) return DDGI_ERR_INVALID_ARGUMENT;
+    if (ctx->fp16) return fail(ctx, DDGI_ERR_UNSUPPORTED, "BF16 blend not available in this build");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const uint32_t* dlist = nullptr;
+    uint32_t n = 0;
+    ddgi_status s = prepare_update(ctx, orientation, probe_list, probe_count, st, &dlist, &n);
+    if (s != DDGI_OK) return s;
+    DeviceScene sc = device_scene(ctx);
+    if (ctx->timing) CK(cudaEventRecord(ctx->ev[0], st), "event");
+    CK(launch_trace_shade(sc, ctx->dg, ctx->dl, dlist, n, ctx->dirs, ctx->ray_order, ctx->states, ctx->color,
+                          ctx->depth, ctx->fp16, ctx->rays, ctx->record_hits ? ctx->hits : nullptr, ctx->err, st),
+       "trace launch");
+    if (ctx->timing) CK(cudaEventRecord(ctx->ev[1], st), "event");
+    CK(launch_blend_fp32(ctx->dg, dlist, n, ctx->rays, ctx->dirs, ctx->states, static_cast<float4*>(ctx->color),
+                         static_cast<float2*>(ctx->depth), st),
+       "blend launch");
+    if (ctx->timing) {
+        CK(cudaEventRecord(ctx->ev[2], st), "event");
+        ctx->timing_pending = true;
+    }
+    ctx->last_count = n;
+    ctx->last_rays = ctx->grid.rays_per_probe;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_count_fetches(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
+                               uint32_t probe_count, uint64_t out[5], ddgi_stream stream) {
+    if (!ctx || !orientation || !out) return DDGI_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const uint32_t* dlist = nullptr;
+    uint32_t n = 0;
+    ddgi_status s = prepare_update(ctx, orientation, probe_list, probe_count, st, &dlist, &n);
+    if (s != DDGI_OK) return s;
+    unsigned long long* dc = nullptr;
+    CK(cudaMalloc(&dc, 5 * sizeof(unsigned long long)), "alloc counters");
+    cudaError_t e = cudaMemsetAsync(dc, 0, 5 * sizeof(unsigned long long), st);
+    if (e == cudaSuccess)
+        e = launch_trace_shade(device_scene(ctx), ctx->dg, ctx->dl, dlist, n, ctx->dirs, ctx->ray_order, ctx->states,
+                               ctx->color, ctx->depth, ctx->fp16, ctx->rays, nullptr, ctx->err, st, dc);
+    unsigned long long h[5] = {0, 0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, dc, sizeof(h), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(dc);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "count fetches");
+    for (int k = 0; k < 5; ++k) out[k] = h[k];
+    ctx->last_count = n;
+    ctx->last_rays = ctx->grid.rays_per_probe;
+    return check_device_error(ctx);
+}
+
+ddgi_status ddgi_get_timings(const ddgi_ctx* cctx, ddgi_timings* out) {
+    ddgi_ctx* ctx = const_cast<ddgi_ctx*>(cctx);
+    if (!ctx || !out) return DDGI_ERR_INVALID_ARGUMENT;
+    if (ctx->timing_pending) {
+        CK(cudaEventSynchronize(ctx->ev[2]), "timing");
+        float a = 0, b = 0;
+        cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
+        cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+        ctx->timings.trace_ms = a;
+        ctx->timings.blend_ms = b;
+        ctx->timings.border_ms = 0.0f;  // fused into the blend
+        ctx->timings.copy_ms = 0.0f;    // atlas updated in place
+        ctx->timings.total_ms = a + b;
+        ctx->timing_pending = false;
+    }
+    *out = ctx->timings;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_synchronize(ddgi_ctx* ctx, ddgi_stream stream, int timeout_ms) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaStreamQuery(st);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) return cuda_fail(ctx, e, "stream");
+        if (timeout_ms >= 0) {
+            auto el = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+            if (el >= timeout_ms) return fail(ctx, DDGI_ERR_TIMEOUT, "stream not idle after %d ms", timeout_ms);
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    return check_device_error(ctx);
+}
+
+ddgi_status ddgi_atlas_dims(const ddgi_ctx* ctx, ddgi_atlas_kind kind, uint32_t* w, uint32_t* h, uint32_t* ch) {
+    if (!ctx || (kind != DDGI_ATLAS_COLOR && kind != DDGI_ATLAS_DEPTH)) return DDGI_ERR_INVALID_ARGUMENT;
+    if (w) *w = kind == DDGI_ATLAS_COLOR ? ctx->dg.color_w : ctx->dg.depth_w;
+    if (h) *h = kind == DDGI_ATLAS_COLOR ? ctx->dg.color_h : ctx->dg.depth_h;
+    if (ch) *ch = kind == DDGI_ATLAS_COLOR ? 4u : 2u;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_get_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, float* dst, size_t bytes, ddgi_stream stream) {
+    if (!ctx || !dst || (kind != DDGI_ATLAS_COLOR && kind != DDGI_ATLAS_DEPTH)) return DDGI_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    uint32_t w, h, ch;
+    ddgi_atlas_dims(ctx, kind, &w, &h, &ch);
+    size_t count = (size_t)w * h * ch;
+    if (bytes != count * sizeof(float)) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "atlas needs %zu bytes", count * 4);
+    void* src = kind == DDGI_ATLAS_COLOR ? ctx->color : ctx->depth;
+    if (!ctx->fp16) {
+        CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st), "atlas download");
+        CK(cudaStreamSynchronize(st), "atlas download");
+    } else {
+        std::vector<__half> tmp(count);
+        CK(cudaMemcpyAsync(tmp.data(), src, count * sizeof(__half), cudaMemcpyDeviceToHost, st), "atlas download");
+        CK(cudaStreamSynchronize(st), "atlas download");
+        for (size_t i = 0; i < count; ++i) dst[i] = __half2float(tmp[i]);
+    }
+    return check_device_error(ctx);
+}
+
+ddgi_status ddgi_set_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, const float* src, size_t bytes, ddgi_stream stream) {
+    if (!ctx || !src || (kind != DDGI_ATLAS_COLOR && kind != DDGI_ATLAS_DEPTH)) return DDGI_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    uint32_t w, h, ch;
+    ddgi_atlas_dims(ctx, kind, &w, &h, &ch);
+    size_t count = (size_t)w * h * ch;
+    if (bytes != count * sizeof(float)) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "atlas needs %zu bytes", count * 4);
+    void* dstp = kind == DDGI_ATLAS_COLOR ? ctx->color : ctx->depth;
+    if (!ctx->fp16) {
+        CK(cudaMemcpyAsync(dstp, src, bytes, cudaMemcpyHostToDevice, st), "atlas upload");
+        CK(cudaStreamSynchronize(st), "atlas upload");
+    } else {
+        std::vector<__half> tmp(count);
+        for (size_t i = 0; i < count; ++i) tmp[i] = __float2half(src[i]);
+        CK(cudaMemcpyAsync(dstp, tmp.data(), count * sizeof(__half), cudaMemcpyHostToDevice, st), "atlas upload");
+        CK(cudaStreamSynchronize(st), "atlas upload");
+    }
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_atlas_device_ptr(const ddgi_ctx* ctx, ddgi_atlas_kind kind, void** ptr) {
+    if (!ctx || !ptr || (kind != DDGI_ATLAS_COLOR && kind != DDGI_ATLAS_DEPTH)) return DDGI_ERR_INVALID_ARGUMENT;
+    *ptr = kind == DDGI_ATLAS_COLOR ? ctx->color : ctx->depth;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_get_ray_records(ddgi_ctx* ctx, float* dst, size_t count, ddgi_stream stream) {
+    if (!ctx || !dst) return DDGI_ERR_INVALID_ARGUMENT;
+    size_t n = (size_t)ctx->last_count * ctx->last_rays;
+    if (count != n) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "expected %zu ray records", n);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaMemcpyAsync(dst, ctx->rays, n * sizeof(float4), cudaMemcpyDeviceToHost, st), "ray download");
+    CK(cudaStreamSynchronize(st), "ray download");
+    return check_device_error(ctx);
+}
+
+ddgi_status ddgi_get_hits(ddgi_ctx* ctx, ddgi_hit* dst, size_t count, ddgi_stream stream) {
+    if (!ctx || !dst) return DDGI_ERR_INVALID_ARGUMENT;
+    if (!ctx->record_hits || !ctx->hits) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "hit recording is off");
+    size_t n = (size_t)ctx->last_count * ctx->last_rays;
+    if (count != n) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "expected %zu hit records", n);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaMemcpyAsync(dst, ctx->hits, n * sizeof(ddgi_hit), cudaMemcpyDeviceToHost, st), "hit download");
+    CK(cudaStreamSynchronize(st), "hit download");
+    return check_device_error(ctx);
+}
+
+ddgi_status ddgi_get_ray_directions(ddgi_ctx* ctx, float* dst, size_t count) {
+    if (!ctx || !dst) return DDGI_ERR_INVALID_ARGUMENT;
+    if (count != ctx->host_dirs.size() / 4)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "expected %zu directions", ctx->host_dirs.size() / 4);
+    std::memcpy(dst, ctx->host_dirs.data(), ctx->host_dirs.size() * sizeof(float));
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_get_probe_states(ddgi_ctx* ctx, uint32_t* dst, size_t count, ddgi_stream stream) {
+    if (!ctx || !dst || count != probe_count_of(ctx->grid)) return DDGI_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaMemcpyAsync(dst, ctx->states, count * sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "state download");
+    CK(cudaStreamSynchronize(st), "state download");
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_set_probe_states(ddgi_ctx* ctx, const uint32_t* src, size_t count, ddgi_stream stream) {
+    if (!ctx || !src || count != probe_count_of(ctx->grid)) return DDGI_ERR_INVALID_ARGUMENT;
+    for (size_t i = 0; i < count; ++i)
+        if (src[i] > 8) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "probe state %u > 8", src[i]);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaMemcpyAsync(ctx->states, src, count * sizeof(uint32_t), cudaMemcpyHostToDevice, st), "state upload");
+    CK(cudaStreamSynchronize(st), "state upload");
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_trace_rays(ddgi_ctx* ctx, const float* origins, const float* dirs, uint32_t n, float tmin, float tmax,
+                            uint32_t mask, int any_hit, ddgi_hit* hits, float* barycentrics, ddgi_stream stream) {
+    if (!ctx || (n && (!origins || !dirs || !hits))) return DDGI_ERR_INVALID_ARGUMENT;
+    if (!ctx->scene.built) return fail(ctx, DDGI_ERR_NO_SCENE, "no scene");
+    if (n == 0) return DDGI_OK;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    float *dor = nullptr, *ddir = nullptr, *dbar = nullptr;
+    ddgi_hit* dh = nullptr;
+    auto cleanup = [&]() {
+        if (dor) cudaFree(dor);
+        if (ddir) cudaFree(ddir);
+        if (dbar) cudaFree(dbar);
+        if (dh) cudaFree(dh);
+    };
+    cudaError_t e = cudaMalloc(&dor, sizeof(float) * 3 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&ddir, sizeof(float) * 3 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&dh, sizeof(ddgi_hit) * n);
+    if (e == cudaSuccess && barycentrics) e = cudaMalloc(&dbar, sizeof(float) * 2 * n);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dor, origins, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ddir, dirs, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = launch_trace_rays(device_scene(ctx), dor, ddir, n, tmin, tmax, mask, any_hit, dh, dbar, ctx->err, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hits, dh, sizeof(ddgi_hit) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && barycentrics)
+        e = cudaMemcpyAsync(barycentrics, dbar, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cleanup();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "trace rays");
+    return check_device_error(ctx);
+}
+
+}  // extern "C"

@@ -1,0 +1,25 @@
+// kernels.h — host-side launchers of the DDGI kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace ddgi {
+
+// trace.cu
+cudaError_t launch_trace_shade(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L,
+                               const uint32_t* probe_list, uint32_t nprobes, const float4* dirs,
+                               const uint32_t* ray_order, const uint32_t* states, const void* color,
+                               const void* depth, bool fp16_atlas, float4* rays_out, ddgi_hit* hits_out,
+                               uint32_t* err, cudaStream_t st, unsigned long long* counters = nullptr);
+cudaError_t launch_trace_rays(const DeviceScene& sc, const float* origins, const float* dirs, uint32_t n, float tmin,
+                              float tmax, uint32_t mask, int any, ddgi_hit* out, float* bary, uint32_t* err,
+                              cudaStream_t st);
+
+// blend.cu
+cudaError_t launch_blend_fp32(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
+                              const float4* dirs, uint32_t* states, float4* color, float2* depth, cudaStream_t st);
+
+}  // namespace ddgi

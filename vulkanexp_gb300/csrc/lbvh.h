@@ -1,0 +1,29 @@
+// lbvh.h — GPU LBVH construction entry points (see lbvh.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace ddgi {
+
+// Device scratch needed by lbvh_build for n primitives.
+size_t lbvh_scratch_bytes(uint32_t n);
+
+// Builds a tree over n primitive boxes (float4 lo/hi, xyz used).  Writes
+// max(n - 1, 1) nodes at nodes[node_base ...]; leaf references point at
+// prim_base + sorted position.  sorted_ids[s] = original primitive of sorted
+// position s.  Root = node_base.
+cudaError_t lbvh_build(const float4* prim_lo, const float4* prim_hi, uint32_t n, int leaf_max, BvhNode* nodes,
+                       int node_base, int prim_base, uint32_t* sorted_ids, void* scratch, cudaStream_t st);
+
+// Bottom-level build of one mesh: triangle boxes from the vertex positions and
+// indices, the tree, and the triangles gathered in leaf order at
+// tris[tri_base ...].  box_lo/box_hi/sorted_ids hold ntri entries of scratch.
+cudaError_t build_mesh_blas(const float4* pos, const uint32_t* indices, uint32_t vbase, uint32_t vcount,
+                            uint32_t ibase, uint32_t ntri, int leaf_max, BvhNode* nodes, int node_base, BvhTri* tris,
+                            int tri_base, float4* box_lo, float4* box_hi, uint32_t* sorted_ids, void* scratch,
+                            uint32_t* err, cudaStream_t st);
+
+}  // namespace ddgi

@@ -1,0 +1,171 @@
+// shade.cuh — hit shading of a probe ray: sampleProbes (the infinite-bounce
+// lookup into the previous atlas), the sun BRDF, and the closest-hit program
+// of the reference with NO_REFLECTION.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "common.cuh"
+
+namespace ddgi {
+
+// Atlas views.  FP32 form: float4 colour (RGBA) and float2 depth texels;
+// FP16 form: 4 x half colour and 2 x half depth texels.
+struct ColorTexF32 {
+    static constexpr uint32_t kBytes = 16;
+    const float4* p;
+    __device__ __forceinline__ void fetch(size_t i, float* o) const {
+        float4 v = __ldg(p + i);
+        o[0] = v.x;
+        o[1] = v.y;
+        o[2] = v.z;
+    }
+};
+struct DepthTexF32 {
+    static constexpr uint32_t kBytes = 8;
+    const float2* p;
+    __device__ __forceinline__ void fetch(size_t i, float* o) const {
+        float2 v = __ldg(p + i);
+        o[0] = v.x;
+        o[1] = v.y;
+    }
+};
+struct ColorTexF16 {
+    static constexpr uint32_t kBytes = 8;
+    const uint2* p;  // 4 halves
+    __device__ __forceinline__ void fetch(size_t i, float* o) const {
+        uint2 v = __ldg(p + i);
+        __half2 a = *reinterpret_cast<__half2*>(&v.x);
+        __half2 b = *reinterpret_cast<__half2*>(&v.y);
+        float2 fa = __half22float2(a), fb = __half22float2(b);
+        o[0] = fa.x;
+        o[1] = fa.y;
+        o[2] = fb.x;
+    }
+};
+struct DepthTexF16 {
+    static constexpr uint32_t kBytes = 4;
+    const uint32_t* p;  // 2 halves
+    __device__ __forceinline__ void fetch(size_t i, float* o) const {
+        uint32_t v = __ldg(p + i);
+        float2 f = __half22float2(*reinterpret_cast<__half2*>(&v));
+        o[0] = f.x;
+        o[1] = f.y;
+    }
+};
+
+template <class CT, class DT>
+struct AtlasView {
+    CT color;
+    DT depth;
+};
+
+__device__ __forceinline__ float3 grid_probe_pos(const DeviceGrid& g, int x, int y, int z) {
+    return f3((float)x * g.cell[0] + g.mn[0], (float)y * g.cell[1] + g.mn[1], (float)z * g.cell[2] + g.mn[2]);
+}
+
+// sampleProbes (src/shaders/irradiance.glsl:145-237)
+template <class AV>
+__device__ float3 sample_probes(float3 position, float3 normal, float3 toCamera, const DeviceGrid& g,
+                                const uint32_t* states, const AV& at) {
+    float3 cs = abs3(f3(g.cell[0], g.cell[1], g.cell[2]));
+    float3 gridCoords = (position - f3(g.mn[0], g.mn[1], g.mn[2])) / cs;
+    if (gridCoords.x < 0.0f || gridCoords.y < 0.0f || gridCoords.z < 0.0f) return f3(0, 0, 0);
+    float3 biasedPosition = position + (normal + toCamera) * g.bias;
+    int fx = (int)gridCoords.x, fy = (int)gridCoords.y, fz = (int)gridCoords.z;
+    float3 alpha = (position - grid_probe_pos(g, fx, fy, fz)) / cs;
+    alpha = f3(clampf(alpha.x, 0.0f, 1.0f), clampf(alpha.y, 0.0f, 1.0f), clampf(alpha.z, 0.0f, 1.0f));
+
+    float3 finalColor = f3(0, 0, 0), fallbackColor = f3(0, 0, 0);
+    float totalWeight = 0.0f, totalFallbackWeight = 0.0f;
+    const float uvsx = (float)(g.res[0] * g.res[1]), uvsy = (float)g.res[2];
+    const float cr = (float)g.color_res, dr = (float)g.depth_res;
+    const float cscale = (float)(g.color_res - 2) / cr;
+    const float dscale = (float)(g.depth_res - 2) / dr;
+    const float2 nuv = sphere_to_oct_uv(normal);
+
+#pragma unroll 1
+    for (int i = 0; i < 8; ++i) {
+        int ox = i & 1, oy = (i >> 1) & 1, oz = (i >> 2) & 1;
+        int px = fx + ox, py = fy + oy, pz = fz + oz;
+        if (px > g.res[0] - 1 || py > g.res[1] - 1 || pz > g.res[2] - 1) continue;
+        uint32_t lin = (uint32_t)(px + g.res[0] * py + g.res[0] * g.res[1] * pz);
+        if (__ldg(states + lin) == 0) continue;
+        float3 probePosition = grid_probe_pos(g, px, py, pz);
+        float3 directionToProbe = norm3(probePosition - position);
+        float3 biasedDirectionToProbe = probePosition - biasedPosition;
+        float2 duv = sphere_to_oct_uv(-norm3(biasedDirectionToProbe));
+        int tile = py * g.res[0] + px;
+        float cu = ((float)((int)g.color_res * tile + 1) / cr + cscale * nuv.x) / uvsx;
+        float cv = ((float)((int)g.color_res * pz + 1) / cr + cscale * nuv.y) / uvsy;
+        float du = ((float)((int)g.depth_res * tile + 1) / dr + dscale * duv.x) / uvsx;
+        float dv = ((float)((int)g.depth_res * pz + 1) / dr + dscale * duv.y) / uvsy;
+        float3 tri = f3(ox ? alpha.x : 1.0f - alpha.x, oy ? alpha.y : 1.0f - alpha.y, oz ? alpha.z : 1.0f - alpha.z);
+        float weight = 1.0f;
+        float bfw = fmaxf(0.0001f, (dot3(directionToProbe, normal) + 1.0f) * 0.5f);
+        weight *= bfw * bfw + 0.2f;
+        float fallbackWeight = weight;
+        float depth[2];
+        bilinear<2>(at.depth, g.depth_w, g.depth_h, du, dv, depth);
+        float mean = depth[0];
+        float variance = fabsf(depth[0] * depth[0] - depth[1]);
+        float dist = len3(probePosition - biasedPosition);
+        float dm = fmaxf(dist - mean, 0.0001f);
+        float cheb = variance / (variance + dm * dm);
+        cheb = fmaxf(cheb * cheb * cheb, 0.0f);
+        weight *= (dist <= mean) ? 1.0f : cheb;
+        weight = fmaxf(0.000001f, weight);
+        const float crush = 0.2f;
+        if (weight < crush) weight *= weight * weight * (1.0f / (crush * crush));
+        float triw = tri.x * tri.y * tri.z + 0.001f;
+        weight *= triw;
+        fallbackWeight *= triw;
+        float col[3];
+        bilinear<3>(at.color, g.color_w, g.color_h, cu, cv, col);
+        float3 color = f3(sqrtf(col[0]), sqrtf(col[1]), sqrtf(col[2]));
+        finalColor = finalColor + color * weight;
+        totalWeight += weight;
+        fallbackColor = fallbackColor + color * fallbackWeight;
+        totalFallbackWeight += fallbackWeight;
+    }
+    if (totalWeight > 1e-3f) finalColor = finalColor * (1.0f / totalWeight);
+    if (totalFallbackWeight > 1e-3f) fallbackColor = fallbackColor * (1.0f / totalFallbackWeight);
+    finalColor = finalColor * finalColor;
+    fallbackColor = fallbackColor * fallbackColor;
+    return mix3(fallbackColor, finalColor, 8.0f * clampf(totalWeight, 0.0f, 1.0f / 8.0f));
+}
+
+// pbrMetallicRoughness (src/shaders/pbrMetallicRoughness.glsl:43-84)
+__device__ __forceinline__ float3 pbr_metallic_roughness(float3 n, float3 v, float3 lightColor, float3 lightDir,
+                                                         float3 albedo, float metal, float rough) {
+    const float pi = DDGI_PI;
+    float3 diffuseColor = albedo * (1.0f - 0.04f) * (1.0f - metal);
+    float alphaRoughness = rough * rough;
+    float3 specularColor = mix3(f3(0.04f, 0.04f, 0.04f), albedo, metal);
+    float reflectance = fmaxf(fmaxf(specularColor.x, specularColor.y), specularColor.z);
+    float reflectance90 = clampf(reflectance * 25.0f, 0.0f, 1.0f);
+    float3 R0 = specularColor;
+    float3 R90 = f3(reflectance90, reflectance90, reflectance90);
+    float3 l = norm3(lightDir);
+    float3 h = norm3(l + v);
+    float NdotL = clampf(dot3(n, l), 0.001f, 1.0f);
+    float NdotV = clampf(fabsf(dot3(n, v)), 0.001f, 1.0f);
+    float NdotH = clampf(dot3(n, h), 0.0f, 1.0f);
+    float VdotH = clampf(dot3(v, h), 0.0f, 1.0f);
+    float x = clampf(1.0f - VdotH, 0.0f, 1.0f);
+    float x2 = x * x;
+    float p5 = x2 * x2 * x;
+    float3 F = R0 + (R90 - R0) * p5;
+    float a2 = alphaRoughness * alphaRoughness;
+    float attL = 2.0f * NdotL / (NdotL + sqrtf(a2 + (1.0f - a2) * (NdotL * NdotL)));
+    float attV = 2.0f * NdotV / (NdotV + sqrtf(a2 + (1.0f - a2) * (NdotV * NdotV)));
+    float G = attL * attV;
+    float a = NdotH * alphaRoughness;
+    float k = alphaRoughness / ((1.0f - NdotH * NdotH) + a * a);
+    float D = clampf(k * k * (1.0f / pi), 0.0f, 4.0f);
+    float3 diffuseContrib = (f3(1, 1, 1) - F) * diffuseColor * (1.0f / pi);
+    float3 specContrib = F * (G * D / (4.0f * NdotL * NdotV));
+    return lightColor * (diffuseContrib + specContrib) * NdotL;
+}
+
+}  // namespace ddgi

@@ -1,0 +1,301 @@
+"""Python binding of the C ABI in include/ddgi.h.
+
+`IrradianceProbes` keeps the names of VulkanExp's class
+(src/IrradianceProbes.hpp:16-129): `GridParameters`, `TargetHysteresis`,
+`init`, `initProbes`, `update`, `updateUniforms`, `setLightBuffer`,
+`getProbeCount`.  The scene binding that the reference does through
+descriptors (`writeDescriptorSet`, src/IrradianceProbes.cpp:312-321) is
+`setScene`, which builds the GPU acceleration structures.
+
+There is no CPU fallback: if the CUDA library cannot be loaded, every call
+raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import HIT_DTYPE, GridDesc, Light, SceneDesc, Timings
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libddgi_gb300.so")
+
+
+class DDGIError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (abi.STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+_lib = None
+
+# (name, restype, argtypes) of every exported entry point
+_SIGNATURES = [
+    ("ddgi_status_string", C.c_char_p, [C.c_int]),
+    ("ddgi_last_error", C.c_char_p, [C.c_void_p]),
+    ("ddgi_create", C.c_int, [C.POINTER(GridDesc), C.POINTER(C.c_void_p)]),
+    ("ddgi_destroy", C.c_int, [C.c_void_p]),
+    ("ddgi_set_grid", C.c_int, [C.c_void_p, C.POINTER(GridDesc)]),
+    ("ddgi_get_grid", C.c_int, [C.c_void_p, C.POINTER(GridDesc)]),
+    ("ddgi_probe_count", C.c_uint32, [C.c_void_p]),
+    ("ddgi_scene_build", C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.c_void_p]),
+    ("ddgi_set_light", C.c_int, [C.c_void_p, C.POINTER(Light)]),
+    ("ddgi_update", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    ("ddgi_get_atlas", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]),
+    ("ddgi_set_atlas", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]),
+    ("ddgi_atlas_dims", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                  C.POINTER(C.c_uint32)]),
+    ("ddgi_get_ray_records", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    ("ddgi_record_hits", C.c_int, [C.c_void_p, C.c_int]),
+    ("ddgi_get_hits", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    ("ddgi_get_ray_directions", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    ("ddgi_get_probe_states", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    ("ddgi_set_probe_states", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    ("ddgi_atlas_device_ptr", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    ("ddgi_trace_rays", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_float, C.c_float, C.c_uint32,
+                                  C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ddgi_count_fetches", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("ddgi_synchronize", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    ("ddgi_get_timings", C.c_int, [C.c_void_p, C.POINTER(Timings)]),
+    ("ddgi_enable_timing", C.c_int, [C.c_void_p, C.c_int]),
+]
+
+
+def load_library(path=None):
+    """Loads libddgi_gb300.so (built by vulkanexp_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise DDGIError(2, "CUDA library %s is missing: run vulkanexp_gb300.build.build()" % path)
+    lib = C.CDLL(path)
+    for name, res, args in _SIGNATURES:
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return [s[0] for s in _SIGNATURES]
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
+    return C.c_void_p(int(getattr(stream, "cuda_stream", stream)))
+
+
+def scene_desc(scene):
+    d = SceneDesc()
+    d.vertices = scene.vertices.ctypes.data
+    d.vertex_count = len(scene.vertices)
+    d.indices = scene.indices.ctypes.data
+    d.index_count = scene.indices.size
+    d.meshes = scene.meshes.ctypes.data
+    d.mesh_count = len(scene.meshes)
+    d.instances = scene.instances.ctypes.data
+    d.instance_count = len(scene.instances)
+    d.offsets = scene.offsets.ctypes.data
+    d.offset_count = len(scene.offsets)
+    d.materials = scene.materials.ctypes.data
+    d.material_count = len(scene.materials)
+    return d
+
+
+class Context:
+    """Owns one ddgi_ctx."""
+
+    def __init__(self, grid):
+        self.lib = load_library()
+        h = C.c_void_p()
+        self._check(self.lib.ddgi_create(C.byref(grid), C.byref(h)), ctx=None)
+        self.h = h
+        self.grid = grid.copy()
+        self._scene_keepalive = None
+
+    def _check(self, status, ctx="self"):
+        if status != 0:
+            handle = self.h if ctx == "self" else None
+            msg = self.lib.ddgi_last_error(handle).decode() if handle else ""
+            raise DDGIError(status, msg)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ddgi_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- setup -----------------------------------------------------------
+    def set_grid(self, grid):
+        self._check(self.lib.ddgi_set_grid(self.h, C.byref(grid)))
+        self.grid = grid.copy()
+
+    def build_scene(self, scene, stream=None):
+        d = scene_desc(scene)
+        self._check(self.lib.ddgi_scene_build(self.h, C.byref(d), _stream_ptr(stream)))
+
+    def set_light(self, light):
+        self._check(self.lib.ddgi_set_light(self.h, C.byref(light)))
+
+    def record_hits(self, on=True):
+        self._check(self.lib.ddgi_record_hits(self.h, int(on)))
+
+    def enable_timing(self, on=True):
+        self._check(self.lib.ddgi_enable_timing(self.h, int(on)))
+
+    # ---- update ----------------------------------------------------------
+    def update(self, orientation, probe_list=None, stream=None):
+        o = np.ascontiguousarray(orientation, np.float32).reshape(9)
+        pl = None if probe_list is None else np.ascontiguousarray(probe_list, np.uint32)
+        self._check(self.lib.ddgi_update(self.h, _ptr(o), _ptr(pl), 0 if pl is None else len(pl),
+                                         _stream_ptr(stream)))
+
+    def count_fetches(self, orientation, probe_list=None, stream=None):
+        """Fetch counters of one trace + shade pass (see ddgi_count_fetches)."""
+        o = np.ascontiguousarray(orientation, np.float32).reshape(9)
+        pl = None if probe_list is None else np.ascontiguousarray(probe_list, np.uint32)
+        out = np.zeros(5, np.uint64)
+        self._check(self.lib.ddgi_count_fetches(self.h, _ptr(o), _ptr(pl), 0 if pl is None else len(pl), _ptr(out),
+                                                _stream_ptr(stream)))
+        keys = ("nodes", "tris", "instances", "rays", "shade_bytes")
+        return {k: int(v) for k, v in zip(keys, out)}
+
+    def synchronize(self, stream=None, timeout_ms=-1):
+        self._check(self.lib.ddgi_synchronize(self.h, _stream_ptr(stream), int(timeout_ms)))
+
+    # ---- readback ----------------------------------------------------------
+    def atlas_shape(self, kind):
+        w, h, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        self._check(self.lib.ddgi_atlas_dims(self.h, kind, C.byref(w), C.byref(h), C.byref(c)))
+        return h.value, w.value, c.value
+
+    def get_atlas(self, kind, out=None, stream=None):
+        shape = self.atlas_shape(kind)
+        if out is None:
+            out = np.empty(shape, np.float32)
+        assert out.shape == shape and out.dtype == np.float32 and out.flags.c_contiguous
+        self._check(self.lib.ddgi_get_atlas(self.h, kind, _ptr(out), out.nbytes, _stream_ptr(stream)))
+        return out
+
+    def set_atlas(self, kind, data, stream=None):
+        data = np.ascontiguousarray(data, np.float32)
+        assert data.shape == self.atlas_shape(kind)
+        self._check(self.lib.ddgi_set_atlas(self.h, kind, _ptr(data), data.nbytes, _stream_ptr(stream)))
+
+    def get_ray_records(self, count_probes, stream=None):
+        R = self.grid.rays_per_probe
+        out = np.empty((count_probes, R, 4), np.float32)
+        self._check(self.lib.ddgi_get_ray_records(self.h, _ptr(out), count_probes * R, _stream_ptr(stream)))
+        return out
+
+    def get_hits(self, count_probes, stream=None):
+        R = self.grid.rays_per_probe
+        out = np.empty((count_probes, R), HIT_DTYPE)
+        self._check(self.lib.ddgi_get_hits(self.h, _ptr(out), count_probes * R, _stream_ptr(stream)))
+        return out
+
+    def get_ray_directions(self):
+        R = self.grid.rays_per_probe
+        out = np.empty((R, 4), np.float32)
+        self._check(self.lib.ddgi_get_ray_directions(self.h, _ptr(out), R))
+        return out
+
+    def get_probe_states(self, stream=None):
+        n = self.grid.probe_count()
+        out = np.empty(n, np.uint32)
+        self._check(self.lib.ddgi_get_probe_states(self.h, _ptr(out), n, _stream_ptr(stream)))
+        return out
+
+    def set_probe_states(self, states, stream=None):
+        s = np.ascontiguousarray(states, np.uint32)
+        self._check(self.lib.ddgi_set_probe_states(self.h, _ptr(s), len(s), _stream_ptr(stream)))
+
+    def atlas_device_ptr(self, kind):
+        p = C.c_void_p()
+        self._check(self.lib.ddgi_atlas_device_ptr(self.h, kind, C.byref(p)))
+        return p.value
+
+    def timings(self):
+        t = Timings()
+        self._check(self.lib.ddgi_get_timings(self.h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in Timings._fields_}
+
+    def trace_rays(self, origins, dirs, tmin, tmax, mask=0xFF, any_hit=False, stream=None):
+        origins = np.ascontiguousarray(origins, np.float32)
+        dirs = np.ascontiguousarray(dirs, np.float32)
+        n = len(origins)
+        hits = np.zeros(n, HIT_DTYPE)
+        bary = np.zeros((n, 2), np.float32)
+        self._check(self.lib.ddgi_trace_rays(self.h, _ptr(origins), _ptr(dirs), n, tmin, tmax, mask, int(any_hit),
+                                             _ptr(hits), _ptr(bary), _stream_ptr(stream)))
+        return hits, bary
+
+
+class IrradianceProbes:
+    """Drop-in mirror of VulkanExp's IrradianceProbes over the C ABI."""
+
+    MaxRaysPerProbe = 1024
+
+    def __init__(self):
+        # GridInfo defaults (src/IrradianceProbes.hpp:49-60)
+        self.GridParameters = abi.make_grid((0, 0, 0), (1, 1, 1), (32, 16, 32), 192, 8, 16, 0.0, 12.0, 0.3)
+        self.TargetHysteresis = 0.98
+        self.ProbesPerUpdate = 0
+        self.ctx = None
+        self._updated = 0
+
+    def init(self, extent_min, extent_max):
+        self.GridParameters.extent_min[:] = [float(v) for v in extent_min]
+        self.GridParameters.extent_max[:] = [float(v) for v in extent_max]
+        if self.ctx:
+            self.ctx.close()
+        self.ctx = Context(self.GridParameters)
+
+    def setScene(self, scene, stream=None):
+        self.ctx.build_scene(scene, stream)
+
+    def setLightBuffer(self, light):
+        self.ctx.set_light(light)
+
+    def updateUniforms(self):
+        self.ctx.set_grid(self.GridParameters)
+
+    def getProbeCount(self):
+        r = self.GridParameters.resolution
+        return int(r[0]) * int(r[1]) * int(r[2])
+
+    def update(self, orientation, probe_list=None, stream=None):
+        """One update; `orientation` is the 3x3 ray-set rotation."""
+        self.ctx.update(orientation, probe_list, stream)
+
+    def getIrradiance(self):
+        return self.ctx.get_atlas(abi.ATLAS_COLOR)
+
+    def getDepth(self):
+        return self.ctx.get_atlas(abi.ATLAS_DEPTH)
+
+    def destroy(self):
+        if self.ctx:
+            self.ctx.close()
+            self.ctx = None
