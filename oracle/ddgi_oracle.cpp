@@ -519,10 +519,11 @@ V3<T> sample_probes(V3<T> position, V3<T> normal, V3<T> toCamera, const Grid& g,
                     const Atlas<T>& at) {
     V3<T> cs = cell_size<T>(g);
     V3<T> gridCoords = (position - V3<T>(g.mn)) / vabs(cs);
-    if (gridCoords.x < T(0) || gridCoords.y < T(0) || gridCoords.z < T(0)) return V3<T>();
+    if (!(gridCoords.x >= T(0) && gridCoords.y >= T(0) && gridCoords.z >= T(0))) return V3<T>();
     V3<T> biasVector = (normal + toCamera) * T(g.bias);
     V3<T> biasedPosition = position + biasVector;
-    int first[3] = {(int)gridCoords.x, (int)gridCoords.y, (int)gridCoords.z};
+    const T lim = T(16777216);
+    int first[3] = {(int)std::min(gridCoords.x, lim), (int)std::min(gridCoords.y, lim), (int)std::min(gridCoords.z, lim)};
     V3<T> fp = probe_pos<T>(first, g);
     V3<T> alpha = (position - fp) / vabs(cs);
     alpha = V3<T>(clampT(alpha.x, T(0), T(1)), clampT(alpha.y, T(0), T(1)), clampT(alpha.z, T(0), T(1)));

@@ -36,9 +36,10 @@ __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t code) {
 //   a = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
 //   b = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
 //   c = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
-//   d = (ref0, ref1, count0, count1)
-// ref >= 0: inner node index; ref < 0: leaf, first primitive ~ref, `count`
-// primitives (triangles in a bottom level, one instance in the top level).
+//   d = (ref0, ref1, unused, unused)
+// ref >= 0: inner node index; ref < 0: leaf, ~ref = (first << 3) | (count - 1)
+// with 1..8 primitives from `first` (triangles in a bottom level, one
+// instance in the top level).
 struct __align__(16) BvhNode {
     float4 a, b, c;
     int4 d;
@@ -70,6 +71,7 @@ struct DeviceScene {
     const ddgi_material* materials;
     int32_t tlas_root;      // -1: empty scene
     uint32_t vertex_count, index_count, offset_count, material_count;
+    uint32_t node_count, tri_count, instance_count;  // bounds of the references above
 };
 
 struct DeviceGrid {

@@ -200,6 +200,9 @@ DeviceScene device_scene(const ddgi_ctx* c) {
     s.index_count = c->scene.index_count;
     s.offset_count = c->scene.offset_count;
     s.material_count = c->scene.material_count;
+    s.node_count = (uint32_t)c->scene.node_count;
+    s.tri_count = (uint32_t)c->scene.tri_count;
+    s.instance_count = c->scene.instance_count;
     return s;
 }
 
@@ -579,7 +582,8 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
     if (ni > 0) {
         CKB(cudaMemcpyAsync(box_lo, ilo.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
         CKB(cudaMemcpyAsync(box_hi, ihi.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
-        CKB(lbvh_build(box_lo, box_hi, ni, kTlasLeafMax, S.nodes, (int)node_base, 0, sorted, scratch, st), "top-level build");
+        CKB(lbvh_build(box_lo, box_hi, ni, kTlasLeafMax, S.nodes, (int)node_base, 0, sorted, scratch, ctx->err, st),
+            "top-level build");
         std::vector<uint32_t> order(ni);
         CKB(cudaMemcpyAsync(order.data(), sorted, sizeof(uint32_t) * ni, cudaMemcpyDeviceToHost, st), "read order");
         CKB(cudaStreamSynchronize(st), "top-level build");

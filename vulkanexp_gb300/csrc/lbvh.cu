@@ -165,8 +165,10 @@ __global__ void k_radix_scatter(const uint32_t* keys_in, const uint32_t* vals_in
         __syncthreads();
         if (valid) {
             uint32_t pos = wcnt[warp][digit] + rank;
-            keys_out[pos] = key;
-            vals_out[pos] = val;
+            if (pos < n) {  // always true for a consistent histogram
+                keys_out[pos] = key;
+                vals_out[pos] = val;
+            }
         }
         __syncthreads();
     }
@@ -219,15 +221,23 @@ struct Box6 {
 
 __global__ void k_refit(const float4* prim_lo, const float4* prim_hi, const uint32_t* sorted_ids, int n,
                         const int2* children, const int* inner_parent, const int* leaf_parent, uint32_t* flags,
-                        float4* node_lo, float4* node_hi) {
+                        float4* node_lo, float4* node_hi, uint32_t* err) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int p = leaf_parent[j];
-    while (p >= 0) {
+    for (int level = 0; p >= 0; ++level) {
+        if (p >= n - 1 || level > n) {  // malformed tree: stop instead of running away
+            raise_error(err, DEV_BAD_INDEX);
+            return;
+        }
         __threadfence();
         if (atomicAdd(&flags[p], 1u) == 0) return;  // first arriver stops
         __threadfence();
         int2 c = children[p];
+        if (c.x >= n - 1 || c.y >= n - 1 || (c.x < 0 && ~c.x >= n) || (c.y < 0 && ~c.y >= n)) {
+            raise_error(err, DEV_BAD_INDEX);
+            return;
+        }
         float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0);
         int cs[2] = {c.x, c.y};
 #pragma unroll
@@ -238,6 +248,7 @@ __global__ void k_refit(const float4* prim_lo, const float4* prim_hi, const uint
                 b = __ldcg(node_hi + cs[k]);
             } else {
                 uint32_t id = sorted_ids[~cs[k]];
+                if (id >= (uint32_t)n) id = 0;
                 a = prim_lo[id];
                 b = prim_hi[id];
             }
@@ -271,10 +282,14 @@ __device__ __forceinline__ int leaf_ref(int first, int count) { return ~((first 
 
 __global__ void k_finalize(const float4* prim_lo, const float4* prim_hi, const uint32_t* sorted_ids, int n,
                            const int2* children, const int2* ranges, const float4* node_lo, const float4* node_hi,
-                           int leaf_max, BvhNode* out, int node_base, int prim_base) {
+                           int leaf_max, BvhNode* out, int node_base, int prim_base, uint32_t* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     int2 c = children[i];
+    if (c.x >= n - 1 || c.y >= n - 1 || (c.x < 0 && ~c.x >= n) || (c.y < 0 && ~c.y >= n)) {
+        raise_error(err, DEV_BAD_INDEX);
+        c = make_int2(~0, ~0);  // keep the node well-formed
+    }
     int cs[2] = {c.x, c.y};
     float4 lo[2], hi[2];
     int ref[2];
@@ -288,6 +303,7 @@ __global__ void k_finalize(const float4* prim_lo, const float4* prim_hi, const u
             ref[k] = cnt <= leaf_max ? leaf_ref(prim_base + r.x, cnt) : node_base + cs[k];
         } else {
             uint32_t id = sorted_ids[~cs[k]];
+            if (id >= (uint32_t)n) id = 0;
             lo[k] = prim_lo[id];
             hi[k] = prim_hi[id];
             ref[k] = leaf_ref(prim_base + ~cs[k], 1);
@@ -339,7 +355,8 @@ size_t lbvh_scratch_bytes(uint32_t n) {
 }
 
 cudaError_t lbvh_build(const float4* prim_lo, const float4* prim_hi, uint32_t n, int leaf_max, BvhNode* nodes,
-                       int node_base, int prim_base, uint32_t* sorted_ids, void* scratch, cudaStream_t st) {
+                       int node_base, int prim_base, uint32_t* sorted_ids, void* scratch, uint32_t* err,
+                       cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     if (n == 1) {
         k_iota<<<1, 32, 0, st>>>(sorted_ids, 1);
@@ -382,12 +399,13 @@ cudaError_t lbvh_build(const float4* prim_lo, const float4* prim_hi, uint32_t n,
     }
     // 4 passes: the sorted data is back in keys0/vals0
     cudaMemcpyAsync(sorted_ids, vi, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(inner_parent, 0xFF, sizeof(int) * 2 * (size_t)n, st);  // parents = -1
     k_karras<<<div_up(n - 1, T), T, 0, st>>>(ki, (int)n, children, ranges, inner_parent, leaf_parent);
     cudaMemsetAsync(flags, 0, sizeof(uint32_t) * n, st);
     k_refit<<<div_up(n, T), T, 0, st>>>(prim_lo, prim_hi, vi, (int)n, children, inner_parent, leaf_parent, flags,
-                                        node_lo, node_hi);
+                                        node_lo, node_hi, err);
     k_finalize<<<div_up(n - 1, T), T, 0, st>>>(prim_lo, prim_hi, vi, (int)n, children, ranges, node_lo, node_hi,
-                                               leaf_max, nodes, node_base, prim_base);
+                                               leaf_max, nodes, node_base, prim_base, err);
     return cudaGetLastError();
 }
 
@@ -419,6 +437,7 @@ __global__ void k_gather_tris(const float4* pos, const uint32_t* indices, uint32
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= ntri) return;
     uint32_t t = sorted_ids[s];
+    if (t >= ntri) t = 0;  // cannot happen for a permutation
     float4 v[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -442,7 +461,8 @@ cudaError_t build_mesh_blas(const float4* pos, const uint32_t* indices, uint32_t
     if (ntri == 0) return cudaSuccess;
     const int T = 256;
     k_tri_boxes<<<div_up(ntri, T), T, 0, st>>>(pos, indices, vbase, ibase, ntri, vcount, box_lo, box_hi, err);
-    cudaError_t e = lbvh_build(box_lo, box_hi, ntri, leaf_max, nodes, node_base, tri_base, sorted_ids, scratch, st);
+    cudaError_t e =
+        lbvh_build(box_lo, box_hi, ntri, leaf_max, nodes, node_base, tri_base, sorted_ids, scratch, err, st);
     if (e != cudaSuccess) return e;
     k_gather_tris<<<div_up(ntri, T), T, 0, st>>>(pos, indices, vbase, ibase, ntri, vcount, sorted_ids,
                                                  tris + tri_base);

@@ -16,7 +16,8 @@ size_t lbvh_scratch_bytes(uint32_t n);
 // prim_base + sorted position.  sorted_ids[s] = original primitive of sorted
 // position s.  Root = node_base.
 cudaError_t lbvh_build(const float4* prim_lo, const float4* prim_hi, uint32_t n, int leaf_max, BvhNode* nodes,
-                       int node_base, int prim_base, uint32_t* sorted_ids, void* scratch, cudaStream_t st);
+                       int node_base, int prim_base, uint32_t* sorted_ids, void* scratch, uint32_t* err,
+                       cudaStream_t st);
 
 // Bottom-level build of one mesh: triangle boxes from the vertex positions and
 // indices, the tree, and the triangles gathered in leaf order at

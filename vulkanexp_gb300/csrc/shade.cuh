@@ -70,9 +70,12 @@ __device__ float3 sample_probes(float3 position, float3 normal, float3 toCamera,
                                 const uint32_t* states, const AV& at) {
     float3 cs = abs3(f3(g.cell[0], g.cell[1], g.cell[2]));
     float3 gridCoords = (position - f3(g.mn[0], g.mn[1], g.mn[2])) / cs;
-    if (gridCoords.x < 0.0f || gridCoords.y < 0.0f || gridCoords.z < 0.0f) return f3(0, 0, 0);
+    // (written so that NaN also returns 0)
+    if (!(gridCoords.x >= 0.0f && gridCoords.y >= 0.0f && gridCoords.z >= 0.0f)) return f3(0, 0, 0);
     float3 biasedPosition = position + (normal + toCamera) * g.bias;
-    int fx = (int)gridCoords.x, fy = (int)gridCoords.y, fz = (int)gridCoords.z;
+    // the clamp only matters beyond 2^24 cells, where every corner is off-grid
+    int fx = (int)fminf(gridCoords.x, 16777216.0f), fy = (int)fminf(gridCoords.y, 16777216.0f),
+        fz = (int)fminf(gridCoords.z, 16777216.0f);
     float3 alpha = (position - grid_probe_pos(g, fx, fy, fz)) / cs;
     alpha = f3(clampf(alpha.x, 0.0f, 1.0f), clampf(alpha.y, 0.0f, 1.0f), clampf(alpha.z, 0.0f, 1.0f));
 

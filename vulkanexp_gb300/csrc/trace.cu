@@ -59,9 +59,19 @@ __device__ __forceinline__ bool traverse(const DeviceScene& sc, float3 wo, float
     bool in_blas = false;
     uint32_t inst_id = 0;
     float tcur = tmax;
-    for (;;) {
+    // A well-formed tree visits each node at most once per ray; the cap only
+    // stops a malformed one from looping.
+    for (uint32_t steps = 0;; ++steps) {
+        if (steps > 4u * (sc.node_count + sc.tri_count + sc.instance_count) + 64u) {
+            raise_error(err, DEV_BAD_INDEX);
+            return best->inst != kNoHit;
+        }
         if (ref >= 0) {
             if (COUNT) fc->nodes++;
+            if ((uint32_t)ref >= sc.node_count) {
+                raise_error(err, DEV_BAD_INDEX);
+                return best->inst != kNoHit;
+            }
             BvhNode n = load_node(sc.nodes, ref);
             bool h0, h1;
             float t0, t1;
@@ -90,6 +100,10 @@ __device__ __forceinline__ bool traverse(const DeviceScene& sc, float3 wo, float
             }
         } else if (!in_blas) {
             // top-level leaf: one instance
+            if ((uint32_t)((~ref) >> 3) >= sc.instance_count) {
+                raise_error(err, DEV_BAD_INDEX);
+                return best->inst != kNoHit;
+            }
             const GpuInstance* gi = sc.instances + ((~ref) >> 3);
             int4 meta = __ldg(reinterpret_cast<const int4*>(gi) + 3);  // blas_root, custom, mask, id
             if (((uint32_t)meta.z & mask) != 0 && meta.x >= 0) {
@@ -110,6 +124,10 @@ __device__ __forceinline__ bool traverse(const DeviceScene& sc, float3 wo, float
             }
         } else {
             int first = (~ref) >> 3, count = ((~ref) & 7) + 1;
+            if ((uint32_t)first + (uint32_t)count > sc.tri_count) {
+                raise_error(err, DEV_BAD_INDEX);
+                return best->inst != kNoHit;
+            }
             if (COUNT) fc->tris += count;
             for (int k = 0; k < count; ++k) {
                 const float4* tp = reinterpret_cast<const float4*>(sc.tris + first + k);
