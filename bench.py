@@ -169,8 +169,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--pipeline", default="wavefront", choices=["wavefront", "fused"])
     ap.add_argument("--cpu-probes", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling target: scene build, then two updates (the second is the one to capture), no timing")
     args = ap.parse_args()
 
     rank, world, local = dist_env()
@@ -194,10 +197,18 @@ def main():
         dist.init_process_group("nccl")
     stream = torch.cuda.current_stream()
     ctx = Context(w.grid)
+    ctx.set_pipeline(abi.PIPELINE_WAVEFRONT if args.pipeline == "wavefront" else abi.PIPELINE_FUSED)
     t0 = time.perf_counter()
     ctx.build_scene(w.scene, stream)
     build_s = time.perf_counter() - t0
     ctx.set_light(w.light)
+    if args.profile:
+        for k in range(2):
+            ctx.update(w.orientation(k), stream=stream)
+        ctx.synchronize(stream)
+        ctx.close()
+        print(json.dumps({"profile_target": w.name, "updates": 2}), flush=True)
+        return
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     P, R = w.grid.probe_count(), w.grid.rays_per_probe
 
@@ -215,7 +226,7 @@ def main():
         torch.distributed.barrier()
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    trace_ms, blend_ms = [], []
+    trace_ms, blend_ms, primary_ms = [], [], []
     wall0 = time.perf_counter()
     for k in range(args.steps):
         flush.fill_(k & 255)
@@ -225,6 +236,7 @@ def main():
         t = ctx.timings()  # synchronises on the update's last event
         trace_ms.append(t["trace_ms"])
         blend_ms.append(t["blend_ms"])
+        primary_ms.append(t["primary_ms"])
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     step_ms = [a.elapsed_time(b) for a, b in ev]
@@ -265,9 +277,11 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config_dict(w, args),
-            "impl": "ours", "form": "plain FP32 (trace+shade kernel, SIMT blend + fused border)",
-            "stage_ms": {"trace_shade": trace_avg, "blend_border": float(np.mean(blend_ms))},
-            "gpu_launches": 2 * args.steps, "clocks": clocks, "roofline": roofline,
+            "impl": "ours", "pipeline": args.pipeline,
+            "stage_ms": {"trace_shade": trace_avg, "primary_traversal": float(np.mean(primary_ms)),
+                         "blend_border": float(np.mean(blend_ms))},
+            "gpu_launches": (4 if args.pipeline == "wavefront" else 2) * args.steps, "clocks": clocks,
+            "roofline": roofline,
             "e2e": {"value": e2e_val, "unit": UNIT, "ms_per_step": float(np.mean(e2e_ms)),
                     "h2d_bytes_per_step": R * 20, "d2h_bytes_per_step": int(host_c.nbytes + host_d.nbytes)},
             "scene_build_s": build_s, "wall_s_timed": wall}

@@ -160,14 +160,23 @@ typedef enum ddgi_atlas_kind {
 
 /* Per-stage device times of the last update, in milliseconds, in the order of
  * the reference's five timestamps (src/IrradianceProbes.cpp:441-452):
- * total, trace+shade, blend, border copy, atlas publish. */
+ * total, trace+shade, blend, border copy, atlas publish; then the part of
+ * trace+shade spent in the primary closest-hit traversal. */
 typedef struct ddgi_timings {
     float total_ms;
     float trace_ms;
     float blend_ms;
     float border_ms;
     float copy_ms;
+    float primary_ms;
 } ddgi_timings;
+
+/* How the trace + shade of an update is scheduled.  Both give identical
+ * results. */
+typedef enum ddgi_pipeline {
+    DDGI_PIPELINE_FUSED = 0,     /* one thread per ray: trace, shade, shadow ray */
+    DDGI_PIPELINE_WAVEFRONT = 1  /* persistent primary traversal, shading, compacted shadow traversal (default) */
+} ddgi_pipeline;
 
 const char* ddgi_status_string(ddgi_status status);
 /* Message of the last failing call on this context (never NULL). */
@@ -248,18 +257,20 @@ ddgi_status ddgi_trace_rays(ddgi_ctx* ctx, const float* origins, const float* di
                             ddgi_stream stream);
 
 /* Measurement: runs the trace + shade of one update (no blend; atlas and
- * probe states untouched) with fetch counters, and returns
- * out[0] inner-node fetches (64 B each), out[1] triangle tests (48 B each),
- * out[2] instance entries (64 B each), out[3] rays traced (primary + shadow),
+ * probe states untouched) with fetch counters, and returns for the primary
+ * (closest-hit) rays out[0] inner-node fetches (64 B each), out[1] triangle
+ * tests (48 B each), out[2] instance entries (64 B each), out[3] rays;
  * out[4] shading bytes (hit data, atlas texels of the bounce lookups, ray
- * record).  Synchronous on `stream`. */
+ * record); and out[5..8] the same four counts for the shadow (any-hit) rays.
+ * Synchronous on `stream`. */
 ddgi_status ddgi_count_fetches(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
-                               uint32_t probe_count, uint64_t out[5], ddgi_stream stream);
+                               uint32_t probe_count, uint64_t out[9], ddgi_stream stream);
 
 /* Waits for `stream` with a timeout (poll), then checks the device error word.
  * timeout_ms < 0 waits forever. */
 ddgi_status ddgi_synchronize(ddgi_ctx* ctx, ddgi_stream stream, int timeout_ms);
 ddgi_status ddgi_get_timings(const ddgi_ctx* ctx, ddgi_timings* out);
+ddgi_status ddgi_set_pipeline(ddgi_ctx* ctx, ddgi_pipeline pipeline);
 /* Enables per-stage CUDA-event timing of updates (off by default). */
 ddgi_status ddgi_enable_timing(ddgi_ctx* ctx, int enable);
 

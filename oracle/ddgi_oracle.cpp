@@ -268,6 +268,12 @@ RayPre make_ray(F3 o, F3 d) {
     return r;
 }
 
+// Box tests use [tmin * kBoxLo, tcur * kBoxHi]: a relative margin far above
+// the few-ulp error of slab and triangle distances, so that pruning never
+// removes a box holding a hit the triangle test reports.
+constexpr float kBoxLo = 0.99999f;
+constexpr float kBoxHi = 1.00001f;
+
 inline bool box_hit(const RayPre& r, const Box& b, float tmin, float tmax, float* tnear) {
     float t0 = tmin, t1 = tmax;
     for (int k = 0; k < 3; ++k) {
@@ -354,7 +360,7 @@ bool trace(const Scene& sc, F3 o, F3 d, float tmin, float tmax, uint32_t mask, b
     while (sp > 0) {
         const Node& nd = sc.tlas.nodes[stack[--sp]];
         float tn;
-        if (!box_hit(wr, nd.box, tmin, tcur, &tn)) continue;
+        if (!box_hit(wr, nd.box, tmin * kBoxLo, tcur * kBoxHi, &tn)) continue;
         if (nd.count == 0) {
             stack[sp++] = nd.right;
             stack[sp++] = nd.first;
@@ -375,7 +381,7 @@ bool trace(const Scene& sc, F3 o, F3 d, float tmin, float tmax, uint32_t mask, b
             while (bsp > 0) {
                 const Node& bn = m.bvh.nodes[bst[--bsp]];
                 float t2;
-                if (!box_hit(r, bn.box, tmin, tcur, &t2)) continue;
+                if (!box_hit(r, bn.box, tmin * kBoxLo, tcur * kBoxHi, &t2)) continue;
                 if (bn.count == 0) {
                     bst[bsp++] = bn.right;
                     bst[bsp++] = bn.first;

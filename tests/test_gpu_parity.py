@@ -18,8 +18,12 @@ TOL = 1e-4
 FLOOR = 1e-2
 
 
-def make_ctx(w, record_hits=True):
+PIPELINES = [abi.PIPELINE_FUSED, abi.PIPELINE_WAVEFRONT]
+
+
+def make_ctx(w, record_hits=True, pipeline=abi.PIPELINE_WAVEFRONT):
     ctx = Context(w.grid)
+    ctx.set_pipeline(pipeline)
     ctx.build_scene(w.scene)
     ctx.set_light(w.light)
     if record_hits:
@@ -72,8 +76,8 @@ def test_trace_rays_masks_and_tmin(gpu_lib, room_workload, room_oracle):
     ctx.close()
 
 
-def run_updates(w, k_updates, probe_list=None):
-    ctx = make_ctx(w)
+def run_updates(w, k_updates, probe_list=None, pipeline=abi.PIPELINE_WAVEFRONT):
+    ctx = make_ctx(w, pipeline=pipeline)
     o = Oracle(w.scene)
     c, d = zero_atlas(w.grid)
     st = np.ones(w.grid.probe_count(), np.uint32)
@@ -94,17 +98,19 @@ def run_updates(w, k_updates, probe_list=None):
     return gc, gd, gs, c, d, st
 
 
-def test_update_room_one_step_from_zero(gpu_lib, room_workload):
-    gc, gd, gs, c, d, st = run_updates(room_workload, 1)
+@pytest.mark.parametrize("pipeline", PIPELINES)
+def test_update_room_one_step_from_zero(gpu_lib, room_workload, pipeline):
+    gc, gd, gs, c, d, st = run_updates(room_workload, 1, pipeline=pipeline)
     assert rel_err(gc, c, FLOOR).max() <= TOL
     assert rel_err(gd, d, FLOOR).max() <= TOL
     assert (gs == st).all()
 
 
-def test_update_room_three_steps_bounce(gpu_lib):
+@pytest.mark.parametrize("pipeline", PIPELINES)
+def test_update_room_three_steps_bounce(gpu_lib, pipeline):
     """Later updates read the previous atlas through sampleProbes."""
     w = scenes.room_workload(99, n_boxes=60, resolution=(6, 5, 6), rays=96)
-    gc, gd, gs, c, d, st = run_updates(w, 3)
+    gc, gd, gs, c, d, st = run_updates(w, 3, pipeline=pipeline)
     assert rel_err(gc, c, FLOOR).max() <= TOL
     assert rel_err(gd, d, FLOOR).max() <= TOL
     assert (gs == st).all()
@@ -129,12 +135,14 @@ def test_update_resolutions_and_ray_counts(gpu_lib, color_res, depth_res, rays):
     assert rel_err(gd, d, FLOOR).max() <= TOL
 
 
-def test_empty_scene_is_sky(gpu_lib):
+@pytest.mark.parametrize("pipeline", PIPELINES)
+def test_empty_scene_is_sky(gpu_lib, pipeline):
     sc = scenes.room_with_boxes(5, n_boxes=0)
     sc.instances = sc.instances[:0]
     g = abi.make_grid((0, 0, 0), (4, 3, 5), (3, 3, 3), 64, hysteresis=0.9)
     L = scenes.default_light()
     ctx = Context(g)
+    ctx.set_pipeline(pipeline)
     ctx.build_scene(sc)
     ctx.set_light(L)
     ctx.update(scenes.random_orientation(3, 0))
@@ -144,13 +152,14 @@ def test_empty_scene_is_sky(gpu_lib):
     ctx.close()
 
 
-def test_terrain_subset_bit_exact_hits(gpu_lib):
+@pytest.mark.parametrize("pipeline", PIPELINES)
+def test_terrain_subset_bit_exact_hits(gpu_lib, pipeline):
     """At-scale scene (terrain + 4096 box-cluster instances, ~1M unique
     triangles): one update from zero on a random subset of 256 probes."""
     w = scenes.workload(1)
     rng = np.random.default_rng(11)
     plist = np.sort(rng.permutation(w.grid.probe_count())[:256]).astype(np.uint32)
-    gc, gd, gs, c, d, st = run_updates(w, 1, plist)
+    gc, gd, gs, c, d, st = run_updates(w, 1, plist, pipeline=pipeline)
     assert rel_err(gc, c, FLOOR).max() <= TOL
     assert rel_err(gd, d, FLOOR).max() <= TOL
 

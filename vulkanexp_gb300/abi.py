@@ -108,7 +108,12 @@ class SceneDesc(C.Structure):
 
 
 class Timings(C.Structure):
-    _fields_ = [("total_ms", C.c_float), ("trace_ms", C.c_float), ("blend_ms", C.c_float), ("border_ms", C.c_float), ("copy_ms", C.c_float)]
+    _fields_ = [("total_ms", C.c_float), ("trace_ms", C.c_float), ("blend_ms", C.c_float), ("border_ms", C.c_float),
+                ("copy_ms", C.c_float), ("primary_ms", C.c_float)]
+
+
+PIPELINE_FUSED = 0
+PIPELINE_WAVEFRONT = 1
 
 
 def make_grid(extent_min, extent_max, resolution, rays, color_res=8, depth_res=16, hysteresis=0.97,

@@ -33,6 +33,9 @@ namespace {
 
 constexpr int kBlasLeafMax = 4;
 constexpr int kTlasLeafMax = 1;
+// deepest traversal stack of the wavefront kernels (entries per thread in
+// shared memory: 96 x 128 threads x 4 bytes = 48 KB per block)
+constexpr int kMaxStack = 96;
 
 struct SceneBuffers {
     BvhNode* nodes = nullptr;
@@ -44,6 +47,8 @@ struct SceneBuffers {
     ddgi_offset_entry* offsets = nullptr;
     ddgi_material* materials = nullptr;
     int32_t tlas_root = -1;
+    int stack_cap = 0;
+    uint32_t depth_blas = 0, depth_tlas = 0;
     uint32_t vertex_count = 0, index_count = 0, offset_count = 0, material_count = 0, instance_count = 0;
     uint64_t node_count = 0, tri_count = 0;
     bool built = false;
@@ -62,6 +67,14 @@ struct ddgi_ctx {
     uint32_t* states = nullptr;
     float4* rays = nullptr;
     size_t rays_cap = 0;  // in records
+    // wavefront pipeline: hit buffer, shadow-ray queue, work counters
+    float4* wave_thit = nullptr;
+    uint32_t* wave_prim = nullptr;
+    uint32_t* q_idx = nullptr;
+    float4* q_pos = nullptr;
+    float4* q_sun = nullptr;
+    uint32_t* counters = nullptr;
+    ddgi_pipeline pipeline = DDGI_PIPELINE_WAVEFRONT;
     ddgi_hit* hits = nullptr;
     size_t hits_cap = 0;
     bool record_hits = false;
@@ -221,7 +234,18 @@ void free_scene(SceneBuffers& s) {
 ddgi_status ensure_ray_capacity(ddgi_ctx* ctx, size_t records) {
     if (records > ctx->rays_cap) {
         dfree(ctx->rays);
+        dfree(ctx->wave_thit);
+        dfree(ctx->wave_prim);
+        dfree(ctx->q_idx);
+        dfree(ctx->q_pos);
+        dfree(ctx->q_sun);
+        ctx->rays_cap = 0;
         CK(cudaMalloc(&ctx->rays, records * sizeof(float4)), "cudaMalloc ray records");
+        CK(cudaMalloc(&ctx->wave_thit, records * sizeof(float4)), "cudaMalloc hit buffer");
+        CK(cudaMalloc(&ctx->wave_prim, records * sizeof(uint32_t)), "cudaMalloc hit buffer");
+        CK(cudaMalloc(&ctx->q_idx, records * sizeof(uint32_t)), "cudaMalloc shadow queue");
+        CK(cudaMalloc(&ctx->q_pos, records * sizeof(float4)), "cudaMalloc shadow queue");
+        CK(cudaMalloc(&ctx->q_sun, records * sizeof(float4)), "cudaMalloc shadow queue");
         ctx->rays_cap = records;
     }
     if (ctx->record_hits && records > ctx->hits_cap) {
@@ -301,7 +325,8 @@ ddgi_status ddgi_create(const ddgi_grid_desc* grid, ddgi_ctx** out) {
         cudaMalloc(&ctx->dirs, sizeof(float4) * DDGI_MAX_RAYS_PER_PROBE) != cudaSuccess ||
         cudaMalloc(&ctx->ray_order, sizeof(uint32_t) * DDGI_MAX_RAYS_PER_PROBE) != cudaSuccess ||
         cudaMalloc(&ctx->probe_list, sizeof(uint32_t) * P) != cudaSuccess ||
-        cudaMalloc(&ctx->err, sizeof(uint32_t)) != cudaSuccess) {
+        cudaMalloc(&ctx->err, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&ctx->counters, 4 * sizeof(uint32_t)) != cudaSuccess) {
         cudaGetLastError();
         return bail(DDGI_ERR_OUT_OF_MEMORY);
     }
@@ -327,6 +352,12 @@ ddgi_status ddgi_destroy(ddgi_ctx* ctx) {
     dfree_v(ctx->depth);
     dfree(ctx->states);
     dfree(ctx->rays);
+    dfree(ctx->wave_thit);
+    dfree(ctx->wave_prim);
+    dfree(ctx->q_idx);
+    dfree(ctx->q_pos);
+    dfree(ctx->q_sun);
+    dfree(ctx->counters);
     dfree(ctx->hits);
     dfree(ctx->dirs);
     dfree(ctx->ray_order);
@@ -380,6 +411,14 @@ ddgi_status ddgi_record_hits(ddgi_ctx* ctx, int enable) {
     if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
     ctx->record_hits = enable != 0;
     if (ctx->record_hits) return ensure_ray_capacity(ctx, ctx->rays_cap);
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_set_pipeline(ddgi_ctx* ctx, ddgi_pipeline pipeline) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    if (pipeline != DDGI_PIPELINE_FUSED && pipeline != DDGI_PIPELINE_WAVEFRONT)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "unknown pipeline %d", (int)pipeline);
+    ctx->pipeline = pipeline;
     return DDGI_OK;
 }
 
@@ -470,16 +509,20 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
     uint32_t ni = d->instance_count;
     uint64_t tlas_nodes = ni > 1 ? ni - 1 : (ni == 1 ? 1 : 0);
     uint32_t max_prims = std::max(max_tris, ni);
+    if (total_tris >= (1ull << 28) - 8 || total_nodes + tlas_nodes >= (1ull << 31))
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "scene too large (%llu triangles)", (unsigned long long)total_tris);
     void* scratch = nullptr;
     float4* box_lo = nullptr;
     float4* box_hi = nullptr;
     uint32_t* sorted = nullptr;
+    uint32_t* depth = nullptr;  // [0] deepest mesh tree, [1] top-level tree
     auto cleanup = [&]() {
         if (dpos) cudaFree(dpos);
         if (scratch) cudaFree(scratch);
         if (box_lo) cudaFree(box_lo);
         if (box_hi) cudaFree(box_hi);
         if (sorted) cudaFree(sorted);
+        if (depth) cudaFree(depth);
     };
 #define CKB(call, what)                               \
     do {                                              \
@@ -504,6 +547,11 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
     CKB(cudaMalloc(&box_lo, sizeof(float4) * std::max<uint32_t>(max_prims, 1)), "alloc build boxes");
     CKB(cudaMalloc(&box_hi, sizeof(float4) * std::max<uint32_t>(max_prims, 1)), "alloc build boxes");
     CKB(cudaMalloc(&sorted, sizeof(uint32_t) * std::max<uint32_t>(max_prims, 1)), "alloc build order");
+    CKB(cudaMalloc(&depth, 2 * sizeof(uint32_t)), "alloc depth");
+    {
+        const uint32_t one[2] = {1u, 1u};
+        CKB(cudaMemcpyAsync(depth, one, sizeof(one), cudaMemcpyHostToDevice, st), "init depth");
+    }
     if (d->vertex_count) {
         CKB(cudaMemcpyAsync(dpos, pos.data(), sizeof(float4) * d->vertex_count, cudaMemcpyHostToDevice, st), "upload");
         CKB(cudaMemcpyAsync(S.normals, nrm.data(), sizeof(float4) * d->vertex_count, cudaMemcpyHostToDevice, st), "upload");
@@ -538,7 +586,7 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
         }
         CKB(build_mesh_blas(dpos, S.indices, me.vertex_offset, me.vertex_count, me.index_offset, nt, kBlasLeafMax,
                             S.nodes, (int)node_base, S.tris, (int)tri_base, box_lo, box_hi, sorted, scratch, ctx->err,
-                            st),
+                            depth, st),
             "bottom-level build");
         mesh_root[m] = (int32_t)node_base;
         node_base += nt > 1 ? nt - 1 : 1;
@@ -582,7 +630,8 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
     if (ni > 0) {
         CKB(cudaMemcpyAsync(box_lo, ilo.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
         CKB(cudaMemcpyAsync(box_hi, ihi.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
-        CKB(lbvh_build(box_lo, box_hi, ni, kTlasLeafMax, S.nodes, (int)node_base, 0, sorted, scratch, ctx->err, st),
+        CKB(lbvh_build(box_lo, box_hi, ni, kTlasLeafMax, S.nodes, (int)node_base, 0, sorted, scratch, ctx->err,
+                       depth + 1, st),
             "top-level build");
         std::vector<uint32_t> order(ni);
         CKB(cudaMemcpyAsync(order.data(), sorted, sizeof(uint32_t) * ni, cudaMemcpyDeviceToHost, st), "read order");
@@ -593,9 +642,21 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
         CKB(cudaMemcpyAsync(S.inst_id, recs.data(), sizeof(GpuInstance) * ni, cudaMemcpyHostToDevice, st), "upload");
         S.tlas_root = (int32_t)node_base;
     }
+    uint32_t depths[2] = {1u, 1u};
+    CKB(cudaMemcpyAsync(depths, depth, sizeof(depths), cudaMemcpyDeviceToHost, st), "read depth");
     CKB(cudaStreamSynchronize(st), "scene build");
     cleanup();
 #undef CKB
+    // traversal stack: one entry per inner node on a root-to-leaf path in each
+    // level, plus the resume node and the EXIT marker of an instance entry
+    S.stack_cap = (int)(depths[0] + depths[1] + 4);
+    S.depth_blas = depths[0];
+    S.depth_tlas = depths[1];
+    if (S.stack_cap > kMaxStack) {
+        free_scene(ctx->scene);
+        return fail(ctx, DDGI_ERR_UNSUPPORTED, "trees too deep for the traversal stack (%u + %u levels)", depths[0],
+                    depths[1]);
+    }
     S.vertex_count = d->vertex_count;
     S.index_count = d->index_count;
     S.offset_count = d->offset_count;
@@ -672,9 +733,20 @@ ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_
     if (s != DDGI_OK) return s;
     DeviceScene sc = device_scene(ctx);
     if (ctx->timing) CK(cudaEventRecord(ctx->ev[0], st), "event");
-    CK(launch_trace_shade(sc, ctx->dg, ctx->dl, dlist, n, ctx->dirs, ctx->ray_order, ctx->states, ctx->color,
-                          ctx->depth, ctx->fp16, ctx->rays, ctx->record_hits ? ctx->hits : nullptr, ctx->err, st),
-       "trace launch");
+    ddgi_hit* hits_out = ctx->record_hits ? ctx->hits : nullptr;
+    if (ctx->pipeline == DDGI_PIPELINE_FUSED) {
+        CK(launch_trace_shade(sc, ctx->dg, ctx->dl, dlist, n, ctx->dirs, ctx->ray_order, ctx->states, ctx->color,
+                              ctx->depth, ctx->fp16, ctx->rays, hits_out, ctx->err, st),
+           "trace launch");
+        if (ctx->timing) CK(cudaEventRecord(ctx->ev[3], st), "event");
+    } else {
+        WaveHits wh{ctx->wave_thit, ctx->wave_prim};
+        ShadowQueue q{ctx->q_idx, ctx->q_pos, ctx->q_sun, nullptr};
+        CK(launch_wavefront(sc, ctx->dg, ctx->dl, dlist, n, ctx->dirs, ctx->ray_order, ctx->states, ctx->color,
+                            ctx->depth, ctx->fp16, wh, q, ctx->counters, ctx->rays, hits_out, ctx->scene.stack_cap,
+                            ctx->err, st, ctx->timing ? ctx->ev[3] : nullptr),
+           "wavefront trace launch");
+    }
     if (ctx->timing) CK(cudaEventRecord(ctx->ev[1], st), "event");
     CK(launch_blend_fp32(ctx->dg, dlist, n, ctx->rays, ctx->dirs, ctx->states, static_cast<float4*>(ctx->color),
                          static_cast<float2*>(ctx->depth), st),
@@ -689,7 +761,7 @@ ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_
 }
 
 ddgi_status ddgi_count_fetches(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
-                               uint32_t probe_count, uint64_t out[5], ddgi_stream stream) {
+                               uint32_t probe_count, uint64_t out[9], ddgi_stream stream) {
     if (!ctx || !orientation || !out) return DDGI_ERR_INVALID_ARGUMENT;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const uint32_t* dlist = nullptr;
@@ -697,17 +769,17 @@ ddgi_status ddgi_count_fetches(ddgi_ctx* ctx, const float orientation[9], const 
     ddgi_status s = prepare_update(ctx, orientation, probe_list, probe_count, st, &dlist, &n);
     if (s != DDGI_OK) return s;
     unsigned long long* dc = nullptr;
-    CK(cudaMalloc(&dc, 5 * sizeof(unsigned long long)), "alloc counters");
-    cudaError_t e = cudaMemsetAsync(dc, 0, 5 * sizeof(unsigned long long), st);
+    CK(cudaMalloc(&dc, 9 * sizeof(unsigned long long)), "alloc counters");
+    cudaError_t e = cudaMemsetAsync(dc, 0, 9 * sizeof(unsigned long long), st);
     if (e == cudaSuccess)
         e = launch_trace_shade(device_scene(ctx), ctx->dg, ctx->dl, dlist, n, ctx->dirs, ctx->ray_order, ctx->states,
                                ctx->color, ctx->depth, ctx->fp16, ctx->rays, nullptr, ctx->err, st, dc);
-    unsigned long long h[5] = {0, 0, 0, 0, 0};
+    unsigned long long h[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(h, dc, sizeof(h), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     cudaFree(dc);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "count fetches");
-    for (int k = 0; k < 5; ++k) out[k] = h[k];
+    for (int k = 0; k < 9; ++k) out[k] = h[k];
     ctx->last_count = n;
     ctx->last_rays = ctx->grid.rays_per_probe;
     return check_device_error(ctx);
@@ -718,9 +790,11 @@ ddgi_status ddgi_get_timings(const ddgi_ctx* cctx, ddgi_timings* out) {
     if (!ctx || !out) return DDGI_ERR_INVALID_ARGUMENT;
     if (ctx->timing_pending) {
         CK(cudaEventSynchronize(ctx->ev[2]), "timing");
-        float a = 0, b = 0;
+        float a = 0, b = 0, p = 0;
         cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
         cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+        cudaEventElapsedTime(&p, ctx->ev[0], ctx->ev[3]);
+        ctx->timings.primary_ms = p;
         ctx->timings.trace_ms = a;
         ctx->timings.blend_ms = b;
         ctx->timings.border_ms = 0.0f;  // fused into the blend

@@ -18,6 +18,24 @@ cudaError_t launch_trace_rays(const DeviceScene& sc, const float* origins, const
                               float tmax, uint32_t mask, int any, ddgi_hit* out, float* bary, uint32_t* err,
                               cudaStream_t st);
 
+// wavefront.cu
+struct WaveHits {
+    float4* thit;    // (t, b1, b2, instance bits) per ray
+    uint32_t* prim;  // primitive | backface << 31
+};
+struct ShadowQueue {
+    uint32_t* idx;   // ray record index
+    float4* pos;     // shadow-ray origin (hit position)
+    float4* sun;     // unshadowed sun term (xyz) and night fade (w)
+    uint32_t* count;
+};
+cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L,
+                             const uint32_t* probe_list, uint32_t nprobes, const float4* dirs,
+                             const uint32_t* ray_order, const uint32_t* states, const void* color, const void* depth,
+                             bool fp16_atlas, WaveHits hits, ShadowQueue q, uint32_t* counters, float4* rays_out,
+                             ddgi_hit* hits_out, int stack_cap, uint32_t* err, cudaStream_t st,
+                             cudaEvent_t after_primary);
+
 // blend.cu
 cudaError_t launch_blend_fp32(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
                               const float4* dirs, uint32_t* states, float4* color, float2* depth, cudaStream_t st);

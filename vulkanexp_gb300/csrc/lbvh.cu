@@ -215,9 +215,19 @@ __global__ void k_karras(const uint32_t* codes, int n, int2* children, int2* ran
     if (i == 0) inner_parent[0] = -1;
 }
 
-struct Box6 {
-    float4 lo, hi;
-};
+// Inner nodes on the path root -> leaf, maximised into *depth (the stack a
+// near-first traversal needs within this tree).
+__global__ void k_depth(const int* inner_parent, const int* leaf_parent, int n, uint32_t* depth) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t d = 0;
+    int p = leaf_parent[j];
+    while (p >= 0 && p < n - 1 && d <= (uint32_t)n) {
+        ++d;
+        p = inner_parent[p];
+    }
+    atomicMax(depth, d);
+}
 
 __global__ void k_refit(const float4* prim_lo, const float4* prim_hi, const uint32_t* sorted_ids, int n,
                         const int2* children, const int* inner_parent, const int* leaf_parent, uint32_t* flags,
@@ -355,7 +365,7 @@ size_t lbvh_scratch_bytes(uint32_t n) {
 }
 
 cudaError_t lbvh_build(const float4* prim_lo, const float4* prim_hi, uint32_t n, int leaf_max, BvhNode* nodes,
-                       int node_base, int prim_base, uint32_t* sorted_ids, void* scratch, uint32_t* err,
+                       int node_base, int prim_base, uint32_t* sorted_ids, void* scratch, uint32_t* err, uint32_t* depth,
                        cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     if (n == 1) {
@@ -406,6 +416,7 @@ cudaError_t lbvh_build(const float4* prim_lo, const float4* prim_hi, uint32_t n,
                                         node_lo, node_hi, err);
     k_finalize<<<div_up(n - 1, T), T, 0, st>>>(prim_lo, prim_hi, vi, (int)n, children, ranges, node_lo, node_hi,
                                                leaf_max, nodes, node_base, prim_base, err);
+    if (depth) k_depth<<<div_up(n, T), T, 0, st>>>(inner_parent, leaf_parent, (int)n, depth);
     return cudaGetLastError();
 }
 
@@ -457,12 +468,12 @@ __global__ void k_gather_tris(const float4* pos, const uint32_t* indices, uint32
 cudaError_t build_mesh_blas(const float4* pos, const uint32_t* indices, uint32_t vbase, uint32_t vcount,
                             uint32_t ibase, uint32_t ntri, int leaf_max, BvhNode* nodes, int node_base, BvhTri* tris,
                             int tri_base, float4* box_lo, float4* box_hi, uint32_t* sorted_ids, void* scratch,
-                            uint32_t* err, cudaStream_t st) {
+                            uint32_t* err, uint32_t* depth, cudaStream_t st) {
     if (ntri == 0) return cudaSuccess;
     const int T = 256;
     k_tri_boxes<<<div_up(ntri, T), T, 0, st>>>(pos, indices, vbase, ibase, ntri, vcount, box_lo, box_hi, err);
     cudaError_t e =
-        lbvh_build(box_lo, box_hi, ntri, leaf_max, nodes, node_base, tri_base, sorted_ids, scratch, err, st);
+        lbvh_build(box_lo, box_hi, ntri, leaf_max, nodes, node_base, tri_base, sorted_ids, scratch, err, depth, st);
     if (e != cudaSuccess) return e;
     k_gather_tris<<<div_up(ntri, T), T, 0, st>>>(pos, indices, vbase, ibase, ntri, vcount, sorted_ids,
                                                  tris + tri_base);

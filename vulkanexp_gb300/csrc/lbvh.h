@@ -16,7 +16,7 @@ size_t lbvh_scratch_bytes(uint32_t n);
 // prim_base + sorted position.  sorted_ids[s] = original primitive of sorted
 // position s.  Root = node_base.
 cudaError_t lbvh_build(const float4* prim_lo, const float4* prim_hi, uint32_t n, int leaf_max, BvhNode* nodes,
-                       int node_base, int prim_base, uint32_t* sorted_ids, void* scratch, uint32_t* err,
+                       int node_base, int prim_base, uint32_t* sorted_ids, void* scratch, uint32_t* err, uint32_t* depth,
                        cudaStream_t st);
 
 // Bottom-level build of one mesh: triangle boxes from the vertex positions and
@@ -25,6 +25,6 @@ cudaError_t lbvh_build(const float4* prim_lo, const float4* prim_hi, uint32_t n,
 cudaError_t build_mesh_blas(const float4* pos, const uint32_t* indices, uint32_t vbase, uint32_t vcount,
                             uint32_t ibase, uint32_t ntri, int leaf_max, BvhNode* nodes, int node_base, BvhTri* tris,
                             int tri_base, float4* box_lo, float4* box_hi, uint32_t* sorted_ids, void* scratch,
-                            uint32_t* err, cudaStream_t st);
+                            uint32_t* err, uint32_t* depth, cudaStream_t st);
 
 }  // namespace ddgi

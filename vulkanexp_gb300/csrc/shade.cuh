@@ -171,4 +171,64 @@ __device__ __forceinline__ float3 pbr_metallic_roughness(float3 n, float3 v, flo
     return lightColor * (diffuseContrib + specContrib) * NdotL;
 }
 
+// Front-face hit shading of src/shaders/closesthit.glsl:143-286 (NO_REFLECTION,
+// no textures), split around the shadow query: `base` is emissive + specular
+// bounce + diffuse bounce, `sun` the unshadowed sun term and `fade` the
+// night fade (1 when the sun is above the horizon).  The shaded colour is
+// base if the shadow ray hits, else (base + sun) * fade, which is the
+// reference's `color += pbr; if (dir.y < 0) color *= fade`.
+struct SurfaceShade {
+    float3 base, sun, position;
+    float fade;
+};
+
+template <class AV>
+__device__ __forceinline__ bool shade_surface(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L,
+                                              const uint32_t* states, const AV& at, float3 origin, float3 dir,
+                                              float t, float b1, float b2, uint32_t inst, uint32_t prim,
+                                              SurfaceShade* out, uint32_t* err) {
+    // hit position: product then sum, each rounded (shared with the shadow ray)
+    out->position = f3(__fadd_rn(__fmul_rn(dir.x, t), origin.x), __fadd_rn(__fmul_rn(dir.y, t), origin.y),
+                       __fadd_rn(__fmul_rn(dir.z, t), origin.z));
+    float3 position = out->position;
+    const GpuInstance* gi = sc.instances_by_id + inst;
+    uint32_t custom = __ldg(&gi->custom);
+    ddgi_offset_entry oe = sc.offsets[custom];
+    uint32_t io = oe.index_offset + 3u * prim;
+    uint32_t i0 = __ldg(sc.indices + io), i1 = __ldg(sc.indices + io + 1), i2 = __ldg(sc.indices + io + 2);
+    uint32_t vb = oe.vertex_offset;
+    if (vb + max(i0, max(i1, i2)) >= sc.vertex_count || oe.material_index >= sc.material_count) {
+        raise_error(err, DEV_BAD_INDEX);
+        out->base = out->sun = f3(0, 0, 0);
+        out->fade = 1.0f;
+        return false;
+    }
+    float4 n0 = __ldg(sc.normals + vb + i0), n1 = __ldg(sc.normals + vb + i1), n2 = __ldg(sc.normals + vb + i2);
+    float b0 = 1.0f - b1 - b2;
+    float3 tsn = norm3(f3(n0.x * b0 + n1.x * b1 + n2.x * b2, n0.y * b0 + n1.y * b1 + n2.y * b2,
+                          n0.z * b0 + n1.z * b1 + n2.z * b2));
+    float4 w0 = __ldg(&gi->w2o[0]), w1 = __ldg(&gi->w2o[1]), w2 = __ldg(&gi->w2o[2]);
+    // normal * gl_WorldToObjectEXT: transpose of the world-to-object 3x3
+    float3 normal = norm3(f3(tsn.x * w0.x + tsn.y * w1.x + tsn.z * w2.x, tsn.x * w0.y + tsn.y * w1.y + tsn.z * w2.y,
+                             tsn.x * w0.z + tsn.y * w1.z + tsn.z * w2.z));
+    const ddgi_material& m = sc.materials[oe.material_index];
+    float3 albedo = f3(m.base_color[0], m.base_color[1], m.base_color[2]);
+    float metal = m.metallic, rough = m.roughness;
+    float3 color = f3(m.emissive[0], m.emissive[1], m.emissive[2]);
+    float3 diffuseColor = albedo * (1.0f - 0.04f) * (1.0f - metal);
+    float3 specularColor = mix3(f3(0.04f, 0.04f, 0.04f), albedo, metal);
+    float3 reflectDir = dir - normal * (2.0f * dot3(normal, dir));
+    float3 reflection = sample_probes(position, reflectDir, -dir, g, states, at);
+    color = color + specularColor * reflection;
+    float3 indirect = sample_probes(position, normal, -dir, g, states, at);
+    color = color + indirect * diffuseColor;
+    out->base = color;
+    out->sun = pbr_metallic_roughness(normal, norm3(-dir), f3(L.color[0], L.color[1], L.color[2]),
+                                      f3(L.dir[0], L.dir[1], L.dir[2]), albedo, metal, rough);
+    out->fade = L.dir[1] < 0.0f ? 1.0f - clampf(-L.dir[1], 0.0f, 0.1f) / 0.1f : 1.0f;
+    return true;
+}
+
+__device__ __forceinline__ float3 lit_color(const SurfaceShade& s) { return (s.base + s.sun) * s.fade; }
+
 }  // namespace ddgi

@@ -1,0 +1,339 @@
+// traverse.cuh — two-level LBVH traversal (closest hit and any hit).
+//
+// The top-level tree is walked in world space; at an instance leaf an EXIT
+// marker is pushed, the ray moves into object space through the instance's
+// world-to-object transform and the mesh tree is walked; popping the marker
+// restores the world ray.  Hits are accepted for t in [tmin, tmax]; among
+// equal t the lowest (instance, primitive) wins, so the result does not
+// depend on the visiting order.
+#pragma once
+
+#include "common.cuh"
+
+namespace ddgi {
+
+constexpr int kStack = 64;
+constexpr int kExit = 0x7fffffff;
+constexpr int kNone = (int)0x80000000;  // no node (never a valid reference)
+constexpr uint32_t kNoHit = 0xFFFFFFFFu;
+// Box tests use [tmin * kBoxLo, tcur * kBoxHi]: a relative margin far above
+// the few-ulp error of slab and triangle distances, so that pruning never
+// removes a box holding a hit the triangle test reports, at any ray length.
+constexpr float kBoxLo = 0.99999f;
+constexpr float kBoxHi = 1.00001f;
+
+struct HitRec {
+    float t, b1, b2;
+    uint32_t inst, prim;
+    bool back;
+};
+
+// Fetch counters of the measurement variant (COUNT = true): inner nodes
+// visited, triangles tested, instances entered, rays traced (index 0 for
+// closest-hit rays, 1 for any-hit rays), and shading bytes.
+struct Fetches {
+    uint32_t nodes[2] = {0, 0}, tris[2] = {0, 0}, insts[2] = {0, 0}, rays[2] = {0, 0}, shade_bytes = 0;
+};
+
+// Closest hit (ANY = false) or any hit (ANY = true) with t in [tmin, tmax];
+// ties on t go to the lowest (instance, primitive).
+template <bool ANY, bool COUNT = false>
+__device__ __forceinline__ bool traverse(const DeviceScene& sc, float3 wo, float3 wd, float tmin, float tmax,
+                                         uint32_t mask, HitRec* best, uint32_t* err, Fetches* fc = nullptr) {
+    if (COUNT) fc->rays[ANY]++;
+    best->inst = kNoHit;
+    best->prim = 0;
+    best->t = tmax;
+    best->b1 = best->b2 = 0.0f;
+    best->back = false;
+    if (sc.tlas_root < 0) return false;
+    Ray r;
+    ray_setup(r, wo, wd);
+    int stack[kStack];
+    int sp = 0;
+    int ref = sc.tlas_root;
+    bool in_blas = false;
+    uint32_t inst_id = 0;
+    float tcur = tmax;
+    // A well-formed tree visits each node at most once per ray; the cap only
+    // stops a malformed one from looping.
+    for (uint32_t steps = 0;; ++steps) {
+        if (steps > 4u * (sc.node_count + sc.tri_count + sc.instance_count) + 64u) {
+            raise_error(err, DEV_BAD_INDEX);
+            return best->inst != kNoHit;
+        }
+        if (ref >= 0) {
+            if (COUNT) fc->nodes[ANY]++;
+            if ((uint32_t)ref >= sc.node_count) {
+                raise_error(err, DEV_BAD_INDEX);
+                return best->inst != kNoHit;
+            }
+            BvhNode n = load_node(sc.nodes, ref);
+            bool h0, h1;
+            float t0, t1;
+            node_hit(r, n, tmin * kBoxLo, tcur * kBoxHi, &h0, &h1, &t0, &t1);
+            if (h0 && h1) {
+                int nearr = n.d.x, farr = n.d.y;
+                if (t1 < t0) {
+                    nearr = n.d.y;
+                    farr = n.d.x;
+                }
+                if (sp >= kStack) {
+                    raise_error(err, DEV_STACK_OVERFLOW);
+                    return best->inst != kNoHit;
+                }
+                stack[sp++] = farr;
+                ref = nearr;
+                continue;
+            }
+            if (h0) {
+                ref = n.d.x;
+                continue;
+            }
+            if (h1) {
+                ref = n.d.y;
+                continue;
+            }
+        } else if (!in_blas) {
+            // top-level leaf: one instance
+            if ((uint32_t)((~ref) >> 3) >= sc.instance_count) {
+                raise_error(err, DEV_BAD_INDEX);
+                return best->inst != kNoHit;
+            }
+            const GpuInstance* gi = sc.instances + ((~ref) >> 3);
+            int4 meta = __ldg(reinterpret_cast<const int4*>(gi) + 3);  // blas_root, custom, mask, id
+            if (((uint32_t)meta.z & mask) != 0 && meta.x >= 0) {
+                if (COUNT) fc->insts[ANY]++;
+                if (sp >= kStack) {
+                    raise_error(err, DEV_STACK_OVERFLOW);
+                    return best->inst != kNoHit;
+                }
+                stack[sp++] = kExit;
+                float4 w[3] = {__ldg(&gi->w2o[0]), __ldg(&gi->w2o[1]), __ldg(&gi->w2o[2])};
+                float3 oo, od;
+                xform_exact(w, wo, wd, &oo, &od);
+                ray_setup(r, oo, od);
+                inst_id = (uint32_t)meta.w;
+                in_blas = true;
+                ref = meta.x;
+                continue;
+            }
+        } else {
+            int first = (~ref) >> 3, count = ((~ref) & 7) + 1;
+            if ((uint32_t)first + (uint32_t)count > sc.tri_count) {
+                raise_error(err, DEV_BAD_INDEX);
+                return best->inst != kNoHit;
+            }
+            if (COUNT) fc->tris[ANY] += count;
+            for (int k = 0; k < count; ++k) {
+                const float4* tp = reinterpret_cast<const float4*>(sc.tris + first + k);
+                float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                float t, b1, b2;
+                bool back;
+                if (tri_hit_exact(r, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), f3(c.x, c.y, c.z), tmin, tcur, &t, &b1, &b2,
+                                  &back)) {
+                    uint32_t prim = (uint32_t)__float_as_int(a.w);
+                    bool better = ANY || best->inst == kNoHit || t < best->t ||
+                                  (t == best->t && (inst_id < best->inst || (inst_id == best->inst && prim < best->prim)));
+                    if (better) {
+                        best->t = t;
+                        best->inst = inst_id;
+                        best->prim = prim;
+                        best->b1 = b1;
+                        best->b2 = b2;
+                        best->back = back;
+                        tcur = t;
+                        if (ANY) return true;
+                    }
+                }
+            }
+        }
+        // pop
+        for (;;) {
+            if (sp == 0) return best->inst != kNoHit;
+            ref = stack[--sp];
+            if (ref != kExit) break;
+            in_blas = false;
+            ray_setup(r, wo, wd);
+        }
+    }
+}
+
+
+// Warp-cooperative traversal for persistent kernels (Aila & Laine 2009,
+// "while-while" with postponed leaves): every lane of the warp calls
+// advance() together.  In phase 1 lanes walk inner nodes; a lane that meets a
+// leaf keeps it and goes on walking until every lane holds a leaf (or has
+// run out of nodes), so inner-node iterations stay busy.  Phase 2 processes
+// the held leaves: an instance leaf moves the ray into the mesh tree, a
+// triangle leaf runs the watertight tests.  The stack lives in shared memory
+// (one column per thread).  Hit set, tie rule and results equal `traverse`.
+struct SmemStack {
+    int* base;
+    int stride;
+    __device__ __forceinline__ int& at(int i) const { return base[i * stride]; }
+};
+
+template <bool ANY>
+struct WarpWalker {
+    Ray wr, r;  // world ray, current ray (world or object space)
+    SmemStack stk;
+    int sp, cap, ref;
+    bool in_blas;
+    uint32_t inst_id, steps, max_steps, mask;
+    float tmin, tcur;
+    HitRec best;
+
+    __device__ __forceinline__ bool start(const DeviceScene& sc, float3 o, float3 d, float tmin_, float tmax_,
+                                          uint32_t mask_) {
+        ray_setup(wr, o, d);
+        r = wr;
+        tmin = tmin_;
+        tcur = tmax_;
+        mask = mask_;
+        best.inst = kNoHit;
+        best.prim = 0;
+        best.t = tmax_;
+        best.b1 = best.b2 = 0.0f;
+        best.back = false;
+        sp = 0;
+        in_blas = false;
+        inst_id = 0;
+        steps = 0;
+        max_steps = 4u * (sc.node_count + sc.tri_count + sc.instance_count) + 64u;
+        ref = sc.tlas_root >= 0 ? sc.tlas_root : kNone;
+        return ref != kNone;
+    }
+
+    __device__ __forceinline__ bool push(int v, uint32_t* err) {
+        if (sp >= cap) {
+            raise_error(err, DEV_STACK_OVERFLOW);
+            return false;
+        }
+        stk.at(sp++) = v;
+        return true;
+    }
+    // pop within the current tree level (stops at an EXIT marker)
+    __device__ __forceinline__ void pop_level() {
+        if (sp == 0 || stk.at(sp - 1) == kExit) {
+            ref = kNone;
+            return;
+        }
+        ref = stk.at(--sp);
+    }
+    // pop across EXIT markers (restoring the world ray); false when empty
+    __device__ __forceinline__ bool pop() {
+        for (;;) {
+            if (sp == 0) return false;
+            ref = stk.at(--sp);
+            if (ref != kExit) return true;
+            in_blas = false;
+            r = wr;
+        }
+    }
+
+    // All lanes call this; returns true when an active lane's ray is finished.
+    __device__ __forceinline__ bool advance(const DeviceScene& sc, uint32_t* err, bool active) {
+        int leaf = kNone;
+        bool searching = active && ref != kNone;
+        bool failed = false;
+        while (__any_sync(0xffffffffu, searching)) {
+            if (searching) {
+                if (ref >= 0) {
+                    if (++steps > max_steps || (uint32_t)ref >= sc.node_count) {
+                        raise_error(err, DEV_BAD_INDEX);
+                        failed = true;
+                        searching = false;
+                    } else {
+                        BvhNode n = load_node(sc.nodes, ref);
+                        bool h0, h1;
+                        float t0, t1;
+                        node_hit(r, n, tmin * kBoxLo, tcur * kBoxHi, &h0, &h1, &t0, &t1);
+                        if (h0 && h1) {
+                            int nearr = n.d.x, farr = n.d.y;
+                            if (t1 < t0) {
+                                nearr = n.d.y;
+                                farr = n.d.x;
+                            }
+                            if (!push(farr, err)) {
+                                failed = true;
+                                searching = false;
+                            }
+                            ref = nearr;
+                        } else if (h0) {
+                            ref = n.d.x;
+                        } else if (h1) {
+                            ref = n.d.y;
+                        } else {
+                            pop_level();
+                        }
+                    }
+                } else if (leaf == kNone) {
+                    leaf = ref;  // postpone it and keep walking
+                    pop_level();
+                } else {
+                    searching = false;  // holding a leaf and at a second one
+                }
+                if (ref == kNone) searching = false;
+            }
+            if (__all_sync(0xffffffffu, !searching || leaf != kNone)) break;
+        }
+        if (!active) return false;
+        if (failed) return true;
+        if (leaf != kNone) {
+            if (!in_blas) {
+                uint32_t slot = (uint32_t)((~leaf) >> 3);
+                if (slot >= sc.instance_count) {
+                    raise_error(err, DEV_BAD_INDEX);
+                    return true;
+                }
+                const GpuInstance* gi = sc.instances + slot;
+                int4 meta = __ldg(reinterpret_cast<const int4*>(gi) + 3);  // blas_root, custom, mask, id
+                if (((uint32_t)meta.z & mask) != 0 && meta.x >= 0) {
+                    if (ref != kNone && !push(ref, err)) return true;
+                    if (!push(kExit, err)) return true;
+                    float4 w[3] = {__ldg(&gi->w2o[0]), __ldg(&gi->w2o[1]), __ldg(&gi->w2o[2])};
+                    float3 oo, od;
+                    xform_exact(w, wr.o, wr.d, &oo, &od);
+                    ray_setup(r, oo, od);
+                    inst_id = (uint32_t)meta.w;
+                    in_blas = true;
+                    ref = meta.x;
+                    return false;
+                }
+            } else {
+                int first = (~leaf) >> 3, count = ((~leaf) & 7) + 1;
+                if ((uint32_t)first + (uint32_t)count > sc.tri_count) {
+                    raise_error(err, DEV_BAD_INDEX);
+                    return true;
+                }
+                for (int k = 0; k < count; ++k) {
+                    const float4* tp = reinterpret_cast<const float4*>(sc.tris + first + k);
+                    float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                    float t, b1, b2;
+                    bool back;
+                    if (tri_hit_exact(r, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), f3(c.x, c.y, c.z), tmin, tcur, &t, &b1,
+                                      &b2, &back)) {
+                        uint32_t prim = (uint32_t)__float_as_int(a.w);
+                        bool better = ANY || best.inst == kNoHit || t < best.t ||
+                                      (t == best.t && (inst_id < best.inst || (inst_id == best.inst && prim < best.prim)));
+                        if (better) {
+                            best.t = t;
+                            best.inst = inst_id;
+                            best.prim = prim;
+                            best.b1 = b1;
+                            best.b2 = b2;
+                            best.back = back;
+                            tcur = t;
+                            if (ANY) return true;
+                        }
+                    }
+                }
+            }
+        }
+        if (ref == kNone && !pop()) return true;
+        return false;
+    }
+};
+
+}  // namespace ddgi

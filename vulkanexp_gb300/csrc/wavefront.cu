@@ -1,0 +1,242 @@
+// wavefront.cu — the probe trace as three kernels instead of one.
+//
+//  1. k_primary: closest hit of every probe ray.  Persistent warps; a lane
+//     whose ray finishes is handed the next ray from a global counter, so the
+//     warp keeps its lanes busy instead of waiting for its longest ray.
+//  2. k_shade: one thread per ray record, coalesced: miss -> sky, backface ->
+//     (0, 0.8 t), front face -> shading split around the shadow query; the
+//     front hits are appended (warp-aggregated) to a shadow-ray queue.
+//  3. k_shadow: any-hit query of the queued rays toward the sun, persistent
+//     like k_primary; an unshadowed ray gets (base + sun) * fade.
+//
+// Results are identical to the single fused kernel (same traversal, same
+// shading arithmetic); only the schedule differs.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "shade.cuh"
+#include "traverse.cuh"
+
+namespace ddgi {
+
+namespace {
+
+constexpr int kPersistThreads = 128;
+constexpr unsigned kFull = 0xffffffffu;
+
+struct PrimaryJob {
+    DeviceGrid g;
+    const uint32_t* probe_list;
+    const float4* dirs;
+    const uint32_t* ray_order;
+    WaveHits hits;
+    uint32_t total;
+
+    __device__ __forceinline__ bool start(WarpWalker<false>& w, const DeviceScene& sc, uint32_t id,
+                                          uint32_t* out) const {
+        uint32_t R = g.rays;
+        uint32_t slot = id / R, j = id - slot * R;
+        uint32_t ray = __ldg(ray_order + j);
+        uint32_t probe = probe_list ? __ldg(probe_list + slot) : slot;
+        *out = slot * R + ray;
+        float4 d4 = __ldg(dirs + ray);
+        return w.start(sc, probe_origin_exact(g, probe), f3(d4.x, d4.y, d4.z), 0.01f, g.tmax, 0x3u);
+    }
+    __device__ __forceinline__ void finish(const WarpWalker<false>& w, uint32_t out) const {
+        const HitRec& h = w.best;
+        hits.thit[out] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.inst));
+        hits.prim[out] = h.prim | (h.back ? 0x80000000u : 0u);
+    }
+};
+
+struct ShadowJob {
+    const ShadowQueue q;
+    float3 dir;
+    float4* rays;
+    uint32_t total;
+
+    __device__ __forceinline__ bool start(WarpWalker<true>& w, const DeviceScene& sc, uint32_t id,
+                                          uint32_t* out) const {
+        *out = id;
+        float4 p = q.pos[id];
+        return w.start(sc, f3(p.x, p.y, p.z), dir, 0.1f, 10000.0f, 0xFFu);
+    }
+    __device__ __forceinline__ void finish(const WarpWalker<true>& w, uint32_t id) const {
+        if (w.best.inst != kNoHit) return;  // shadowed: the record keeps the base colour
+        uint32_t idx = q.idx[id];
+        float4 sun = q.sun[id];
+        float4 rec = rays[idx];
+        float3 c = (f3(rec.x, rec.y, rec.z) + f3(sun.x, sun.y, sun.z)) * sun.w;
+        rays[idx] = make_float4(c.x, c.y, c.z, rec.w);
+    }
+};
+
+// Persistent traversal loop with per-lane refill.  A warp refills when at
+// least `kRefill` of its lanes are idle (or all are), taking as many rays as
+// it has idle lanes with one atomic.
+template <bool ANY, class Job>
+__device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job& job, uint32_t total,
+                                                uint32_t* counter, int stack_cap, uint32_t* err) {
+    constexpr int kRefill = 8;
+    extern __shared__ int s_stack[];
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    WarpWalker<ANY> w;
+    w.stk.base = s_stack + threadIdx.x;
+    w.stk.stride = blockDim.x;
+    w.cap = stack_cap;
+    w.ref = kNone;
+    bool active = false, exhausted = false;
+    uint32_t out = 0;
+    for (;;) {
+        unsigned idle = __ballot_sync(kFull, !active && !exhausted);
+        unsigned busy = __ballot_sync(kFull, active);
+        if (idle && (__popc(idle) >= kRefill || busy == 0)) {
+            int leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(idle));
+            base = __shfl_sync(kFull, base, leader);
+            if (!active && !exhausted) {
+                uint32_t id = base + (uint32_t)__popc(idle & lt);
+                if (id < total) {
+                    if (job.start(w, sc, id, &out)) active = true;
+                    else job.finish(w, out);  // empty scene: immediate miss
+                } else {
+                    exhausted = true;
+                }
+            }
+            busy = __ballot_sync(kFull, active);
+        }
+        if (busy == 0) {
+            if (__all_sync(kFull, exhausted)) break;
+            continue;
+        }
+        bool fin = w.advance(sc, err, active);  // every lane takes part (warp votes)
+        if (active && fin) {
+            job.finish(w, out);
+            active = false;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kPersistThreads) k_primary(DeviceScene sc, PrimaryJob job, uint32_t* counter,
+                                                             int stack_cap, uint32_t* err) {
+    persistent_walk<false>(sc, job, job.total, counter, stack_cap, err);
+}
+
+__global__ void __launch_bounds__(kPersistThreads) k_shadow(DeviceScene sc, ShadowJob job, const uint32_t* qcount,
+                                                            uint32_t* counter, int stack_cap, uint32_t* err) {
+    persistent_walk<true>(sc, job, *qcount, counter, stack_cap, err);
+}
+
+template <class AV>
+__global__ void __launch_bounds__(128) k_shade(DeviceScene sc, DeviceGrid g, DeviceLight L,
+                                               const uint32_t* __restrict__ probe_list, uint32_t total,
+                                               const float4* __restrict__ dirs, const uint32_t* __restrict__ states,
+                                               AV at, WaveHits hits, float4* rays_out, ddgi_hit* hits_out,
+                                               ShadowQueue q, uint32_t* err) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool enqueue = false;
+    SurfaceShade s;
+    if (i < total) {
+        uint32_t R = g.rays;
+        uint32_t slot = i / R, ray = i - slot * R;
+        float4 th = hits.thit[i];
+        uint32_t pb = hits.prim[i];
+        uint32_t inst = __float_as_uint(th.w), prim = pb & 0x7fffffffu;
+        bool back = (pb >> 31) != 0;
+        float4 rec;
+        if (inst == kNoHit) {
+            rec = make_float4(L.sky[0], L.sky[1], L.sky[2], -1.0f);  // miss.rmiss:17-23
+        } else if (back) {
+            rec = make_float4(0.0f, 0.0f, 0.0f, th.x * 0.80f);  // closesthit.glsl:137-141
+        } else {
+            uint32_t probe = probe_list ? __ldg(probe_list + slot) : slot;
+            float4 d4 = __ldg(dirs + ray);
+            float3 d = f3(d4.x, d4.y, d4.z);
+            if (shade_surface(sc, g, L, states, at, probe_origin_exact(g, probe), d, th.x, th.y, th.z, inst, prim, &s,
+                              err))
+                enqueue = true;
+            rec = make_float4(s.base.x, s.base.y, s.base.z, th.x);
+        }
+        rays_out[i] = rec;
+        if (hits_out) {
+            ddgi_hit hr;
+            hr.instance = inst;
+            hr.primitive = inst == kNoHit ? 0u : prim;
+            hr.t = inst == kNoHit ? 0.0f : th.x;
+            hr.backface = (inst != kNoHit && back) ? 1u : 0u;
+            hits_out[i] = hr;
+        }
+    }
+    unsigned m = __ballot_sync(kFull, enqueue);
+    if (m) {
+        int leader = __ffs(m) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(q.count, (uint32_t)__popc(m));
+        base = __shfl_sync(kFull, base, leader);
+        if (enqueue) {
+            uint32_t k = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+            q.idx[k] = i;
+            q.pos[k] = make_float4(s.position.x, s.position.y, s.position.z, 0.0f);
+            q.sun[k] = make_float4(s.sun.x, s.sun.y, s.sun.z, s.fade);
+        }
+    }
+}
+
+uint32_t persistent_blocks(const void* kernel, size_t smem) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kPersistThreads, smem);
+    if (per <= 0) per = 1;
+    return (uint32_t)(sms * per);
+}
+
+}  // namespace
+
+cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L,
+                             const uint32_t* probe_list, uint32_t nprobes, const float4* dirs,
+                             const uint32_t* ray_order, const uint32_t* states, const void* color, const void* depth,
+                             bool fp16_atlas, WaveHits hits, ShadowQueue q, uint32_t* counters, float4* rays_out,
+                             ddgi_hit* hits_out, int stack_cap, uint32_t* err, cudaStream_t st,
+                             cudaEvent_t after_primary) {
+    uint32_t total = nprobes * g.rays;
+    if (total == 0) return cudaSuccess;
+    // counters[0]: primary work, counters[1]: shadow queue length, counters[2]: shadow work
+    cudaError_t e = cudaMemsetAsync(counters, 0, 3 * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    const size_t smem = (size_t)stack_cap * kPersistThreads * sizeof(int);
+    PrimaryJob pj{g, probe_list, dirs, ray_order, hits, total};
+    k_primary<<<persistent_blocks((const void*)k_primary, smem), kPersistThreads, smem, st>>>(sc, pj, counters,
+                                                                                             stack_cap, err);
+    if (after_primary) cudaEventRecord(after_primary, st);
+    ShadowQueue qq = q;
+    qq.count = counters + 1;
+    uint32_t blocks = (total + 127) / 128;
+    if (fp16_atlas) {
+        AtlasView<ColorTexF16, DepthTexF16> at{{static_cast<const uint2*>(color)},
+                                               {static_cast<const uint32_t*>(depth)}};
+        k_shade<<<blocks, 128, 0, st>>>(sc, g, L, probe_list, total, dirs, states, at, hits, rays_out, hits_out, qq,
+                                        err);
+    } else {
+        AtlasView<ColorTexF32, DepthTexF32> at{{static_cast<const float4*>(color)},
+                                               {static_cast<const float2*>(depth)}};
+        k_shade<<<blocks, 128, 0, st>>>(sc, g, L, probe_list, total, dirs, states, at, hits, rays_out, hits_out, qq,
+                                        err);
+    }
+    ShadowJob sj{qq, make_float3(L.dir[0], L.dir[1], L.dir[2]), rays_out, 0};
+    k_shadow<<<persistent_blocks((const void*)k_shadow, smem), kPersistThreads, smem, st>>>(
+        sc, sj, counters + 1, counters + 2, stack_cap, err);
+    return cudaGetLastError();
+}
+
+}  // namespace ddgi

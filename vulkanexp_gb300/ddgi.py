@@ -59,6 +59,7 @@ _SIGNATURES = [
     ("ddgi_synchronize", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     ("ddgi_get_timings", C.c_int, [C.c_void_p, C.POINTER(Timings)]),
     ("ddgi_enable_timing", C.c_int, [C.c_void_p, C.c_int]),
+    ("ddgi_set_pipeline", C.c_int, [C.c_void_p, C.c_int]),
 ]
 
 
@@ -164,6 +165,9 @@ class Context:
     def enable_timing(self, on=True):
         self._check(self.lib.ddgi_enable_timing(self.h, int(on)))
 
+    def set_pipeline(self, pipeline):
+        self._check(self.lib.ddgi_set_pipeline(self.h, int(pipeline)))
+
     # ---- update ----------------------------------------------------------
     def update(self, orientation, probe_list=None, stream=None):
         o = np.ascontiguousarray(orientation, np.float32).reshape(9)
@@ -175,10 +179,11 @@ class Context:
         """Fetch counters of one trace + shade pass (see ddgi_count_fetches)."""
         o = np.ascontiguousarray(orientation, np.float32).reshape(9)
         pl = None if probe_list is None else np.ascontiguousarray(probe_list, np.uint32)
-        out = np.zeros(5, np.uint64)
+        out = np.zeros(9, np.uint64)
         self._check(self.lib.ddgi_count_fetches(self.h, _ptr(o), _ptr(pl), 0 if pl is None else len(pl), _ptr(out),
                                                 _stream_ptr(stream)))
-        keys = ("nodes", "tris", "instances", "rays", "shade_bytes")
+        keys = ("nodes", "tris", "instances", "rays", "shade_bytes", "shadow_nodes", "shadow_tris",
+                "shadow_instances", "shadow_rays")
         return {k: int(v) for k, v in zip(keys, out)}
 
     def synchronize(self, stream=None, timeout_ms=-1):
