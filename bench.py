@@ -162,6 +162,48 @@ def config_dict(w, args):
             "seed": w.seed}
 
 
+def build_context(w, precision, pipeline, stream):
+    from vulkanexp_gb300 import abi
+    from vulkanexp_gb300.ddgi import Context
+
+    g = w.grid.copy()
+    g.precision = precision
+    ctx = Context(g)
+    ctx.set_pipeline(pipeline)
+    t0 = time.perf_counter()
+    ctx.build_scene(w.scene, stream)
+    build_s = time.perf_counter() - t0
+    ctx.set_light(w.light)
+    return ctx, build_s
+
+
+def time_updates(ctx, w, steps, warmup, stream, flush, first=0):
+    """Device time of `steps` updates (CUDA events on the launching stream,
+    L2 flushed before each), after `warmup` untimed updates."""
+    import torch
+
+    for k in range(warmup):
+        ctx.update(w.orientation(first + k), stream=stream)
+    ctx.synchronize(stream)
+    ctx.enable_timing(True)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    stages = {"trace_shade": [], "primary_traversal": [], "blend_border": []}
+    for k in range(steps):
+        flush.fill_(k & 255)
+        ev[k][0].record(stream)
+        ctx.update(w.orientation(first + warmup + k), stream=stream)
+        ev[k][1].record(stream)
+        t = ctx.timings()  # waits for this update's last event
+        stages["trace_shade"].append(t["trace_ms"])
+        stages["primary_traversal"].append(t["primary_ms"])
+        stages["blend_border"].append(t["blend_ms"])
+    torch.cuda.synchronize()
+    ctx.enable_timing(False)
+    ms = [a.elapsed_time(b) for a, b in ev]
+    return float(np.mean(ms)), {k: float(np.mean(v)) for k, v in stages.items()}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -169,11 +211,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=1)
-    ap.add_argument("--pipeline", default="wavefront", choices=["wavefront", "fused"])
     ap.add_argument("--cpu-probes", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
-                    help="profiling target: scene build, then two updates (the second is the one to capture), no timing")
+                    help="profiling target: scene build, then two BF16 wavefront updates and two FP32 ones, no timing")
     args = ap.parse_args()
 
     rank, world, local = dist_env()
@@ -187,7 +228,6 @@ def main():
     import torch
 
     from vulkanexp_gb300 import abi, build
-    from vulkanexp_gb300.ddgi import Context
 
     build.build()
     torch.cuda.set_device(local)
@@ -196,64 +236,50 @@ def main():
 
         dist.init_process_group("nccl")
     stream = torch.cuda.current_stream()
-    ctx = Context(w.grid)
-    ctx.set_pipeline(abi.PIPELINE_WAVEFRONT if args.pipeline == "wavefront" else abi.PIPELINE_FUSED)
-    t0 = time.perf_counter()
-    ctx.build_scene(w.scene, stream)
-    build_s = time.perf_counter() - t0
-    ctx.set_light(w.light)
-    if args.profile:
-        for k in range(2):
-            ctx.update(w.orientation(k), stream=stream)
-        ctx.synchronize(stream)
-        ctx.close()
-        print(json.dumps({"profile_target": w.name, "updates": 2}), flush=True)
-        return
-    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     P, R = w.grid.probe_count(), w.grid.rays_per_probe
 
-    # measurement pass (untimed): algorithmic fetch bytes of one trace launch
-    fetches = ctx.count_fetches(w.orientation(0), stream=stream)
+    if args.profile:
+        for prec in (abi.PRECISION_BF16, abi.PRECISION_FP32):
+            ctx, _ = build_context(w, prec, abi.PIPELINE_WAVEFRONT, stream)
+            for k in range(2):
+                ctx.update(w.orientation(k), stream=stream)
+            ctx.synchronize(stream)
+            ctx.close()
+        print(json.dumps({"profile_target": w.name, "updates": 4}), flush=True)
+        return
 
-    for k in range(args.warmup):
-        ctx.update(w.orientation(k), stream=stream)
-    ctx.synchronize(stream)
-    ctx.enable_timing(True)
-
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    forms = {}
     sampler = ClockSampler(local)
     sampler.start()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    trace_ms, blend_ms, primary_ms = [], [], []
-    wall0 = time.perf_counter()
-    for k in range(args.steps):
-        flush.fill_(k & 255)
-        ev[k][0].record(stream)
-        ctx.update(w.orientation(args.warmup + k), stream=stream)
-        ev[k][1].record(stream)
-        t = ctx.timings()  # synchronises on the update's last event
-        trace_ms.append(t["trace_ms"])
-        blend_ms.append(t["blend_ms"])
-        primary_ms.append(t["primary_ms"])
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - wall0
-    step_ms = [a.elapsed_time(b) for a, b in ev]
+    # the reference-like plain FP32 form, the FP32 wavefront form, and the
+    # headline: wavefront trace + BF16 tensor-core blend with an FP16 atlas
+    for name, prec, pipe in (("plain_fp32", abi.PRECISION_FP32, abi.PIPELINE_FUSED),
+                             ("wavefront_fp32", abi.PRECISION_FP32, abi.PIPELINE_WAVEFRONT),
+                             ("wavefront_bf16", abi.PRECISION_BF16, abi.PIPELINE_WAVEFRONT)):
+        ctx, build_s = build_context(w, prec, pipe, stream)
+        if world > 1:
+            torch.distributed.barrier()
+        ms, stages = time_updates(ctx, w, args.steps, args.warmup, stream, flush)
+        forms[name] = {"ms_per_update": ms, "value": P * R / (ms * 1e-3) / 1e9, "stage_ms": stages,
+                       "scene_build_s": build_s}
+        if name != "wavefront_bf16":
+            ctx.close()
     clocks = sampler.stop()
-    ms = float(np.mean(step_ms))
+    head = forms["wavefront_bf16"]
+    ms = head["ms_per_update"]
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = world * P * R / (ms * 1e-3) / 1e9
 
-    # e2e through the host-buffer API: inputs up, both atlases down (pinned)
+    # e2e through the host-buffer API: the step's ray table up, both atlases
+    # down into pinned host memory (FP32 values converted from the FP16 atlas)
     ch, cw, cc = ctx.atlas_shape(abi.ATLAS_COLOR)
     dh, dw, dc = ctx.atlas_shape(abi.ATLAS_DEPTH)
     host_c = torch.empty((ch, cw, cc), dtype=torch.float32, pin_memory=True).numpy()
     host_d = torch.empty((dh, dw, dc), dtype=torch.float32, pin_memory=True).numpy()
-    ctx.enable_timing(False)
     e2e_ms = []
     for k in range(max(args.steps, 1)):
         flush.fill_(k & 255)
@@ -265,29 +291,43 @@ def main():
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_val = world * P * R / (np.mean(e2e_ms) * 1e-3) / 1e9
 
-    hbm, _, peak_kind = load_peaks()
-    trace_avg = float(np.mean(trace_ms))
-    alg_bytes = fetches["nodes"] * 64 + fetches["tris"] * 48 + fetches["instances"] * 64 + fetches["shade_bytes"]
-    achieved = alg_bytes / (trace_avg * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "k_trace_shade", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+    # rooflines: the dominant kernel (primary traversal, L1/L2-resident node
+    # fetches counted per launch) and the tensor-core blend
+    fetches = ctx.count_fetches(w.orientation(0), stream=stream)
+    hbm, bf16_peak, peak_kind = load_peaks()
+    prim_ms = head["stage_ms"]["primary_traversal"]
+    alg_bytes = fetches["nodes"] * 64 + fetches["tris"] * 48 + fetches["instances"] * 64
+    achieved = alg_bytes / (prim_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_primary", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_source": peak_kind, "traffic": None,
-                "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": trace_avg,
+                "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": prim_ms,
+                "note": "fetch-counted node/triangle/instance bytes of the primary rays; they are served mostly by "
+                        "L1/L2, so frac > 1 is cache reuse, not DRAM traffic",
                 "fetches_per_launch": fetches}
-
+    nc, nd = w.grid.color_res - 2, w.grid.depth_res - 2
+    blend_flop = 2.0 * P * R * (nc * nc * 3 + nd * nd * 2)
+    blend_ms = head["stage_ms"]["blend_border"]
+    blend_bytes = P * R * 16 + 2 * (w.grid.atlas_shape(0)[0] * w.grid.atlas_shape(0)[1] * 8 +
+                                     w.grid.atlas_shape(1)[0] * w.grid.atlas_shape(1)[1] * 4)
+    roofline_blend = {"kernel": "k_blend_tc (+ k_tc_weights)", "bound": "hbm", "kernel_ms": blend_ms,
+                      "algorithmic_bytes": blend_bytes, "achieved_gbs": blend_bytes / (blend_ms * 1e-3) / 1e9,
+                      "frac_hbm": blend_bytes / (blend_ms * 1e-3) / 1e9 / hbm,
+                      "useful_tflops": blend_flop / (blend_ms * 1e-3) / 1e12, "peak_bf16_tflops": bf16_peak}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config_dict(w, args),
-            "impl": "ours", "pipeline": args.pipeline,
-            "stage_ms": {"trace_shade": trace_avg, "primary_traversal": float(np.mean(primary_ms)),
-                         "blend_border": float(np.mean(blend_ms))},
-            "gpu_launches": (4 if args.pipeline == "wavefront" else 2) * args.steps, "clocks": clocks,
-            "roofline": roofline,
+            "vs_baseline": None, "dtype": "f32 trace / bf16 blend", "data": "synthetic (seeded)",
+            "config": config_dict(w, args), "impl": "ours",
+            "form": "wavefront trace (persistent traversal) + BF16 tcgen05 blend, FP16 atlas",
+            "forms": forms,
+            "speedup_vs_plain_fp32": forms["plain_fp32"]["ms_per_update"] / head["ms_per_update"],
+            # per update: k_primary, k_shade, k_shadow, k_tc_weights, k_blend_tc
+            "gpu_launches": 5 * args.steps, "clocks": clocks, "roofline": roofline,
+            "roofline_blend": roofline_blend,
             "e2e": {"value": e2e_val, "unit": UNIT, "ms_per_step": float(np.mean(e2e_ms)),
-                    "h2d_bytes_per_step": R * 20, "d2h_bytes_per_step": int(host_c.nbytes + host_d.nbytes)},
-            "scene_build_s": build_s, "wall_s_timed": wall}
+                    "h2d_bytes_per_step": R * 20, "d2h_bytes_per_step": int(host_c.nbytes + host_d.nbytes)}}
+    ctx.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_probes)
-    ctx.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -212,6 +212,14 @@ ddgi_status ddgi_set_light(ddgi_ctx* ctx, const ddgi_light* light);
 ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
                         uint32_t probe_count, ddgi_stream stream);
 
+/* The blend + border-copy stage of an update alone (probesUpdate.glsl and
+ * probesCopyBorders.comp), fed with caller-provided ray records
+ * (r, g, b, depth) per (probe slot, ray) instead of traced ones; uses the
+ * context's precision.  `count` = listed probes * rays_per_probe.  No scene
+ * is needed.  Synchronous on `stream`. */
+ddgi_status ddgi_blend_records(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
+                               uint32_t probe_count, const float* records, size_t count, ddgi_stream stream);
+
 /* Copies an atlas to host memory as FP32 (RGBA for colour, RG for depth),
  * row-major, width = res*resolution.x*resolution.y, height = res*resolution.z.
  * `bytes` must equal width*height*channels*4.  Synchronous on `stream`. */

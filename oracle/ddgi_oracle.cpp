@@ -1010,6 +1010,46 @@ int oracle_update(const oracle_scene* s, const ddgi_grid_desc* g, const ddgi_lig
 // Blend + border only, from given ray records (R x 4 per listed probe) — for
 // checking the blend kernel in isolation.
 int oracle_blend(const ddgi_grid_desc* gd, const float orientation[9], const uint32_t* list, uint32_t nlist,
+                 const float* rays, uint32_t* states, float* color, float* depth, int nthreads);
+
+// FP64 form of oracle_blend (float ray records, double atlases).
+int oracle_blend64(const ddgi_grid_desc* gd, const float orientation[9], const uint32_t* list, uint32_t nlist,
+                   const float* rays, uint32_t* states, double* color, double* depth, int nthreads) {
+    Grid g = make_grid(gd);
+    std::vector<float> dirs(4 * (size_t)g.rays);
+    ddgi_ray_direction_table(orientation, g.rays, dirs.data());
+    Atlas<double> at;
+    at.color = color;
+    at.depth = depth;
+    at.cw = g.colorRes * g.res[0] * g.res[1];
+    at.ch = g.colorRes * g.res[2];
+    at.dw = g.depthRes * g.res[0] * g.res[1];
+    at.dh = g.depthRes * g.res[2];
+    std::vector<uint32_t> probes;
+    if (list) probes.assign(list, list + nlist);
+    else {
+        probes.resize(g.count());
+        for (uint32_t i = 0; i < g.count(); ++i) probes[i] = i;
+    }
+    std::vector<uint32_t> ns(states, states + g.count());
+    parallel_for(probes.size(), nthreads, [&](size_t b, size_t e) {
+        std::vector<double> rd(4 * (size_t)g.rays);
+        for (size_t s2 = b; s2 < e; ++s2) {
+            uint32_t p = probes[s2];
+            for (size_t i = 0; i < rd.size(); ++i) rd[i] = rays[s2 * g.rays * 4 + i];
+            blend_probe<double>(g, p, rd.data(), dirs.data(), at, ns.data(), true);
+            int idx[3];
+            grid_index(p, g, idx);
+            int tile = idx[1] * g.res[0] + idx[0];
+            copy_borders<double>(at.color, at.cw, 4, (int)g.colorRes * tile, (int)g.colorRes * idx[2], (int)g.colorRes);
+            copy_borders<double>(at.depth, at.dw, 2, (int)g.depthRes * tile, (int)g.depthRes * idx[2], (int)g.depthRes);
+        }
+    });
+    std::memcpy(states, ns.data(), sizeof(uint32_t) * g.count());
+    return 0;
+}
+
+int oracle_blend(const ddgi_grid_desc* gd, const float orientation[9], const uint32_t* list, uint32_t nlist,
                  const float* rays, uint32_t* states, float* color, float* depth, int nthreads) {
     Grid g = make_grid(gd);
     std::vector<float> dirs(4 * (size_t)g.rays);

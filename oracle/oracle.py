@@ -77,6 +77,7 @@ class Oracle:
                                           C.c_void_p, C.c_int]
             lib.oracle_blend.argtypes = [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+            lib.oracle_blend64.argtypes = lib.oracle_blend.argtypes
             lib.oracle_border_table.restype = C.c_uint32
             lib.oracle_border_table.argtypes = [C.c_int, C.c_void_p]
             lib.oracle_oct_decode.argtypes = [C.c_float, C.c_float, C.c_void_p]
@@ -139,11 +140,14 @@ class Oracle:
     # -- scene-independent entry points ---------------------------------------
     @classmethod
     def blend(cls, grid, orientation, rays, color, depth, states, probe_list=None, threads=None):
+        """Blend + border copy of given float ray records into `color`/`depth`
+        (float32 atlases, or float64 for the FP64 form)."""
         orient = np.ascontiguousarray(orientation, np.float32).reshape(9)
         plist = None if probe_list is None else np.ascontiguousarray(probe_list, np.uint32)
         rays = np.ascontiguousarray(rays, np.float32)
-        cls.lib().oracle_blend(C.byref(grid), _ptr(orient), _ptr(plist), 0 if plist is None else len(plist),
-                               _ptr(rays), _ptr(states), _ptr(color), _ptr(depth), int(threads or os.cpu_count()))
+        fn = cls.lib().oracle_blend64 if color.dtype == np.float64 else cls.lib().oracle_blend
+        fn(C.byref(grid), _ptr(orient), _ptr(plist), 0 if plist is None else len(plist), _ptr(rays), _ptr(states),
+           _ptr(color), _ptr(depth), int(threads or os.cpu_count()))
 
     @classmethod
     def border_table(cls, n):

@@ -75,6 +75,12 @@ struct ddgi_ctx {
     float4* q_sun = nullptr;
     uint32_t* counters = nullptr;
     ddgi_pipeline pipeline = DDGI_PIPELINE_WAVEFRONT;
+    // BF16 tensor-core blend: per-update weight matrices and their row sums
+    uint8_t* tc_weights = nullptr;
+    float* tc_rowsum = nullptr;
+    // BF16 form: FP32 hysteresis accumulators behind the FP16 atlas
+    float4* acc_color = nullptr;
+    float2* acc_depth = nullptr;
     ddgi_hit* hits = nullptr;
     size_t hits_cap = 0;
     bool record_hits = false;
@@ -330,6 +336,19 @@ ddgi_status ddgi_create(const ddgi_grid_desc* grid, ddgi_ctx** out) {
         cudaGetLastError();
         return bail(DDGI_ERR_OUT_OF_MEMORY);
     }
+    if (ctx->fp16) {
+        if (!tc_blend_supported(grid->color_res, grid->depth_res)) return bail(DDGI_ERR_UNSUPPORTED);
+        if (cudaMalloc(&ctx->tc_weights, tc_weight_bytes(DDGI_MAX_RAYS_PER_PROBE, grid->color_res, grid->depth_res)) !=
+                cudaSuccess ||
+            cudaMalloc(&ctx->tc_rowsum, 512 * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&ctx->acc_color, atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, false)) != cudaSuccess ||
+            cudaMalloc(&ctx->acc_depth, atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, false)) != cudaSuccess) {
+            cudaGetLastError();
+            return bail(DDGI_ERR_OUT_OF_MEMORY);
+        }
+        cudaMemset(ctx->acc_color, 0, atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, false));
+        cudaMemset(ctx->acc_depth, 0, atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, false));
+    }
     st = ensure_ray_capacity(ctx, (size_t)P * grid->rays_per_probe);
     if (st != DDGI_OK) return bail(st);
     cudaMemset(ctx->color, 0, atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, ctx->fp16));
@@ -358,6 +377,10 @@ ddgi_status ddgi_destroy(ddgi_ctx* ctx) {
     dfree(ctx->q_pos);
     dfree(ctx->q_sun);
     dfree(ctx->counters);
+    dfree(ctx->tc_weights);
+    dfree(ctx->tc_rowsum);
+    dfree(ctx->acc_color);
+    dfree(ctx->acc_depth);
     dfree(ctx->hits);
     dfree(ctx->dirs);
     dfree(ctx->ray_order);
@@ -720,12 +743,44 @@ ddgi_status prepare_update(ddgi_ctx* ctx, const float orientation[9], const uint
     return DDGI_OK;
 }
 
+// Blend + border copy of the ray records in ctx->rays: the FP32 SIMT kernel or
+// the BF16 tensor-core kernel, by the context's precision.
+cudaError_t launch_blend(ddgi_ctx* ctx, const uint32_t* dlist, uint32_t n, cudaStream_t st) {
+    if (ctx->fp16)
+        return launch_blend_tc(ctx->dg, dlist, n, ctx->rays, ctx->dirs, ctx->tc_weights, ctx->tc_rowsum, ctx->states,
+                               ctx->color, ctx->depth, ctx->acc_color, ctx->acc_depth, ctx->err, st);
+    return launch_blend_fp32(ctx->dg, dlist, n, ctx->rays, ctx->dirs, ctx->states, static_cast<float4*>(ctx->color),
+                             static_cast<float2*>(ctx->depth), st);
+}
+
 }  // namespace
+
+ddgi_status ddgi_blend_records(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
+                               uint32_t probe_count, const float* records, size_t count, ddgi_stream stream) {
+    if (!ctx || !orientation || !records) return DDGI_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const uint32_t n = probe_list ? probe_count : probe_count_of(ctx->grid);
+    if (count != (size_t)n * ctx->grid.rays_per_probe)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "expected %zu ray records", (size_t)n * ctx->grid.rays_per_probe);
+    // the blend needs no scene: mark one as present only for the preparation step
+    const bool built = ctx->scene.built;
+    ctx->scene.built = true;
+    const uint32_t* dlist = nullptr;
+    uint32_t n2 = 0;
+    ddgi_status s = prepare_update(ctx, orientation, probe_list, probe_count, st, &dlist, &n2);
+    ctx->scene.built = built;
+    if (s != DDGI_OK) return s;
+    CK(cudaMemcpyAsync(ctx->rays, records, count * sizeof(float4), cudaMemcpyHostToDevice, st), "upload records");
+    CK(launch_blend(ctx, dlist, n, st), "blend launch");
+    CK(cudaStreamSynchronize(st), "blend");
+    ctx->last_count = n;
+    ctx->last_rays = ctx->grid.rays_per_probe;
+    return check_device_error(ctx);
+}
 
 ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list, uint32_t probe_count,
                         ddgi_stream stream) {
     if (!ctx || !orientation) return DDGI_ERR_INVALID_ARGUMENT;
-    if (ctx->fp16) return fail(ctx, DDGI_ERR_UNSUPPORTED, "BF16 blend not available in this build");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const uint32_t* dlist = nullptr;
     uint32_t n = 0;
@@ -748,9 +803,7 @@ ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_
            "wavefront trace launch");
     }
     if (ctx->timing) CK(cudaEventRecord(ctx->ev[1], st), "event");
-    CK(launch_blend_fp32(ctx->dg, dlist, n, ctx->rays, ctx->dirs, ctx->states, static_cast<float4*>(ctx->color),
-                         static_cast<float2*>(ctx->depth), st),
-       "blend launch");
+    CK(launch_blend(ctx, dlist, n, st), "blend launch");
     if (ctx->timing) {
         CK(cudaEventRecord(ctx->ev[2], st), "event");
         ctx->timing_pending = true;
@@ -866,6 +919,9 @@ ddgi_status ddgi_set_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, const float* src
         std::vector<__half> tmp(count);
         for (size_t i = 0; i < count; ++i) tmp[i] = __float2half(src[i]);
         CK(cudaMemcpyAsync(dstp, tmp.data(), count * sizeof(__half), cudaMemcpyHostToDevice, st), "atlas upload");
+        // the FP32 hysteresis accumulator takes the values as given
+        void* acc = kind == DDGI_ATLAS_COLOR ? (void*)ctx->acc_color : (void*)ctx->acc_depth;
+        CK(cudaMemcpyAsync(acc, src, bytes, cudaMemcpyHostToDevice, st), "atlas upload");
         CK(cudaStreamSynchronize(st), "atlas upload");
     }
     return DDGI_OK;

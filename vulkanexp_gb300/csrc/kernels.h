@@ -36,6 +36,13 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
                              ddgi_hit* hits_out, int stack_cap, uint32_t* err, cudaStream_t st,
                              cudaEvent_t after_primary);
 
+// blend_tc.cu
+size_t tc_weight_bytes(uint32_t rays, uint32_t color_res, uint32_t depth_res);
+bool tc_blend_supported(uint32_t color_res, uint32_t depth_res);
+cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
+                            const float4* dirs, uint8_t* wbuf, float* rowsum, uint32_t* states, void* color,
+                            void* depth, float4* acc_color, float2* acc_depth, uint32_t* err, cudaStream_t st);
+
 // blend.cu
 cudaError_t launch_blend_fp32(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
                               const float4* dirs, uint32_t* states, float4* color, float2* depth, cudaStream_t st);

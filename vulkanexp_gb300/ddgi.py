@@ -60,6 +60,8 @@ _SIGNATURES = [
     ("ddgi_get_timings", C.c_int, [C.c_void_p, C.POINTER(Timings)]),
     ("ddgi_enable_timing", C.c_int, [C.c_void_p, C.c_int]),
     ("ddgi_set_pipeline", C.c_int, [C.c_void_p, C.c_int]),
+    ("ddgi_blend_records", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t,
+                                     C.c_void_p]),
 ]
 
 
@@ -185,6 +187,14 @@ class Context:
         keys = ("nodes", "tris", "instances", "rays", "shade_bytes", "shadow_nodes", "shadow_tris",
                 "shadow_instances", "shadow_rays")
         return {k: int(v) for k, v in zip(keys, out)}
+
+    def blend_records(self, orientation, records, probe_list=None, stream=None):
+        """Blend + border copy of given ray records (n x R x 4 float32)."""
+        o = np.ascontiguousarray(orientation, np.float32).reshape(9)
+        pl = None if probe_list is None else np.ascontiguousarray(probe_list, np.uint32)
+        rec = np.ascontiguousarray(records, np.float32)
+        self._check(self.lib.ddgi_blend_records(self.h, _ptr(o), _ptr(pl), 0 if pl is None else len(pl), _ptr(rec),
+                                                rec.size // 4, _stream_ptr(stream)))
 
     def synchronize(self, stream=None, timeout_ms=-1):
         self._check(self.lib.ddgi_synchronize(self.h, _stream_ptr(stream), int(timeout_ms)))
