@@ -96,11 +96,6 @@ __device__ __forceinline__ int4 border_entry(int e, int n) {
     return make_int4(j, n - 1, n - 1 - j, n - 2);
 }
 
-__device__ __forceinline__ float4 half4_to_float4(uint2 v) {
-    float2 a = __half22float2(*reinterpret_cast<__half2*>(&v.x));
-    float2 b = __half22float2(*reinterpret_cast<__half2*>(&v.y));
-    return make_float4(a.x, a.y, b.x, b.y);
-}
 __device__ __forceinline__ uint2 float4_to_half4(float a, float b, float c, float d) {
     __half2 x = __floats2half2_rn(a, b), y = __floats2half2_rn(c, d);
     return make_uint2(*reinterpret_cast<uint32_t*>(&x), *reinterpret_cast<uint32_t*>(&y));
@@ -339,9 +334,14 @@ __global__ void __launch_bounds__(kThreads) k_blend_tc(TcArgs a) {
         const float hy = a.g.hyst;
         const uint32_t rx = (uint32_t)a.g.res[0], rxy = (uint32_t)(a.g.res[0] * a.g.res[1]);
         const uint32_t ntc = a.nc * a.nc, ntd = a.nd * a.nd;
+        const uint32_t nprobes_grid = rxy * (uint32_t)a.g.res[2];
         for (uint32_t i = tid; i < np * (ntc + ntd); i += kThreads) {
             uint32_t pl2 = i / (ntc + ntd), t = i % (ntc + ntd);
             uint32_t probe = a.probe_list ? a.probe_list[p0 + pl2] : p0 + pl2;
+            if (probe >= nprobes_grid) {  // a probe list entry outside the grid
+                raise_error(a.err, DEV_BAD_INDEX);
+                continue;
+            }
             int ix = (int)(probe % rx), iy = (int)((probe % rxy) / rx), iz = (int)(probe / rxy);
             int tile = iy * a.g.res[0] + ix;
             if (t < ntc) {
@@ -378,6 +378,7 @@ __global__ void __launch_bounds__(kThreads) k_blend_tc(TcArgs a) {
         for (uint32_t i = tid; i < np * (nbc + nbd); i += kThreads) {
             uint32_t pl2 = i / (nbc + nbd), e = i % (nbc + nbd);
             uint32_t probe = a.probe_list ? a.probe_list[p0 + pl2] : p0 + pl2;
+            if (probe >= nprobes_grid) continue;
             int ix = (int)(probe % rx), iy = (int)((probe % rxy) / rx), iz = (int)(probe / rxy);
             int tile = iy * a.g.res[0] + ix;
             if (e < nbc) {
@@ -390,8 +391,9 @@ __global__ void __launch_bounds__(kThreads) k_blend_tc(TcArgs a) {
                 a.depth[(oy + b.y) * a.g.depth_w + ox + b.x] = a.depth[(oy + b.w) * a.g.depth_w + ox + b.z];
             }
         }
-        if ((uint32_t)tid < np) {  // probesUpdate.glsl:110-119
-            uint32_t probe = a.probe_list ? a.probe_list[p0 + tid] : p0 + tid;
+        uint32_t probe_t = (uint32_t)tid < np ? (a.probe_list ? a.probe_list[p0 + tid] : p0 + tid) : nprobes_grid;
+        if (probe_t < nprobes_grid) {  // probesUpdate.glsl:110-119
+            uint32_t probe = probe_t;
             uint32_t s = a.states[probe];
             if (s_oor[tid] >= R) {
                 s = 8;
