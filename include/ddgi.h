@@ -220,6 +220,34 @@ ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_
 ddgi_status ddgi_blend_records(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
                                uint32_t probe_count, const float* records, size_t count, ddgi_stream stream);
 
+/* Allocation-free BF16 blend.  This entry point has no counterpart in the
+ * reference; it exists for callers that cannot allocate device memory at the
+ * time they blend: an engine that reserves its whole device-memory budget up
+ * front, or a frame loop that must not call cudaMalloc/cudaFree (they can
+ * synchronise the device and stall the frame).  It runs the same blend +
+ * border copy + state update as ddgi_blend_records on a BF16 context, but on
+ * device buffers the caller owns and without a context:
+ *   probe_list  device, probe_count distinct linear probe indices (NULL = all);
+ *   records     device, (r, g, b, depth) float4 per (probe slot, ray);
+ *   states      device, one uint32 per probe (read and updated);
+ *   color/depth device, the FP16 atlases (4 x half / 2 x half per texel);
+ *   acc_color/acc_depth device, their FP32 hysteresis accumulators
+ *               (float4 / float2 per texel, same layout).
+ * Its own working memory (ray-direction table, weight matrices, row sums,
+ * error word; about 2 MB) is one fixed __device__ array that every GPU using
+ * the library holds until the process exits; requests that would need more
+ * (rays_per_probe x texel rows beyond 2 MB of weights, or interior tiles
+ * above 16 x 16 texels) return DDGI_ERR_UNSUPPORTED.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress) and
+ * should therefore come before any stream capture.  All calls share the
+ * array, so calls that overlap on the GPU (other streams, other host threads)
+ * race: serialise them.  Synchronous on `stream`; kernel-detected errors
+ * (a probe index outside the grid) return DDGI_ERR_DEVICE. */
+ddgi_status ddgi_blend_records_noalloc(const ddgi_grid_desc* grid, const float orientation[9],
+                                       const uint32_t* probe_list, uint32_t probe_count, const float* records,
+                                       uint32_t* states, void* color, void* depth, float* acc_color,
+                                       float* acc_depth, ddgi_stream stream);
+
 /* Copies an atlas to host memory as FP32 (RGBA for colour, RG for depth),
  * row-major, width = res*resolution.x*resolution.y, height = res*resolution.z.
  * `bytes` must equal width*height*channels*4.  Synchronous on `stream`. */

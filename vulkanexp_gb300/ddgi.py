@@ -62,6 +62,9 @@ _SIGNATURES = [
     ("ddgi_set_pipeline", C.c_int, [C.c_void_p, C.c_int]),
     ("ddgi_blend_records", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t,
                                      C.c_void_p]),
+    ("ddgi_blend_records_noalloc", C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_void_p]),
 ]
 
 
