@@ -302,6 +302,27 @@ ddgi_status ddgi_trace_rays(ddgi_ctx* ctx, const float* origins, const float* di
 ddgi_status ddgi_count_fetches(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
                                uint32_t probe_count, uint64_t out[9], ddgi_stream stream);
 
+/* Replaces the material table of the built scene (same count), e.g. new
+ * albedos, without rebuilding the acceleration structures. */
+ddgi_status ddgi_set_materials(ddgi_ctx* ctx, const ddgi_material* materials, uint32_t count);
+
+/* Differentiation (FP32 form, all probes).  Runs K updates from the current
+ * atlas, with orientations K x 9, and records what the reverse pass needs:
+ * every ray's closest hit and shadow result (the hit set is then held fixed)
+ * and an atlas checkpoint every `checkpoint_every` updates.  The atlas ends
+ * as after K ordinary updates. */
+ddgi_status ddgi_forward_record(ddgi_ctx* ctx, uint32_t K, const float* orientations, uint32_t checkpoint_every,
+                                ddgi_stream stream);
+/* Reverse pass of the last ddgi_forward_record: given dL/d(colour atlas
+ * after the K updates) (host, FP32 RGBA per texel, A ignored, `bytes` = the
+ * colour atlas size), returns dL/d albedo (material_count x 3), dL/d sun
+ * radiance and dL/d sky radiance, carried back through every update's blend,
+ * hysteresis, shading and bounce lookup into the previous atlas.  Atlases
+ * between checkpoints are recomputed from the recorded hits.  The context's
+ * atlas is not modified.  Synchronous on `stream`. */
+ddgi_status ddgi_backward(ddgi_ctx* ctx, const float* dL_dcolor, size_t bytes, float* grad_albedo, float grad_sun[3],
+                          float grad_sky[3], ddgi_stream stream);
+
 /* Waits for `stream` with a timeout (poll), then checks the device error word.
  * timeout_ms < 0 waits forever. */
 ddgi_status ddgi_synchronize(ddgi_ctx* ctx, ddgi_stream stream, int timeout_ms);

@@ -638,17 +638,44 @@ struct Light {
     F3 dir, color, sky;
 };
 
+// The differentiable parameters of an update: per-material albedo (NULL =
+// the materials' base colour), sun radiance and sky radiance, in T.
+template <class T>
+struct ShadeParams {
+    const T* albedo;  // material_count x 3
+    V3<T> sun, sky;
+};
+
+template <class T>
+ShadeParams<T> default_params(const Light& L) {
+    return ShadeParams<T>{nullptr, V3<T>(L.color), V3<T>(L.sky)};
+}
+
+// Shading of one probe ray given its closest hit (closesthit.glsl
+// NO_REFLECTION + miss).  shadow: -1 traces the shadow query, 0/1 uses a
+// recorded result; *shadowed_out receives it.
+template <class T>
+void shade_hit(const Scene& sc, const Grid& g, const Light& L, const ShadeParams<T>& P, const uint32_t* states,
+               const Atlas<T>& prev, F3 origin, F3 dir, const Hit& h, int shadow, bool* shadowed_out, T out[4]);
+
 // Hit shading of one probe ray (traceProbes.rgen + closesthit.glsl NO_REFLECTION + miss + shadow).
 template <class T>
 void shade_ray(const Scene& sc, const Grid& g, const Light& L, const uint32_t* states, const Atlas<T>& prev,
-               F3 origin, F3 dir, float tmax, T out[4], Hit* hit_out) {
+               F3 origin, F3 dir, float tmax, T out[4], Hit* hit_out, bool* shadowed_out = nullptr) {
     Hit h;
     trace(sc, origin, dir, 0.01f, tmax, 0x3u, false, &h);
     if (hit_out) *hit_out = h;
+    shade_hit<T>(sc, g, L, default_params<T>(L), states, prev, origin, dir, h, -1, shadowed_out, out);
+}
+
+template <class T>
+void shade_hit(const Scene& sc, const Grid& g, const Light& L, const ShadeParams<T>& P, const uint32_t* states,
+               const Atlas<T>& prev, F3 origin, F3 dir, const Hit& h, int shadow, bool* shadowed_out, T out[4]) {
+    if (shadowed_out) *shadowed_out = false;
     if (!h.valid()) {  // miss.rmiss:17-23 with a constant sky
-        out[0] = T(L.sky.x);
-        out[1] = T(L.sky.y);
-        out[2] = T(L.sky.z);
+        out[0] = P.sky.x;
+        out[1] = P.sky.y;
+        out[2] = P.sky.z;
         out[3] = T(-1);
         return;
     }
@@ -677,6 +704,10 @@ void shade_ray(const Scene& sc, const Grid& g, const Light& L, const uint32_t* s
              tsn.x * T(w[2]) + tsn.y * T(w[6]) + tsn.z * T(w[10]));
     V3<T> normal = normalize(nw);
     V3<T> albedo(T(m.base_color[0]), T(m.base_color[1]), T(m.base_color[2]));
+    if (P.albedo) {
+        const T* a = P.albedo + 3 * (size_t)oe.material_index;
+        albedo = V3<T>(a[0], a[1], a[2]);
+    }
     T metal = T(m.metallic), rough = T(m.roughness);
     V3<T> color(T(m.emissive[0]), T(m.emissive[1]), T(m.emissive[2]));
     V3<T> f0(T(0.04));
@@ -690,10 +721,16 @@ void shade_ray(const Scene& sc, const Grid& g, const Light& L, const uint32_t* s
     color = color + specularColor * reflection;
     V3<T> indirect = sample_probes<T>(position, normal, -D, g, states, prev);
     color = color + indirect * diffuseColor;
-    Hit sh;
-    bool shadowed = trace(sc, posf, L.dir, 0.1f, 10000.0f, 0xFFu, true, &sh);
+    bool shadowed;
+    if (shadow < 0) {
+        Hit sh;
+        shadowed = trace(sc, posf, L.dir, 0.1f, 10000.0f, 0xFFu, true, &sh);
+    } else {
+        shadowed = shadow != 0;
+    }
+    if (shadowed_out) *shadowed_out = shadowed;
     if (!shadowed) {
-        color = color + pbr<T>(normal, normalize(-D), V3<T>(L.color), V3<T>(L.dir), albedo, metal, rough);
+        color = color + pbr<T>(normal, normalize(-D), P.sun, V3<T>(L.dir), albedo, metal, rough);
         if (L.dir.y < 0.0f) {
             T f = T(1) - clampT(-T(L.dir.y), T(0), T(0.1)) / T(0.1);
             color = color * f;
@@ -727,7 +764,7 @@ inline float exact_tmax(const Grid& g) {
 // Blend of one probe (probesUpdate.glsl:49-121) + border copy (probesCopyBorders.comp).
 template <class T>
 void blend_probe(const Grid& g, uint32_t linear, const T* rays /* R x 4 */, const float* dirs /* R x 4 */,
-                 Atlas<T>& at, uint32_t* states, bool update_state) {
+                 Atlas<T>& at, uint32_t* states, bool update_state, bool do_depth = true) {
     int idx[3];
     grid_index(linear, g, idx);
     V3<T> cs = cell_size<T>(g);
@@ -784,7 +821,7 @@ void blend_probe(const Grid& g, uint32_t linear, const T* rays /* R x 4 */, cons
         }
     }
     // ---- depth ----
-    {
+    if (do_depth) {
         uint32_t n = g.depthRes - 2;
         T scale = T(texel_scale(n));
         T centre = T(0.5) * T(n - 1);
@@ -898,6 +935,103 @@ int run_update(const Scene& sc, const ddgi_grid_desc* gd, const ddgi_light* ld, 
         }
     });
     std::memcpy(states, new_states.data(), sizeof(uint32_t) * g.count());
+    return 0;
+}
+
+// A recorded probe ray: closest hit and shadow result, so that later
+// forward passes can replay shading + blend with other parameters while the
+// hit set stays fixed (the differentiation workload's assumption).
+struct RecHit {
+    uint32_t inst, prim;
+    float t, b1, b2;
+    uint32_t flags;  // bit 0 backface, bit 1 shadowed
+};
+
+// K successive updates of every probe.  replay = false traces (and records
+// into `rec` when given); replay = true shades the recorded hits instead.
+// depth_snap (K depth atlases) receives the depth atlas after every update
+// when recording; replays copy it back instead of re-blending depth, which
+// does not depend on the parameters once the hits are fixed.
+template <class T>
+int run_chain(const Scene& sc, const ddgi_grid_desc* gd, const ddgi_light* ld, const ShadeParams<T>* Pover,
+              const float* orientations, uint32_t K, uint32_t* states, T* color, T* depth, RecHit* rec, bool replay,
+              T* depth_snap, int nthreads) {
+    Grid g = make_grid(gd);
+    Light L;
+    L.dir = F3(ld->direction[0], ld->direction[1], ld->direction[2]);
+    L.color = F3(ld->color[0], ld->color[1], ld->color[2]);
+    L.sky = F3(ld->sky[0], ld->sky[1], ld->sky[2]);
+    ShadeParams<T> P = Pover ? *Pover : default_params<T>(L);
+    const uint32_t R = g.rays, NP = g.count();
+    Atlas<T> at;
+    at.color = color;
+    at.depth = depth;
+    at.cw = g.colorRes * g.res[0] * g.res[1];
+    at.ch = g.colorRes * g.res[2];
+    at.dw = g.depthRes * g.res[0] * g.res[1];
+    at.dh = g.depthRes * g.res[2];
+    const float tmax = exact_tmax(g);
+    std::vector<float> dirs(4 * (size_t)R);
+    std::vector<T> rays((size_t)NP * R * 4);
+    for (uint32_t k = 0; k < K; ++k) {
+        ddgi_ray_direction_table(orientations + 9 * (size_t)k, R, dirs.data());
+        RecHit* rk = rec ? rec + (size_t)k * NP * R : nullptr;
+        parallel_for(NP, nthreads, [&](size_t b, size_t e) {
+            for (size_t p = b; p < e; ++p) {
+                F3 o = exact_probe_origin(g, (uint32_t)p);
+                for (uint32_t r = 0; r < R; ++r) {
+                    F3 d(dirs[4 * r], dirs[4 * r + 1], dirs[4 * r + 2]);
+                    T* out = &rays[(p * R + r) * 4];
+                    size_t ri = p * R + r;
+                    if (replay) {
+                        const RecHit& q = rk[ri];
+                        Hit h;
+                        h.inst = q.inst;
+                        h.prim = q.prim;
+                        h.t = q.t;
+                        h.b1 = q.b1;
+                        h.b2 = q.b2;
+                        h.backface = (q.flags & 1u) != 0;
+                        shade_hit<T>(sc, g, L, P, states, at, o, d, h, (q.flags & 2u) ? 1 : 0, nullptr, out);
+                    } else {
+                        Hit h;
+                        trace(sc, o, d, 0.01f, tmax, 0x3u, false, &h);
+                        bool sh = false;
+                        shade_hit<T>(sc, g, L, P, states, at, o, d, h, -1, &sh, out);
+                        if (rk) {
+                            RecHit& q = rk[ri];
+                            q.inst = h.inst;
+                            q.prim = h.valid() ? h.prim : 0;
+                            q.t = h.valid() ? h.t : 0.0f;
+                            q.b1 = h.b1;
+                            q.b2 = h.b2;
+                            q.flags = (h.valid() && h.backface ? 1u : 0u) | (sh ? 2u : 0u);
+                        }
+                    }
+                }
+            }
+        });
+        std::vector<uint32_t> ns(states, states + NP);
+        const bool depth_from_snap = replay && depth_snap;
+        parallel_for(NP, nthreads, [&](size_t b, size_t e) {
+            for (size_t p = b; p < e; ++p) {
+                blend_probe<T>(g, (uint32_t)p, &rays[p * R * 4], dirs.data(), at, ns.data(), true, !depth_from_snap);
+                int idx[3];
+                grid_index((uint32_t)p, g, idx);
+                int tile = idx[1] * g.res[0] + idx[0];
+                copy_borders<T>(at.color, at.cw, 4, (int)g.colorRes * tile, (int)g.colorRes * idx[2], (int)g.colorRes);
+                if (!depth_from_snap)
+                    copy_borders<T>(at.depth, at.dw, 2, (int)g.depthRes * tile, (int)g.depthRes * idx[2],
+                                    (int)g.depthRes);
+            }
+        });
+        std::memcpy(states, ns.data(), sizeof(uint32_t) * NP);
+        const size_t dn = (size_t)at.dw * at.dh * 2;
+        if (depth_snap) {
+            if (depth_from_snap) std::memcpy(depth, depth_snap + (size_t)k * dn, dn * sizeof(T));
+            else std::memcpy(depth_snap + (size_t)k * dn, depth, dn * sizeof(T));
+        }
+    }
     return 0;
 }
 
@@ -1133,6 +1267,39 @@ void oracle_sample_probes(const ddgi_grid_desc* gd, const uint32_t* states, cons
     F3 r = sample_probes<float>(F3(pos[0], pos[1], pos[2]), F3(nrm[0], nrm[1], nrm[2]), F3(view[0], view[1], view[2]), g,
                                 states, at);
     out3[0] = r.x; out3[1] = r.y; out3[2] = r.z;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Differentiation support: K-update chains in FP64 with a recorded hit set.
+// ---------------------------------------------------------------------------
+extern "C" {
+
+uint32_t oracle_rec_hit_bytes(void) { return (uint32_t)sizeof(RecHit); }
+
+// FP64 forward over all probes for K updates (orientations: K x 9), tracing
+// and recording every ray's hit and shadow result into rec (K * P * R).
+int oracle_record(const oracle_scene* s, const ddgi_grid_desc* g, const ddgi_light* l, const float* orientations,
+                  uint32_t K, uint32_t* states, double* color, double* depth, void* rec, double* depth_snap,
+                  int nthreads) {
+    return run_chain<double>(s->s, g, l, nullptr, orientations, K, states, color, depth, static_cast<RecHit*>(rec),
+                             false, depth_snap, nthreads);
+}
+
+// FP64 forward replaying a recorded hit set with the given parameters:
+// albedo (material_count x 3, NULL = the materials' base colour), sun and
+// sky radiance (3 doubles each).
+int oracle_replay(const oracle_scene* s, const ddgi_grid_desc* g, const ddgi_light* l, const double* albedo,
+                  const double* sun, const double* sky, const float* orientations, uint32_t K, uint32_t* states,
+                  double* color, double* depth, const void* rec, const double* depth_snap, int nthreads) {
+    ShadeParams<double> P;
+    P.albedo = albedo;
+    P.sun = V3<double>(sun[0], sun[1], sun[2]);
+    P.sky = V3<double>(sky[0], sky[1], sky[2]);
+    return run_chain<double>(s->s, g, l, &P, orientations, K, states, color, depth,
+                             const_cast<RecHit*>(static_cast<const RecHit*>(rec)), true,
+                             const_cast<double*>(depth_snap), nthreads);
 }
 
 }  // extern "C"

@@ -11,6 +11,9 @@ import numpy as np
 
 from vulkanexp_gb300.abi import HIT_DTYPE, GridDesc, Light, SceneDesc
 
+REC_DTYPE = np.dtype([("inst", "<u4"), ("prim", "<u4"), ("t", "<f4"), ("b1", "<f4"), ("b2", "<f4"),
+                      ("flags", "<u4")])
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 BUILD_DIR = os.path.join(HERE, "_build")
@@ -78,6 +81,13 @@ class Oracle:
             lib.oracle_blend.argtypes = [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
             lib.oracle_blend64.argtypes = lib.oracle_blend.argtypes
+            lib.oracle_rec_hit_bytes.restype = C.c_uint32
+            lib.oracle_record.argtypes = [C.c_void_p, C.POINTER(GridDesc), C.POINTER(Light), C.c_void_p, C.c_uint32,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+            lib.oracle_replay.argtypes = [C.c_void_p, C.POINTER(GridDesc), C.POINTER(Light), C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_int]
+            assert lib.oracle_rec_hit_bytes() == REC_DTYPE.itemsize
             lib.oracle_border_table.restype = C.c_uint32
             lib.oracle_border_table.argtypes = [C.c_int, C.c_void_p]
             lib.oracle_oct_decode.argtypes = [C.c_float, C.c_float, C.c_void_p]
@@ -136,6 +146,34 @@ class Oracle:
                                  0 if plist is None else len(plist), _ptr(states), _ptr(color), _ptr(depth), int(fp64),
                                  _ptr(rays), _ptr(hits), self.threads)
         return rays, hits
+
+    # -- differentiation support (FP64, all probes, hit set recorded once) -----
+    def record(self, grid, light, orientations, states, color, depth):
+        """K FP64 updates (orientations K x 9) in place on color/depth
+        (float64) and states; returns the recording: hits (K, P, R) and the
+        depth atlas after every update."""
+        o = np.ascontiguousarray(orientations, np.float32).reshape(-1, 9)
+        K, P, R = len(o), grid.probe_count(), grid.rays_per_probe
+        assert color.dtype == np.float64 and depth.dtype == np.float64
+        rec = np.zeros((K, P, R), REC_DTYPE)
+        snap = np.zeros((K,) + depth.shape, np.float64)
+        self.lib().oracle_record(self._h, C.byref(grid), C.byref(light), _ptr(o), K, _ptr(states), _ptr(color),
+                                 _ptr(depth), _ptr(rec), _ptr(snap), self.threads)
+        return rec, snap
+
+    def replay(self, grid, light, orientations, states, color, depth, recording, albedo=None, sun=None, sky=None):
+        """K FP64 updates shading the recorded hits with the given parameters
+        (albedo: material_count x 3; sun, sky: 3 each; None = the scene's)."""
+        rec, snap = recording
+        o = np.ascontiguousarray(orientations, np.float32).reshape(-1, 9)
+        K = len(o)
+        assert rec.shape[0] == K and snap.shape[0] == K
+        alb = None if albedo is None else np.ascontiguousarray(albedo, np.float64)
+        sun = np.ascontiguousarray(light.color[:3] if sun is None else sun, np.float64)
+        sky = np.ascontiguousarray(light.sky[:3] if sky is None else sky, np.float64)
+        self.lib().oracle_replay(self._h, C.byref(grid), C.byref(light), _ptr(alb), _ptr(sun), _ptr(sky), _ptr(o), K,
+                                 _ptr(states), _ptr(color), _ptr(depth), _ptr(np.ascontiguousarray(rec)), _ptr(snap),
+                                 self.threads)
 
     # -- scene-independent entry points ---------------------------------------
     @classmethod

@@ -81,6 +81,26 @@ struct ddgi_ctx {
     // BF16 form: FP32 hysteresis accumulators behind the FP16 atlas
     float4* acc_color = nullptr;
     float2* acc_depth = nullptr;
+    // differentiation: recorded hits of K updates, atlas checkpoints, and the
+    // reverse-pass buffers
+    uint32_t rec_K = 0, rec_C = 0;
+    size_t rec_cap = 0;  // rays per update the record buffers hold
+    uint32_t rec_updates_cap = 0;
+    std::vector<float> rec_orient;
+    float4* rec_thit = nullptr;
+    uint32_t* rec_prim = nullptr;
+    float4* ckpt_color = nullptr;
+    float2* ckpt_depth = nullptr;
+    uint32_t ckpt_cap = 0;
+    uint32_t* rec_states = nullptr;
+    uint32_t* work_states = nullptr;
+    float4* work_color = nullptr;
+    float2* work_depth = nullptr;
+    float4* g_a = nullptr;
+    float4* g_b = nullptr;
+    float4* g_x = nullptr;
+    double* d_grad = nullptr;
+    uint32_t grad_cap = 0;
     ddgi_hit* hits = nullptr;
     size_t hits_cap = 0;
     bool record_hits = false;
@@ -381,6 +401,18 @@ ddgi_status ddgi_destroy(ddgi_ctx* ctx) {
     dfree(ctx->tc_rowsum);
     dfree(ctx->acc_color);
     dfree(ctx->acc_depth);
+    dfree(ctx->rec_thit);
+    dfree(ctx->rec_prim);
+    dfree(ctx->ckpt_color);
+    dfree(ctx->ckpt_depth);
+    dfree(ctx->rec_states);
+    dfree(ctx->work_states);
+    dfree(ctx->work_color);
+    dfree(ctx->work_depth);
+    dfree(ctx->g_a);
+    dfree(ctx->g_b);
+    dfree(ctx->g_x);
+    dfree(ctx->d_grad);
     dfree(ctx->hits);
     dfree(ctx->dirs);
     dfree(ctx->ray_order);
@@ -1008,6 +1040,166 @@ ddgi_status ddgi_trace_rays(ddgi_ctx* ctx, const float* origins, const float* di
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     cleanup();
     if (e != cudaSuccess) return cuda_fail(ctx, e, "trace rays");
+    return check_device_error(ctx);
+}
+
+ddgi_status ddgi_set_materials(ddgi_ctx* ctx, const ddgi_material* materials, uint32_t count) {
+    if (!ctx || (count && !materials)) return DDGI_ERR_INVALID_ARGUMENT;
+    if (!ctx->scene.built) return fail(ctx, DDGI_ERR_NO_SCENE, "no scene");
+    if (count != ctx->scene.material_count)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "expected %u materials", ctx->scene.material_count);
+    for (uint32_t m = 0; m < count; ++m)
+        for (int k = 0; k < 3; ++k)
+            if (!std::isfinite(materials[m].base_color[k]) || !std::isfinite(materials[m].emissive[k]))
+                return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "material %u not finite", m);
+    CK(cudaMemcpy(ctx->scene.materials, materials, sizeof(ddgi_material) * count, cudaMemcpyHostToDevice),
+       "upload materials");
+    return DDGI_OK;
+}
+
+namespace {
+
+ddgi_status ensure_rec_buffers(ddgi_ctx* ctx, uint32_t K, uint32_t ncheck) {
+    const size_t rays = (size_t)probe_count_of(ctx->grid) * ctx->grid.rays_per_probe;
+    if (rays != ctx->rec_cap || K > ctx->rec_updates_cap) {
+        dfree(ctx->rec_thit);
+        dfree(ctx->rec_prim);
+        dfree(ctx->g_x);
+        ctx->rec_cap = 0;
+        ctx->rec_updates_cap = 0;
+        CK(cudaMalloc(&ctx->rec_thit, rays * K * sizeof(float4)), "alloc hit record");
+        CK(cudaMalloc(&ctx->rec_prim, rays * K * sizeof(uint32_t)), "alloc hit record");
+        CK(cudaMalloc(&ctx->g_x, rays * sizeof(float4)), "alloc ray gradients");
+        ctx->rec_cap = rays;
+        ctx->rec_updates_cap = K;
+    }
+    const size_t cb = atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, false), db = atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, false);
+    if (ncheck > ctx->ckpt_cap) {
+        dfree(ctx->ckpt_color);
+        dfree(ctx->ckpt_depth);
+        ctx->ckpt_cap = 0;
+        CK(cudaMalloc(&ctx->ckpt_color, cb * ncheck), "alloc checkpoints");
+        CK(cudaMalloc(&ctx->ckpt_depth, db * ncheck), "alloc checkpoints");
+        ctx->ckpt_cap = ncheck;
+    }
+    const uint32_t P = probe_count_of(ctx->grid);
+    if (!ctx->rec_states) {
+        CK(cudaMalloc(&ctx->rec_states, sizeof(uint32_t) * P), "alloc states");
+        CK(cudaMalloc(&ctx->work_states, sizeof(uint32_t) * P), "alloc states");
+        CK(cudaMalloc(&ctx->work_color, cb), "alloc work atlas");
+        CK(cudaMalloc(&ctx->work_depth, db), "alloc work atlas");
+        CK(cudaMalloc(&ctx->g_a, cb), "alloc atlas gradients");
+        CK(cudaMalloc(&ctx->g_b, cb), "alloc atlas gradients");
+    }
+    const uint32_t ng = ctx->scene.material_count * 3 + 6;
+    if (ng > ctx->grad_cap) {
+        dfree(ctx->d_grad);
+        ctx->grad_cap = 0;
+        CK(cudaMalloc(&ctx->d_grad, sizeof(double) * ng), "alloc gradients");
+        ctx->grad_cap = ng;
+    }
+    return DDGI_OK;
+}
+
+ddgi_status upload_dirs(ddgi_ctx* ctx, const float* orientation, cudaStream_t st) {
+    const uint32_t R = ctx->grid.rays_per_probe;
+    ctx->host_dirs.resize(4 * (size_t)R);
+    ddgi_ray_direction_table(orientation, R, ctx->host_dirs.data());
+    CK(cudaMemcpyAsync(ctx->dirs, ctx->host_dirs.data(), sizeof(float4) * R, cudaMemcpyHostToDevice, st),
+       "upload dirs");
+    return DDGI_OK;
+}
+
+}  // namespace
+
+ddgi_status ddgi_forward_record(ddgi_ctx* ctx, uint32_t K, const float* orientations, uint32_t checkpoint_every,
+                                ddgi_stream stream) {
+    if (!ctx || !orientations || K == 0 || checkpoint_every == 0) return DDGI_ERR_INVALID_ARGUMENT;
+    if (ctx->fp16) return fail(ctx, DDGI_ERR_UNSUPPORTED, "gradients need the FP32 form");
+    if (!ctx->scene.built) return fail(ctx, DDGI_ERR_NO_SCENE, "no scene");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const uint32_t C = checkpoint_every, ncheck = (K + C - 1) / C;
+    ddgi_status s = ensure_rec_buffers(ctx, K, ncheck);
+    if (s != DDGI_OK) return s;
+    const uint32_t P = probe_count_of(ctx->grid);
+    const size_t rays = (size_t)P * ctx->grid.rays_per_probe;
+    const size_t cb = atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, false), db = atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, false);
+    CK(cudaMemcpyAsync(ctx->rec_states, ctx->states, sizeof(uint32_t) * P, cudaMemcpyDeviceToDevice, st), "states");
+    const ddgi_pipeline saved = ctx->pipeline;
+    ctx->pipeline = DDGI_PIPELINE_WAVEFRONT;  // the wavefront form keeps the hit buffer and shadow flags
+    for (uint32_t k = 0; k < K; ++k) {
+        if (k % C == 0) {
+            CK(cudaMemcpyAsync((char*)ctx->ckpt_color + cb * (k / C), ctx->color, cb, cudaMemcpyDeviceToDevice, st),
+               "checkpoint");
+            CK(cudaMemcpyAsync((char*)ctx->ckpt_depth + db * (k / C), ctx->depth, db, cudaMemcpyDeviceToDevice, st),
+               "checkpoint");
+        }
+        s = ddgi_update(ctx, orientations + 9 * (size_t)k, nullptr, 0, stream);
+        if (s != DDGI_OK) {
+            ctx->pipeline = saved;
+            return s;
+        }
+        CK(cudaMemcpyAsync(ctx->rec_thit + rays * k, ctx->wave_thit, rays * sizeof(float4), cudaMemcpyDeviceToDevice,
+                           st),
+           "record hits");
+        CK(cudaMemcpyAsync(ctx->rec_prim + rays * k, ctx->wave_prim, rays * sizeof(uint32_t),
+                           cudaMemcpyDeviceToDevice, st),
+           "record hits");
+    }
+    ctx->pipeline = saved;
+    ctx->rec_K = K;
+    ctx->rec_C = C;
+    ctx->rec_orient.assign(orientations, orientations + 9 * (size_t)K);
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_backward(ddgi_ctx* ctx, const float* dL_dcolor, size_t bytes, float* grad_albedo, float grad_sun[3],
+                          float grad_sky[3], ddgi_stream stream) {
+    if (!ctx || !dL_dcolor || !grad_albedo || !grad_sun || !grad_sky) return DDGI_ERR_INVALID_ARGUMENT;
+    if (ctx->rec_K == 0) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "ddgi_backward without ddgi_forward_record");
+    const size_t cb = atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, false), db = atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, false);
+    if (bytes != cb) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "gradient needs %zu bytes", cb);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const uint32_t P = probe_count_of(ctx->grid), M = ctx->scene.material_count;
+    const size_t rays = (size_t)P * ctx->grid.rays_per_probe;
+    const uint32_t K = ctx->rec_K, C = ctx->rec_C;
+    DeviceScene sc = device_scene(ctx);
+    CK(cudaMemcpyAsync(ctx->g_a, dL_dcolor, cb, cudaMemcpyHostToDevice, st), "upload gradient");
+    CK(cudaMemsetAsync(ctx->d_grad, 0, sizeof(double) * (M * 3 + 6), st), "zero gradients");
+    for (uint32_t u = K; u-- > 0;) {
+        // atlas before update u: checkpoint, then replay the updates after it
+        const uint32_t c0 = (u / C) * C;
+        CK(cudaMemcpyAsync(ctx->work_color, (char*)ctx->ckpt_color + cb * (u / C), cb, cudaMemcpyDeviceToDevice, st),
+           "restore");
+        CK(cudaMemcpyAsync(ctx->work_depth, (char*)ctx->ckpt_depth + db * (u / C), db, cudaMemcpyDeviceToDevice, st),
+           "restore");
+        CK(cudaMemcpyAsync(ctx->work_states, ctx->rec_states, sizeof(uint32_t) * P, cudaMemcpyDeviceToDevice, st),
+           "restore");
+        for (uint32_t v = c0; v < u; ++v) {
+            ddgi_status s = upload_dirs(ctx, &ctx->rec_orient[9 * (size_t)v], st);
+            if (s != DDGI_OK) return s;
+            CK(launch_replay_update(sc, ctx->dg, ctx->dl, ctx->dirs, ctx->work_states, ctx->work_color, ctx->work_depth,
+                                    ctx->rec_thit + rays * v, ctx->rec_prim + rays * v, ctx->rays, ctx->err, st),
+               "replay");
+        }
+        CK(cudaMemcpyAsync(ctx->work_states, ctx->rec_states, sizeof(uint32_t) * P, cudaMemcpyDeviceToDevice, st),
+           "restore");
+        ddgi_status s = upload_dirs(ctx, &ctx->rec_orient[9 * (size_t)u], st);
+        if (s != DDGI_OK) return s;
+        CK(launch_adjoint_step(sc, ctx->dg, ctx->dl, ctx->dirs, ctx->work_states, ctx->work_color, ctx->work_depth,
+                               ctx->rec_thit + rays * u, ctx->rec_prim + rays * u, ctx->g_a, ctx->g_b, ctx->g_x,
+                               ctx->d_grad, ctx->err, st),
+           "adjoint");
+        std::swap(ctx->g_a, ctx->g_b);
+    }
+    std::vector<double> h(M * 3 + 6);
+    CK(cudaMemcpyAsync(h.data(), ctx->d_grad, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st), "gradients");
+    CK(cudaStreamSynchronize(st), "backward");
+    for (uint32_t i = 0; i < M * 3; ++i) grad_albedo[i] = (float)h[i];
+    for (int k = 0; k < 3; ++k) {
+        grad_sun[k] = (float)h[M * 3 + k];
+        grad_sky[k] = (float)h[M * 3 + 3 + k];
+    }
     return check_device_error(ctx);
 }
 

@@ -36,6 +36,15 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
                              ddgi_hit* hits_out, int stack_cap, uint32_t* err, cudaStream_t st,
                              cudaEvent_t after_primary);
 
+// adjoint.cu
+cudaError_t launch_replay_update(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L, const float4* dirs,
+                                 uint32_t* states, float4* color, float2* depth, const float4* thit,
+                                 const uint32_t* prim, float4* rays, uint32_t* err, cudaStream_t st);
+cudaError_t launch_adjoint_step(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L, const float4* dirs,
+                                const uint32_t* states, const float4* color_prev, const float2* depth_prev,
+                                const float4* thit, const uint32_t* prim, float4* gk, float4* gprev, float4* gx,
+                                double* grad, uint32_t* err, cudaStream_t st);
+
 // blend_tc.cu
 size_t tc_weight_bytes(uint32_t rays, uint32_t color_res, uint32_t depth_res);
 bool tc_blend_supported(uint32_t color_res, uint32_t depth_res);

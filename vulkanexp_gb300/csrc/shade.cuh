@@ -182,15 +182,19 @@ struct SurfaceShade {
     float fade;
 };
 
-template <class AV>
-__device__ __forceinline__ bool shade_surface(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L,
-                                              const uint32_t* states, const AV& at, float3 origin, float3 dir,
-                                              float t, float b1, float b2, uint32_t inst, uint32_t prim,
-                                              SurfaceShade* out, uint32_t* err) {
+// Geometry and material at a front-face hit (closesthit.glsl:143-190, no
+// textures).
+struct Surface {
+    float3 position, normal, albedo, emissive;
+    float metal, rough;
+    uint32_t material;
+};
+
+__device__ __forceinline__ bool surface_at(const DeviceScene& sc, float3 origin, float3 dir, float t, float b1,
+                                           float b2, uint32_t inst, uint32_t prim, Surface* s, uint32_t* err) {
     // hit position: product then sum, each rounded (shared with the shadow ray)
-    out->position = f3(__fadd_rn(__fmul_rn(dir.x, t), origin.x), __fadd_rn(__fmul_rn(dir.y, t), origin.y),
-                       __fadd_rn(__fmul_rn(dir.z, t), origin.z));
-    float3 position = out->position;
+    s->position = f3(__fadd_rn(__fmul_rn(dir.x, t), origin.x), __fadd_rn(__fmul_rn(dir.y, t), origin.y),
+                     __fadd_rn(__fmul_rn(dir.z, t), origin.z));
     const GpuInstance* gi = sc.instances_by_id + inst;
     uint32_t custom = __ldg(&gi->custom);
     ddgi_offset_entry oe = sc.offsets[custom];
@@ -199,8 +203,6 @@ __device__ __forceinline__ bool shade_surface(const DeviceScene& sc, const Devic
     uint32_t vb = oe.vertex_offset;
     if (vb + max(i0, max(i1, i2)) >= sc.vertex_count || oe.material_index >= sc.material_count) {
         raise_error(err, DEV_BAD_INDEX);
-        out->base = out->sun = f3(0, 0, 0);
-        out->fade = 1.0f;
         return false;
     }
     float4 n0 = __ldg(sc.normals + vb + i0), n1 = __ldg(sc.normals + vb + i1), n2 = __ldg(sc.normals + vb + i2);
@@ -209,12 +211,33 @@ __device__ __forceinline__ bool shade_surface(const DeviceScene& sc, const Devic
                           n0.z * b0 + n1.z * b1 + n2.z * b2));
     float4 w0 = __ldg(&gi->w2o[0]), w1 = __ldg(&gi->w2o[1]), w2 = __ldg(&gi->w2o[2]);
     // normal * gl_WorldToObjectEXT: transpose of the world-to-object 3x3
-    float3 normal = norm3(f3(tsn.x * w0.x + tsn.y * w1.x + tsn.z * w2.x, tsn.x * w0.y + tsn.y * w1.y + tsn.z * w2.y,
-                             tsn.x * w0.z + tsn.y * w1.z + tsn.z * w2.z));
+    s->normal = norm3(f3(tsn.x * w0.x + tsn.y * w1.x + tsn.z * w2.x, tsn.x * w0.y + tsn.y * w1.y + tsn.z * w2.y,
+                         tsn.x * w0.z + tsn.y * w1.z + tsn.z * w2.z));
     const ddgi_material& m = sc.materials[oe.material_index];
-    float3 albedo = f3(m.base_color[0], m.base_color[1], m.base_color[2]);
-    float metal = m.metallic, rough = m.roughness;
-    float3 color = f3(m.emissive[0], m.emissive[1], m.emissive[2]);
+    s->albedo = f3(m.base_color[0], m.base_color[1], m.base_color[2]);
+    s->emissive = f3(m.emissive[0], m.emissive[1], m.emissive[2]);
+    s->metal = m.metallic;
+    s->rough = m.roughness;
+    s->material = oe.material_index;
+    return true;
+}
+
+template <class AV>
+__device__ __forceinline__ bool shade_surface(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L,
+                                              const uint32_t* states, const AV& at, float3 origin, float3 dir,
+                                              float t, float b1, float b2, uint32_t inst, uint32_t prim,
+                                              SurfaceShade* out, uint32_t* err) {
+    Surface s;
+    if (!surface_at(sc, origin, dir, t, b1, b2, inst, prim, &s, err)) {
+        out->position = s.position;
+        out->base = out->sun = f3(0, 0, 0);
+        out->fade = 1.0f;
+        return false;
+    }
+    out->position = s.position;
+    const float3 position = s.position, normal = s.normal, albedo = s.albedo;
+    const float metal = s.metal, rough = s.rough;
+    float3 color = s.emissive;
     float3 diffuseColor = albedo * (1.0f - 0.04f) * (1.0f - metal);
     float3 specularColor = mix3(f3(0.04f, 0.04f, 0.04f), albedo, metal);
     float3 reflectDir = dir - normal * (2.0f * dot3(normal, dir));

@@ -55,6 +55,7 @@ struct ShadowJob {
     const ShadowQueue q;
     float3 dir;
     float4* rays;
+    uint32_t* prim;  // hit words: bit 30 marks a shadowed front hit (kept for replays)
     uint32_t total;
 
     __device__ __forceinline__ bool start(WarpWalker<true>& w, const DeviceScene& sc, uint32_t id,
@@ -64,8 +65,11 @@ struct ShadowJob {
         return w.start(sc, f3(p.x, p.y, p.z), dir, 0.1f, 10000.0f, 0xFFu);
     }
     __device__ __forceinline__ void finish(const WarpWalker<true>& w, uint32_t id) const {
-        if (w.best.inst != kNoHit) return;  // shadowed: the record keeps the base colour
         uint32_t idx = q.idx[id];
+        if (w.best.inst != kNoHit) {  // shadowed: the record keeps the base colour
+            prim[idx] |= 1u << 30;
+            return;
+        }
         float4 sun = q.sun[id];
         float4 rec = rays[idx];
         float3 c = (f3(rec.x, rec.y, rec.z) + f3(sun.x, sun.y, sun.z)) * sun.w;
@@ -146,7 +150,7 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene sc, DeviceGrid g, Dev
         uint32_t slot = i / R, ray = i - slot * R;
         float4 th = hits.thit[i];
         uint32_t pb = hits.prim[i];
-        uint32_t inst = __float_as_uint(th.w), prim = pb & 0x7fffffffu;
+        uint32_t inst = __float_as_uint(th.w), prim = pb & 0x0fffffffu;
         bool back = (pb >> 31) != 0;
         float4 rec;
         if (inst == kNoHit) {
@@ -233,7 +237,7 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
         k_shade<<<blocks, 128, 0, st>>>(sc, g, L, probe_list, total, dirs, states, at, hits, rays_out, hits_out, qq,
                                         err);
     }
-    ShadowJob sj{qq, make_float3(L.dir[0], L.dir[1], L.dir[2]), rays_out, 0};
+    ShadowJob sj{qq, make_float3(L.dir[0], L.dir[1], L.dir[2]), rays_out, hits.prim, 0};
     k_shadow<<<persistent_blocks((const void*)k_shadow, smem), kPersistThreads, smem, st>>>(
         sc, sj, counters + 1, counters + 2, stack_cap, err);
     return cudaGetLastError();

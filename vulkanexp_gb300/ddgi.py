@@ -62,6 +62,9 @@ _SIGNATURES = [
     ("ddgi_set_pipeline", C.c_int, [C.c_void_p, C.c_int]),
     ("ddgi_blend_records", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t,
                                      C.c_void_p]),
+    ("ddgi_set_materials", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    ("ddgi_forward_record", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p]),
+    ("ddgi_backward", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ddgi_blend_records_noalloc", C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p]),
@@ -198,6 +201,28 @@ class Context:
         rec = np.ascontiguousarray(records, np.float32)
         self._check(self.lib.ddgi_blend_records(self.h, _ptr(o), _ptr(pl), 0 if pl is None else len(pl), _ptr(rec),
                                                 rec.size // 4, _stream_ptr(stream)))
+
+    def set_materials(self, materials):
+        m = np.ascontiguousarray(materials)
+        self._check(self.lib.ddgi_set_materials(self.h, _ptr(m), len(m)))
+
+    def forward_record(self, orientations, checkpoint_every=2, stream=None):
+        """K recorded updates (orientations K x 9) for a later backward()."""
+        o = np.ascontiguousarray(orientations, np.float32).reshape(-1, 9)
+        self._check(self.lib.ddgi_forward_record(self.h, len(o), _ptr(o), int(checkpoint_every),
+                                                 _stream_ptr(stream)))
+
+    def backward(self, dL_dcolor, n_materials, stream=None):
+        """Gradients (albedo [M, 3], sun [3], sky [3]) of a loss whose
+        gradient with respect to the final colour atlas is dL_dcolor."""
+        g = np.ascontiguousarray(dL_dcolor, np.float32)
+        assert g.shape == self.atlas_shape(abi.ATLAS_COLOR)
+        ga = np.zeros((n_materials, 3), np.float32)
+        gs = np.zeros(3, np.float32)
+        gk = np.zeros(3, np.float32)
+        self._check(self.lib.ddgi_backward(self.h, _ptr(g), g.nbytes, _ptr(ga), _ptr(gs), _ptr(gk),
+                                           _stream_ptr(stream)))
+        return ga, gs, gk
 
     def synchronize(self, stream=None, timeout_ms=-1):
         self._check(self.lib.ddgi_synchronize(self.h, _stream_ptr(stream), int(timeout_ms)))
