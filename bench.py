@@ -204,6 +204,45 @@ def time_updates(ctx, w, steps, warmup, stream, flush, first=0):
     return float(np.mean(ms)), {k: float(np.mean(v)) for k, v in stages.items()}
 
 
+def measure_differentiation(stream, reps=3):
+    """Forward (K recorded updates) and backward (adjoint through them) on the
+    differentiation workload: room + 1000 boxes, 16x8x16 probes, 256 rays,
+    K = 8, checkpoints every 2 updates.  CUDA events around each call."""
+    import torch
+
+    from vulkanexp_gb300 import abi, scenes
+    from vulkanexp_gb300.ddgi import Context
+
+    w = scenes.workload(3)
+    K = 8
+    orients = np.stack([w.orientation(k) for k in range(K)])
+    ctx = Context(w.grid)
+    ctx.build_scene(w.scene, stream)
+    ctx.set_light(w.light)
+    zc = np.zeros(ctx.atlas_shape(abi.ATLAS_COLOR), np.float32)
+    zd = np.zeros(ctx.atlas_shape(abi.ATLAS_DEPTH), np.float32)
+    grad = np.ones_like(zc)
+    fwd, bwd = [], []
+    for rep in range(reps + 1):
+        ctx.set_atlas(abi.ATLAS_COLOR, zc, stream)
+        ctx.set_atlas(abi.ATLAS_DEPTH, zd, stream)
+        torch.cuda.synchronize()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        ctx.forward_record(orients, 2, stream)
+        e1.record(stream)
+        ctx.backward(grad, len(w.scene.materials), stream)
+        e2.record(stream)
+        torch.cuda.synchronize()
+        if rep > 0:  # the first repetition warms up
+            fwd.append(e0.elapsed_time(e1))
+            bwd.append(e1.elapsed_time(e2))
+    ctx.close()
+    f, b = float(np.mean(fwd)), float(np.mean(bwd))
+    return {"workload": w.name, "updates": K, "checkpoint_every": 2, "forward_ms": f, "backward_ms": b,
+            "bwd_fwd_ratio": b / f, "parameters": len(w.scene.materials) * 3 + 6}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -326,6 +365,7 @@ def main():
             "e2e": {"value": e2e_val, "unit": UNIT, "ms_per_step": float(np.mean(e2e_ms)),
                     "h2d_bytes_per_step": R * 20, "d2h_bytes_per_step": int(host_c.nbytes + host_d.nbytes)}}
     ctx.close()
+    line["differentiation"] = measure_differentiation(stream)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_probes)
     if rank == 0:
