@@ -243,6 +243,77 @@ def measure_differentiation(stream, reps=3):
             "bwd_fwd_ratio": b / f, "parameters": len(w.scene.materials) * 3 + 6}
 
 
+def measure_batching(stream, steps, warmup, flush):
+    """The batching workload: 48 seeded volumes (room or terrain generator,
+    5k-300k triangles, 4x4x4..24x12x24 probes, 64-512 rays, 8/16 or 6/14
+    tiles, FP32 or BF16 form) updated together per step: one persistent
+    work-queue traversal over every volume's rays, replayed from a CUDA graph,
+    launch parameters from the autotuner.  Reports aggregate primary rays/s,
+    per-volume completion time (update start -> the volume's last blend work
+    item) p50/p99 over all timed steps, and the same volumes updated one
+    context at a time for comparison.  CUDA events on the launching stream;
+    the per-ray buffers (~1.3 GB) exceed L2, which is also flushed."""
+    import torch
+
+    from vulkanexp_gb300 import scenes
+    from vulkanexp_gb300.ddgi import Batch, Context
+
+    ws = scenes.batch_workloads()
+    ctxs = []
+    for w in ws:
+        c = Context(w.grid)
+        c.build_scene(w.scene, stream)
+        c.set_light(w.light)
+        ctxs.append(c)
+    b = Batch(ctxs, stream)
+
+    def orient(k):
+        return np.stack([scenes.random_orientation(w.seed, k) for w in ws])
+
+    t0 = time.perf_counter()
+    tuning = b.autotune(orient(0), reps=3, stream=stream)
+    tune_s = time.perf_counter() - t0
+    for k in range(warmup):
+        b.update(orient(1 + k), stream)
+    b.synchronize(stream)
+    ms, comp = [], []
+    for k in range(steps):
+        flush.fill_(k & 255)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.update(orient(1 + warmup + k), stream)
+        e1.record(stream)
+        b.synchronize(stream)
+        ms.append(e0.elapsed_time(e1))
+        comp.append(b.completion_ms())
+    seq = []
+    for k in range(steps):
+        flush.fill_(k & 255)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for c, w in zip(ctxs, ws):
+            c.update(scenes.random_orientation(w.seed, 100 + k), stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        seq.append(e0.elapsed_time(e1))
+    rays = b.ray_count
+    comp = np.concatenate(comp)
+    t = float(np.median(ms))
+    out = {"workload": "48 volumes (seed 1238): room/terrain, 5k-300k triangles, 4x4x4..24x12x24 probes, "
+                       "64-512 rays, 8/16 or 6/14 tiles, mixed FP32/BF16",
+           "volumes": len(ws), "bf16_volumes": int(sum(w.grid.precision for w in ws)),
+           "probes": int(sum(w.grid.probe_count() for w in ws)), "rays_per_update": rays,
+           "unique_triangles": int(sum(w.scene.unique_triangle_count for w in ws)),
+           "ms_per_update": t, "value": rays / (t * 1e-3) / 1e9, "unit": "Grays/s",
+           "completion_ms_p50": float(np.percentile(comp, 50)), "completion_ms_p99": float(np.percentile(comp, 99)),
+           "tuning": tuning, "autotune_s": tune_s, "graph": True,
+           "one_by_one_ms": float(np.median(seq)), "speedup_vs_one_by_one": float(np.median(seq)) / t}
+    b.close()
+    for c in ctxs:
+        c.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -252,6 +323,8 @@ def main():
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--cpu-probes", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", default=None, choices=["batching"],
+                    help="run one sub-measurement alone and print it")
     ap.add_argument("--profile", action="store_true",
                     help="profiling target: scene build, then two BF16 wavefront updates and two FP32 ones, no timing")
     args = ap.parse_args()
@@ -288,6 +361,9 @@ def main():
         return
 
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    if args.only == "batching":
+        print(json.dumps({"batching": measure_batching(stream, args.steps, args.warmup, flush)}), flush=True)
+        return
     forms = {}
     sampler = ClockSampler(local)
     sampler.start()
@@ -366,6 +442,7 @@ def main():
                     "h2d_bytes_per_step": R * 20, "d2h_bytes_per_step": int(host_c.nbytes + host_d.nbytes)}}
     ctx.close()
     line["differentiation"] = measure_differentiation(stream)
+    line["batching"] = measure_batching(stream, args.steps, args.warmup, flush)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_probes)
     if rank == 0:

@@ -323,6 +323,60 @@ ddgi_status ddgi_forward_record(ddgi_ctx* ctx, uint32_t K, const float* orientat
 ddgi_status ddgi_backward(ddgi_ctx* ctx, const float* dL_dcolor, size_t bytes, float* grad_albedo, float grad_sun[3],
                           float grad_sky[3], ddgi_stream stream);
 
+/* ---- Batched update of many probe volumes ------------------------------
+ * No single counterpart in the reference, which updates one IrradianceProbes
+ * volume per call (src/IrradianceProbes.cpp:426-594); a batch runs that
+ * update for several contexts ("volumes") at once.  Each volume keeps its own
+ * grid, scene, light, precision and atlases.  One update of the batch is:
+ * one persistent work-queue traversal launch over the primary rays of every
+ * volume, one shading launch, one persistent shadow-ray launch, and one blend
+ * launch per precision (FP32 SIMT, BF16 tensor core), captured once into a
+ * CUDA graph and replayed per update.  The result of every volume equals
+ * ddgi_update of that volume alone over all its probes.
+ *
+ * ddgi_batch_create copies the volumes' acceleration structures into one
+ * node/triangle/instance arena, so every volume needs a built scene at that
+ * point and a scene rebuilt later needs a new batch (ddgi_batch_update then
+ * returns DDGI_ERR_INVALID_ARGUMENT); light and material changes reach the
+ * next update.  Ray records and hit records of the volumes are not written by
+ * batch updates.  A batch borrows its contexts: destroy it first. */
+typedef struct ddgi_batch ddgi_batch;
+
+/* Launch parameters of a batch (ddgi_batch_autotune picks them). */
+typedef struct ddgi_batch_tuning {
+    uint32_t trace_ctas_per_sm; /* persistent traversal CTAs per SM; 0 = as many as fit */
+    uint32_t refill_lanes;      /* a warp requests new rays once this many lanes are idle (1..32) */
+    uint32_t smem_stack;        /* traversal-stack entries per thread in shared memory, deeper ones
+                                   in local memory; 0 = the whole stack in shared memory */
+    uint32_t blend_threads;     /* threads per probe of the FP32 blend (32..256, multiple of 32) */
+} ddgi_batch_tuning;
+
+ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_stream stream, ddgi_batch** out);
+ddgi_status ddgi_batch_destroy(ddgi_batch* batch);
+const char* ddgi_batch_last_error(const ddgi_batch* batch);
+/* Primary rays of one batch update (sum over the volumes of probes x rays). */
+uint64_t ddgi_batch_ray_count(const ddgi_batch* batch);
+ddgi_status ddgi_batch_get_tuning(const ddgi_batch* batch, ddgi_batch_tuning* out);
+ddgi_status ddgi_batch_set_tuning(ddgi_batch* batch, const ddgi_batch_tuning* tuning);
+/* Graph replay (default, enable = 1) or plain stream launches (0). */
+ddgi_status ddgi_batch_use_graph(ddgi_batch* batch, int enable);
+/* One update of every volume; `orientations` = count x 9 row-major ray-set
+ * rotations, one per volume.  Waits for the previous batch update's inputs to
+ * be consumed, then enqueues on `stream` and returns. */
+ddgi_status ddgi_batch_update(ddgi_batch* batch, const float* orientations, ddgi_stream stream);
+/* Waits for `stream` (poll, timeout_ms < 0 = forever), then checks the
+ * batch's device error word. */
+ddgi_status ddgi_batch_synchronize(ddgi_batch* batch, ddgi_stream stream, int timeout_ms);
+/* After a synchronised update: per volume, milliseconds from the start of
+ * the update to the end of the volume's last blend work item. */
+ddgi_status ddgi_batch_completion_ms(ddgi_batch* batch, float* ms, uint32_t count);
+/* Times candidate tunings on updates with the given orientations (`reps`
+ * timed updates each, coordinate descent over the four parameters), keeps
+ * the fastest and writes it to *chosen (may be NULL).  The volumes' atlases,
+ * accumulators and probe states are restored afterwards.  Synchronous. */
+ddgi_status ddgi_batch_autotune(ddgi_batch* batch, const float* orientations, uint32_t reps, ddgi_stream stream,
+                                ddgi_batch_tuning* chosen);
+
 /* Waits for `stream` with a timeout (poll), then checks the device error word.
  * timeout_ms < 0 waits forever. */
 ddgi_status ddgi_synchronize(ddgi_ctx* ctx, ddgi_stream stream, int timeout_ms);

@@ -112,6 +112,15 @@ class Timings(C.Structure):
                 ("copy_ms", C.c_float), ("primary_ms", C.c_float)]
 
 
+class BatchTuning(C.Structure):
+    """ddgi_batch_tuning: launch parameters of a batch."""
+    _fields_ = [("trace_ctas_per_sm", C.c_uint32), ("refill_lanes", C.c_uint32), ("smem_stack", C.c_uint32),
+                ("blend_threads", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
 PIPELINE_FUSED = 0
 PIPELINE_WAVEFRONT = 1
 

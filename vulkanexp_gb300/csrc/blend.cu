@@ -35,9 +35,10 @@ __device__ __forceinline__ int4 border_entry(int e, int n) {
     return make_int4(j, n - 1, n - 1 - j, n - 2);
 }
 
-__global__ void __launch_bounds__(256) k_blend_fp32(DeviceGrid g, const uint32_t* __restrict__ probe_list,
-                                                    const float4* __restrict__ rays, const float4* __restrict__ dirs,
-                                                    uint32_t* states, float4* color, float2* depth) {
+// Blend of one probe by the whole block: `pr` = its R ray records.
+__device__ __forceinline__ void blend_probe_fp32(const DeviceGrid& g, uint32_t probe, const float4* __restrict__ pr,
+                                                 const float4* __restrict__ dirs, uint32_t* states, float4* color,
+                                                 float2* depth) {
     extern __shared__ float4 smem[];
     const uint32_t R = g.rays;
     float4* s_rays = smem;
@@ -45,9 +46,6 @@ __global__ void __launch_bounds__(256) k_blend_fp32(DeviceGrid g, const uint32_t
     __shared__ uint32_t s_max_change;
     __shared__ uint32_t s_out_of_range;
 
-    const uint32_t slot = blockIdx.x;
-    const uint32_t probe = probe_list ? probe_list[slot] : slot;
-    const float4* pr = rays + (size_t)slot * R;
     if (threadIdx.x == 0) {
         s_max_change = 0u;
         s_out_of_range = 0u;
@@ -154,6 +152,38 @@ __global__ void __launch_bounds__(256) k_blend_fp32(DeviceGrid g, const uint32_t
     }
 }
 
+__global__ void __launch_bounds__(256) k_blend_fp32(DeviceGrid g, const uint32_t* __restrict__ probe_list,
+                                                    const float4* __restrict__ rays, const float4* __restrict__ dirs,
+                                                    uint32_t* states, float4* color, float2* depth) {
+    const uint32_t slot = blockIdx.x;
+    const uint32_t probe = probe_list ? probe_list[slot] : slot;
+    blend_probe_fp32(g, probe, rays + (size_t)slot * g.rays, dirs, states, color, depth);
+}
+
+// Batched form: block b blends probe (b - tile_base[i]) of volume list[i];
+// the block that finishes a volume's last probe stamps its completion time.
+__global__ void __launch_bounds__(256) k_batch_blend_fp32(BatchTables bt, BatchBlendList bl,
+                                                          const float4* __restrict__ rays) {
+    uint32_t lo = 0, hi = bl.n;  // tile_base[lo] <= b < tile_base[hi]
+    const uint32_t b = blockIdx.x;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(bl.tile_base + mid) <= b) lo = mid;
+        else hi = mid;
+    }
+    const uint32_t v = __ldg(bl.list + lo);
+    const BatchVolume& vol = bt.vols[v];
+    const uint32_t probe = b - __ldg(bl.tile_base + lo);
+    blend_probe_fp32(vol.g, probe, rays + vol.ray_base + (size_t)probe * vol.g.rays, bt.dirs + vol.dir_base,
+                     vol.states, static_cast<float4*>(vol.color), static_cast<float2*>(vol.depth));
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const uint32_t items = __ldg(bl.tile_base + lo + 1) - __ldg(bl.tile_base + lo);
+        if (atomicAdd(bt.done + v, 1u) == items - 1u) bt.clock[1 + v] = globaltimer_ns();
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_blend_fp32(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
@@ -161,6 +191,15 @@ cudaError_t launch_blend_fp32(const DeviceGrid& g, const uint32_t* probe_list, u
     if (nprobes == 0) return cudaSuccess;
     size_t smem = sizeof(float4) * 2 * g.rays;
     k_blend_fp32<<<nprobes, 256, smem, st>>>(g, probe_list, rays, dirs, states, color, depth);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_blend_fp32(const BatchTables& bt, const BatchBlendList& bl, uint32_t max_rays,
+                                    const float4* rays, uint32_t threads, cudaStream_t st) {
+    if (bl.ntiles == 0) return cudaSuccess;
+    threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads / 32 * 32);
+    size_t smem = sizeof(float4) * 2 * max_rays;
+    k_batch_blend_fp32<<<bl.ntiles, threads, smem, st>>>(bt, bl, rays);
     return cudaGetLastError();
 }
 

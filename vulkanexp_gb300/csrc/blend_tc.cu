@@ -46,6 +46,10 @@ constexpr uint32_t kSBO = (kKChunk / 8) * 128;  // bytes between 8-row groups
 constexpr uint32_t kLBO = 128;                  // bytes between K-adjacent core matrices
 constexpr uint32_t kDepthCol = 256;             // TMEM column of the depth accumulator
 constexpr uint32_t kTmemCols = 512;
+// Every CTA allocates all 512 tensor-memory columns of its SM, so no two
+// CTAs may share an SM: the shared-memory request is at least this much
+// (two of them exceed the SM's 228 KB).
+constexpr size_t kMinSmem = 120 * 1024;
 
 struct TcArgs {
     DeviceGrid g;
@@ -101,10 +105,11 @@ __device__ __forceinline__ uint2 float4_to_half4(float a, float b, float c, floa
     return make_uint2(*reinterpret_cast<uint32_t*>(&x), *reinterpret_cast<uint32_t*>(&y));
 }
 
-// Weight matrices of one update in the B-operand layout, plus row sums.
-__global__ void k_tc_weights(const float4* dirs, uint32_t R, uint32_t nc, uint32_t nd, float sharp, uint32_t Nc,
-                             uint32_t Nd, uint32_t nchunks, uint8_t* wout, float* rowsum) {
-    uint32_t row = blockIdx.x * blockDim.x + threadIdx.x;
+// Row `row` of the weight matrices of one update in the B-operand layout
+// (depth rows first, then colour rows), plus its row sum.
+__device__ __forceinline__ void tc_weight_row(uint32_t row, const float4* dirs, uint32_t R, uint32_t nc, uint32_t nd,
+                                              float sharp, uint32_t Nc, uint32_t Nd, uint32_t nchunks, uint8_t* wout,
+                                              float* rowsum) {
     if (row >= Nd + Nc) return;
     const bool colour = row >= Nd;
     const uint32_t t = colour ? row - Nd : row;
@@ -136,7 +141,13 @@ __global__ void k_tc_weights(const float4* dirs, uint32_t R, uint32_t nc, uint32
     rowsum[row] = sum;
 }
 
-__global__ void __launch_bounds__(kThreads) k_blend_tc(TcArgs a) {
+__global__ void k_tc_weights(const float4* dirs, uint32_t R, uint32_t nc, uint32_t nd, float sharp, uint32_t Nc,
+                             uint32_t Nd, uint32_t nchunks, uint8_t* wout, float* rowsum) {
+    tc_weight_row(blockIdx.x * blockDim.x + threadIdx.x, dirs, R, nc, nd, sharp, Nc, Nd, nchunks, wout, rowsum);
+}
+
+// Blend of the 32-probe tile starting at probe slot p0 by the whole CTA.
+__device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0) {
     extern __shared__ __align__(1024) uint8_t smem[];
     // A operands (128 x 64 BF16 = 16 KB each): colour hi/lo, depth hi/lo;
     // then B: high parts of (Nd + Nc) x 64, then the remainders
@@ -151,7 +162,6 @@ __global__ void __launch_bounds__(kThreads) k_blend_tc(TcArgs a) {
     __shared__ uint32_t s_oor[kTileProbes], s_maxc[kTileProbes];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t p0 = blockIdx.x * kTileProbes;
     const uint32_t np = min((uint32_t)kTileProbes, a.nprobes - p0);
     const uint32_t R = a.g.rays;
     const float cell = a.g.cell_len;
@@ -416,6 +426,88 @@ __global__ void __launch_bounds__(kThreads) k_blend_tc(TcArgs a) {
     }
 }
 
+__global__ void __launch_bounds__(kThreads) k_blend_tc(TcArgs a) { blend_tc_tile(a, blockIdx.x * kTileProbes); }
+
+// Interior sides, padded texel counts and ray chunks of a grid.
+struct TcShape {
+    uint32_t nc, nd, Nc, Nd, nchunks;
+};
+__host__ __device__ __forceinline__ TcShape tc_shape(const DeviceGrid& g) {
+    TcShape t;
+    t.nc = g.color_res - 2;
+    t.nd = g.depth_res - 2;
+    t.Nc = (t.nc * t.nc + 15) / 16 * 16;
+    t.Nd = (t.nd * t.nd + 15) / 16 * 16;
+    t.nchunks = (g.rays + kKChunk - 1) / kKChunk;
+    return t;
+}
+
+// Batched weights: blockIdx.y picks the volume of the list.
+__global__ void k_batch_tc_weights(BatchTables bt, BatchBlendList bl) {
+    const BatchVolume& vol = bt.vols[__ldg(bl.list + blockIdx.y)];
+    const TcShape t = tc_shape(vol.g);
+    tc_weight_row(blockIdx.x * blockDim.x + threadIdx.x, bt.dirs + vol.dir_base, vol.g.rays, t.nc, t.nd, vol.g.sharp,
+                  t.Nc, t.Nd, t.nchunks, vol.wbuf, vol.rowsum);
+}
+
+// Batched blend: CTA b takes tile (b - tile_base[i]) of volume list[i]; the
+// CTA that finishes a volume's last tile stamps its completion time.
+__global__ void __launch_bounds__(kThreads) k_batch_blend_tc(BatchTables bt, BatchBlendList bl,
+                                                             const float4* __restrict__ rays) {
+    __shared__ TcArgs s_args;
+    __shared__ uint32_t s_v, s_tile, s_items;
+    if (threadIdx.x == 0) {
+        uint32_t lo = 0, hi = bl.n;  // tile_base[lo] <= b < tile_base[hi]
+        const uint32_t b = blockIdx.x;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(bl.tile_base + mid) <= b) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t v = __ldg(bl.list + lo);
+        const BatchVolume& vol = bt.vols[v];
+        const TcShape t = tc_shape(vol.g);
+        TcArgs& a = s_args;
+        a.g = vol.g;
+        a.probe_list = nullptr;
+        a.nprobes = (uint32_t)vol.g.res[0] * (uint32_t)vol.g.res[1] * (uint32_t)vol.g.res[2];
+        a.rays = rays + vol.ray_base;
+        a.wchunks = reinterpret_cast<const uint4*>(vol.wbuf);
+        a.rowsum = vol.rowsum;
+        a.nc = t.nc;
+        a.nd = t.nd;
+        a.Nc = t.Nc;
+        a.Nd = t.Nd;
+        a.nchunks = t.nchunks;
+        a.states = vol.states;
+        a.color = static_cast<uint2*>(vol.color);
+        a.depth = static_cast<uint32_t*>(vol.depth);
+        a.acc_color = vol.acc_color;
+        a.acc_depth = vol.acc_depth;
+        a.err = bt.err;
+        s_v = v;
+        s_tile = b - __ldg(bl.tile_base + lo);
+        s_items = __ldg(bl.tile_base + lo + 1) - __ldg(bl.tile_base + lo);
+    }
+    __syncthreads();
+    blend_tc_tile(s_args, s_tile * kTileProbes);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(bt.done + s_v, 1u) == s_items - 1u) bt.clock[1 + s_v] = globaltimer_ns();
+    }
+}
+
+cudaError_t set_tc_smem_limit() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_blend_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch_blend_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
 }  // namespace
 
 size_t tc_weight_bytes(uint32_t rays, uint32_t color_res, uint32_t depth_res) {
@@ -460,14 +552,40 @@ cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uin
     size_t stage = 65536 + 2 * (size_t)(Nd + Nc) * 128;
     size_t staging = (size_t)kTileProbes * (nc * nc * 3 + nd * nd * 2) * sizeof(float);
     size_t smem = stage > staging ? stage : staging;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_blend_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    if (smem < kMinSmem) smem = kMinSmem;
+    cudaError_t e = set_tc_smem_limit();
+    if (e != cudaSuccess) return e;
     uint32_t blocks = (nprobes + kTileProbes - 1) / kTileProbes;
     k_blend_tc<<<blocks, kThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+uint32_t tc_tiles(uint32_t nprobes) { return (nprobes + kTileProbes - 1) / kTileProbes; }
+
+cudaError_t prepare_batch_kernels() { return set_tc_smem_limit(); }
+
+size_t batch_tc_smem(uint32_t color_res, uint32_t depth_res) {
+    const uint32_t nc = color_res - 2, nd = depth_res - 2;
+    const uint32_t Nc = (nc * nc + 15) / 16 * 16, Nd = (nd * nd + 15) / 16 * 16;
+    size_t stage = 65536 + 2 * (size_t)(Nd + Nc) * 128;
+    size_t staging = (size_t)kTileProbes * (nc * nc * 3 + nd * nd * 2) * sizeof(float);
+    size_t smem = stage > staging ? stage : staging;
+    return smem < kMinSmem ? kMinSmem : smem;
+}
+
+cudaError_t launch_batch_tc_weights(const BatchTables& bt, const BatchBlendList& bl, uint32_t max_rows,
+                                    cudaStream_t st) {
+    if (bl.n == 0) return cudaSuccess;
+    k_batch_tc_weights<<<dim3((max_rows + 127) / 128, bl.n), 128, 0, st>>>(bt, bl);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_blend_tc(const BatchTables& bt, const BatchBlendList& bl, const float4* rays, size_t smem,
+                                  cudaStream_t st) {
+    if (bl.ntiles == 0) return cudaSuccess;
+    cudaError_t e = set_tc_smem_limit();
+    if (e != cudaSuccess) return e;
+    k_batch_blend_tc<<<bl.ntiles, kThreads, smem, st>>>(bt, bl, rays);
     return cudaGetLastError();
 }
 

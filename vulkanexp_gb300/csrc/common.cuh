@@ -29,6 +29,13 @@ __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t code) {
     if (err) atomicCAS(err, 0u, code);
 }
 
+// Device wall clock in nanoseconds (for per-volume completion stamps).
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // ---------------------------------------------------------------------------
 // Acceleration-structure records (16-byte vectorised)
 // ---------------------------------------------------------------------------

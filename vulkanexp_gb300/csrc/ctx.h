@@ -1,0 +1,130 @@
+// ctx.h — the context behind the opaque ddgi_ctx handle (internal; shared
+// by the translation units that implement the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/ddgi.h"
+#include "common.cuh"
+
+namespace ddgi {
+
+constexpr int kBlasLeafMax = 4;
+constexpr int kTlasLeafMax = 1;
+// deepest traversal stack of the wavefront kernels (entries per thread in
+// shared memory: 96 x 128 threads x 4 bytes = 48 KB per block)
+constexpr int kMaxStack = 96;
+
+struct SceneBuffers {
+    BvhNode* nodes = nullptr;
+    BvhTri* tris = nullptr;
+    GpuInstance* inst_leaf = nullptr;
+    GpuInstance* inst_id = nullptr;
+    float4* normals = nullptr;
+    uint32_t* indices = nullptr;
+    ddgi_offset_entry* offsets = nullptr;
+    ddgi_material* materials = nullptr;
+    int32_t tlas_root = -1;
+    int stack_cap = 0;
+    uint32_t depth_blas = 0, depth_tlas = 0;
+    uint32_t vertex_count = 0, index_count = 0, offset_count = 0, material_count = 0, instance_count = 0;
+    uint64_t node_count = 0, tri_count = 0;
+    uint64_t build_id = 0;  // distinct for every successful build in the process
+    bool built = false;
+};
+
+}  // namespace ddgi
+
+struct ddgi_ctx {
+    ddgi_grid_desc grid{};
+    ddgi::DeviceGrid dg{};
+    ddgi::DeviceLight dl{};
+    int device = 0;
+    bool fp16 = false;
+    void* color = nullptr;
+    void* depth = nullptr;
+    uint32_t* states = nullptr;
+    float4* rays = nullptr;
+    size_t rays_cap = 0;  // in records
+    // wavefront pipeline: hit buffer, shadow-ray queue, work counters
+    float4* wave_thit = nullptr;
+    uint32_t* wave_prim = nullptr;
+    uint32_t* q_idx = nullptr;
+    float4* q_pos = nullptr;
+    float4* q_sun = nullptr;
+    uint32_t* counters = nullptr;
+    ddgi_pipeline pipeline = DDGI_PIPELINE_WAVEFRONT;
+    // BF16 tensor-core blend: per-update weight matrices and their row sums
+    uint8_t* tc_weights = nullptr;
+    float* tc_rowsum = nullptr;
+    // BF16 form: FP32 hysteresis accumulators behind the FP16 atlas
+    float4* acc_color = nullptr;
+    float2* acc_depth = nullptr;
+    // differentiation: recorded hits of K updates, atlas checkpoints, and the
+    // reverse-pass buffers
+    uint32_t rec_K = 0, rec_C = 0;
+    size_t rec_cap = 0;  // rays per update the record buffers hold
+    uint32_t rec_updates_cap = 0;
+    std::vector<float> rec_orient;
+    float4* rec_thit = nullptr;
+    uint32_t* rec_prim = nullptr;
+    float4* ckpt_color = nullptr;
+    float2* ckpt_depth = nullptr;
+    uint32_t ckpt_cap = 0;
+    uint32_t* rec_states = nullptr;
+    uint32_t* work_states = nullptr;
+    float4* work_color = nullptr;
+    float2* work_depth = nullptr;
+    float4* g_a = nullptr;
+    float4* g_b = nullptr;
+    float4* g_x = nullptr;
+    double* d_grad = nullptr;
+    uint32_t grad_cap = 0;
+    ddgi_hit* hits = nullptr;
+    size_t hits_cap = 0;
+    bool record_hits = false;
+    float4* dirs = nullptr;
+    uint32_t* ray_order = nullptr;
+    uint32_t* probe_list = nullptr;
+    uint32_t* err = nullptr;
+    uint32_t last_count = 0;
+    uint32_t last_rays = 0;
+    std::vector<float> host_dirs;
+    std::vector<uint32_t> host_order;
+    ddgi::SceneBuffers scene;
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool timing_pending = false;
+    ddgi_timings timings{};
+    char msg[512] = "";
+};
+
+
+namespace ddgi {
+
+// Traversal view of a context's scene buffers.
+inline DeviceScene device_scene(const ddgi_ctx* c) {
+    DeviceScene s{};
+    s.nodes = c->scene.nodes;
+    s.tris = c->scene.tris;
+    s.instances = c->scene.inst_leaf;
+    s.instances_by_id = c->scene.inst_id;
+    s.normals = c->scene.normals;
+    s.indices = c->scene.indices;
+    s.offsets = c->scene.offsets;
+    s.materials = c->scene.materials;
+    s.tlas_root = c->scene.tlas_root;
+    s.vertex_count = c->scene.vertex_count;
+    s.index_count = c->scene.index_count;
+    s.offset_count = c->scene.offset_count;
+    s.material_count = c->scene.material_count;
+    s.node_count = (uint32_t)c->scene.node_count;
+    s.tri_count = (uint32_t)c->scene.tri_count;
+    s.instance_count = c->scene.instance_count;
+    return s;
+}
+
+}  // namespace ddgi

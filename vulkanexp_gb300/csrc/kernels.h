@@ -36,6 +36,73 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
                              ddgi_hit* hits_out, int stack_cap, uint32_t* err, cudaStream_t st,
                              cudaEvent_t after_primary);
 
+// ---------------------------------------------------------------------------
+// Batched update of many probe volumes (batch.cu drives these launchers)
+// ---------------------------------------------------------------------------
+constexpr uint32_t kMaxBatchVolumes = 1024;
+
+// One volume of a batch.  `sc` points at the volume's own shading data;
+// traversal runs over the batch arena, where the volume's trees start at
+// `root`.  Ray records of the volume are [ray_base, ray_base + P * R) of the
+// batch buffers; its direction table and ray order start at dir_base.
+struct BatchVolume {
+    DeviceScene sc;
+    DeviceGrid g;
+    DeviceLight L;
+    int32_t root;
+    uint32_t fp16;  // BF16 form: FP16 atlas + FP32 accumulators, tensor-core blend
+    uint32_t ray_base, dir_base;
+    uint32_t* states;
+    void* color;
+    void* depth;
+    float4* acc_color;
+    float2* acc_depth;
+    uint8_t* wbuf;  // tensor-core weight chunks of this update (BF16 form)
+    float* rowsum;
+};
+
+struct BatchTables {
+    const BatchVolume* vols;
+    uint32_t nvol;
+    const uint32_t* ray_base;  // nvol + 1 record offsets
+    const float4* dirs;
+    const uint32_t* ray_order;
+    unsigned long long* clock;  // [0] batch start, [1 + v] blend completion of volume v (ns, globaltimer)
+    uint32_t* done;             // blend work items finished, per volume
+    uint32_t* err;
+};
+
+// Volumes one blend kernel covers: list[i] is a volume index, its work items
+// are [tile_base[i], tile_base[i + 1]).
+struct BatchBlendList {
+    const uint32_t* list;
+    const uint32_t* tile_base;
+    uint32_t n, ntiles;
+};
+
+struct TraceTuning {
+    uint32_t ctas_per_sm;  // 0: occupancy limit
+    uint32_t refill;       // idle lanes that trigger a warp's work request
+    uint32_t split;        // stack entries in shared memory (>= cap: all)
+};
+
+// wavefront.cu: primary trace, shading and shadow rays of all volumes
+cudaError_t launch_batch_trace(const DeviceScene& arena, const BatchTables& bt, uint32_t total, WaveHits hits,
+                               ShadowQueue q, uint32_t* counters, float4* rays_out, int stack_cap,
+                               const TraceTuning& tune, cudaStream_t st, cudaEvent_t after_primary,
+                               cudaEvent_t after_shade);
+// blend.cu
+cudaError_t launch_batch_blend_fp32(const BatchTables& bt, const BatchBlendList& bl, uint32_t max_rays,
+                                    const float4* rays, uint32_t threads, cudaStream_t st);
+// blend_tc.cu
+cudaError_t launch_batch_tc_weights(const BatchTables& bt, const BatchBlendList& bl, uint32_t max_rows,
+                                    cudaStream_t st);
+size_t batch_tc_smem(uint32_t color_res, uint32_t depth_res);
+uint32_t tc_tiles(uint32_t nprobes);  // tensor-core blend work items of a volume
+cudaError_t prepare_batch_kernels();  // kernel attributes, set once before any graph capture
+cudaError_t launch_batch_blend_tc(const BatchTables& bt, const BatchBlendList& bl, const float4* rays, size_t smem,
+                                  cudaStream_t st);
+
 // adjoint.cu
 cudaError_t launch_replay_update(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L, const float4* dirs,
                                  uint32_t* states, float4* color, float2* depth, const float4* thit,

@@ -171,13 +171,32 @@ __device__ __forceinline__ bool traverse(const DeviceScene& sc, float3 wo, float
 struct SmemStack {
     int* base;
     int stride;
-    __device__ __forceinline__ int& at(int i) const { return base[i * stride]; }
+    __device__ __forceinline__ int get(int i) const { return base[i * stride]; }
+    __device__ __forceinline__ void set(int i, int v) { base[i * stride] = v; }
 };
 
-template <bool ANY>
+// The first `split` entries in shared memory, deeper ones in a per-thread
+// local-memory array (L1-cached).  A smaller shared-memory part lets more
+// warps reside per SM; traversals deeper than `split` pay local accesses.
+// The local part is an array of the caller's (kSpillMax entries), kept out of
+// the walker so that the walker's own fields stay in registers.
+constexpr int kSpillMax = 96;
+struct SplitStack {
+    int* base;
+    int stride;
+    int split;
+    int* spill;
+    __device__ __forceinline__ int get(int i) const { return i < split ? base[i * stride] : spill[i - split]; }
+    __device__ __forceinline__ void set(int i, int v) {
+        if (i < split) base[i * stride] = v;
+        else spill[i - split] = v;
+    }
+};
+
+template <bool ANY, class Stack = SmemStack>
 struct WarpWalker {
     Ray wr, r;  // world ray, current ray (world or object space)
-    SmemStack stk;
+    Stack stk;
     int sp, cap, ref;
     bool in_blas;
     uint32_t inst_id, steps, max_steps, mask;
@@ -186,6 +205,11 @@ struct WarpWalker {
 
     __device__ __forceinline__ bool start(const DeviceScene& sc, float3 o, float3 d, float tmin_, float tmax_,
                                           uint32_t mask_) {
+        return start_at(sc, sc.tlas_root, o, d, tmin_, tmax_, mask_);
+    }
+    // Start at an explicit top-level root (several scenes in one node arena).
+    __device__ __forceinline__ bool start_at(const DeviceScene& sc, int32_t root, float3 o, float3 d, float tmin_,
+                                             float tmax_, uint32_t mask_) {
         ray_setup(wr, o, d);
         r = wr;
         tmin = tmin_;
@@ -201,7 +225,7 @@ struct WarpWalker {
         inst_id = 0;
         steps = 0;
         max_steps = 4u * (sc.node_count + sc.tri_count + sc.instance_count) + 64u;
-        ref = sc.tlas_root >= 0 ? sc.tlas_root : kNone;
+        ref = root >= 0 ? root : kNone;
         return ref != kNone;
     }
 
@@ -210,22 +234,22 @@ struct WarpWalker {
             raise_error(err, DEV_STACK_OVERFLOW);
             return false;
         }
-        stk.at(sp++) = v;
+        stk.set(sp++, v);
         return true;
     }
     // pop within the current tree level (stops at an EXIT marker)
     __device__ __forceinline__ void pop_level() {
-        if (sp == 0 || stk.at(sp - 1) == kExit) {
+        if (sp == 0 || stk.get(sp - 1) == kExit) {
             ref = kNone;
             return;
         }
-        ref = stk.at(--sp);
+        ref = stk.get(--sp);
     }
     // pop across EXIT markers (restoring the world ray); false when empty
     __device__ __forceinline__ bool pop() {
         for (;;) {
             if (sp == 0) return false;
-            ref = stk.at(--sp);
+            ref = stk.get(--sp);
             if (ref != kExit) return true;
             in_blas = false;
             r = wr;

@@ -34,8 +34,8 @@ struct PrimaryJob {
     WaveHits hits;
     uint32_t total;
 
-    __device__ __forceinline__ bool start(WarpWalker<false>& w, const DeviceScene& sc, uint32_t id,
-                                          uint32_t* out) const {
+    template <class W>
+    __device__ __forceinline__ bool start(W& w, const DeviceScene& sc, uint32_t id, uint32_t* out) const {
         uint32_t R = g.rays;
         uint32_t slot = id / R, j = id - slot * R;
         uint32_t ray = __ldg(ray_order + j);
@@ -44,7 +44,8 @@ struct PrimaryJob {
         float4 d4 = __ldg(dirs + ray);
         return w.start(sc, probe_origin_exact(g, probe), f3(d4.x, d4.y, d4.z), 0.01f, g.tmax, 0x3u);
     }
-    __device__ __forceinline__ void finish(const WarpWalker<false>& w, uint32_t out) const {
+    template <class W>
+    __device__ __forceinline__ void finish(const W& w, uint32_t out) const {
         const HitRec& h = w.best;
         hits.thit[out] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.inst));
         hits.prim[out] = h.prim | (h.back ? 0x80000000u : 0u);
@@ -58,13 +59,14 @@ struct ShadowJob {
     uint32_t* prim;  // hit words: bit 30 marks a shadowed front hit (kept for replays)
     uint32_t total;
 
-    __device__ __forceinline__ bool start(WarpWalker<true>& w, const DeviceScene& sc, uint32_t id,
-                                          uint32_t* out) const {
+    template <class W>
+    __device__ __forceinline__ bool start(W& w, const DeviceScene& sc, uint32_t id, uint32_t* out) const {
         *out = id;
         float4 p = q.pos[id];
         return w.start(sc, f3(p.x, p.y, p.z), dir, 0.1f, 10000.0f, 0xFFu);
     }
-    __device__ __forceinline__ void finish(const WarpWalker<true>& w, uint32_t id) const {
+    template <class W>
+    __device__ __forceinline__ void finish(const W& w, uint32_t id) const {
         uint32_t idx = q.idx[id];
         if (w.best.inst != kNoHit) {  // shadowed: the record keeps the base colour
             prim[idx] |= 1u << 30;
@@ -77,19 +79,39 @@ struct ShadowJob {
     }
 };
 
+__device__ __forceinline__ void init_stack(SmemStack& s, int* base, int stride, int, int*) {
+    s.base = base;
+    s.stride = stride;
+}
+__device__ __forceinline__ void init_stack(SplitStack& s, int* base, int stride, int split, int* spill) {
+    s.base = base;
+    s.stride = stride;
+    s.split = split;
+    s.spill = spill;
+}
+template <class Stack>
+struct SpillArea {  // local-memory tail of a SplitStack
+    __device__ __forceinline__ int* ptr() { return nullptr; }
+};
+template <>
+struct SpillArea<SplitStack> {
+    int a[kSpillMax];
+    __device__ __forceinline__ int* ptr() { return a; }
+};
+
 // Persistent traversal loop with per-lane refill.  A warp refills when at
-// least `kRefill` of its lanes are idle (or all are), taking as many rays as
+// least `refill` of its lanes are idle (or all are), taking as many rays as
 // it has idle lanes with one atomic.
-template <bool ANY, class Job>
+template <bool ANY, class Stack, class Job>
 __device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job& job, uint32_t total,
-                                                uint32_t* counter, int stack_cap, uint32_t* err) {
-    constexpr int kRefill = 8;
+                                                uint32_t* counter, int stack_cap, int split, int refill,
+                                                uint32_t* err) {
     extern __shared__ int s_stack[];
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    WarpWalker<ANY> w;
-    w.stk.base = s_stack + threadIdx.x;
-    w.stk.stride = blockDim.x;
+    SpillArea<Stack> spill;
+    WarpWalker<ANY, Stack> w;
+    init_stack(w.stk, s_stack + threadIdx.x, blockDim.x, split, spill.ptr());
     w.cap = stack_cap;
     w.ref = kNone;
     bool active = false, exhausted = false;
@@ -97,7 +119,7 @@ __device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job
     for (;;) {
         unsigned idle = __ballot_sync(kFull, !active && !exhausted);
         unsigned busy = __ballot_sync(kFull, active);
-        if (idle && (__popc(idle) >= kRefill || busy == 0)) {
+        if (idle && (__popc(idle) >= refill || busy == 0)) {
             int leader = __ffs(idle) - 1;
             uint32_t base = 0;
             if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(idle));
@@ -127,12 +149,12 @@ __device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job
 
 __global__ void __launch_bounds__(kPersistThreads) k_primary(DeviceScene sc, PrimaryJob job, uint32_t* counter,
                                                              int stack_cap, uint32_t* err) {
-    persistent_walk<false>(sc, job, job.total, counter, stack_cap, err);
+    persistent_walk<false, SmemStack>(sc, job, job.total, counter, stack_cap, stack_cap, 8, err);
 }
 
 __global__ void __launch_bounds__(kPersistThreads) k_shadow(DeviceScene sc, ShadowJob job, const uint32_t* qcount,
                                                             uint32_t* counter, int stack_cap, uint32_t* err) {
-    persistent_walk<true>(sc, job, *qcount, counter, stack_cap, err);
+    persistent_walk<true, SmemStack>(sc, job, *qcount, counter, stack_cap, stack_cap, 8, err);
 }
 
 template <class AV>
@@ -191,7 +213,151 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene sc, DeviceGrid g, Dev
     }
 }
 
-uint32_t persistent_blocks(const void* kernel, size_t smem) {
+// ---------------------------------------------------------------------------
+// Batched form: the records of all volumes form one index space; the volume
+// of record `id` is found by binary search of the record offsets.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t batch_volume(const BatchTables& bt, uint32_t id) {
+    uint32_t lo = 0, hi = bt.nvol;  // ray_base[lo] <= id < ray_base[hi]
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(bt.ray_base + mid) <= id) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+struct BatchPrimaryJob {
+    BatchTables bt;
+    WaveHits hits;
+
+    template <class W>
+    __device__ __forceinline__ bool start(W& w, const DeviceScene& sc, uint32_t id, uint32_t* out) const {
+        const uint32_t v = batch_volume(bt, id);
+        const BatchVolume& vol = bt.vols[v];
+        const uint32_t R = vol.g.rays;
+        const uint32_t local = id - __ldg(bt.ray_base + v);
+        const uint32_t slot = local / R, j = local - slot * R;
+        const uint32_t ray = __ldg(bt.ray_order + vol.dir_base + j);
+        *out = id - j + ray;  // record ray_base + slot * R + ray
+        float4 d4 = __ldg(bt.dirs + vol.dir_base + ray);
+        return w.start_at(sc, vol.root, probe_origin_exact(vol.g, slot), f3(d4.x, d4.y, d4.z), 0.01f, vol.g.tmax,
+                          0x3u);
+    }
+    template <class W>
+    __device__ __forceinline__ void finish(const W& w, uint32_t out) const {
+        const HitRec& h = w.best;
+        hits.thit[out] = make_float4(h.t, h.b1, h.b2, __uint_as_float(h.inst));
+        hits.prim[out] = h.prim | (h.back ? 0x80000000u : 0u);
+    }
+};
+
+struct BatchShadowJob {
+    const ShadowQueue q;
+    BatchTables bt;
+    float4* rays;
+    uint32_t* prim;
+
+    template <class W>
+    __device__ __forceinline__ bool start(W& w, const DeviceScene& sc, uint32_t id, uint32_t* out) const {
+        *out = id;
+        float4 p = q.pos[id];
+        uint32_t v = __float_as_uint(p.w);
+        if (v >= bt.nvol) {
+            raise_error(bt.err, DEV_BAD_INDEX);
+            v = 0;
+        }
+        const BatchVolume& vol = bt.vols[v];
+        return w.start_at(sc, vol.root, f3(p.x, p.y, p.z), f3(vol.L.dir[0], vol.L.dir[1], vol.L.dir[2]), 0.1f,
+                          10000.0f, 0xFFu);
+    }
+    template <class W>
+    __device__ __forceinline__ void finish(const W& w, uint32_t id) const {
+        uint32_t idx = q.idx[id];
+        if (w.best.inst != kNoHit) {
+            prim[idx] |= 1u << 30;
+            return;
+        }
+        float4 sun = q.sun[id];
+        float4 rec = rays[idx];
+        float3 c = (f3(rec.x, rec.y, rec.z) + f3(sun.x, sun.y, sun.z)) * sun.w;
+        rays[idx] = make_float4(c.x, c.y, c.z, rec.w);
+    }
+};
+
+template <class Stack>
+__global__ void __launch_bounds__(kPersistThreads, 8) k_batch_primary(DeviceScene arena, BatchPrimaryJob job,
+                                                                   uint32_t total, uint32_t* counter, int stack_cap,
+                                                                   int split, int refill) {
+    persistent_walk<false, Stack>(arena, job, total, counter, stack_cap, split, refill, job.bt.err);
+}
+
+template <class Stack>
+__global__ void __launch_bounds__(kPersistThreads, 8) k_batch_shadow(DeviceScene arena, BatchShadowJob job,
+                                                                  const uint32_t* qcount, uint32_t* counter,
+                                                                  int stack_cap, int split, int refill) {
+    persistent_walk<true, Stack>(arena, job, *qcount, counter, stack_cap, split, refill, job.bt.err);
+}
+
+// Shading of every record of the batch (the per-volume k_shade, with the
+// volume's scene, grid, light, states and atlas looked up per record).
+__global__ void __launch_bounds__(128) k_batch_shade(BatchTables bt, uint32_t total, WaveHits hits,
+                                                     float4* rays_out, ShadowQueue q) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool enqueue = false;
+    SurfaceShade s;
+    uint32_t v = 0;
+    if (i < total) {
+        v = batch_volume(bt, i);
+        const BatchVolume& vol = bt.vols[v];
+        const uint32_t R = vol.g.rays;
+        const uint32_t local = i - __ldg(bt.ray_base + v);
+        const uint32_t slot = local / R, ray = local - slot * R;
+        float4 th = hits.thit[i];
+        uint32_t pb = hits.prim[i];
+        uint32_t inst = __float_as_uint(th.w), prim = pb & 0x0fffffffu;
+        bool back = (pb >> 31) != 0;
+        float4 rec;
+        if (inst == kNoHit) {
+            rec = make_float4(vol.L.sky[0], vol.L.sky[1], vol.L.sky[2], -1.0f);
+        } else if (back) {
+            rec = make_float4(0.0f, 0.0f, 0.0f, th.x * 0.80f);
+        } else {
+            float4 d4 = __ldg(bt.dirs + vol.dir_base + ray);
+            float3 d = f3(d4.x, d4.y, d4.z);
+            float3 o = probe_origin_exact(vol.g, slot);
+            if (vol.fp16) {
+                AtlasView<ColorTexF16, DepthTexF16> at{{static_cast<const uint2*>(vol.color)},
+                                                       {static_cast<const uint32_t*>(vol.depth)}};
+                enqueue = shade_surface(vol.sc, vol.g, vol.L, vol.states, at, o, d, th.x, th.y, th.z, inst, prim, &s,
+                                        bt.err);
+            } else {
+                AtlasView<ColorTexF32, DepthTexF32> at{{static_cast<const float4*>(vol.color)},
+                                                       {static_cast<const float2*>(vol.depth)}};
+                enqueue = shade_surface(vol.sc, vol.g, vol.L, vol.states, at, o, d, th.x, th.y, th.z, inst, prim, &s,
+                                        bt.err);
+            }
+            rec = make_float4(s.base.x, s.base.y, s.base.z, th.x);
+        }
+        rays_out[i] = rec;
+    }
+    unsigned m = __ballot_sync(kFull, enqueue);
+    if (m) {
+        int leader = __ffs(m) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(q.count, (uint32_t)__popc(m));
+        base = __shfl_sync(kFull, base, leader);
+        if (enqueue) {
+            uint32_t k = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+            q.idx[k] = i;
+            q.pos[k] = make_float4(s.position.x, s.position.y, s.position.z, __uint_as_float(v));
+            q.sun[k] = make_float4(s.sun.x, s.sun.y, s.sun.z, s.fade);
+        }
+    }
+}
+
+uint32_t persistent_blocks(const void* kernel, size_t smem, uint32_t cap_per_sm = 0) {
     static int sms = 0;
     if (sms == 0) {
         int dev = 0;
@@ -202,6 +368,7 @@ uint32_t persistent_blocks(const void* kernel, size_t smem) {
     int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kPersistThreads, smem);
     if (per <= 0) per = 1;
+    if (cap_per_sm > 0 && (uint32_t)per > cap_per_sm) per = (int)cap_per_sm;
     return (uint32_t)(sms * per);
 }
 
@@ -241,6 +408,46 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
     k_shadow<<<persistent_blocks((const void*)k_shadow, smem), kPersistThreads, smem, st>>>(
         sc, sj, counters + 1, counters + 2, stack_cap, err);
     return cudaGetLastError();
+}
+
+namespace {
+
+template <class Stack>
+cudaError_t batch_trace_kernels(const DeviceScene& arena, const BatchTables& bt, uint32_t total, WaveHits hits,
+                                ShadowQueue q, uint32_t* counters, float4* rays_out, int stack_cap, int split,
+                                const TraceTuning& tune, cudaStream_t st, cudaEvent_t after_primary,
+                                cudaEvent_t after_shade) {
+    const size_t smem = (size_t)split * kPersistThreads * sizeof(int);
+    const int refill = (int)(tune.refill < 1 ? 1 : (tune.refill > 32 ? 32 : tune.refill));
+    BatchPrimaryJob pj{bt, hits};
+    k_batch_primary<Stack><<<persistent_blocks((const void*)k_batch_primary<Stack>, smem, tune.ctas_per_sm),
+                             kPersistThreads, smem, st>>>(arena, pj, total, counters, stack_cap, split, refill);
+    if (after_primary) cudaEventRecord(after_primary, st);
+    ShadowQueue qq = q;
+    qq.count = counters + 1;
+    k_batch_shade<<<(total + 127) / 128, 128, 0, st>>>(bt, total, hits, rays_out, qq);
+    if (after_shade) cudaEventRecord(after_shade, st);
+    BatchShadowJob sj{qq, bt, rays_out, hits.prim};
+    k_batch_shadow<Stack><<<persistent_blocks((const void*)k_batch_shadow<Stack>, smem, tune.ctas_per_sm),
+                            kPersistThreads, smem, st>>>(arena, sj, counters + 1, counters + 2, stack_cap, split,
+                                                         refill);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// counters[0..2] (primary work, shadow queue length, shadow work) must be
+// zero when the launch sequence starts.
+cudaError_t launch_batch_trace(const DeviceScene& arena, const BatchTables& bt, uint32_t total, WaveHits hits,
+                               ShadowQueue q, uint32_t* counters, float4* rays_out, int stack_cap,
+                               const TraceTuning& tune, cudaStream_t st, cudaEvent_t after_primary,
+                               cudaEvent_t after_shade) {
+    if (total == 0) return cudaSuccess;
+    if (tune.split == 0 || (int)tune.split >= stack_cap)
+        return batch_trace_kernels<SmemStack>(arena, bt, total, hits, q, counters, rays_out, stack_cap, stack_cap,
+                                              tune, st, after_primary, after_shade);
+    return batch_trace_kernels<SplitStack>(arena, bt, total, hits, q, counters, rays_out, stack_cap, (int)tune.split,
+                                           tune, st, after_primary, after_shade);
 }
 
 }  // namespace ddgi

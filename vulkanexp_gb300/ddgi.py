@@ -16,7 +16,7 @@ import os
 import numpy as np
 
 from . import abi
-from .abi import HIT_DTYPE, GridDesc, Light, SceneDesc, Timings
+from .abi import HIT_DTYPE, BatchTuning, GridDesc, Light, SceneDesc, Timings
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libddgi_gb300.so")
@@ -68,6 +68,17 @@ _SIGNATURES = [
     ("ddgi_blend_records_noalloc", C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p]),
+    ("ddgi_batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("ddgi_batch_destroy", C.c_int, [C.c_void_p]),
+    ("ddgi_batch_last_error", C.c_char_p, [C.c_void_p]),
+    ("ddgi_batch_ray_count", C.c_uint64, [C.c_void_p]),
+    ("ddgi_batch_get_tuning", C.c_int, [C.c_void_p, C.POINTER(BatchTuning)]),
+    ("ddgi_batch_set_tuning", C.c_int, [C.c_void_p, C.POINTER(BatchTuning)]),
+    ("ddgi_batch_use_graph", C.c_int, [C.c_void_p, C.c_int]),
+    ("ddgi_batch_update", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ddgi_batch_synchronize", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    ("ddgi_batch_completion_ms", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    ("ddgi_batch_autotune", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(BatchTuning)]),
 ]
 
 
@@ -293,6 +304,82 @@ class Context:
         self._check(self.lib.ddgi_trace_rays(self.h, _ptr(origins), _ptr(dirs), n, tmin, tmax, mask, int(any_hit),
                                              _ptr(hits), _ptr(bary), _stream_ptr(stream)))
         return hits, bary
+
+
+class Batch:
+    """Owns one ddgi_batch over a list of Contexts (which must outlive it)."""
+
+    def __init__(self, contexts, stream=None):
+        self.lib = load_library()
+        self.contexts = list(contexts)
+        arr = (C.c_void_p * len(self.contexts))(*[c.h.value for c in self.contexts])
+        h = C.c_void_p()
+        st = self.lib.ddgi_batch_create(arr, len(self.contexts), _stream_ptr(stream), C.byref(h))
+        if st != 0:
+            raise DDGIError(st, "ddgi_batch_create")
+        self.h = h
+
+    def _check(self, status):
+        if status != 0:
+            raise DDGIError(status, self.lib.ddgi_batch_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ddgi_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def ray_count(self):
+        return int(self.lib.ddgi_batch_ray_count(self.h))
+
+    def tuning(self):
+        t = BatchTuning()
+        self._check(self.lib.ddgi_batch_get_tuning(self.h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        t = BatchTuning()
+        self._check(self.lib.ddgi_batch_get_tuning(self.h, C.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        self._check(self.lib.ddgi_batch_set_tuning(self.h, C.byref(t)))
+
+    def use_graph(self, on=True):
+        self._check(self.lib.ddgi_batch_use_graph(self.h, int(on)))
+
+    def _orients(self, orientations):
+        o = np.ascontiguousarray(orientations, np.float32).reshape(len(self.contexts), 9)
+        return o
+
+    def update(self, orientations, stream=None):
+        o = self._orients(orientations)
+        self._check(self.lib.ddgi_batch_update(self.h, _ptr(o), _stream_ptr(stream)))
+
+    def synchronize(self, stream=None, timeout_ms=-1):
+        self._check(self.lib.ddgi_batch_synchronize(self.h, _stream_ptr(stream), int(timeout_ms)))
+
+    def completion_ms(self):
+        out = np.zeros(len(self.contexts), np.float32)
+        self._check(self.lib.ddgi_batch_completion_ms(self.h, _ptr(out), len(out)))
+        return out
+
+    def autotune(self, orientations, reps=3, stream=None):
+        o = self._orients(orientations)
+        t = BatchTuning()
+        self._check(self.lib.ddgi_batch_autotune(self.h, _ptr(o), int(reps), _stream_ptr(stream), C.byref(t)))
+        return t.as_dict()
 
 
 class IrradianceProbes:

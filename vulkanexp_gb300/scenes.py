@@ -368,6 +368,41 @@ def terrain_workload(seed=1235, resolution=(32, 16, 32), rays=256, updates=10, p
     return Workload("terrain_%dx%dx%d_r%d" % (*resolution, rays), sc, g, default_light(), updates, seed)
 
 
+def batch_workloads(seed=1238, count=48, tri_range=(5000, 300000)):
+    """The batching workload: `count` independent probe volumes of uneven
+    sizes.  Volume v (own PCG64 stream [seed, v]) uses the room or the
+    terrain generator with a unique-triangle count log-uniform in
+    `tri_range`, a probe grid between 4x4x4 and 24x12x24, 64/128/256/512
+    rays per probe, 8/16 or 6/14 atlas tiles and the FP32 or BF16 form."""
+    out = []
+    for v in range(count):
+        rng = np.random.default_rng([int(seed), int(v)])
+        target = float(np.exp(rng.uniform(np.log(tri_range[0]), np.log(tri_range[1]))))
+        kind = "room" if rng.uniform() < 0.5 else "terrain"
+        res = (int(rng.integers(4, 25)), int(rng.integers(4, 13)), int(rng.integers(4, 25)))
+        rays = int(rng.choice([64, 128, 256, 512]))
+        color_res, depth_res = (8, 16) if rng.uniform() < 0.5 else (6, 14)
+        precision = int(rng.integers(0, 2))
+        vseed = int(rng.integers(0, 2 ** 31 - 1))
+        if kind == "room":
+            n_boxes = max(1, int(round((target - 12) / 12)))
+            sc = room_with_boxes(vseed, n_boxes)
+            sc.bounds = (np.zeros(3), np.array([10.0, 6.0, 10.0]))
+        else:
+            cells = max(24, int(round(np.sqrt(target / 4.0))))
+            boxes = max(1, int(round(target / 2.0 / 24.0)))
+            sc = terrain_with_clusters(vseed, n_instances=max(16, int(target) // 2000), n_cluster_meshes=2,
+                                       boxes_per_cluster=boxes, cells=cells, size=cells * 0.5,
+                                       amplitude=4.0)
+        g = fit_grid(sc, res, rays, precision, color_res, depth_res)
+        # room: instanced triangles (one box mesh), terrain: unique triangles
+        tris = sc.triangle_count if kind == "room" else sc.unique_triangle_count
+        name = "%s%d_%dx%dx%d_r%d_%d_%s" % (kind, tris, *res, rays, color_res,
+                                            "bf16" if precision else "fp32")
+        out.append(Workload(name, sc, g, default_light(), 1, vseed))
+    return out
+
+
 def workload(config, seed=None):
     """Workload of a numbered configuration: 0 room (plain FP32, 1 update),
     1 terrain at scale (FP32, 10 updates), 2 terrain with the BF16 blend,
