@@ -323,6 +323,35 @@ ddgi_status ddgi_forward_record(ddgi_ctx* ctx, uint32_t K, const float* orientat
 ddgi_status ddgi_backward(ddgi_ctx* ctx, const float* dL_dcolor, size_t bytes, float* grad_albedo, float grad_sun[3],
                           float grad_sky[3], ddgi_stream stream);
 
+/* ---- Probe classification and adaptive schedule -------------------------
+ * IrradianceProbes::initProbes (src/IrradianceProbes.cpp:357-394,
+ * src/shaders/probesInit.rgen:31-64): classifies every probe from 512 rays
+ * (orientation x spherical-Fibonacci direction i of a raysPerProbe-point set,
+ * i = 0..511, as the shader does), closest hits among instances with mask
+ * bit 0 set, t in [0.01, 1.5 |cell|]: a probe with more than raysPerProbe / 2
+ * back-face hits closer than |cell| becomes OFF (state 0, skipped by the
+ * updates and by the bounce lookup), else a probe with such a hit within one
+ * cell on every axis gets state 1 (refreshed every update), else 8.
+ * Synchronous.  The reference also zeroes the grid hysteresis here for a
+ * host-side ramp; this call leaves the grid unchanged. */
+ddgi_status ddgi_init_probes(ddgi_ctx* ctx, const float orientation[9], ddgi_stream stream);
+/* ddgi_update over the probes selectProbesToUpdate
+ * (src/IrradianceProbes.cpp:396-424) picks, chosen on the device with no
+ * host readback: visiting probes cyclically from where the previous
+ * selection stopped, probe i is refreshed when state s != 0 and
+ * (i + loop) % s == 0 (loop counts the visit's wraps); max_probes > 0 stops
+ * the visit after that many (ProbesPerUpdate), 0 = no cap.  The selection
+ * and the schedule state stay on the device; the trace and blend read the
+ * selected count there.  Asynchronous like ddgi_update; always the wavefront
+ * trace.  Ray/hit records hold the selected probes first, in list order. */
+ddgi_status ddgi_update_scheduled(ddgi_ctx* ctx, const float orientation[9], uint32_t max_probes, ddgi_stream stream);
+/* The last selection (count, list in visit order) and the schedule state
+ * (offset, loop index); any pointer may be NULL.  Synchronous. */
+ddgi_status ddgi_get_schedule(ddgi_ctx* ctx, uint32_t* count, uint32_t* offset, uint32_t* loop, uint32_t* list,
+                              size_t list_capacity, ddgi_stream stream);
+/* Sets the schedule state (a new context starts at offset 0, loop 0). */
+ddgi_status ddgi_set_schedule(ddgi_ctx* ctx, uint32_t offset, uint32_t loop, ddgi_stream stream);
+
 /* ---- Batched update of many probe volumes ------------------------------
  * No single counterpart in the reference, which updates one IrradianceProbes
  * volume per call (src/IrradianceProbes.cpp:426-594); a batch runs that

@@ -1290,6 +1290,48 @@ int oracle_record(const oracle_scene* s, const ddgi_grid_desc* g, const ddgi_lig
 // FP64 forward replaying a recorded hit set with the given parameters:
 // albedo (material_count x 3, NULL = the materials' base colour), sun and
 // sky radiance (3 doubles each).
+// Probe classification, probesInit.rgen:31-64 with probeInitMiss.rmiss:11-14
+// and backfaceTest.rchit:11-15: 512 closest-hit rays per probe (mask
+// INSTANCE_STATIC = 1, InstanceMasks.glsl:1), direction i = orientation *
+// sphericalFibonacci(i, raysPerProbe) (for i >= raysPerProbe the formula
+// gives the degenerate (0, 0, cos) directions, kept as the shader has them),
+// t in [0.01, 1.5 |cell|].  Hits closer than |cell| (:44): back faces are
+// counted (:45); a hit position within one cell of the probe on every axis
+// (:46-48, position rounded as product then sum) marks the probe near
+// geometry.  State (:52-59): 0 if back-face hits > raysPerProbe / 2, else 1
+// near geometry, else 8.
+void oracle_init_probes(const oracle_scene* s, const ddgi_grid_desc* gd, const float orientation[9], uint32_t* states,
+                        int nthreads) {
+    const Grid g = make_grid(gd);
+    const F3 cell = cell_size<float>(g);
+    const float max_distance = length(cell);
+    const float tmax = 1.5f * max_distance;
+    std::vector<F3> dirs(512);
+    for (uint32_t i = 0; i < 512; ++i) {
+        float d[4];
+        ddgi_ray_direction(orientation, i, g.rays, d);
+        dirs[i] = F3(d[0], d[1], d[2]);
+    }
+    parallel_for(g.count(), nthreads, [&](size_t b, size_t e) {
+        for (size_t p = b; p < e; ++p) {
+            const F3 o = exact_probe_origin(g, (uint32_t)p);
+            uint32_t back = 0;
+            bool near = false;
+            for (uint32_t i = 0; i < 512; ++i) {
+                Hit h;
+                trace(s->s, o, dirs[i], 0.01f, tmax, 0x1u, false, &h);
+                if (!h.valid() || !(h.t < max_distance)) continue;
+                if (h.backface) ++back;
+                F3 pos;
+                for (int k = 0; k < 3; ++k) pos[k] = dirs[i][k] * h.t + o[k];
+                F3 dist = vabs(pos - o);
+                if (dist.x < cell.x && dist.y < cell.y && dist.z < cell.z) near = true;
+            }
+            states[p] = (float)back > 0.5f * (float)g.rays ? 0u : (near ? 1u : 8u);
+        }
+    }, 1);
+}
+
 int oracle_replay(const oracle_scene* s, const ddgi_grid_desc* g, const ddgi_light* l, const double* albedo,
                   const double* sun, const double* sky, const float* orientations, uint32_t K, uint32_t* states,
                   double* color, double* depth, const void* rec, const double* depth_snap, int nthreads) {

@@ -97,6 +97,7 @@ class Oracle:
             lib.oracle_texel_scale.argtypes = [C.c_uint32]
             lib.oracle_pbr.argtypes = [C.c_void_p] * 5 + [C.c_float, C.c_float, C.c_void_p]
             lib.oracle_sample_probes.argtypes = [C.POINTER(GridDesc)] + [C.c_void_p] * 7
+            lib.oracle_init_probes.argtypes = [C.c_void_p, C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_int]
             cls._lib = lib
         return cls._lib
 
@@ -118,6 +119,13 @@ class Oracle:
             pass
 
     # -- queries -------------------------------------------------------------
+    def init_probes(self, grid, orientation):
+        """Probe states from the probesInit classification (0 OFF, 1, 8)."""
+        o = np.ascontiguousarray(orientation, np.float32).reshape(9)
+        states = np.zeros(grid.probe_count(), np.uint32)
+        self.lib().oracle_init_probes(self._h, C.byref(grid), _ptr(o), _ptr(states), self.threads)
+        return states
+
     def trace(self, origins, dirs, tmin, tmax, mask=0xFF, any_hit=False):
         origins = np.ascontiguousarray(origins, np.float32)
         dirs = np.ascontiguousarray(dirs, np.float32)
@@ -239,3 +247,26 @@ def zero_atlas(grid, fp64=False):
     ch, cw, _ = grid.atlas_shape(0)
     dh, dw, _ = grid.atlas_shape(1)
     return np.zeros((ch, cw, 4), dt), np.zeros((dh, dw, 2), dt)
+
+
+def select_probes(states, offset, loop, max_probes=0):
+    """IrradianceProbes::selectProbesToUpdate (src/IrradianceProbes.cpp:396-424)
+    restated as the reference's host loop: visit probes cyclically from
+    `offset`; probe idx is picked when its state s != 0 and
+    (idx + loop) % s == 0; `loop` (the reference's static s_LoopIndex) grows
+    by one at every wrap past the last probe; with max_probes > 0 the visit
+    stops once that many are picked.  Returns (picked, next offset, next
+    loop)."""
+    n = len(states)
+    picked = []
+    idx, checked = offset, 0
+    while checked < n and (max_probes == 0 or len(picked) < max_probes):
+        s = int(states[idx])
+        if s != 0 and (idx + loop) % s == 0:
+            picked.append(idx)
+        idx += 1
+        if idx >= n:
+            idx = 0
+            loop += 1
+        checked += 1
+    return np.array(picked, np.uint32), idx, loop

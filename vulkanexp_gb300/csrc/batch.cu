@@ -224,8 +224,13 @@ ddgi_status check_volumes(ddgi_batch* b) {
         const ddgi_ctx* c = b->vols[v];
         if (!c->scene.built || c->scene.build_id != b->scene_builds[v])
             return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "volume %zu: scene rebuilt or released since the batch was made", v);
-        if (memcmp(&c->grid, &b->grids[v], sizeof(ddgi_grid_desc)) != 0)
-            return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "volume %zu: grid changed since the batch was made", v);
+        // extent, hysteresis, sharpness and bias are read per update; the
+        // sizes fix the batch's buffers and tables
+        const ddgi_grid_desc& g0 = b->grids[v];
+        if (memcmp(c->grid.resolution, g0.resolution, sizeof(g0.resolution)) != 0 ||
+            c->grid.rays_per_probe != g0.rays_per_probe || c->grid.color_res != g0.color_res ||
+            c->grid.depth_res != g0.depth_res || c->grid.precision != g0.precision)
+            return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "volume %zu: grid sizes changed since the batch was made", v);
     }
     return DDGI_OK;
 }

@@ -154,8 +154,10 @@ __device__ __forceinline__ void blend_probe_fp32(const DeviceGrid& g, uint32_t p
 
 __global__ void __launch_bounds__(256) k_blend_fp32(DeviceGrid g, const uint32_t* __restrict__ probe_list,
                                                     const float4* __restrict__ rays, const float4* __restrict__ dirs,
-                                                    uint32_t* states, float4* color, float2* depth) {
+                                                    uint32_t* states, float4* color, float2* depth,
+                                                    const uint32_t* dev_count) {
     const uint32_t slot = blockIdx.x;
+    if (dev_count && slot >= *dev_count) return;  // whole block
     const uint32_t probe = probe_list ? probe_list[slot] : slot;
     blend_probe_fp32(g, probe, rays + (size_t)slot * g.rays, dirs, states, color, depth);
 }
@@ -187,10 +189,11 @@ __global__ void __launch_bounds__(256) k_batch_blend_fp32(BatchTables bt, BatchB
 }  // namespace
 
 cudaError_t launch_blend_fp32(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
-                              const float4* dirs, uint32_t* states, float4* color, float2* depth, cudaStream_t st) {
+                              const float4* dirs, uint32_t* states, float4* color, float2* depth, cudaStream_t st,
+                              const uint32_t* dev_count) {
     if (nprobes == 0) return cudaSuccess;
     size_t smem = sizeof(float4) * 2 * g.rays;
-    k_blend_fp32<<<nprobes, 256, smem, st>>>(g, probe_list, rays, dirs, states, color, depth);
+    k_blend_fp32<<<nprobes, 256, smem, st>>>(g, probe_list, rays, dirs, states, color, depth, dev_count);
     return cudaGetLastError();
 }
 

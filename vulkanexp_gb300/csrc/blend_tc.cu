@@ -69,6 +69,7 @@ struct TcArgs {
     float4* acc_color;   // FP32 hysteresis accumulators (interior texels)
     float2* acc_depth;
     uint32_t* err;
+    const uint32_t* dev_count;  // listed probes, read on the device (NULL: nprobes)
 };
 
 // Byte offset of (row, 8-element K group) in a K-chunk operand.
@@ -146,8 +147,9 @@ __global__ void k_tc_weights(const float4* dirs, uint32_t R, uint32_t nc, uint32
     tc_weight_row(blockIdx.x * blockDim.x + threadIdx.x, dirs, R, nc, nd, sharp, Nc, Nd, nchunks, wout, rowsum);
 }
 
-// Blend of the 32-probe tile starting at probe slot p0 by the whole CTA.
-__device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0) {
+// Blend of the 32-probe tile starting at probe slot p0 (< nprobes) by the
+// whole CTA.
+__device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0, const uint32_t nprobes) {
     extern __shared__ __align__(1024) uint8_t smem[];
     // A operands (128 x 64 BF16 = 16 KB each): colour hi/lo, depth hi/lo;
     // then B: high parts of (Nd + Nc) x 64, then the remainders
@@ -162,7 +164,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
     __shared__ uint32_t s_oor[kTileProbes], s_maxc[kTileProbes];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t np = min((uint32_t)kTileProbes, a.nprobes - p0);
+    const uint32_t np = min((uint32_t)kTileProbes, nprobes - p0);
     const uint32_t R = a.g.rays;
     const float cell = a.g.cell_len;
 
@@ -426,7 +428,12 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_blend_tc(TcArgs a) { blend_tc_tile(a, blockIdx.x * kTileProbes); }
+__global__ void __launch_bounds__(kThreads) k_blend_tc(TcArgs a) {
+    const uint32_t n = a.dev_count ? *a.dev_count : a.nprobes;
+    const uint32_t p0 = blockIdx.x * kTileProbes;
+    if (p0 >= n) return;  // whole CTA, before any tensor-memory allocation
+    blend_tc_tile(a, p0, n);
+}
 
 // Interior sides, padded texel counts and ray chunks of a grid.
 struct TcShape {
@@ -485,12 +492,13 @@ __global__ void __launch_bounds__(kThreads) k_batch_blend_tc(BatchTables bt, Bat
         a.acc_color = vol.acc_color;
         a.acc_depth = vol.acc_depth;
         a.err = bt.err;
+        a.dev_count = nullptr;
         s_v = v;
         s_tile = b - __ldg(bl.tile_base + lo);
         s_items = __ldg(bl.tile_base + lo + 1) - __ldg(bl.tile_base + lo);
     }
     __syncthreads();
-    blend_tc_tile(s_args, s_tile * kTileProbes);
+    blend_tc_tile(s_args, s_tile * kTileProbes, s_args.nprobes);
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -524,7 +532,8 @@ bool tc_blend_supported(uint32_t color_res, uint32_t depth_res) {
 
 cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
                             const float4* dirs, uint8_t* wbuf, float* rowsum, uint32_t* states, void* color,
-                            void* depth, float4* acc_color, float2* acc_depth, uint32_t* err, cudaStream_t st) {
+                            void* depth, float4* acc_color, float2* acc_depth, uint32_t* err, cudaStream_t st,
+                            const uint32_t* dev_count) {
     if (nprobes == 0) return cudaSuccess;
     const uint32_t nc = g.color_res - 2, nd = g.depth_res - 2;
     const uint32_t Nc = (nc * nc + 15) / 16 * 16, Nd = (nd * nd + 15) / 16 * 16;
@@ -548,6 +557,7 @@ cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uin
     a.acc_color = acc_color;
     a.acc_depth = acc_depth;
     a.err = err;
+    a.dev_count = dev_count;
     // operand stage (A 64 KB + B up to 128 KB), reused by the epilogue staging
     size_t stage = 65536 + 2 * (size_t)(Nd + Nc) * 128;
     size_t staging = (size_t)kTileProbes * (nc * nc * 3 + nd * nd * 2) * sizeof(float);

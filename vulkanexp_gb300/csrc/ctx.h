@@ -89,6 +89,12 @@ struct ddgi_ctx {
     float4* dirs = nullptr;
     uint32_t* ray_order = nullptr;
     uint32_t* probe_list = nullptr;
+    // adaptive schedule (selectProbesToUpdate on the device): {offset, loop
+    // index, selected count}; probe classification scratch
+    uint32_t* sched = nullptr;
+    float4* init_dirs = nullptr;
+    uint32_t* init_back = nullptr;
+    uint32_t* init_near = nullptr;
     uint32_t* err = nullptr;
     uint32_t last_count = 0;
     uint32_t last_rays = 0;

@@ -241,6 +241,7 @@ ddgi_status ddgi_create(const ddgi_grid_desc* grid, ddgi_ctx** out) {
         cudaMalloc(&ctx->dirs, sizeof(float4) * DDGI_MAX_RAYS_PER_PROBE) != cudaSuccess ||
         cudaMalloc(&ctx->ray_order, sizeof(uint32_t) * DDGI_MAX_RAYS_PER_PROBE) != cudaSuccess ||
         cudaMalloc(&ctx->probe_list, sizeof(uint32_t) * P) != cudaSuccess ||
+        cudaMalloc(&ctx->sched, 4 * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&ctx->err, sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&ctx->counters, 4 * sizeof(uint32_t)) != cudaSuccess) {
         cudaGetLastError();
@@ -264,6 +265,7 @@ ddgi_status ddgi_create(const ddgi_grid_desc* grid, ddgi_ctx** out) {
     cudaMemset(ctx->color, 0, atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, ctx->fp16));
     cudaMemset(ctx->depth, 0, atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, ctx->fp16));
     cudaMemset(ctx->err, 0, sizeof(uint32_t));
+    cudaMemset(ctx->sched, 0, 4 * sizeof(uint32_t));
     std::vector<uint32_t> ones(P, 1u);
     cudaMemcpy(ctx->states, ones.data(), sizeof(uint32_t) * P, cudaMemcpyHostToDevice);
     for (int i = 0; i < 4; ++i)
@@ -307,6 +309,10 @@ ddgi_status ddgi_destroy(ddgi_ctx* ctx) {
     dfree(ctx->dirs);
     dfree(ctx->ray_order);
     dfree(ctx->probe_list);
+    dfree(ctx->sched);
+    dfree(ctx->init_dirs);
+    dfree(ctx->init_back);
+    dfree(ctx->init_near);
     dfree(ctx->err);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -734,6 +740,99 @@ ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_
     }
     ctx->last_count = n;
     ctx->last_rays = ctx->grid.rays_per_probe;
+    return DDGI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Probe classification and adaptive schedule (IrradianceProbes::initProbes,
+// src/IrradianceProbes.cpp:357-394, and selectProbesToUpdate, :396-424)
+// ---------------------------------------------------------------------------
+ddgi_status ddgi_init_probes(ddgi_ctx* ctx, const float orientation[9], ddgi_stream stream) {
+    if (!ctx || !orientation) return DDGI_ERR_INVALID_ARGUMENT;
+    if (!ctx->scene.built) return fail(ctx, DDGI_ERR_NO_SCENE, "ddgi_init_probes before ddgi_scene_build");
+    for (int k = 0; k < 9; ++k)
+        if (!std::isfinite(orientation[k])) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "non-finite orientation");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const uint32_t P = probe_count_of(ctx->grid);
+    if (!ctx->init_dirs) {
+        CK(cudaMalloc(&ctx->init_dirs, sizeof(float4) * kInitRays), "alloc init directions");
+        CK(cudaMalloc(&ctx->init_back, sizeof(uint32_t) * P), "alloc init counters");
+        CK(cudaMalloc(&ctx->init_near, sizeof(uint32_t) * P), "alloc init counters");
+    }
+    // probesInit.rgen:41-42: direction i of 512 from the raysPerProbe-point
+    // spherical Fibonacci set (i >= raysPerProbe: the degenerate directions
+    // the shader's formula gives there)
+    std::vector<float> d(4 * (size_t)kInitRays);
+    for (uint32_t i = 0; i < kInitRays; ++i) ddgi_ray_direction(orientation, i, ctx->grid.rays_per_probe, &d[4 * i]);
+    CK(cudaMemcpyAsync(ctx->init_dirs, d.data(), sizeof(float4) * kInitRays, cudaMemcpyHostToDevice, st), "upload");
+    CK(launch_init_probes(device_scene(ctx), ctx->dg, ctx->init_dirs, P, ctx->init_back, ctx->init_near, ctx->states,
+                          ctx->counters, ctx->scene.stack_cap, ctx->err, st),
+       "init launch");
+    CK(cudaStreamSynchronize(st), "init probes");  // also keeps `d` alive for the copy
+    return check_device_error(ctx);
+}
+
+ddgi_status ddgi_update_scheduled(ddgi_ctx* ctx, const float orientation[9], uint32_t max_probes, ddgi_stream stream) {
+    if (!ctx || !orientation) return DDGI_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const uint32_t* unused = nullptr;
+    uint32_t P = 0;
+    ddgi_status s = prepare_update(ctx, orientation, nullptr, 0, st, &unused, &P);
+    if (s != DDGI_OK) return s;
+    uint32_t* dcount = ctx->sched + 2;
+    if (ctx->timing) CK(cudaEventRecord(ctx->ev[0], st), "event");
+    CK(launch_select_probes(ctx->states, P, max_probes, ctx->sched, ctx->probe_list, st), "schedule launch");
+    WaveHits wh{ctx->wave_thit, ctx->wave_prim};
+    ShadowQueue q{ctx->q_idx, ctx->q_pos, ctx->q_sun, nullptr};
+    ddgi_hit* hits_out = ctx->record_hits ? ctx->hits : nullptr;
+    CK(launch_wavefront(device_scene(ctx), ctx->dg, ctx->dl, ctx->probe_list, P, ctx->dirs, ctx->ray_order,
+                        ctx->states, ctx->color, ctx->depth, ctx->fp16, wh, q, ctx->counters, ctx->rays, hits_out,
+                        ctx->scene.stack_cap, ctx->err, st, ctx->timing ? ctx->ev[3] : nullptr, dcount),
+       "wavefront trace launch");
+    if (ctx->timing) CK(cudaEventRecord(ctx->ev[1], st), "event");
+    if (ctx->fp16)
+        CK(launch_blend_tc(ctx->dg, ctx->probe_list, P, ctx->rays, ctx->dirs, ctx->tc_weights, ctx->tc_rowsum,
+                           ctx->states, ctx->color, ctx->depth, ctx->acc_color, ctx->acc_depth, ctx->err, st, dcount),
+           "blend launch");
+    else
+        CK(launch_blend_fp32(ctx->dg, ctx->probe_list, P, ctx->rays, ctx->dirs, ctx->states,
+                             static_cast<float4*>(ctx->color), static_cast<float2*>(ctx->depth), st, dcount),
+           "blend launch");
+    if (ctx->timing) {
+        CK(cudaEventRecord(ctx->ev[2], st), "event");
+        ctx->timing_pending = true;
+    }
+    ctx->last_count = P;  // records of the selected probes come first
+    ctx->last_rays = ctx->grid.rays_per_probe;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_get_schedule(ddgi_ctx* ctx, uint32_t* count, uint32_t* offset, uint32_t* loop, uint32_t* list,
+                              size_t list_capacity, ddgi_stream stream) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    uint32_t h[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(h, ctx->sched, sizeof(h), cudaMemcpyDeviceToHost, st), "read schedule");
+    CK(cudaStreamSynchronize(st), "read schedule");
+    if (offset) *offset = h[0];
+    if (loop) *loop = h[1];
+    if (count) *count = h[2];
+    if (list) {
+        if (list_capacity < h[2]) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "list holds %zu of %u", list_capacity, h[2]);
+        if (h[2])
+            CK(cudaMemcpy(list, ctx->probe_list, sizeof(uint32_t) * h[2], cudaMemcpyDeviceToHost), "read schedule");
+    }
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_set_schedule(ddgi_ctx* ctx, uint32_t offset, uint32_t loop, ddgi_stream stream) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    if (offset >= probe_count_of(ctx->grid))
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "offset %u outside the grid", offset);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const uint32_t h[4] = {offset, loop, 0, 0};
+    CK(cudaMemcpyAsync(ctx->sched, h, sizeof(h), cudaMemcpyHostToDevice, st), "write schedule");
+    CK(cudaStreamSynchronize(st), "write schedule");
     return DDGI_OK;
 }
 

@@ -34,7 +34,17 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
                              const uint32_t* ray_order, const uint32_t* states, const void* color, const void* depth,
                              bool fp16_atlas, WaveHits hits, ShadowQueue q, uint32_t* counters, float4* rays_out,
                              ddgi_hit* hits_out, int stack_cap, uint32_t* err, cudaStream_t st,
-                             cudaEvent_t after_primary);
+                             cudaEvent_t after_primary, const uint32_t* dev_count = nullptr);
+// Probe classification (probesInit): kInitRays rays per probe.
+constexpr uint32_t kInitRays = 512;
+cudaError_t launch_init_probes(const DeviceScene& sc, const DeviceGrid& g, const float4* dirs, uint32_t P,
+                               uint32_t* back, uint32_t* near, uint32_t* states, uint32_t* counters, int stack_cap,
+                               uint32_t* err, cudaStream_t st);
+// schedule.cu: selectProbesToUpdate on the device.  sched = {offset, loop
+// index, selected count} (kept on the device between updates); the selected
+// probes go to list[0 .. count).
+cudaError_t launch_select_probes(const uint32_t* states, uint32_t P, uint32_t max_probes, uint32_t* sched,
+                                 uint32_t* list, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Batched update of many probe volumes (batch.cu drives these launchers)
@@ -117,10 +127,12 @@ size_t tc_weight_bytes(uint32_t rays, uint32_t color_res, uint32_t depth_res);
 bool tc_blend_supported(uint32_t color_res, uint32_t depth_res);
 cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
                             const float4* dirs, uint8_t* wbuf, float* rowsum, uint32_t* states, void* color,
-                            void* depth, float4* acc_color, float2* acc_depth, uint32_t* err, cudaStream_t st);
+                            void* depth, float4* acc_color, float2* acc_depth, uint32_t* err, cudaStream_t st,
+                            const uint32_t* dev_count = nullptr);
 
 // blend.cu
 cudaError_t launch_blend_fp32(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
-                              const float4* dirs, uint32_t* states, float4* color, float2* depth, cudaStream_t st);
+                              const float4* dirs, uint32_t* states, float4* color, float2* depth, cudaStream_t st,
+                              const uint32_t* dev_count = nullptr);
 
 }  // namespace ddgi

@@ -33,6 +33,7 @@ struct PrimaryJob {
     const uint32_t* ray_order;
     WaveHits hits;
     uint32_t total;
+    const uint32_t* dev_count;  // listed probes, read on the device (NULL: total / rays)
 
     template <class W>
     __device__ __forceinline__ bool start(W& w, const DeviceScene& sc, uint32_t id, uint32_t* out) const {
@@ -149,7 +150,8 @@ __device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job
 
 __global__ void __launch_bounds__(kPersistThreads) k_primary(DeviceScene sc, PrimaryJob job, uint32_t* counter,
                                                              int stack_cap, uint32_t* err) {
-    persistent_walk<false, SmemStack>(sc, job, job.total, counter, stack_cap, stack_cap, 8, err);
+    const uint32_t total = job.dev_count ? *job.dev_count * job.g.rays : job.total;
+    persistent_walk<false, SmemStack>(sc, job, total, counter, stack_cap, stack_cap, 8, err);
 }
 
 __global__ void __launch_bounds__(kPersistThreads) k_shadow(DeviceScene sc, ShadowJob job, const uint32_t* qcount,
@@ -162,11 +164,12 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene sc, DeviceGrid g, Dev
                                                const uint32_t* __restrict__ probe_list, uint32_t total,
                                                const float4* __restrict__ dirs, const uint32_t* __restrict__ states,
                                                AV at, WaveHits hits, float4* rays_out, ddgi_hit* hits_out,
-                                               ShadowQueue q, uint32_t* err) {
+                                               ShadowQueue q, const uint32_t* dev_count, uint32_t* err) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     bool enqueue = false;
     SurfaceShade s;
+    if (dev_count) total = *dev_count * g.rays;
     if (i < total) {
         uint32_t R = g.rays;
         uint32_t slot = i / R, ray = i - slot * R;
@@ -211,6 +214,55 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene sc, DeviceGrid g, Dev
             q.sun[k] = make_float4(s.sun.x, s.sun.y, s.sun.z, s.fade);
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Probe classification (src/shaders/probesInit.rgen:31-64 with
+// probeInitMiss.rmiss and backfaceTest.rchit): 512 closest-hit rays per
+// probe among INSTANCE_STATIC (mask 1) instances, t in [0.01, 1.5 |cell|].
+// A hit closer than |cell| counts as a back-face hit when back-facing, and
+// marks the probe as near geometry when it lies within one cell of the probe
+// on every axis (hit position rounded product, then sum).
+// ---------------------------------------------------------------------------
+struct InitJob {
+    DeviceGrid g;
+    const float4* dirs;  // kInitRays directions
+    float tmax;
+    uint32_t* back;  // per probe
+    uint32_t* near;  // per probe
+
+    template <class W>
+    __device__ __forceinline__ bool start(W& w, const DeviceScene& sc, uint32_t id, uint32_t* out) const {
+        *out = id;
+        const uint32_t probe = id / kInitRays, i = id - probe * kInitRays;
+        float4 d4 = __ldg(dirs + i);
+        return w.start(sc, probe_origin_exact(g, probe), f3(d4.x, d4.y, d4.z), 0.01f, tmax, 0x1u);
+    }
+    template <class W>
+    __device__ __forceinline__ void finish(const W& w, uint32_t id) const {
+        const HitRec& h = w.best;
+        if (h.inst == kNoHit || !(h.t < g.cell_len)) return;
+        const uint32_t probe = id / kInitRays;
+        if (h.back) atomicAdd(back + probe, 1u);
+        const float3 o = w.wr.o, d = w.wr.d;
+        const float dx = fabsf(__fsub_rn(__fadd_rn(__fmul_rn(d.x, h.t), o.x), o.x));
+        const float dy = fabsf(__fsub_rn(__fadd_rn(__fmul_rn(d.y, h.t), o.y), o.y));
+        const float dz = fabsf(__fsub_rn(__fadd_rn(__fmul_rn(d.z, h.t), o.z), o.z));
+        if (dx < g.cell[0] && dy < g.cell[1] && dz < g.cell[2]) near[probe] = 1u;
+    }
+};
+
+__global__ void __launch_bounds__(kPersistThreads) k_init_probes(DeviceScene sc, InitJob job, uint32_t total,
+                                                                 uint32_t* counter, int stack_cap, uint32_t* err) {
+    persistent_walk<false, SmemStack>(sc, job, total, counter, stack_cap, stack_cap, 8, err);
+}
+
+// State per probe: OFF (0) when more than half of raysPerProbe back-face
+// hits, else 1 near geometry, else 8.
+__global__ void k_init_states(uint32_t P, uint32_t R, const uint32_t* back, const uint32_t* near, uint32_t* states) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    states[p] = 2u * back[p] > R ? 0u : (near[p] ? 1u : 8u);
 }
 
 // ---------------------------------------------------------------------------
@@ -379,14 +431,14 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
                              const uint32_t* ray_order, const uint32_t* states, const void* color, const void* depth,
                              bool fp16_atlas, WaveHits hits, ShadowQueue q, uint32_t* counters, float4* rays_out,
                              ddgi_hit* hits_out, int stack_cap, uint32_t* err, cudaStream_t st,
-                             cudaEvent_t after_primary) {
+                             cudaEvent_t after_primary, const uint32_t* dev_count) {
     uint32_t total = nprobes * g.rays;
     if (total == 0) return cudaSuccess;
     // counters[0]: primary work, counters[1]: shadow queue length, counters[2]: shadow work
     cudaError_t e = cudaMemsetAsync(counters, 0, 3 * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     const size_t smem = (size_t)stack_cap * kPersistThreads * sizeof(int);
-    PrimaryJob pj{g, probe_list, dirs, ray_order, hits, total};
+    PrimaryJob pj{g, probe_list, dirs, ray_order, hits, total, dev_count};
     k_primary<<<persistent_blocks((const void*)k_primary, smem), kPersistThreads, smem, st>>>(sc, pj, counters,
                                                                                              stack_cap, err);
     if (after_primary) cudaEventRecord(after_primary, st);
@@ -397,12 +449,12 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
         AtlasView<ColorTexF16, DepthTexF16> at{{static_cast<const uint2*>(color)},
                                                {static_cast<const uint32_t*>(depth)}};
         k_shade<<<blocks, 128, 0, st>>>(sc, g, L, probe_list, total, dirs, states, at, hits, rays_out, hits_out, qq,
-                                        err);
+                                        dev_count, err);
     } else {
         AtlasView<ColorTexF32, DepthTexF32> at{{static_cast<const float4*>(color)},
                                                {static_cast<const float2*>(depth)}};
         k_shade<<<blocks, 128, 0, st>>>(sc, g, L, probe_list, total, dirs, states, at, hits, rays_out, hits_out, qq,
-                                        err);
+                                        dev_count, err);
     }
     ShadowJob sj{qq, make_float3(L.dir[0], L.dir[1], L.dir[2]), rays_out, hits.prim, 0};
     k_shadow<<<persistent_blocks((const void*)k_shadow, smem), kPersistThreads, smem, st>>>(
@@ -448,6 +500,24 @@ cudaError_t launch_batch_trace(const DeviceScene& arena, const BatchTables& bt, 
                                               tune, st, after_primary, after_shade);
     return batch_trace_kernels<SplitStack>(arena, bt, total, hits, q, counters, rays_out, stack_cap, (int)tune.split,
                                            tune, st, after_primary, after_shade);
+}
+
+// Probe classification of all P probes into `states`.  `dirs` holds the
+// kInitRays init directions; back/near are P-entry scratch arrays.
+cudaError_t launch_init_probes(const DeviceScene& sc, const DeviceGrid& g, const float4* dirs, uint32_t P,
+                               uint32_t* back, uint32_t* near, uint32_t* states, uint32_t* counters, int stack_cap,
+                               uint32_t* err, cudaStream_t st) {
+    if (P == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(back, 0, sizeof(uint32_t) * P, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(near, 0, sizeof(uint32_t) * P, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    const size_t smem = (size_t)stack_cap * kPersistThreads * sizeof(int);
+    InitJob job{g, dirs, 1.5f * g.cell_len, back, near};
+    k_init_probes<<<persistent_blocks((const void*)k_init_probes, smem), kPersistThreads, smem, st>>>(
+        sc, job, P * kInitRays, counters, stack_cap, err);
+    k_init_states<<<(P + 255) / 256, 256, 0, st>>>(P, g.rays, back, near, states);
+    return cudaGetLastError();
 }
 
 }  // namespace ddgi

@@ -68,6 +68,11 @@ _SIGNATURES = [
     ("ddgi_blend_records_noalloc", C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p]),
+    ("ddgi_init_probes", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ddgi_update_scheduled", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    ("ddgi_get_schedule", C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                    C.c_void_p, C.c_size_t, C.c_void_p]),
+    ("ddgi_set_schedule", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
     ("ddgi_batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.c_void_p, C.POINTER(C.c_void_p)]),
     ("ddgi_batch_destroy", C.c_int, [C.c_void_p]),
     ("ddgi_batch_last_error", C.c_char_p, [C.c_void_p]),
@@ -193,6 +198,31 @@ class Context:
         pl = None if probe_list is None else np.ascontiguousarray(probe_list, np.uint32)
         self._check(self.lib.ddgi_update(self.h, _ptr(o), _ptr(pl), 0 if pl is None else len(pl),
                                          _stream_ptr(stream)))
+
+    def init_probes(self, orientation, stream=None):
+        """Probe classification (probesInit): states 0 (OFF), 1 or 8."""
+        o = np.ascontiguousarray(orientation, np.float32).reshape(9)
+        self._check(self.lib.ddgi_init_probes(self.h, _ptr(o), _stream_ptr(stream)))
+
+    def update_scheduled(self, orientation, max_probes=0, stream=None):
+        """Update of the probes the on-device schedule selects."""
+        o = np.ascontiguousarray(orientation, np.float32).reshape(9)
+        self._check(self.lib.ddgi_update_scheduled(self.h, _ptr(o), int(max_probes), _stream_ptr(stream)))
+
+    def schedule(self, with_list=True, stream=None):
+        """The last selection and the schedule state (synchronises)."""
+        cnt, off, loop = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        P = self.grid.probe_count()
+        lst = np.zeros(P, np.uint32) if with_list else None
+        self._check(self.lib.ddgi_get_schedule(self.h, C.byref(cnt), C.byref(off), C.byref(loop), _ptr(lst),
+                                               P if with_list else 0, _stream_ptr(stream)))
+        out = {"count": int(cnt.value), "offset": int(off.value), "loop": int(loop.value)}
+        if with_list:
+            out["list"] = lst[:cnt.value].copy()
+        return out
+
+    def set_schedule(self, offset, loop, stream=None):
+        self._check(self.lib.ddgi_set_schedule(self.h, int(offset), int(loop), _stream_ptr(stream)))
 
     def count_fetches(self, orientation, probe_list=None, stream=None):
         """Fetch counters of one trace + shade pass (see ddgi_count_fetches)."""
@@ -415,9 +445,39 @@ class IrradianceProbes:
         r = self.GridParameters.resolution
         return int(r[0]) * int(r[1]) * int(r[2])
 
+    def initProbes(self, orientation, stream=None):
+        """IrradianceProbes::initProbes (src/IrradianceProbes.cpp:357-394):
+        classify the probes, and restart the hysteresis ramp from 0."""
+        self.ctx.init_probes(orientation, stream)
+        self.GridParameters.hysteresis = 0.0
+        self.updateUniforms()
+        self._updated = 0
+
     def update(self, orientation, probe_list=None, stream=None):
-        """One update; `orientation` is the 3x3 ray-set rotation."""
-        self.ctx.update(orientation, probe_list, stream)
+        """IrradianceProbes::update (src/IrradianceProbes.cpp:426-594):
+        `orientation` is the 3x3 ray-set rotation.  Without a probe list the
+        probes are the ones selectProbesToUpdate picks (chosen on the device,
+        at most ProbesPerUpdate, 0 = no cap), and the grid hysteresis ramps
+        towards TargetHysteresis once per probe count of refreshed probes
+        (:462-476; the new value is used by the same update, where the
+        reference uploads it one ramp step later).  The ramp reads the
+        selected count back from the device."""
+        if probe_list is not None:
+            self.ctx.update(orientation, probe_list, stream)
+            return
+        P = self.getProbeCount()
+        if self._updated >= P:
+            h = np.float32(self.GridParameters.hysteresis)
+            t = np.float32(self.TargetHysteresis)
+            if abs(h - t) > np.float32(0.05):
+                self.GridParameters.hysteresis = float(h + np.float32(0.1) * (t - h))
+                self.updateUniforms()
+            elif h != t:
+                self.GridParameters.hysteresis = float(t)
+                self.updateUniforms()
+            self._updated -= P
+        self.ctx.update_scheduled(orientation, self.ProbesPerUpdate, stream)
+        self._updated += self.ctx.schedule(with_list=False, stream=stream)["count"]
 
     def getIrradiance(self):
         return self.ctx.get_atlas(abi.ATLAS_COLOR)
