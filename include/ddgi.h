@@ -352,6 +352,28 @@ ddgi_status ddgi_get_schedule(ddgi_ctx* ctx, uint32_t* count, uint32_t* offset, 
 /* Sets the schedule state (a new context starts at offset 0, loop 0). */
 ddgi_status ddgi_set_schedule(ddgi_ctx* ctx, uint32_t offset, uint32_t loop, ddgi_stream stream);
 
+/* ---- Launch tuning of the persistent traversals -------------------------
+ * Results do not depend on these; speed does. */
+typedef struct ddgi_trace_tuning {
+    uint32_t rays_per_warp; /* 0: each warp traces 32 rays of one probe, probes in index order (default);
+                               n = 1, 2, 4, 8, 16, 32 (n dividing rays_per_probe): each warp traces n
+                               consecutive directions of the octant-binned ray order from 32 / n neighbouring
+                               probes (Morton order of the grid); used when all probes are updated */
+    uint32_t refill_lanes;  /* a warp requests new rays once this many lanes are idle (1..32, default 8) */
+    uint32_t smem_stack;    /* traversal-stack entries per thread in shared memory, deeper ones in local
+                               memory; 0 = the whole stack in shared memory (default) */
+    uint32_t ctas_per_sm;   /* persistent CTAs per SM; 0 = as many as fit (default) */
+} ddgi_trace_tuning;
+ddgi_status ddgi_set_trace_tuning(ddgi_ctx* ctx, const ddgi_trace_tuning* tuning);
+ddgi_status ddgi_get_trace_tuning(const ddgi_ctx* ctx, ddgi_trace_tuning* out);
+/* Times candidate tunings on updates of all probes with the given
+ * orientation (`reps` timed updates each, coordinate descent), keeps the
+ * fastest trace (primary + shading + shadow rays) and writes it to *chosen
+ * (may be NULL).  The atlases, accumulators and probe states are restored
+ * afterwards.  Synchronous. */
+ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t reps, ddgi_stream stream,
+                          ddgi_trace_tuning* chosen);
+
 /* ---- Batched update of many probe volumes ------------------------------
  * No single counterpart in the reference, which updates one IrradianceProbes
  * volume per call (src/IrradianceProbes.cpp:426-594); a batch runs that
@@ -378,6 +400,8 @@ typedef struct ddgi_batch_tuning {
     uint32_t smem_stack;        /* traversal-stack entries per thread in shared memory, deeper ones
                                    in local memory; 0 = the whole stack in shared memory */
     uint32_t blend_threads;     /* threads per probe of the FP32 blend (32..256, multiple of 32) */
+    uint32_t rays_per_warp;     /* as in ddgi_trace_tuning, per volume (values a volume's ray count
+                                   does not allow fall back to 0 for that volume) */
 } ddgi_batch_tuning;
 
 ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_stream stream, ddgi_batch** out);

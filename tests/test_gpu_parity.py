@@ -182,3 +182,41 @@ def test_errors_are_reported(gpu_lib, room_workload):
         ctx.build_scene(broken)
     ctx.synchronize(timeout_ms=10000)
     ctx.close()
+
+
+@pytest.mark.parametrize("tuning", [
+    dict(rays_per_warp=32), dict(rays_per_warp=8, refill_lanes=16), dict(rays_per_warp=1, smem_stack=16),
+    dict(rays_per_warp=4, refill_lanes=1, ctas_per_sm=3, smem_stack=24),
+])
+def test_trace_tunings_do_not_change_results(gpu_lib, room_workload, tuning):
+    """Work order, refill, stack placement and occupancy change only the
+    schedule: hits, records and atlases stay bit-identical."""
+    w = room_workload
+    ref = make_ctx(w)
+    ref.update(w.orientation(0))
+    ctx = make_ctx(w)
+    ctx.set_trace_tuning(**tuning)
+    assert ctx.trace_tuning() == {**ctx.trace_tuning(), **tuning}
+    ctx.update(w.orientation(0))
+    n = w.grid.probe_count()
+    assert (ctx.get_hits(n) == ref.get_hits(n)).all()
+    assert (ctx.get_ray_records(n).view(np.uint32) == ref.get_ray_records(n).view(np.uint32)).all()
+    for kind in (abi.ATLAS_COLOR, abi.ATLAS_DEPTH):
+        assert (ctx.get_atlas(kind).view(np.uint32) == ref.get_atlas(kind).view(np.uint32)).all()
+    ref.close()
+    ctx.close()
+
+
+def test_autotune_restores_state(gpu_lib, room_workload):
+    w = room_workload
+    ctx = make_ctx(w)
+    ctx.update(w.orientation(0))
+    before = [ctx.get_atlas(k) for k in (abi.ATLAS_COLOR, abi.ATLAS_DEPTH)] + [ctx.get_probe_states()]
+    chosen = ctx.autotune(w.orientation(1), reps=1)
+    assert ctx.trace_tuning() == chosen
+    after = [ctx.get_atlas(k) for k in (abi.ATLAS_COLOR, abi.ATLAS_DEPTH)] + [ctx.get_probe_states()]
+    for a, b in zip(before, after):
+        assert (a == b).all()
+    with pytest.raises(DDGIError):
+        ctx.set_trace_tuning(rays_per_warp=3)
+    ctx.close()

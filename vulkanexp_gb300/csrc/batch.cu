@@ -78,7 +78,7 @@ struct ddgi_batch {
     uint8_t* d_stage = nullptr;
     size_t stage_bytes = 0, off_order = 0, off_vols = 0;
     // launch state
-    ddgi_batch_tuning tuning{0, 8, 0, 256};
+    ddgi_batch_tuning tuning{0, 8, 0, 256, 0};
     bool use_graph = true;
     cudaStream_t cap = nullptr, side = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr, done_ev = nullptr;
@@ -253,16 +253,7 @@ ddgi_status stage_inputs(ddgi_batch* b, const float* orientations) {
         ddgi_ray_direction_table(&orientations[9 * v], R, d);
         // the volume's own record of its current direction table
         c->host_dirs.assign(d, d + 4 * (size_t)R);
-        uint32_t counts[9] = {0};
-        std::vector<uint8_t> oct(R);
-        for (uint32_t r = 0; r < R; ++r) {
-            const float* dd = d + 4 * (size_t)r;
-            oct[r] = (uint8_t)((dd[0] < 0.0f ? 1 : 0) | (dd[1] < 0.0f ? 2 : 0) | (dd[2] < 0.0f ? 4 : 0));
-            counts[oct[r] + 1]++;
-        }
-        for (int k = 0; k < 8; ++k) counts[k + 1] += counts[k];
-        uint32_t* o = order + b->dir_base[v];
-        for (uint32_t r = 0; r < R; ++r) o[counts[oct[r]]++] = r;
+        ray_order_of(d, R, order + b->dir_base[v]);
 
         BatchVolume& x = bv[v];
         memset(&x, 0, sizeof(x));
@@ -280,6 +271,8 @@ ddgi_status stage_inputs(ddgi_batch* b, const float* orientations) {
         x.acc_depth = c->acc_depth;
         x.wbuf = c->tc_weights;
         x.rowsum = c->tc_rowsum;
+        x.rays_per_warp = grouped_rays_per_warp(b->tuning.rays_per_warp, R);
+        x.perm = x.rays_per_warp ? c->probe_perm : nullptr;
     }
     return DDGI_OK;
 }
@@ -301,6 +294,7 @@ cudaError_t enqueue(ddgi_batch* b, cudaStream_t st, bool timed) {
     tt.ctas_per_sm = b->tuning.trace_ctas_per_sm;
     tt.refill = b->tuning.refill_lanes;
     tt.split = b->tuning.smem_stack;
+    tt.rays_per_warp = b->tuning.rays_per_warp;  // applied per volume through the volume table
     WaveHits wh{b->thit, b->prim};
     ShadowQueue q{b->q_idx, b->q_pos, b->q_sun, nullptr};
     e = launch_batch_trace(arena_scene(b), bt, b->total, wh, q, b->counters, b->rays, b->stack_cap, tt, st,
@@ -582,6 +576,9 @@ ddgi_status ddgi_batch_set_tuning(ddgi_batch* b, const ddgi_batch_tuning* t) {
                      t->blend_threads);
     if (t->smem_stack > (uint32_t)kSpillMax || t->trace_ctas_per_sm > 32)
         return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "smem_stack or trace_ctas_per_sm out of range");
+    const uint32_t r = t->rays_per_warp;
+    if (!(r == 0 || r == 1 || r == 2 || r == 4 || r == 8 || r == 16 || r == 32))
+        return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "rays_per_warp = %u: want 0, 1, 2, 4, 8, 16 or 32", r);
     ddgi_status s = wait_previous(b);
     if (s != DDGI_OK) return s;
     b->tuning = *t;
@@ -697,17 +694,19 @@ ddgi_status ddgi_batch_autotune(ddgi_batch* b, const float* orientations, uint32
     ddgi_status err = DDGI_OK;
     float best_t = 0.0f;
     err = measure(best, 0, &best_t);
+    const uint32_t rpw_c[] = {0u, 32u, 16u, 8u, 4u, 2u, 1u};
     const uint32_t split_c[] = {0u, 32u, 24u, 16u};
     const uint32_t refill_c[] = {4u, 8u, 16u, 24u};
     const uint32_t ctas_c[] = {0u, 6u, 4u};
-    for (int p = 0; p < 3 && err == DDGI_OK; ++p) {
-        const uint32_t* cand = p == 0 ? split_c : (p == 1 ? refill_c : ctas_c);
-        const int nc = p == 0 ? 4 : (p == 1 ? 4 : 3);
+    for (int p = 0; p < 4 && err == DDGI_OK; ++p) {
+        const uint32_t* cand = p == 0 ? rpw_c : p == 1 ? split_c : p == 2 ? refill_c : ctas_c;
+        const int nc = p == 0 ? 7 : p == 3 ? 3 : 4;
         for (int i = 0; i < nc && err == DDGI_OK; ++i) {
             ddgi_batch_tuning t = best;
-            uint32_t* field = p == 0 ? &t.smem_stack : (p == 1 ? &t.refill_lanes : &t.trace_ctas_per_sm);
+            uint32_t* field = p == 0 ? &t.rays_per_warp : p == 1 ? &t.smem_stack : p == 2 ? &t.refill_lanes
+                                                                                        : &t.trace_ctas_per_sm;
             if (*field == cand[i]) continue;
-            if (p == 0 && cand[i] != 0 && (int)cand[i] >= b->stack_cap) continue;
+            if (p == 1 && cand[i] != 0 && (int)cand[i] >= b->stack_cap) continue;
             *field = cand[i];
             float tt = 0.0f;
             err = measure(t, 0, &tt);

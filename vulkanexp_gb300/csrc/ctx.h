@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "../../include/ddgi.h"
@@ -92,6 +94,9 @@ struct ddgi_ctx {
     // adaptive schedule (selectProbesToUpdate on the device): {offset, loop
     // index, selected count}; probe classification scratch
     uint32_t* sched = nullptr;
+    // traversal launch tuning; probes in Morton order of the grid (grouped warps)
+    ddgi_trace_tuning tune{0, 8, 0, 0};
+    uint32_t* probe_perm = nullptr;
     float4* init_dirs = nullptr;
     uint32_t* init_back = nullptr;
     uint32_t* init_near = nullptr;
@@ -110,6 +115,46 @@ struct ddgi_ctx {
 
 
 namespace ddgi {
+
+// Ray order of one update: octant-binned (sign bits of x, y, z), and within
+// an octant along a Morton curve over the octahedral map (|x|, |y| of the
+// direction scaled to |x| + |y| + |z| = 1), so that consecutive entries are
+// close directions.  Only the order in which rays are traced depends on it.
+inline void ray_order_of(const float* dirs4, uint32_t R, uint32_t* order) {
+    std::vector<uint64_t> key(R);
+    for (uint32_t r = 0; r < R; ++r) {
+        const float* d = dirs4 + 4 * (size_t)r;
+        uint32_t oct = (d[0] < 0.0f ? 1u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 4u : 0u);
+        float s = std::fabs(d[0]) + std::fabs(d[1]) + std::fabs(d[2]);
+        float u = s > 0.0f ? std::fabs(d[0]) / s : 0.0f, v = s > 0.0f ? std::fabs(d[1]) / s : 0.0f;
+        uint32_t qu = (uint32_t)std::min(1023.0f, u * 1024.0f), qv = (uint32_t)std::min(1023.0f, v * 1024.0f);
+        uint32_t m = 0;
+        for (int b = 0; b < 10; ++b) m |= ((qu >> b) & 1u) << (2 * b) | ((qv >> b) & 1u) << (2 * b + 1);
+        key[r] = ((uint64_t)oct << 40) | ((uint64_t)m << 12) | r;
+    }
+    std::sort(key.begin(), key.end());
+    for (uint32_t r = 0; r < R; ++r) order[r] = (uint32_t)(key[r] & 0xFFFu);
+}
+
+// Probes of a grid sorted by the Morton code of (x, y, z).
+inline std::vector<uint32_t> probe_morton_order(const int32_t res[3]) {
+    const uint32_t P = (uint32_t)res[0] * (uint32_t)res[1] * (uint32_t)res[2];
+    auto spread = [](uint64_t x) {
+        uint64_t r = 0;
+        for (int b = 0; b < 21; ++b) r |= ((x >> b) & 1ull) << (3 * b);
+        return r;
+    };
+    std::vector<uint64_t> key(P);
+    for (uint32_t p = 0; p < P; ++p) {
+        uint32_t x = p % (uint32_t)res[0], y = (p / (uint32_t)res[0]) % (uint32_t)res[1];
+        uint32_t z = p / ((uint32_t)res[0] * (uint32_t)res[1]);
+        key[p] = spread(x) | spread(y) << 1 | spread(z) << 2;
+    }
+    std::vector<uint32_t> order(P);
+    for (uint32_t p = 0; p < P; ++p) order[p] = p;
+    std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
+    return order;
+}
 
 // Traversal view of a context's scene buffers.
 inline DeviceScene device_scene(const ddgi_ctx* c) {

@@ -242,6 +242,7 @@ ddgi_status ddgi_create(const ddgi_grid_desc* grid, ddgi_ctx** out) {
         cudaMalloc(&ctx->ray_order, sizeof(uint32_t) * DDGI_MAX_RAYS_PER_PROBE) != cudaSuccess ||
         cudaMalloc(&ctx->probe_list, sizeof(uint32_t) * P) != cudaSuccess ||
         cudaMalloc(&ctx->sched, 4 * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&ctx->probe_perm, sizeof(uint32_t) * P) != cudaSuccess ||
         cudaMalloc(&ctx->err, sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&ctx->counters, 4 * sizeof(uint32_t)) != cudaSuccess) {
         cudaGetLastError();
@@ -266,6 +267,10 @@ ddgi_status ddgi_create(const ddgi_grid_desc* grid, ddgi_ctx** out) {
     cudaMemset(ctx->depth, 0, atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, ctx->fp16));
     cudaMemset(ctx->err, 0, sizeof(uint32_t));
     cudaMemset(ctx->sched, 0, 4 * sizeof(uint32_t));
+    {
+        std::vector<uint32_t> perm = probe_morton_order(grid->resolution);
+        cudaMemcpy(ctx->probe_perm, perm.data(), sizeof(uint32_t) * P, cudaMemcpyHostToDevice);
+    }
     std::vector<uint32_t> ones(P, 1u);
     cudaMemcpy(ctx->states, ones.data(), sizeof(uint32_t) * P, cudaMemcpyHostToDevice);
     for (int i = 0; i < 4; ++i)
@@ -310,6 +315,7 @@ ddgi_status ddgi_destroy(ddgi_ctx* ctx) {
     dfree(ctx->ray_order);
     dfree(ctx->probe_list);
     dfree(ctx->sched);
+    dfree(ctx->probe_perm);
     dfree(ctx->init_dirs);
     dfree(ctx->init_back);
     dfree(ctx->init_near);
@@ -648,17 +654,7 @@ ddgi_status prepare_update(ddgi_ctx* ctx, const float orientation[9], const uint
     ctx->host_dirs.resize(4 * (size_t)R);
     ddgi_ray_direction_table(orientation, R, ctx->host_dirs.data());
     ctx->host_order.resize(R);
-    {
-        uint32_t counts[9] = {0};
-        std::vector<uint8_t> oct(R);
-        for (uint32_t r = 0; r < R; ++r) {
-            const float* dd = &ctx->host_dirs[4 * (size_t)r];
-            oct[r] = (uint8_t)((dd[0] < 0.0f ? 1 : 0) | (dd[1] < 0.0f ? 2 : 0) | (dd[2] < 0.0f ? 4 : 0));
-            counts[oct[r] + 1]++;
-        }
-        for (int k = 0; k < 8; ++k) counts[k + 1] += counts[k];
-        for (uint32_t r = 0; r < R; ++r) ctx->host_order[counts[oct[r]]++] = r;
-    }
+    ray_order_of(ctx->host_dirs.data(), R, ctx->host_order.data());
     CK(cudaMemcpyAsync(ctx->dirs, ctx->host_dirs.data(), sizeof(float4) * R, cudaMemcpyHostToDevice, st), "upload dirs");
     CK(cudaMemcpyAsync(ctx->ray_order, ctx->host_order.data(), sizeof(uint32_t) * R, cudaMemcpyHostToDevice, st),
        "upload order");
@@ -671,6 +667,15 @@ ddgi_status prepare_update(ddgi_ctx* ctx, const float orientation[9], const uint
     if (s != DDGI_OK) return s;
     *n_out = n;
     return DDGI_OK;
+}
+
+TraceTuning trace_tuning(const ddgi_ctx* ctx) {
+    TraceTuning t;
+    t.ctas_per_sm = ctx->tune.ctas_per_sm;
+    t.refill = ctx->tune.refill_lanes;
+    t.split = ctx->tune.smem_stack;
+    t.rays_per_warp = ctx->tune.rays_per_warp;
+    return t;
 }
 
 // Blend + border copy of the ray records in ctx->rays: the FP32 SIMT kernel or
@@ -729,7 +734,8 @@ ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_
         ShadowQueue q{ctx->q_idx, ctx->q_pos, ctx->q_sun, nullptr};
         CK(launch_wavefront(sc, ctx->dg, ctx->dl, dlist, n, ctx->dirs, ctx->ray_order, ctx->states, ctx->color,
                             ctx->depth, ctx->fp16, wh, q, ctx->counters, ctx->rays, hits_out, ctx->scene.stack_cap,
-                            ctx->err, st, ctx->timing ? ctx->ev[3] : nullptr),
+                            ctx->err, st, ctx->timing ? ctx->ev[3] : nullptr, nullptr, trace_tuning(ctx),
+                            ctx->probe_perm),
            "wavefront trace launch");
     }
     if (ctx->timing) CK(cudaEventRecord(ctx->ev[1], st), "event");
@@ -787,7 +793,8 @@ ddgi_status ddgi_update_scheduled(ddgi_ctx* ctx, const float orientation[9], uin
     ddgi_hit* hits_out = ctx->record_hits ? ctx->hits : nullptr;
     CK(launch_wavefront(device_scene(ctx), ctx->dg, ctx->dl, ctx->probe_list, P, ctx->dirs, ctx->ray_order,
                         ctx->states, ctx->color, ctx->depth, ctx->fp16, wh, q, ctx->counters, ctx->rays, hits_out,
-                        ctx->scene.stack_cap, ctx->err, st, ctx->timing ? ctx->ev[3] : nullptr, dcount),
+                        ctx->scene.stack_cap, ctx->err, st, ctx->timing ? ctx->ev[3] : nullptr, dcount,
+                        trace_tuning(ctx), nullptr),
        "wavefront trace launch");
     if (ctx->timing) CK(cudaEventRecord(ctx->ev[1], st), "event");
     if (ctx->fp16)
@@ -833,6 +840,119 @@ ddgi_status ddgi_set_schedule(ddgi_ctx* ctx, uint32_t offset, uint32_t loop, ddg
     const uint32_t h[4] = {offset, loop, 0, 0};
     CK(cudaMemcpyAsync(ctx->sched, h, sizeof(h), cudaMemcpyHostToDevice, st), "write schedule");
     CK(cudaStreamSynchronize(st), "write schedule");
+    return DDGI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Traversal launch tuning
+// ---------------------------------------------------------------------------
+ddgi_status ddgi_set_trace_tuning(ddgi_ctx* ctx, const ddgi_trace_tuning* t) {
+    if (!ctx || !t) return DDGI_ERR_INVALID_ARGUMENT;
+    const uint32_t r = t->rays_per_warp;
+    if (!(r == 0 || r == 1 || r == 2 || r == 4 || r == 8 || r == 16 || r == 32))
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "rays_per_warp = %u: want 0, 1, 2, 4, 8, 16 or 32", r);
+    if (t->refill_lanes < 1 || t->refill_lanes > 32)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "refill_lanes = %u outside [1, 32]", t->refill_lanes);
+    if (t->smem_stack > (uint32_t)kMaxStack || t->ctas_per_sm > 32)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "smem_stack or ctas_per_sm out of range");
+    ctx->tune = *t;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_get_trace_tuning(const ddgi_ctx* ctx, ddgi_trace_tuning* out) {
+    if (!ctx || !out) return DDGI_ERR_INVALID_ARGUMENT;
+    *out = ctx->tune;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t reps, ddgi_stream stream,
+                          ddgi_trace_tuning* chosen) {
+    if (!ctx || !orientation) return DDGI_ERR_INVALID_ARGUMENT;
+    if (!ctx->scene.built) return fail(ctx, DDGI_ERR_NO_SCENE, "ddgi_autotune before ddgi_scene_build");
+    if (reps == 0) reps = 3;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    // save what the trial updates overwrite
+    struct Saved {
+        void* dst;
+        void* copy;
+        size_t bytes;
+    };
+    std::vector<Saved> saved;
+    const size_t cb = atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, ctx->fp16), db = atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, ctx->fp16);
+    std::vector<std::pair<void*, size_t>> parts = {
+        {ctx->color, cb}, {ctx->depth, db}, {ctx->states, sizeof(uint32_t) * probe_count_of(ctx->grid)}};
+    if (ctx->fp16) {
+        parts.push_back({ctx->acc_color, atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, false)});
+        parts.push_back({ctx->acc_depth, atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, false)});
+    }
+    auto release = [&]() {
+        for (auto& x : saved) cudaFree(x.copy);
+        saved.clear();
+    };
+    for (auto& pt : parts) {
+        void* c = nullptr;
+        if (cudaMalloc(&c, pt.second) != cudaSuccess) {
+            cudaGetLastError();
+            release();
+            return fail(ctx, DDGI_ERR_OUT_OF_MEMORY, "autotune: no room to save the atlases");
+        }
+        saved.push_back({pt.first, c, pt.second});
+        CK(cudaMemcpyAsync(c, pt.first, pt.second, cudaMemcpyDeviceToDevice, st), "autotune save");
+    }
+    const ddgi_trace_tuning start = ctx->tune;
+    const bool timing = ctx->timing;
+    ctx->timing = true;
+    auto measure = [&](const ddgi_trace_tuning& t, float* out) -> ddgi_status {
+        ctx->tune = t;
+        std::vector<float> v;
+        for (uint32_t r = 0; r <= reps; ++r) {  // the first run is not timed
+            ddgi_status q = ddgi_update(ctx, orientation, nullptr, 0, stream);
+            if (q != DDGI_OK) return q;
+            CK(cudaEventSynchronize(ctx->ev[2]), "autotune");
+            ctx->timing_pending = false;
+            float a = 0.0f;
+            cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);  // trace: primary + shading + shadow rays
+            if (r > 0) v.push_back(a);
+        }
+        std::sort(v.begin(), v.end());
+        *out = v[v.size() / 2];
+        return check_device_error(ctx);
+    };
+    ddgi_trace_tuning best = start;
+    float best_t = 0.0f;
+    ddgi_status err = measure(best, &best_t);
+    const uint32_t R = ctx->grid.rays_per_probe;
+    const uint32_t rpw_c[] = {0u, 32u, 16u, 8u, 4u, 2u, 1u};
+    const uint32_t refill_c[] = {4u, 8u, 16u, 24u};
+    const uint32_t split_c[] = {0u, 32u, 24u, 16u};
+    const uint32_t ctas_c[] = {0u, 6u, 4u};
+    for (int p = 0; p < 4 && err == DDGI_OK; ++p) {
+        const uint32_t* cand = p == 0 ? rpw_c : p == 1 ? refill_c : p == 2 ? split_c : ctas_c;
+        const int nc = p == 0 ? 7 : p == 3 ? 3 : 4;
+        for (int i = 0; i < nc && err == DDGI_OK; ++i) {
+            ddgi_trace_tuning t = best;
+            uint32_t* field = p == 0 ? &t.rays_per_warp : p == 1 ? &t.refill_lanes : p == 2 ? &t.smem_stack
+                                                                                      : &t.ctas_per_sm;
+            if (*field == cand[i]) continue;
+            if (p == 0 && grouped_rays_per_warp(cand[i], R) != cand[i]) continue;
+            if (p == 2 && cand[i] != 0 && (int)cand[i] >= ctx->scene.stack_cap) continue;
+            *field = cand[i];
+            float tt = 0.0f;
+            err = measure(t, &tt);
+            if (err == DDGI_OK && tt < best_t) {
+                best_t = tt;
+                best = t;
+            }
+        }
+    }
+    for (auto& x : saved) cudaMemcpyAsync(x.dst, x.copy, x.bytes, cudaMemcpyDeviceToDevice, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    release();
+    ctx->timing = timing;
+    ctx->tune = err == DDGI_OK ? best : start;
+    if (err != DDGI_OK) return err;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "autotune restore");
+    if (chosen) *chosen = best;
     return DDGI_OK;
 }
 

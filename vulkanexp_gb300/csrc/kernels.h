@@ -29,12 +29,30 @@ struct ShadowQueue {
     float4* sun;     // unshadowed sun term (xyz) and night fade (w)
     uint32_t* count;
 };
+// Launch shape of the persistent traversals.
+struct TraceTuning {
+    uint32_t ctas_per_sm;    // 0: occupancy limit
+    uint32_t refill;         // idle lanes that trigger a warp's work request
+    uint32_t split;          // stack entries in shared memory (0 or >= cap: all)
+    uint32_t rays_per_warp;  // 0: a warp per probe in slot order; 1..32: grouped order (see below)
+};
+// Grouped order: lane groups of rays_per_warp consecutive directions (of the
+// octant-binned ray order) from 32 / rays_per_warp probes taken in `perm`
+// order (Morton order of the grid).  Usable values divide 32 and R (32
+// always); anything else falls back to 0.
+inline uint32_t grouped_rays_per_warp(uint32_t rpw, uint32_t R) {
+    if (rpw == 32u) return 32u;
+    return (rpw == 1 || rpw == 2 || rpw == 4 || rpw == 8 || rpw == 16) && R % rpw == 0 ? rpw : 0u;
+}
+// perm: probes in the order lane groups take them (all probes, no list), or
+// NULL for a warp per probe in slot order.
 cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L,
                              const uint32_t* probe_list, uint32_t nprobes, const float4* dirs,
                              const uint32_t* ray_order, const uint32_t* states, const void* color, const void* depth,
                              bool fp16_atlas, WaveHits hits, ShadowQueue q, uint32_t* counters, float4* rays_out,
                              ddgi_hit* hits_out, int stack_cap, uint32_t* err, cudaStream_t st,
-                             cudaEvent_t after_primary, const uint32_t* dev_count = nullptr);
+                             cudaEvent_t after_primary, const uint32_t* dev_count, const TraceTuning& tune,
+                             const uint32_t* perm);
 // Probe classification (probesInit): kInitRays rays per probe.
 constexpr uint32_t kInitRays = 512;
 cudaError_t launch_init_probes(const DeviceScene& sc, const DeviceGrid& g, const float4* dirs, uint32_t P,
@@ -69,6 +87,8 @@ struct BatchVolume {
     float2* acc_depth;
     uint8_t* wbuf;  // tensor-core weight chunks of this update (BF16 form)
     float* rowsum;
+    const uint32_t* perm;  // probe order of grouped warps (NULL: a warp per probe)
+    uint32_t rays_per_warp;
 };
 
 struct BatchTables {
@@ -88,12 +108,6 @@ struct BatchBlendList {
     const uint32_t* list;
     const uint32_t* tile_base;
     uint32_t n, ntiles;
-};
-
-struct TraceTuning {
-    uint32_t ctas_per_sm;  // 0: occupancy limit
-    uint32_t refill;       // idle lanes that trigger a warp's work request
-    uint32_t split;        // stack entries in shared memory (>= cap: all)
 };
 
 // wavefront.cu: primary trace, shading and shadow rays of all volumes

@@ -26,6 +26,23 @@ namespace {
 constexpr int kPersistThreads = 128;
 constexpr unsigned kFull = 0xffffffffu;
 
+// Work item `id` of a grouped order: groups of G = 32 / rpw probes (in perm
+// order) take rpw consecutive directions of the ray order each per 32 items,
+// so a warp traces similar directions from neighbouring probes.  Returns the
+// probe slot and the position in the ray order.
+__device__ __forceinline__ void grouped_ray(uint32_t id, uint32_t R, uint32_t rpw, uint32_t n,
+                                            const uint32_t* perm, uint32_t* slot, uint32_t* j) {
+    const uint32_t G = 32u / rpw;
+    const uint32_t first = (id / (G * R)) * G;
+    const uint32_t m = min(G, n - first);
+    const uint32_t local = id - first * R;
+    const uint32_t span = m * rpw;
+    const uint32_t c = local / span, r = local - c * span;
+    const uint32_t q = r / rpw;
+    *j = c * rpw + (r - q * rpw);
+    *slot = __ldg(perm + first + q);
+}
+
 struct PrimaryJob {
     DeviceGrid g;
     const uint32_t* probe_list;
@@ -34,11 +51,19 @@ struct PrimaryJob {
     WaveHits hits;
     uint32_t total;
     const uint32_t* dev_count;  // listed probes, read on the device (NULL: total / rays)
+    const uint32_t* perm;       // grouped order over all probes (NULL: a warp per probe slot)
+    uint32_t rpw, nprobes;
 
     template <class W>
     __device__ __forceinline__ bool start(W& w, const DeviceScene& sc, uint32_t id, uint32_t* out) const {
-        uint32_t R = g.rays;
-        uint32_t slot = id / R, j = id - slot * R;
+        const uint32_t R = g.rays;
+        uint32_t slot, j;
+        if (perm) {
+            grouped_ray(id, R, rpw, nprobes, perm, &slot, &j);
+        } else {
+            slot = id / R;
+            j = id - slot * R;
+        }
         uint32_t ray = __ldg(ray_order + j);
         uint32_t probe = probe_list ? __ldg(probe_list + slot) : slot;
         *out = slot * R + ray;
@@ -148,15 +173,18 @@ __device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job
     }
 }
 
-__global__ void __launch_bounds__(kPersistThreads) k_primary(DeviceScene sc, PrimaryJob job, uint32_t* counter,
-                                                             int stack_cap, uint32_t* err) {
+template <class Stack>
+__global__ void __launch_bounds__(kPersistThreads, 8) k_primary(DeviceScene sc, PrimaryJob job, uint32_t* counter,
+                                                                int stack_cap, int split, int refill, uint32_t* err) {
     const uint32_t total = job.dev_count ? *job.dev_count * job.g.rays : job.total;
-    persistent_walk<false, SmemStack>(sc, job, total, counter, stack_cap, stack_cap, 8, err);
+    persistent_walk<false, Stack>(sc, job, total, counter, stack_cap, split, refill, err);
 }
 
-__global__ void __launch_bounds__(kPersistThreads) k_shadow(DeviceScene sc, ShadowJob job, const uint32_t* qcount,
-                                                            uint32_t* counter, int stack_cap, uint32_t* err) {
-    persistent_walk<true, SmemStack>(sc, job, *qcount, counter, stack_cap, stack_cap, 8, err);
+template <class Stack>
+__global__ void __launch_bounds__(kPersistThreads, 8) k_shadow(DeviceScene sc, ShadowJob job, const uint32_t* qcount,
+                                                               uint32_t* counter, int stack_cap, int split, int refill,
+                                                               uint32_t* err) {
+    persistent_walk<true, Stack>(sc, job, *qcount, counter, stack_cap, split, refill, err);
 }
 
 template <class AV>
@@ -288,10 +316,18 @@ struct BatchPrimaryJob {
         const uint32_t v = batch_volume(bt, id);
         const BatchVolume& vol = bt.vols[v];
         const uint32_t R = vol.g.rays;
-        const uint32_t local = id - __ldg(bt.ray_base + v);
-        const uint32_t slot = local / R, j = local - slot * R;
+        const uint32_t base = __ldg(bt.ray_base + v);
+        const uint32_t local = id - base;
+        uint32_t slot, j;
+        if (vol.perm) {
+            grouped_ray(local, R, vol.rays_per_warp,
+                        (uint32_t)vol.g.res[0] * (uint32_t)vol.g.res[1] * (uint32_t)vol.g.res[2], vol.perm, &slot, &j);
+        } else {
+            slot = local / R;
+            j = local - slot * R;
+        }
         const uint32_t ray = __ldg(bt.ray_order + vol.dir_base + j);
-        *out = id - j + ray;  // record ray_base + slot * R + ray
+        *out = base + slot * R + ray;
         float4 d4 = __ldg(bt.dirs + vol.dir_base + ray);
         return w.start_at(sc, vol.root, probe_origin_exact(vol.g, slot), f3(d4.x, d4.y, d4.z), 0.01f, vol.g.tmax,
                           0x3u);
@@ -426,21 +462,19 @@ uint32_t persistent_blocks(const void* kernel, size_t smem, uint32_t cap_per_sm 
 
 }  // namespace
 
-cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L,
-                             const uint32_t* probe_list, uint32_t nprobes, const float4* dirs,
-                             const uint32_t* ray_order, const uint32_t* states, const void* color, const void* depth,
-                             bool fp16_atlas, WaveHits hits, ShadowQueue q, uint32_t* counters, float4* rays_out,
-                             ddgi_hit* hits_out, int stack_cap, uint32_t* err, cudaStream_t st,
-                             cudaEvent_t after_primary, const uint32_t* dev_count) {
-    uint32_t total = nprobes * g.rays;
-    if (total == 0) return cudaSuccess;
-    // counters[0]: primary work, counters[1]: shadow queue length, counters[2]: shadow work
-    cudaError_t e = cudaMemsetAsync(counters, 0, 3 * sizeof(uint32_t), st);
-    if (e != cudaSuccess) return e;
-    const size_t smem = (size_t)stack_cap * kPersistThreads * sizeof(int);
-    PrimaryJob pj{g, probe_list, dirs, ray_order, hits, total, dev_count};
-    k_primary<<<persistent_blocks((const void*)k_primary, smem), kPersistThreads, smem, st>>>(sc, pj, counters,
-                                                                                             stack_cap, err);
+namespace {
+
+template <class Stack>
+cudaError_t wavefront_kernels(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L,
+                              const uint32_t* probe_list, uint32_t total, const float4* dirs, const uint32_t* states,
+                              const void* color, const void* depth, bool fp16_atlas, WaveHits hits, ShadowQueue q,
+                              uint32_t* counters, float4* rays_out, ddgi_hit* hits_out, int stack_cap, int split,
+                              uint32_t* err, cudaStream_t st, cudaEvent_t after_primary, const uint32_t* dev_count,
+                              const TraceTuning& tune, const PrimaryJob& pj) {
+    const size_t smem = (size_t)split * kPersistThreads * sizeof(int);
+    const int refill = (int)(tune.refill < 1 ? 1 : (tune.refill > 32 ? 32 : tune.refill));
+    k_primary<Stack><<<persistent_blocks((const void*)k_primary<Stack>, smem, tune.ctas_per_sm), kPersistThreads,
+                       smem, st>>>(sc, pj, counters, stack_cap, split, refill, err);
     if (after_primary) cudaEventRecord(after_primary, st);
     ShadowQueue qq = q;
     qq.count = counters + 1;
@@ -457,9 +491,36 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
                                         dev_count, err);
     }
     ShadowJob sj{qq, make_float3(L.dir[0], L.dir[1], L.dir[2]), rays_out, hits.prim, 0};
-    k_shadow<<<persistent_blocks((const void*)k_shadow, smem), kPersistThreads, smem, st>>>(
-        sc, sj, counters + 1, counters + 2, stack_cap, err);
+    k_shadow<Stack><<<persistent_blocks((const void*)k_shadow<Stack>, smem, tune.ctas_per_sm), kPersistThreads, smem,
+                      st>>>(sc, sj, counters + 1, counters + 2, stack_cap, split, refill, err);
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L,
+                             const uint32_t* probe_list, uint32_t nprobes, const float4* dirs,
+                             const uint32_t* ray_order, const uint32_t* states, const void* color, const void* depth,
+                             bool fp16_atlas, WaveHits hits, ShadowQueue q, uint32_t* counters, float4* rays_out,
+                             ddgi_hit* hits_out, int stack_cap, uint32_t* err, cudaStream_t st,
+                             cudaEvent_t after_primary, const uint32_t* dev_count, const TraceTuning& tune,
+                             const uint32_t* perm) {
+    uint32_t total = nprobes * g.rays;
+    if (total == 0) return cudaSuccess;
+    // counters[0]: primary work, counters[1]: shadow queue length, counters[2]: shadow work
+    cudaError_t e = cudaMemsetAsync(counters, 0, 3 * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    const uint32_t rpw = grouped_rays_per_warp(tune.rays_per_warp, g.rays);
+    // the grouped order covers all probes in perm order: no list, no device count
+    const uint32_t* pm = (perm && !probe_list && !dev_count && rpw != 0u) ? perm : nullptr;
+    PrimaryJob pj{g, probe_list, dirs, ray_order, hits, total, dev_count, pm, rpw, nprobes};
+    if (tune.split == 0 || (int)tune.split >= stack_cap)
+        return wavefront_kernels<SmemStack>(sc, g, L, probe_list, total, dirs, states, color, depth, fp16_atlas, hits,
+                                            q, counters, rays_out, hits_out, stack_cap, stack_cap, err, st,
+                                            after_primary, dev_count, tune, pj);
+    return wavefront_kernels<SplitStack>(sc, g, L, probe_list, total, dirs, states, color, depth, fp16_atlas, hits, q,
+                                         counters, rays_out, hits_out, stack_cap, (int)tune.split, err, st,
+                                         after_primary, dev_count, tune, pj);
 }
 
 namespace {

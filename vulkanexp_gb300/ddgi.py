@@ -16,7 +16,7 @@ import os
 import numpy as np
 
 from . import abi
-from .abi import HIT_DTYPE, BatchTuning, GridDesc, Light, SceneDesc, Timings
+from .abi import HIT_DTYPE, BatchTuning, GridDesc, Light, SceneDesc, Timings, TraceTuning
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libddgi_gb300.so")
@@ -68,6 +68,9 @@ _SIGNATURES = [
     ("ddgi_blend_records_noalloc", C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p]),
+    ("ddgi_set_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
+    ("ddgi_get_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
+    ("ddgi_autotune", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_init_probes", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ddgi_update_scheduled", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     ("ddgi_get_schedule", C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
@@ -198,6 +201,25 @@ class Context:
         pl = None if probe_list is None else np.ascontiguousarray(probe_list, np.uint32)
         self._check(self.lib.ddgi_update(self.h, _ptr(o), _ptr(pl), 0 if pl is None else len(pl),
                                          _stream_ptr(stream)))
+
+    def trace_tuning(self):
+        t = TraceTuning()
+        self._check(self.lib.ddgi_get_trace_tuning(self.h, C.byref(t)))
+        return {k: int(getattr(t, k)) for k, _ in t._fields_}
+
+    def set_trace_tuning(self, **kw):
+        t = TraceTuning()
+        self._check(self.lib.ddgi_get_trace_tuning(self.h, C.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        self._check(self.lib.ddgi_set_trace_tuning(self.h, C.byref(t)))
+
+    def autotune(self, orientation, reps=3, stream=None):
+        """Picks the fastest traversal launch tuning (see ddgi_autotune)."""
+        o = np.ascontiguousarray(orientation, np.float32).reshape(9)
+        t = TraceTuning()
+        self._check(self.lib.ddgi_autotune(self.h, _ptr(o), int(reps), _stream_ptr(stream), C.byref(t)))
+        return {k: int(getattr(t, k)) for k, _ in t._fields_}
 
     def init_probes(self, orientation, stream=None):
         """Probe classification (probesInit): states 0 (OFF), 1 or 8."""
