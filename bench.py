@@ -314,6 +314,50 @@ def measure_batching(stream, steps, warmup, flush):
     return out
 
 
+def measure_final_gather(ctx, w, stream, flush, reps=10, width=1920, height=1080):
+    """The atlas consumer: FinalGather.frag over a seeded 1920x1080 G-buffer
+    (positions inside the probe grid, random normals and materials, 10% sky
+    pixels) on the context's current atlas.  CUDA events over `reps`
+    launches, L2 flushed before each; algorithmic bytes per pixel: the
+    G-buffer read (4 x float4 + float + float4 reflection) and the float4
+    written = 100 B (probe-atlas texels are L2-resident)."""
+    import torch
+
+    g = w.grid
+    n = width * height
+    gen = torch.Generator(device="cuda").manual_seed(1239)
+    lo = torch.tensor(list(g.extent_min), device="cuda")
+    hi = torch.tensor(list(g.extent_max), device="cuda")
+    pos = lo + (hi - lo) * torch.rand((n, 3), device="cuda", generator=gen)
+    depth = torch.where(torch.rand(n, device="cuda", generator=gen) < 0.1, 0.0, 1.0)
+    u = lambda *sh: torch.rand(sh, device="cuda", generator=gen)
+    gb = {"position_depth": torch.cat([pos, depth[:, None]], 1).reshape(height, width, 4).contiguous(),
+          "normal_metalness": torch.cat([torch.randn((n, 3), device="cuda", generator=gen), u(n, 1)], 1)
+          .reshape(height, width, 4).contiguous(),
+          "albedo_roughness": u(n, 4).reshape(height, width, 4).contiguous(),
+          "emissive": (0.1 * u(n, 4)).reshape(height, width, 4).contiguous(),
+          "direct_light": u(n).reshape(height, width).contiguous(),
+          "reflection": u(n, 4).reshape(height, width, 4).contiguous()}
+    out = torch.empty((height, width, 4), dtype=torch.float32, device="cuda")
+    origin = [0.5 * (a + b) for a, b in zip(g.extent_min, g.extent_max)]
+    for _ in range(3):
+        ctx.final_gather(gb, origin, out, stream)
+    ms = []
+    for k in range(reps):
+        flush.fill_(k & 255)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.final_gather(gb, origin, out, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    t = float(np.median(ms))
+    hbm, _, _ = load_peaks()
+    gbs = n * 100 / (t * 1e-3) / 1e9
+    return {"kernel": "k_final_gather", "pixels": n, "ms": t, "gpixels_per_s": n / (t * 1e-3) / 1e9,
+            "achieved_gbs": gbs, "frac_hbm": gbs / hbm, "bytes_per_pixel": 100}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -440,6 +484,7 @@ def main():
             "roofline_blend": roofline_blend,
             "e2e": {"value": e2e_val, "unit": UNIT, "ms_per_step": float(np.mean(e2e_ms)),
                     "h2d_bytes_per_step": R * 20, "d2h_bytes_per_step": int(host_c.nbytes + host_d.nbytes)}}
+    line["final_gather"] = measure_final_gather(ctx, w, stream, flush)
     ctx.close()
     line["differentiation"] = measure_differentiation(stream)
     line["batching"] = measure_batching(stream, args.steps, args.warmup, flush)

@@ -323,6 +323,17 @@ ddgi_status ddgi_forward_record(ddgi_ctx* ctx, uint32_t K, const float* orientat
 ddgi_status ddgi_backward(ddgi_ctx* ctx, const float* dL_dcolor, size_t bytes, float* grad_albedo, float grad_sun[3],
                           float grad_sky[3], ddgi_stream stream);
 
+/* Moves instances: Renderer::updateAccelerationStructureInstances +
+ * updateTLAS (src/Renderer.cpp:671-742).  `transforms` = count new
+ * object-to-world transforms (row-major 3x4) for the instances `ids` (NULL:
+ * instances 0 .. count-1).  rebuild = 0: the top-level tree keeps its
+ * topology and its boxes are recomputed bottom-up on the device (the
+ * reference's UPDATE-mode build); rebuild = 1: the top-level tree is built
+ * again over the new instance boxes.  Mesh trees are not touched.  Ordered
+ * on `stream`; a batch made from this context must be made again. */
+ddgi_status ddgi_update_instances(ddgi_ctx* ctx, const uint32_t* ids, const float* transforms, uint32_t count,
+                                  int rebuild, ddgi_stream stream);
+
 /* ---- Probe classification and adaptive schedule -------------------------
  * IrradianceProbes::initProbes (src/IrradianceProbes.cpp:357-394,
  * src/shaders/probesInit.rgen:31-64): classifies every probe from 512 rays
@@ -351,6 +362,26 @@ ddgi_status ddgi_get_schedule(ddgi_ctx* ctx, uint32_t* count, uint32_t* offset, 
                               size_t list_capacity, ddgi_stream stream);
 /* Sets the schedule state (a new context starts at offset 0, loop 0). */
 ddgi_status ddgi_set_schedule(ddgi_ctx* ctx, uint32_t offset, uint32_t loop, ddgi_stream stream);
+
+/* ---- Final gather (the atlas's consumer) --------------------------------
+ * src/shaders/FinalGather.frag:39-80 as a headless pass over a G-buffer in
+ * device memory (all arrays width x height, tightly packed, row-major). */
+typedef struct ddgi_gbuffer {
+    const float* position_depth;   /* float4: world position, depth (<= 0: no geometry, sky) */
+    const float* normal_metalness; /* float4: normal (normalised here), metalness */
+    const float* albedo_roughness; /* float4: albedo rgb, roughness */
+    const float* emissive;         /* float4: emissive rgb */
+    const float* direct_light;     /* float: the sun's visibility (the reference's direct-light .r) */
+    const float* reflection;       /* float4: the reflection pass at this pixel; NULL = none */
+    uint32_t width, height;
+} ddgi_gbuffer;
+/* color_out (device, float4 per pixel) = direct * GGX sun + mix(0.004,
+ * albedo, metal) * reflection + sampleProbes(position, normal, view) *
+ * albedo * 0.996 * (1 - metal) + emissive, or the sky radiance on a miss;
+ * view = normalize(camera_origin - position).  Reads the context's current
+ * atlas and probe states.  Asynchronous on `stream`. */
+ddgi_status ddgi_final_gather(ddgi_ctx* ctx, const ddgi_gbuffer* gbuffer, const float camera_origin[3],
+                              float* color_out, ddgi_stream stream);
 
 /* ---- Launch tuning of the persistent traversals -------------------------
  * Results do not depend on these; speed does. */

@@ -19,6 +19,7 @@
  *   src/shaders/probesUpdate.glsl:29-121      colour/depth blend + state update
  *   src/shaders/probesCopyBorders.comp:21-245 border copy (generalised)
  *   src/shaders/probesInit.rgen:31-64         probe classification
+ *   src/shaders/FinalGather.frag:39-80        final gather (the atlas consumer)
  *
  * Traversal is opaque in the reference (driver-built Vulkan acceleration
  * structures on RT cores).  Its closest-hit SEMANTICS are restated: the hit
@@ -1330,6 +1331,61 @@ void oracle_init_probes(const oracle_scene* s, const ddgi_grid_desc* gd, const f
             states[p] = (float)back > 0.5f * (float)g.rays ? 0u : (near ? 1u : 8u);
         }
     }, 1);
+}
+
+// Final gather, src/shaders/FinalGather.frag:39-80 per pixel: sky radiance
+// where depth <= 0 (the constant sky replacing sky.glsl), else
+// direct * pbrMetallicRoughness(sun) + mix(0.004, albedo, metal) * reflection
+// + sampleProbes(position, normal, view) * albedo * (1 - 0.004) * (1 - metal)
+// + emissive, view = normalize(camera - position), normal normalised.
+void oracle_final_gather(const ddgi_grid_desc* gd, const ddgi_light* ld, const uint32_t* states, const float* color,
+                         const float* depth, uint32_t pixels, const float* position_depth,
+                         const float* normal_metalness, const float* albedo_roughness, const float* emissive,
+                         const float* direct_light, const float* reflection, const float* origin, float* out,
+                         int nthreads) {
+    const Grid g = make_grid(gd);
+    Atlas<float> at;
+    at.color = const_cast<float*>(color);
+    at.depth = const_cast<float*>(depth);
+    at.cw = g.colorRes * g.res[0] * g.res[1];
+    at.ch = g.colorRes * g.res[2];
+    at.dw = g.depthRes * g.res[0] * g.res[1];
+    at.dh = g.depthRes * g.res[2];
+    const F3 cam(origin[0], origin[1], origin[2]);
+    const F3 lc(ld->color[0], ld->color[1], ld->color[2]), ldir(ld->direction[0], ld->direction[1], ld->direction[2]);
+    parallel_for(pixels, nthreads, [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; ++i) {
+            const float* pd = position_depth + 4 * i;
+            float* o = out + 4 * i;
+            if (!(pd[3] > 0.0f)) {
+                o[0] = ld->sky[0];
+                o[1] = ld->sky[1];
+                o[2] = ld->sky[2];
+                o[3] = 1.0f;
+                continue;
+            }
+            const float* nm = normal_metalness + 4 * i;
+            const float* ar = albedo_roughness + 4 * i;
+            const F3 position(pd[0], pd[1], pd[2]);
+            const F3 normal = normalize(F3(nm[0], nm[1], nm[2]));
+            const F3 albedo(ar[0], ar[1], ar[2]);
+            const float metal = nm[3], rough = ar[3];
+            const F3 view = normalize(cam - position);
+            F3 c = pbr<float>(normal, view, lc, ldir, albedo, metal, rough) * direct_light[i];
+            const float f0 = 0.004f;
+            const F3 diffuse = albedo * (1.0f - f0) * (1.0f - metal);
+            const F3 specular = mix3(F3(f0, f0, f0), albedo, metal);
+            const F3 refl = reflection ? F3(reflection[4 * i], reflection[4 * i + 1], reflection[4 * i + 2])
+                                       : F3(0.0f, 0.0f, 0.0f);
+            c = c + specular * refl;
+            c = c + sample_probes<float>(position, normal, view, g, states, at) * diffuse;
+            c = c + F3(emissive[4 * i], emissive[4 * i + 1], emissive[4 * i + 2]);
+            o[0] = c.x;
+            o[1] = c.y;
+            o[2] = c.z;
+            o[3] = 1.0f;
+        }
+    }, 256);
 }
 
 int oracle_replay(const oracle_scene* s, const ddgi_grid_desc* g, const ddgi_light* l, const double* albedo,

@@ -98,6 +98,8 @@ class Oracle:
             lib.oracle_pbr.argtypes = [C.c_void_p] * 5 + [C.c_float, C.c_float, C.c_void_p]
             lib.oracle_sample_probes.argtypes = [C.POINTER(GridDesc)] + [C.c_void_p] * 7
             lib.oracle_init_probes.argtypes = [C.c_void_p, C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_int]
+            lib.oracle_final_gather.argtypes = [C.POINTER(GridDesc), C.POINTER(Light), C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_uint32] + [C.c_void_p] * 8 + [C.c_int]
             cls._lib = lib
         return cls._lib
 
@@ -194,6 +196,25 @@ class Oracle:
         fn = cls.lib().oracle_blend64 if color.dtype == np.float64 else cls.lib().oracle_blend
         fn(C.byref(grid), _ptr(orient), _ptr(plist), 0 if plist is None else len(plist), _ptr(rays), _ptr(states),
            _ptr(color), _ptr(depth), int(threads or os.cpu_count()))
+
+    @classmethod
+    def final_gather(cls, grid, light, states, color, depth, gbuffer, origin, threads=None):
+        """FinalGather.frag per pixel.  gbuffer: dict of float32 arrays
+        position_depth, normal_metalness, albedo_roughness, emissive (N x 4),
+        direct_light (N), reflection (N x 4 or None).  Returns N x 4."""
+        f = lambda a: None if a is None else np.ascontiguousarray(a, np.float32)
+        pd = f(gbuffer["position_depth"])
+        n = len(pd)
+        out = np.zeros((n, 4), np.float32)
+        o = np.ascontiguousarray(origin, np.float32)
+        keep = [f(gbuffer[k]) for k in ("normal_metalness", "albedo_roughness", "emissive", "direct_light")]
+        refl = f(gbuffer.get("reflection"))
+        cls.lib().oracle_final_gather(C.byref(grid), C.byref(light), _ptr(np.ascontiguousarray(states, np.uint32)),
+                                      _ptr(np.ascontiguousarray(color, np.float32)),
+                                      _ptr(np.ascontiguousarray(depth, np.float32)), n, _ptr(pd),
+                                      *[_ptr(k) for k in keep], _ptr(refl), _ptr(o), _ptr(out),
+                                      int(threads or os.cpu_count() or 1))
+        return out
 
     @classmethod
     def border_table(cls, n):

@@ -1,5 +1,6 @@
 """CPU checks of the oracle: pins against the reference's own tables and
 known-answer tests derived from the shader math (no GPU)."""
+import ctypes
 import json
 import os
 
@@ -197,3 +198,43 @@ def test_blend_entry_point_normalises(res):
     n = res[0]
     np.testing.assert_allclose(c[1:n - 1, 1:n - 1, :3], np.broadcast_to([0.125, 0.25, 0.5], (n - 2, n - 2, 3)),
                                rtol=1e-5)
+
+
+def test_final_gather_known_answers():
+    """FinalGather.frag with a zero atlas, no direct light and no
+    reflection leaves the emissive term; misses return the sky radiance;
+    with only direct light it is the GGX sun term."""
+    from oracle.oracle import Oracle, zero_atlas
+    from vulkanexp_gb300 import abi, scenes
+
+    g = abi.make_grid((0, 0, 0), (4, 4, 4), (3, 3, 3), 32)
+    L = scenes.default_light()
+    c, d = zero_atlas(g)
+    st = np.ones(g.probe_count(), np.uint32)
+    n = 6
+    rng = np.random.default_rng(1)
+    gb = {"position_depth": np.column_stack([rng.uniform(0, 4, (n, 3)), [1, 1, 1, 0, -1, 1]]),
+          "normal_metalness": np.column_stack([rng.normal(size=(n, 3)), rng.uniform(0, 1, n)]),
+          "albedo_roughness": np.column_stack([rng.uniform(0, 1, (n, 3)), rng.uniform(0.1, 1, n)]),
+          "emissive": np.column_stack([rng.uniform(0, 1, (n, 3)), np.zeros(n)]),
+          "direct_light": np.zeros(n), "reflection": None}
+    gb = {k: None if v is None else v.astype(np.float32) for k, v in gb.items()}
+    out = Oracle.final_gather(g, L, st, c, d, gb, (2, 2, 9))
+    hit = gb["position_depth"][:, 3] > 0
+    assert np.array_equal(out[hit, :3], gb["emissive"][hit, :3])
+    assert np.allclose(out[~hit, :3], np.asarray(L.sky[:3], np.float32), rtol=0, atol=0)
+    gb["emissive"][:] = 0
+    gb["direct_light"][:] = 1
+    out = Oracle.final_gather(g, L, st, c, d, gb, (2, 2, 9))
+    for i in np.flatnonzero(hit):
+        p = gb["position_depth"][i, :3].astype(np.float64)
+        nrm = gb["normal_metalness"][i, :3].astype(np.float64)
+        nrm /= np.linalg.norm(nrm)
+        v = np.array([2, 2, 9.0]) - p
+        v /= np.linalg.norm(v)
+        ref = np.zeros(3, np.float32)
+        Oracle.lib().oracle_pbr(*[np.ascontiguousarray(x, np.float32).ctypes.data_as(ctypes.c_void_p) for x in
+                                  (nrm, v, L.color[:3], L.direction[:3], gb["albedo_roughness"][i, :3])],
+                                float(gb["normal_metalness"][i, 3]), float(gb["albedo_roughness"][i, 3]),
+                                ref.ctypes.data_as(ctypes.c_void_p))
+        assert np.allclose(out[i, :3], ref, rtol=1e-5, atol=1e-7)

@@ -121,6 +121,13 @@ class BatchTuning(C.Structure):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
+class GBuffer(C.Structure):
+    """ddgi_gbuffer: device pointers of a G-buffer (width x height pixels)."""
+    _fields_ = [("position_depth", C.c_void_p), ("normal_metalness", C.c_void_p), ("albedo_roughness", C.c_void_p),
+                ("emissive", C.c_void_p), ("direct_light", C.c_void_p), ("reflection", C.c_void_p),
+                ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
 class TraceTuning(C.Structure):
     """ddgi_trace_tuning: launch parameters of a context's traversals."""
     _fields_ = [("rays_per_warp", C.c_uint32), ("refill_lanes", C.c_uint32), ("smem_stack", C.c_uint32),

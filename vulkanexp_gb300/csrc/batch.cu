@@ -253,7 +253,8 @@ ddgi_status stage_inputs(ddgi_batch* b, const float* orientations) {
         ddgi_ray_direction_table(&orientations[9 * v], R, d);
         // the volume's own record of its current direction table
         c->host_dirs.assign(d, d + 4 * (size_t)R);
-        ray_order_of(d, R, order + b->dir_base[v]);
+        const uint32_t rpw = grouped_rays_per_warp(b->tuning.rays_per_warp, R);
+        ray_order_of(d, R, order + b->dir_base[v], rpw > 0 && rpw < 32);
 
         BatchVolume& x = bv[v];
         memset(&x, 0, sizeof(x));

@@ -34,8 +34,21 @@ struct SceneBuffers {
     uint32_t depth_blas = 0, depth_tlas = 0;
     uint32_t vertex_count = 0, index_count = 0, offset_count = 0, material_count = 0, instance_count = 0;
     uint64_t node_count = 0, tri_count = 0;
-    uint64_t build_id = 0;  // distinct for every successful build in the process
+    uint64_t build_id = 0;  // distinct for every successful build or instance update in the process
     bool built = false;
+    // top level, kept for instance updates (refit / rebuild)
+    std::vector<GpuInstance> host_inst;      // caller order
+    std::vector<float> mesh_lo, mesh_hi;     // object-space bounds, 3 per mesh
+    std::vector<uint32_t> mesh_of_inst;
+    std::vector<float4> inst_lo, inst_hi;    // world boxes, caller order
+    std::vector<uint32_t> leaf_of_id;        // leaf slot of each instance
+    float4* leaf_lo = nullptr;               // world boxes in leaf order (device)
+    float4* leaf_hi = nullptr;
+    uint32_t* leaf_parent = nullptr;         // parent links of the top level (node << 1 | side)
+    uint32_t* node_parent = nullptr;
+    uint32_t* refit_flags = nullptr;
+    float4* sub_lo = nullptr;
+    float4* sub_hi = nullptr;
 };
 
 }  // namespace ddgi
@@ -116,11 +129,13 @@ struct ddgi_ctx {
 
 namespace ddgi {
 
-// Ray order of one update: octant-binned (sign bits of x, y, z), and within
-// an octant along a Morton curve over the octahedral map (|x|, |y| of the
-// direction scaled to |x| + |y| + |z| = 1), so that consecutive entries are
-// close directions.  Only the order in which rays are traced depends on it.
-inline void ray_order_of(const float* dirs4, uint32_t R, uint32_t* order) {
+// Ray order of one update: octant-binned (sign bits of x, y, z); within an
+// octant by ray index (`fine` = false: the spherical-Fibonacci index, i.e.
+// by elevation) or along a Morton curve over the octahedral map (`fine`:
+// |x|, |y| of the direction scaled to |x| + |y| + |z| = 1, so that short
+// runs are close directions, for warps that take a few rays per probe).
+// Only the order in which rays are traced depends on it.
+inline void ray_order_of(const float* dirs4, uint32_t R, uint32_t* order, bool fine) {
     std::vector<uint64_t> key(R);
     for (uint32_t r = 0; r < R; ++r) {
         const float* d = dirs4 + 4 * (size_t)r;
@@ -130,7 +145,7 @@ inline void ray_order_of(const float* dirs4, uint32_t R, uint32_t* order) {
         uint32_t qu = (uint32_t)std::min(1023.0f, u * 1024.0f), qv = (uint32_t)std::min(1023.0f, v * 1024.0f);
         uint32_t m = 0;
         for (int b = 0; b < 10; ++b) m |= ((qu >> b) & 1u) << (2 * b) | ((qv >> b) & 1u) << (2 * b + 1);
-        key[r] = ((uint64_t)oct << 40) | ((uint64_t)m << 12) | r;
+        key[r] = ((uint64_t)oct << 40) | ((uint64_t)(fine ? m : 0u) << 12) | r;
     }
     std::sort(key.begin(), key.end());
     for (uint32_t r = 0; r < R; ++r) order[r] = (uint32_t)(key[r] & 0xFFFu);

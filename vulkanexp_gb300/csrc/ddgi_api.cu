@@ -136,6 +136,13 @@ size_t atlas_bytes(const DeviceGrid& d, ddgi_atlas_kind k, bool fp16) {
 }
 
 void free_scene(SceneBuffers& s) {
+    dfree(s.leaf_lo);
+    dfree(s.leaf_hi);
+    dfree(s.leaf_parent);
+    dfree(s.node_parent);
+    dfree(s.refit_flags);
+    dfree(s.sub_lo);
+    dfree(s.sub_hi);
     dfree(s.nodes);
     dfree(s.tris);
     dfree(s.inst_leaf);
@@ -388,6 +395,112 @@ ddgi_status ddgi_enable_timing(ddgi_ctx* ctx, int enable) {
 // ---------------------------------------------------------------------------
 // Scene build (replaces the BLAS/TLAS build of src/Renderer.cpp:272-642)
 // ---------------------------------------------------------------------------
+namespace {
+
+uint64_t next_build_id() {
+    static std::atomic<uint64_t> builds{0};
+    return ++builds;
+}
+
+// World box of an instance: the 8 corners of its mesh's object-space bounds
+// through the object-to-world transform (in double), rounded to float and
+// enlarged like the tree builder's boxes; empty for an empty mesh.
+void instance_world_box(const float* transform, const float* ml, const float* mh, bool valid, float4* olo,
+                        float4* ohi) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    if (valid && ml[0] <= mh[0]) {
+        for (int c = 0; c < 8; ++c) {
+            double p[3] = {(c & 1) ? mh[0] : ml[0], (c & 2) ? mh[1] : ml[1], (c & 4) ? mh[2] : ml[2]};
+            for (int k = 0; k < 3; ++k) {
+                float q = (float)(transform[4 * k] * p[0] + transform[4 * k + 1] * p[1] + transform[4 * k + 2] * p[2] +
+                                  transform[4 * k + 3]);
+                lo[k] = std::min(lo[k], q);
+                hi[k] = std::max(hi[k], q);
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            float e = (hi[k] - lo[k]) * 1e-5f + (std::fabs(lo[k]) + std::fabs(hi[k])) * 1e-6f + 1e-7f;
+            lo[k] -= e;
+            hi[k] += e;
+        }
+    }
+    *olo = make_float4(lo[0], lo[1], lo[2], 0.0f);
+    *ohi = make_float4(hi[0], hi[1], hi[2], 0.0f);
+}
+
+// Top level over S.inst_lo/inst_hi (caller order) at nodes[node_base ...]:
+// the LBVH, the instance records in leaf order, the leaf boxes and the
+// parent links that a later refit needs.  Scratch for ni primitives; the
+// top-level depth goes to depth_dev[0] (which must hold 1 on entry).
+ddgi_status build_top_level(ddgi_ctx* ctx, uint64_t node_base, void* scratch, float4* box_lo, float4* box_hi,
+                            uint32_t* sorted, uint32_t* depth_dev, cudaStream_t st) {
+    SceneBuffers& S = ctx->scene;
+    const uint32_t ni = (uint32_t)S.host_inst.size();
+    if (ni == 0) {
+        S.tlas_root = -1;
+        return DDGI_OK;
+    }
+    const uint32_t inner = ni > 1 ? ni - 1 : 1;
+    if (!S.leaf_lo) {
+        CK(cudaMalloc(&S.leaf_lo, sizeof(float4) * ni), "alloc top level");
+        CK(cudaMalloc(&S.leaf_hi, sizeof(float4) * ni), "alloc top level");
+        CK(cudaMalloc(&S.leaf_parent, sizeof(uint32_t) * ni), "alloc top level");
+        CK(cudaMalloc(&S.node_parent, sizeof(uint32_t) * inner), "alloc top level");
+        CK(cudaMalloc(&S.refit_flags, sizeof(uint32_t) * inner), "alloc top level");
+        CK(cudaMalloc(&S.sub_lo, sizeof(float4) * 2 * inner), "alloc top level");
+        CK(cudaMalloc(&S.sub_hi, sizeof(float4) * 2 * inner), "alloc top level");
+    }
+    CK(cudaMemcpyAsync(box_lo, S.inst_lo.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
+    CK(cudaMemcpyAsync(box_hi, S.inst_hi.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
+    CK(lbvh_build(box_lo, box_hi, ni, kTlasLeafMax, S.nodes, (int)node_base, 0, sorted, scratch, ctx->err, depth_dev,
+                  st),
+       "top-level build");
+    std::vector<uint32_t> order(ni);
+    std::vector<BvhNode> top(inner);
+    CK(cudaMemcpyAsync(order.data(), sorted, sizeof(uint32_t) * ni, cudaMemcpyDeviceToHost, st), "read order");
+    CK(cudaMemcpyAsync(top.data(), S.nodes + node_base, sizeof(BvhNode) * inner, cudaMemcpyDeviceToHost, st),
+       "read top level");
+    CK(cudaStreamSynchronize(st), "top-level build");
+    std::vector<GpuInstance> leaf(ni);
+    std::vector<float4> llo(ni), lhi(ni);
+    S.leaf_of_id.assign(ni, 0);
+    for (uint32_t s = 0; s < ni; ++s) {
+        const uint32_t id = order[s] < ni ? order[s] : 0;
+        leaf[s] = S.host_inst[id];
+        llo[s] = S.inst_lo[id];
+        lhi[s] = S.inst_hi[id];
+        S.leaf_of_id[id] = s;
+    }
+    // parent links from the node references (a one-instance tree references
+    // its leaf from both sides; the second side is the empty box)
+    std::vector<uint32_t> lp(ni, 0xFFFFFFFFu), np(inner, 0xFFFFFFFFu);
+    for (uint32_t k = 0; k < inner; ++k) {
+        const int refs[2] = {top[k].d.x, top[k].d.y};
+        for (uint32_t side = 0; side < 2; ++side) {
+            const int r = refs[side];
+            if (r >= 0) {
+                const uint64_t c = (uint64_t)r - node_base;
+                if (r < (int)node_base || c >= inner) return fail(ctx, DDGI_ERR_DEVICE, "top level: bad child link");
+                np[c] = k << 1 | side;
+            } else {
+                const uint32_t slot = (uint32_t)((~r) >> 3);
+                if (slot >= ni) return fail(ctx, DDGI_ERR_DEVICE, "top level: bad leaf link");
+                if (lp[slot] == 0xFFFFFFFFu) lp[slot] = k << 1 | side;
+            }
+        }
+    }
+    CK(cudaMemcpyAsync(S.inst_leaf, leaf.data(), sizeof(GpuInstance) * ni, cudaMemcpyHostToDevice, st), "upload");
+    CK(cudaMemcpyAsync(S.inst_id, S.host_inst.data(), sizeof(GpuInstance) * ni, cudaMemcpyHostToDevice, st), "upload");
+    CK(cudaMemcpyAsync(S.leaf_lo, llo.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload");
+    CK(cudaMemcpyAsync(S.leaf_hi, lhi.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload");
+    CK(cudaMemcpyAsync(S.leaf_parent, lp.data(), sizeof(uint32_t) * ni, cudaMemcpyHostToDevice, st), "upload");
+    CK(cudaMemcpyAsync(S.node_parent, np.data(), sizeof(uint32_t) * inner, cudaMemcpyHostToDevice, st), "upload");
+    S.tlas_root = (int32_t)node_base;
+    return DDGI_OK;
+}
+
+}  // namespace
+
 ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_stream stream) {
     if (!ctx || !d) return DDGI_ERR_INVALID_ARGUMENT;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -551,53 +664,32 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
     }
 
     // ---- top level over instance world boxes ----
-    std::vector<float4> ilo(ni), ihi(ni);
-    std::vector<GpuInstance> recs(ni);
+    S.host_inst.assign(ni, GpuInstance{});
+    S.inst_lo.assign(ni, make_float4(0, 0, 0, 0));
+    S.inst_hi.assign(ni, make_float4(0, 0, 0, 0));
+    S.mesh_of_inst.assign(ni, 0);
+    S.mesh_lo = mesh_lo;
+    S.mesh_hi = mesh_hi;
     for (uint32_t i = 0; i < ni; ++i) {
         const ddgi_instance& in = d->instances[i];
-        GpuInstance& r = recs[i];
+        GpuInstance& r = S.host_inst[i];
         const float* w = &w2o[(size_t)i * 12];
         for (int k = 0; k < 3; ++k) r.w2o[k] = make_float4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
         r.blas_root = mesh_root[in.mesh_index];
         r.custom = in.custom_index & 0xFFFFFFu;
         r.mask = in.mask & 0xFFu;
         r.id = i;
-        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        const float* ml = &mesh_lo[(size_t)in.mesh_index * 3];
-        const float* mh = &mesh_hi[(size_t)in.mesh_index * 3];
-        if (r.blas_root >= 0 && ml[0] <= mh[0]) {
-            for (int c = 0; c < 8; ++c) {
-                double p[3] = {(c & 1) ? mh[0] : ml[0], (c & 2) ? mh[1] : ml[1], (c & 4) ? mh[2] : ml[2]};
-                for (int k = 0; k < 3; ++k) {
-                    float q = (float)(in.transform[4 * k] * p[0] + in.transform[4 * k + 1] * p[1] +
-                                      in.transform[4 * k + 2] * p[2] + in.transform[4 * k + 3]);
-                    lo[k] = std::min(lo[k], q);
-                    hi[k] = std::max(hi[k], q);
-                }
-            }
-            for (int k = 0; k < 3; ++k) {
-                float e = (hi[k] - lo[k]) * 1e-5f + (std::fabs(lo[k]) + std::fabs(hi[k])) * 1e-6f + 1e-7f;
-                lo[k] -= e;
-                hi[k] += e;
-            }
-        }
-        ilo[i] = make_float4(lo[0], lo[1], lo[2], 0.0f);
-        ihi[i] = make_float4(hi[0], hi[1], hi[2], 0.0f);
+        S.mesh_of_inst[i] = in.mesh_index;
+        instance_world_box(in.transform, &mesh_lo[(size_t)in.mesh_index * 3], &mesh_hi[(size_t)in.mesh_index * 3],
+                           r.blas_root >= 0, &S.inst_lo[i], &S.inst_hi[i]);
     }
-    if (ni > 0) {
-        CKB(cudaMemcpyAsync(box_lo, ilo.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
-        CKB(cudaMemcpyAsync(box_hi, ihi.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
-        CKB(lbvh_build(box_lo, box_hi, ni, kTlasLeafMax, S.nodes, (int)node_base, 0, sorted, scratch, ctx->err,
-                       depth + 1, st),
-            "top-level build");
-        std::vector<uint32_t> order(ni);
-        CKB(cudaMemcpyAsync(order.data(), sorted, sizeof(uint32_t) * ni, cudaMemcpyDeviceToHost, st), "read order");
-        CKB(cudaStreamSynchronize(st), "top-level build");
-        std::vector<GpuInstance> leaf(ni);
-        for (uint32_t s = 0; s < ni; ++s) leaf[s] = recs[order[s]];
-        CKB(cudaMemcpyAsync(S.inst_leaf, leaf.data(), sizeof(GpuInstance) * ni, cudaMemcpyHostToDevice, st), "upload");
-        CKB(cudaMemcpyAsync(S.inst_id, recs.data(), sizeof(GpuInstance) * ni, cudaMemcpyHostToDevice, st), "upload");
-        S.tlas_root = (int32_t)node_base;
+    {
+        ddgi_status ts = build_top_level(ctx, node_base, scratch, box_lo, box_hi, sorted, depth + 1, st);
+        if (ts != DDGI_OK) {
+            cleanup();
+            free_scene(ctx->scene);
+            return ts;
+        }
     }
     uint32_t depths[2] = {1u, 1u};
     CKB(cudaMemcpyAsync(depths, depth, sizeof(depths), cudaMemcpyDeviceToHost, st), "read depth");
@@ -621,10 +713,104 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
     S.instance_count = ni;
     S.node_count = total_nodes + tlas_nodes;
     S.tri_count = total_tris;
-    static std::atomic<uint64_t> builds{0};
-    S.build_id = ++builds;
+    S.build_id = next_build_id();
     S.built = true;
     return check_device_error(ctx);
+}
+
+// ---------------------------------------------------------------------------
+// Moving instances (Renderer::updateAccelerationStructureInstances +
+// updateTLAS, src/Renderer.cpp:671-742)
+// ---------------------------------------------------------------------------
+ddgi_status ddgi_update_instances(ddgi_ctx* ctx, const uint32_t* ids, const float* transforms, uint32_t count,
+                                  int rebuild, ddgi_stream stream) {
+    if (!ctx || (count && !transforms)) return DDGI_ERR_INVALID_ARGUMENT;
+    SceneBuffers& S = ctx->scene;
+    if (!S.built) return fail(ctx, DDGI_ERR_NO_SCENE, "ddgi_update_instances before ddgi_scene_build");
+    const uint32_t ni = (uint32_t)S.host_inst.size();
+    if (count > ni) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "%u transforms for %u instances", count, ni);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    // validate everything before changing anything
+    std::vector<float> w2o((size_t)count * 12);
+    std::vector<uint8_t> seen(ni, 0);
+    for (uint32_t q = 0; q < count; ++q) {
+        const uint32_t id = ids ? ids[q] : q;
+        if (id >= ni) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "instance %u out of range", id);
+        if (seen[id]++) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "instance %u listed twice", id);
+        for (int k = 0; k < 12; ++k)
+            if (!std::isfinite(transforms[12 * (size_t)q + k]))
+                return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "instance %u: non-finite transform", id);
+        if (!ddgi_affine_inverse(&transforms[12 * (size_t)q], &w2o[12 * (size_t)q]))
+            return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "instance %u: singular transform", id);
+    }
+    for (uint32_t q = 0; q < count; ++q) {
+        const uint32_t id = ids ? ids[q] : q;
+        GpuInstance& r = S.host_inst[id];
+        const float* w = &w2o[12 * (size_t)q];
+        for (int k = 0; k < 3; ++k) r.w2o[k] = make_float4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+        const uint32_t m = S.mesh_of_inst[id];
+        instance_world_box(&transforms[12 * (size_t)q], &S.mesh_lo[(size_t)m * 3], &S.mesh_hi[(size_t)m * 3],
+                           r.blas_root >= 0, &S.inst_lo[id], &S.inst_hi[id]);
+    }
+    if (ni == 0) return DDGI_OK;
+    if (rebuild) {
+        // a new top-level tree over the new boxes (same node range)
+        void* scratch = nullptr;
+        float4 *blo = nullptr, *bhi = nullptr;
+        uint32_t *sorted = nullptr, *depth = nullptr;
+        auto release = [&]() {
+            if (scratch) cudaFree(scratch);
+            if (blo) cudaFree(blo);
+            if (bhi) cudaFree(bhi);
+            if (sorted) cudaFree(sorted);
+            if (depth) cudaFree(depth);
+        };
+        if (cudaMalloc(&scratch, lbvh_scratch_bytes(ni)) != cudaSuccess ||
+            cudaMalloc(&blo, sizeof(float4) * ni) != cudaSuccess || cudaMalloc(&bhi, sizeof(float4) * ni) != cudaSuccess ||
+            cudaMalloc(&sorted, sizeof(uint32_t) * ni) != cudaSuccess ||
+            cudaMalloc(&depth, sizeof(uint32_t)) != cudaSuccess) {
+            release();
+            cudaGetLastError();
+            return fail(ctx, DDGI_ERR_OUT_OF_MEMORY, "instance rebuild scratch");
+        }
+        const uint32_t one = 1;
+        uint32_t dtop = 1;
+        ddgi_status s = DDGI_OK;
+        if (cudaMemcpyAsync(depth, &one, sizeof(one), cudaMemcpyHostToDevice, st) != cudaSuccess)
+            s = fail(ctx, DDGI_ERR_CUDA, "instance rebuild");
+        if (s == DDGI_OK) s = build_top_level(ctx, (uint64_t)S.tlas_root, scratch, blo, bhi, sorted, depth, st);
+        if (s == DDGI_OK && (cudaMemcpyAsync(&dtop, depth, sizeof(dtop), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                             cudaStreamSynchronize(st) != cudaSuccess))
+            s = fail(ctx, DDGI_ERR_CUDA, "instance rebuild");
+        release();
+        if (s != DDGI_OK) return s;
+        const int cap = (int)(S.depth_blas + dtop + 4);
+        if (cap > kMaxStack)
+            return fail(ctx, DDGI_ERR_UNSUPPORTED, "rebuilt top level too deep (%u levels)", dtop);
+        S.depth_tlas = dtop;
+        S.stack_cap = cap;
+    } else {
+        // refit: same topology, new leaf boxes, boxes recomputed bottom-up
+        std::vector<GpuInstance> leaf(ni);
+        std::vector<float4> llo(ni), lhi(ni);
+        for (uint32_t id = 0; id < ni; ++id) {
+            const uint32_t slot = S.leaf_of_id[id];
+            leaf[slot] = S.host_inst[id];
+            llo[slot] = S.inst_lo[id];
+            lhi[slot] = S.inst_hi[id];
+        }
+        CK(cudaMemcpyAsync(S.inst_leaf, leaf.data(), sizeof(GpuInstance) * ni, cudaMemcpyHostToDevice, st), "upload");
+        CK(cudaMemcpyAsync(S.inst_id, S.host_inst.data(), sizeof(GpuInstance) * ni, cudaMemcpyHostToDevice, st),
+           "upload");
+        CK(cudaMemcpyAsync(S.leaf_lo, llo.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload");
+        CK(cudaMemcpyAsync(S.leaf_hi, lhi.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload");
+        CK(lbvh_refit_top(S.nodes, S.tlas_root, S.leaf_lo, S.leaf_hi, ni, S.leaf_parent, S.node_parent, S.refit_flags,
+                          S.sub_lo, S.sub_hi, ctx->err, st),
+           "top-level refit");
+        // the host vectors above are staged by the copies before they return
+    }
+    S.build_id = next_build_id();  // batches made from the old top level are stale
+    return DDGI_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -654,7 +840,10 @@ ddgi_status prepare_update(ddgi_ctx* ctx, const float orientation[9], const uint
     ctx->host_dirs.resize(4 * (size_t)R);
     ddgi_ray_direction_table(orientation, R, ctx->host_dirs.data());
     ctx->host_order.resize(R);
-    ray_order_of(ctx->host_dirs.data(), R, ctx->host_order.data());
+    {
+        const uint32_t rpw = ctx->tune.rays_per_warp;
+        ray_order_of(ctx->host_dirs.data(), R, ctx->host_order.data(), rpw > 0 && rpw < 32);
+    }
     CK(cudaMemcpyAsync(ctx->dirs, ctx->host_dirs.data(), sizeof(float4) * R, cudaMemcpyHostToDevice, st), "upload dirs");
     CK(cudaMemcpyAsync(ctx->ray_order, ctx->host_order.data(), sizeof(uint32_t) * R, cudaMemcpyHostToDevice, st),
        "upload order");
@@ -840,6 +1029,41 @@ ddgi_status ddgi_set_schedule(ddgi_ctx* ctx, uint32_t offset, uint32_t loop, ddg
     const uint32_t h[4] = {offset, loop, 0, 0};
     CK(cudaMemcpyAsync(ctx->sched, h, sizeof(h), cudaMemcpyHostToDevice, st), "write schedule");
     CK(cudaStreamSynchronize(st), "write schedule");
+    return DDGI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Final gather (src/shaders/FinalGather.frag:39-80)
+// ---------------------------------------------------------------------------
+ddgi_status ddgi_final_gather(ddgi_ctx* ctx, const ddgi_gbuffer* gb, const float camera_origin[3], float* color_out,
+                              ddgi_stream stream) {
+    if (!ctx || !gb || !camera_origin || !color_out) return DDGI_ERR_INVALID_ARGUMENT;
+    const uint64_t px = (uint64_t)gb->width * gb->height;
+    if (px == 0) return DDGI_OK;
+    if (px >= (1ull << 31)) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "G-buffer too large");
+    if (!gb->position_depth || !gb->normal_metalness || !gb->albedo_roughness || !gb->emissive || !gb->direct_light)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "a required G-buffer array is NULL");
+    const uintptr_t al = (uintptr_t)gb->position_depth | (uintptr_t)gb->normal_metalness |
+                         (uintptr_t)gb->albedo_roughness | (uintptr_t)gb->emissive | (uintptr_t)gb->reflection |
+                         (uintptr_t)color_out;
+    if (al & 15u) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "float4 G-buffer arrays must be 16-byte aligned");
+    for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(camera_origin[k])) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "non-finite camera origin");
+    GatherArgs a;
+    a.position_depth = reinterpret_cast<const float4*>(gb->position_depth);
+    a.normal_metalness = reinterpret_cast<const float4*>(gb->normal_metalness);
+    a.albedo_roughness = reinterpret_cast<const float4*>(gb->albedo_roughness);
+    a.emissive = reinterpret_cast<const float4*>(gb->emissive);
+    a.direct_light = gb->direct_light;
+    a.reflection = reinterpret_cast<const float4*>(gb->reflection);
+    a.out = reinterpret_cast<float4*>(color_out);
+    a.pixels = (uint32_t)px;
+    a.origin = make_float3(camera_origin[0], camera_origin[1], camera_origin[2]);
+    a.g = ctx->dg;
+    a.L = ctx->dl;
+    a.states = ctx->states;
+    CK(launch_final_gather(a, ctx->color, ctx->depth, ctx->fp16, reinterpret_cast<cudaStream_t>(stream)),
+       "final gather launch");
     return DDGI_OK;
 }
 

@@ -127,6 +127,24 @@ cudaError_t prepare_batch_kernels();  // kernel attributes, set once before any 
 cudaError_t launch_batch_blend_tc(const BatchTables& bt, const BatchBlendList& bl, const float4* rays, size_t smem,
                                   cudaStream_t st);
 
+// gather.cu: the final-gather consumer over a device G-buffer
+struct GatherArgs {
+    const float4* position_depth;
+    const float4* normal_metalness;
+    const float4* albedo_roughness;
+    const float4* emissive;
+    const float* direct_light;
+    const float4* reflection;  // may be NULL
+    float4* out;
+    uint32_t pixels;
+    float3 origin;  // camera
+    DeviceGrid g;
+    DeviceLight L;
+    const uint32_t* states;
+};
+cudaError_t launch_final_gather(const GatherArgs& a, const void* color, const void* depth, bool fp16_atlas,
+                                cudaStream_t st);
+
 // adjoint.cu
 cudaError_t launch_replay_update(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L, const float4* dirs,
                                  uint32_t* states, float4* color, float2* depth, const float4* thit,

@@ -420,6 +420,68 @@ cudaError_t lbvh_build(const float4* prim_lo, const float4* prim_hi, uint32_t n,
     return cudaGetLastError();
 }
 
+// --- refit of a top-level tree with fixed topology -------------------------
+namespace {
+
+// One thread per leaf slot: writes the slot's (enlarged) box into its
+// parent's child box and climbs; the second thread to reach a node unites
+// the two children's subtree bounds (kept un-enlarged in sub_lo/sub_hi, as
+// k_refit keeps them) and continues, so every box is the enlarged union of
+// its subtree's primitive boxes, as a fresh build makes it.
+__global__ void k_refit_top(BvhNode* nodes, int node_base, const float4* lo_in, const float4* hi_in, uint32_t n,
+                            const uint32_t* leaf_parent, const uint32_t* node_parent, uint32_t* flags, float4* sub_lo,
+                            float4* sub_hi, uint32_t* err) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    float4 lo = lo_in[s], hi = hi_in[s];
+    uint32_t p = leaf_parent[s];
+    const uint32_t inner = n > 1 ? n - 1 : 1;
+    for (uint32_t guard = 0; guard < n + 1; ++guard) {
+        const uint32_t node = p >> 1, side = p & 1u;
+        if (node >= inner) {
+            raise_error(err, DEV_BAD_INDEX);
+            return;
+        }
+        float4 elo = lo, ehi = hi;
+        enlarge(elo, ehi);
+        BvhNode* nd = nodes + node_base + node;
+        if (side == 0) {
+            nd->a = make_float4(elo.x, ehi.x, elo.y, ehi.y);
+            nd->c.x = elo.z;
+            nd->c.y = ehi.z;
+        } else {
+            nd->b = make_float4(elo.x, ehi.x, elo.y, ehi.y);
+            nd->c.z = elo.z;
+            nd->c.w = ehi.z;
+        }
+        sub_lo[2 * node + side] = lo;
+        sub_hi[2 * node + side] = hi;
+        __threadfence();
+        if (atomicAdd(flags + node, 1u) == 0u) return;  // the sibling subtree is not finished
+        __threadfence();
+        const float4 l0 = __ldcg(sub_lo + 2 * node), l1 = __ldcg(sub_lo + 2 * node + 1);
+        const float4 h0 = __ldcg(sub_hi + 2 * node), h1 = __ldcg(sub_hi + 2 * node + 1);
+        lo = make_float4(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z), 0.0f);
+        hi = make_float4(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z), 0.0f);
+        p = node_parent[node];
+        if (p == 0xFFFFFFFFu) return;  // root done
+    }
+    raise_error(err, DEV_BAD_INDEX);  // a cycle in the parent links
+}
+
+}  // namespace
+
+cudaError_t lbvh_refit_top(BvhNode* nodes, int node_base, const float4* leaf_lo, const float4* leaf_hi, uint32_t n,
+                           const uint32_t* leaf_parent, const uint32_t* node_parent, uint32_t* flags, float4* sub_lo,
+                           float4* sub_hi, uint32_t* err, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(flags, 0, sizeof(uint32_t) * (n > 1 ? n - 1 : 1), st);
+    if (e != cudaSuccess) return e;
+    k_refit_top<<<div_up(n, 256), 256, 0, st>>>(nodes, node_base, leaf_lo, leaf_hi, n, leaf_parent, node_parent,
+                                                flags, sub_lo, sub_hi, err);
+    return cudaGetLastError();
+}
+
 // --- helpers used by the scene build --------------------------------------
 namespace {
 

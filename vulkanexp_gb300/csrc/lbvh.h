@@ -27,4 +27,12 @@ cudaError_t build_mesh_blas(const float4* pos, const uint32_t* indices, uint32_t
                             int tri_base, float4* box_lo, float4* box_hi, uint32_t* sorted_ids, void* scratch,
                             uint32_t* err, uint32_t* depth, cudaStream_t st);
 
+// Refit of a top-level tree whose topology is kept: new boxes for its n
+// leaf slots (leaf order); leaf_parent[s] / node_parent[k] = parent node
+// (relative to node_base) << 1 | side, 0xFFFFFFFF for the root; flags
+// (n - 1 entries) and sub_lo/sub_hi (2 (n - 1) entries) are scratch.
+cudaError_t lbvh_refit_top(BvhNode* nodes, int node_base, const float4* leaf_lo, const float4* leaf_hi, uint32_t n,
+                           const uint32_t* leaf_parent, const uint32_t* node_parent, uint32_t* flags, float4* sub_lo,
+                           float4* sub_hi, uint32_t* err, cudaStream_t st);
+
 }  // namespace ddgi

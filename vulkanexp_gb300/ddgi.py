@@ -16,7 +16,7 @@ import os
 import numpy as np
 
 from . import abi
-from .abi import HIT_DTYPE, BatchTuning, GridDesc, Light, SceneDesc, Timings, TraceTuning
+from .abi import HIT_DTYPE, BatchTuning, GBuffer, GridDesc, Light, SceneDesc, Timings, TraceTuning
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libddgi_gb300.so")
@@ -68,6 +68,8 @@ _SIGNATURES = [
     ("ddgi_blend_records_noalloc", C.c_int, [C.POINTER(GridDesc), C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                              C.c_void_p]),
+    ("ddgi_update_instances", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]),
+    ("ddgi_final_gather", C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ddgi_set_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_get_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_autotune", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(TraceTuning)]),
@@ -183,6 +185,14 @@ class Context:
         d = scene_desc(scene)
         self._check(self.lib.ddgi_scene_build(self.h, C.byref(d), _stream_ptr(stream)))
 
+    def update_instances(self, transforms, ids=None, rebuild=False, stream=None):
+        """New object-to-world transforms (n x 12, row-major 3x4) for the
+        instances `ids` (default 0..n-1): top-level refit, or rebuild."""
+        t = np.ascontiguousarray(transforms, np.float32).reshape(-1, 12)
+        i = None if ids is None else np.ascontiguousarray(ids, np.uint32)
+        self._check(self.lib.ddgi_update_instances(self.h, _ptr(i), _ptr(t), len(t), int(bool(rebuild)),
+                                                   _stream_ptr(stream)))
+
     def set_light(self, light):
         self._check(self.lib.ddgi_set_light(self.h, C.byref(light)))
 
@@ -201,6 +211,24 @@ class Context:
         pl = None if probe_list is None else np.ascontiguousarray(probe_list, np.uint32)
         self._check(self.lib.ddgi_update(self.h, _ptr(o), _ptr(pl), 0 if pl is None else len(pl),
                                          _stream_ptr(stream)))
+
+    def final_gather(self, gbuffer, origin, out, stream=None):
+        """FinalGather.frag over a device G-buffer.  gbuffer: dict of
+        contiguous float32 CUDA tensors position_depth, normal_metalness,
+        albedo_roughness, emissive (H x W x 4), direct_light (H x W) and
+        optionally reflection (H x W x 4); out: H x W x 4 CUDA tensor."""
+        h, w = out.shape[0], out.shape[1]
+        gb = GBuffer()
+        for k in ("position_depth", "normal_metalness", "albedo_roughness", "emissive", "direct_light"):
+            t = gbuffer[k]
+            assert t.is_cuda and t.is_contiguous() and t.shape[0] == h and t.shape[1] == w
+            setattr(gb, k, t.data_ptr())
+        r = gbuffer.get("reflection")
+        gb.reflection = None if r is None else r.data_ptr()
+        gb.width, gb.height = w, h
+        o = np.ascontiguousarray(origin, np.float32).reshape(3)
+        self._check(self.lib.ddgi_final_gather(self.h, C.byref(gb), _ptr(o), C.c_void_p(out.data_ptr()),
+                                               _stream_ptr(stream)))
 
     def trace_tuning(self):
         t = TraceTuning()
