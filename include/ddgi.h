@@ -297,10 +297,11 @@ ddgi_status ddgi_trace_rays(ddgi_ctx* ctx, const float* origins, const float* di
  * (closest-hit) rays out[0] inner-node fetches (64 B each), out[1] triangle
  * tests (48 B each), out[2] instance entries (64 B each), out[3] rays;
  * out[4] shading bytes (hit data, atlas texels of the bounce lookups, ray
- * record); and out[5..8] the same four counts for the shadow (any-hit) rays.
+ * record); out[5..8] the same four counts for the shadow (any-hit) rays;
+ * out[9], out[10] the part of out[0], out[5] in the top-level tree.
  * Synchronous on `stream`. */
 ddgi_status ddgi_count_fetches(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
-                               uint32_t probe_count, uint64_t out[9], ddgi_stream stream);
+                               uint32_t probe_count, uint64_t out[11], ddgi_stream stream);
 
 /* Replaces the material table of the built scene (same count), e.g. new
  * albedos, without rebuilding the acceleration structures. */
@@ -394,8 +395,12 @@ typedef struct ddgi_trace_tuning {
     uint32_t smem_stack;    /* traversal-stack entries per thread in shared memory, deeper ones in local
                                memory; 0 = the whole stack in shared memory (default) */
     uint32_t ctas_per_sm;   /* persistent CTAs per SM; 0 = as many as fit (default) */
+    uint32_t node_width;    /* 2: binary nodes (default), 4: four-wide nodes collapsed from the binary trees */
 } ddgi_trace_tuning;
 ddgi_status ddgi_set_trace_tuning(ddgi_ctx* ctx, const ddgi_trace_tuning* tuning);
+/* Most triangles per leaf of the mesh trees built by the next
+ * ddgi_scene_build (1..8, default 2). */
+ddgi_status ddgi_set_leaf_size(ddgi_ctx* ctx, uint32_t max_triangles);
 ddgi_status ddgi_get_trace_tuning(const ddgi_ctx* ctx, ddgi_trace_tuning* out);
 /* Times candidate tunings on updates of all probes with the given
  * orientation (`reps` timed updates each, coordinate descent), keeps the
@@ -433,6 +438,7 @@ typedef struct ddgi_batch_tuning {
     uint32_t blend_threads;     /* threads per probe of the FP32 blend (32..256, multiple of 32) */
     uint32_t rays_per_warp;     /* as in ddgi_trace_tuning, per volume (values a volume's ray count
                                    does not allow fall back to 0 for that volume) */
+    uint32_t node_width;        /* as in ddgi_trace_tuning */
 } ddgi_batch_tuning;
 
 ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_stream stream, ddgi_batch** out);

@@ -185,6 +185,7 @@ def test_errors_are_reported(gpu_lib, room_workload):
 
 
 @pytest.mark.parametrize("tuning", [
+    dict(node_width=2), dict(node_width=2, rays_per_warp=8, smem_stack=16),
     dict(rays_per_warp=32), dict(rays_per_warp=8, refill_lanes=16), dict(rays_per_warp=1, smem_stack=16),
     dict(rays_per_warp=4, refill_lanes=1, ctas_per_sm=3, smem_stack=24),
 ])
@@ -219,4 +220,6 @@ def test_autotune_restores_state(gpu_lib, room_workload):
         assert (a == b).all()
     with pytest.raises(DDGIError):
         ctx.set_trace_tuning(rays_per_warp=3)
+    with pytest.raises(DDGIError):
+        ctx.set_trace_tuning(node_width=8)
     ctx.close()

@@ -37,6 +37,7 @@
 #include "ctx.h"
 #include "kernels.h"
 #include "traverse.cuh"
+#include "wide.h"
 
 using namespace ddgi;
 
@@ -52,6 +53,12 @@ struct ddgi_batch {
     uint64_t node_count = 0, tri_count = 0, inst_count = 0;
     std::vector<int32_t> roots;
     int stack_cap = 1;
+    // the four-wide trees of every volume (wstack_cap 0: some volume has none)
+    WideNode* wnodes = nullptr;
+    GpuInstance* winsts = nullptr;
+    uint64_t wnode_count = 0;
+    std::vector<int32_t> wroots;
+    int wstack_cap = 0;
     // per-ray buffers (all volumes)
     uint32_t total = 0;
     float4* thit = nullptr;
@@ -78,7 +85,7 @@ struct ddgi_batch {
     uint8_t* d_stage = nullptr;
     size_t stage_bytes = 0, off_order = 0, off_vols = 0;
     // launch state
-    ddgi_batch_tuning tuning{0, 8, 0, 256, 0};
+    ddgi_batch_tuning tuning{0, 8, 0, 256, 0, 2};
     bool use_graph = true;
     cudaStream_t cap = nullptr, side = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr, done_ev = nullptr;
@@ -215,6 +222,10 @@ DeviceScene arena_scene(const ddgi_batch* b) {
     s.node_count = (uint32_t)b->node_count;
     s.tri_count = (uint32_t)b->tri_count;
     s.instance_count = (uint32_t)b->inst_count;
+    s.wnodes = b->wstack_cap > 0 ? b->wnodes : nullptr;
+    s.winstances = b->wstack_cap > 0 ? b->winsts : nullptr;
+    s.wtlas_root = -1;
+    s.wnode_count = (uint32_t)b->wnode_count;
     return s;
 }
 
@@ -272,6 +283,7 @@ ddgi_status stage_inputs(ddgi_batch* b, const float* orientations) {
         x.acc_depth = c->acc_depth;
         x.wbuf = c->tc_weights;
         x.rowsum = c->tc_rowsum;
+        x.wroot = b->wroots[v];
         x.rays_per_warp = grouped_rays_per_warp(b->tuning.rays_per_warp, R);
         x.perm = x.rays_per_warp ? c->probe_perm : nullptr;
     }
@@ -296,10 +308,11 @@ cudaError_t enqueue(ddgi_batch* b, cudaStream_t st, bool timed) {
     tt.refill = b->tuning.refill_lanes;
     tt.split = b->tuning.smem_stack;
     tt.rays_per_warp = b->tuning.rays_per_warp;  // applied per volume through the volume table
+    tt.wide = b->tuning.node_width == 4 ? 1u : 0u;
     WaveHits wh{b->thit, b->prim};
     ShadowQueue q{b->q_idx, b->q_pos, b->q_sun, nullptr};
-    e = launch_batch_trace(arena_scene(b), bt, b->total, wh, q, b->counters, b->rays, b->stack_cap, tt, st,
-                           timed ? b->ev[1] : nullptr, timed ? b->ev[2] : nullptr);
+    e = launch_batch_trace(arena_scene(b), bt, b->total, wh, q, b->counters, b->rays, b->stack_cap, b->wstack_cap,
+                           tt, st, timed ? b->ev[1] : nullptr, timed ? b->ev[2] : nullptr);
     if (e != cudaSuccess) return e;
     if (timed) cudaEventRecord(b->ev[3], st);
     const bool both = b->fp32_bl.ntiles > 0 && b->tc_bl.ntiles > 0;
@@ -419,6 +432,9 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
         tris += c->scene.tri_count;
         insts += c->scene.instance_count;
         b->stack_cap = std::max(b->stack_cap, c->scene.stack_cap);
+        b->wnode_count += c->scene.wnode_count;
+        if (v == 0) b->wstack_cap = c->scene.wstack_cap;
+        b->wstack_cap = c->scene.wstack_cap > 0 && b->wstack_cap > 0 ? std::max(b->wstack_cap, c->scene.wstack_cap) : 0;
         if (c->fp16) {
             tc_list.push_back(v);
             tc_base.push_back(tc_base.back() + tc_tiles(P));
@@ -446,6 +462,8 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
     if (cudaMalloc(&b->nodes, sizeof(BvhNode) * std::max<uint64_t>(nodes, 1)) != cudaSuccess ||
         cudaMalloc(&b->tris, sizeof(BvhTri) * std::max<uint64_t>(tris, 1)) != cudaSuccess ||
         cudaMalloc(&b->insts, sizeof(GpuInstance) * std::max<uint64_t>(insts, 1)) != cudaSuccess ||
+        cudaMalloc(&b->wnodes, sizeof(WideNode) * std::max<uint64_t>(b->wnode_count, 1)) != cudaSuccess ||
+        cudaMalloc(&b->winsts, sizeof(GpuInstance) * std::max<uint64_t>(insts, 1)) != cudaSuccess ||
         cudaMalloc(&b->thit, sizeof(float4) * N) != cudaSuccess ||
         cudaMalloc(&b->prim, sizeof(uint32_t) * N) != cudaSuccess ||
         cudaMalloc(&b->rays, sizeof(float4) * N) != cudaSuccess ||
@@ -497,7 +515,7 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
     b->tc_bl = BatchBlendList{b->d_lists + 2 * nf + 1, b->d_lists + 2 * nf + 1 + nt, nt, tc_base.back()};
 
     // ---- arena: copy every volume's trees with rebased references ----
-    uint64_t node_off = 0, tri_off = 0, inst_off = 0;
+    uint64_t node_off = 0, tri_off = 0, inst_off = 0, wnode_off = 0;
     for (uint32_t v = 0; v < count; ++v) {
         const ddgi_ctx* c = b->vols[v];
         const SceneBuffers& S = c->scene;
@@ -515,6 +533,16 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
             k_rebase_instances<<<(S.instance_count + 255) / 256, 256, 0, st>>>(S.inst_leaf, S.instance_count,
                                                                                (int)node_off, b->insts + inst_off);
         b->roots.push_back(S.tlas_root >= 0 ? (int32_t)(S.tlas_root + node_off) : -1);
+        if (b->wstack_cap > 0) {
+            if (launch_rebase_wide(S.wnodes, S.wnode_count, S.wide_tlas_start, (int)wnode_off, (int)tri_off,
+                                   (int)inst_off, b->wnodes + wnode_off, st) != cudaSuccess)
+                return bail(DDGI_ERR_CUDA);
+            if (S.instance_count > 0)
+                k_rebase_instances<<<(S.instance_count + 255) / 256, 256, 0, st>>>(
+                    S.winst_leaf, S.instance_count, (int)wnode_off, b->winsts + inst_off);
+        }
+        b->wroots.push_back(S.wtlas_root >= 0 ? (int32_t)(S.wtlas_root + wnode_off) : -1);
+        wnode_off += S.wnode_count;
         node_off += S.node_count;
         tri_off += S.tri_count;
         inst_off += S.instance_count;
@@ -533,6 +561,8 @@ ddgi_status ddgi_batch_destroy(ddgi_batch* b) {
     bfree(b->nodes);
     bfree(b->tris);
     bfree(b->insts);
+    bfree(b->wnodes);
+    bfree(b->winsts);
     bfree(b->thit);
     bfree(b->prim);
     bfree(b->rays);
@@ -580,6 +610,8 @@ ddgi_status ddgi_batch_set_tuning(ddgi_batch* b, const ddgi_batch_tuning* t) {
     const uint32_t r = t->rays_per_warp;
     if (!(r == 0 || r == 1 || r == 2 || r == 4 || r == 8 || r == 16 || r == 32))
         return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "rays_per_warp = %u: want 0, 1, 2, 4, 8, 16 or 32", r);
+    if (t->node_width != 2 && t->node_width != 4)
+        return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "node_width = %u: want 2 or 4", t->node_width);
     ddgi_status s = wait_previous(b);
     if (s != DDGI_OK) return s;
     b->tuning = *t;
@@ -695,19 +727,21 @@ ddgi_status ddgi_batch_autotune(ddgi_batch* b, const float* orientations, uint32
     ddgi_status err = DDGI_OK;
     float best_t = 0.0f;
     err = measure(best, 0, &best_t);
+    const uint32_t width_c[] = {4u, 2u};
     const uint32_t rpw_c[] = {0u, 32u, 16u, 8u, 4u, 2u, 1u};
     const uint32_t split_c[] = {0u, 32u, 24u, 16u};
     const uint32_t refill_c[] = {4u, 8u, 16u, 24u};
     const uint32_t ctas_c[] = {0u, 6u, 4u};
-    for (int p = 0; p < 4 && err == DDGI_OK; ++p) {
-        const uint32_t* cand = p == 0 ? rpw_c : p == 1 ? split_c : p == 2 ? refill_c : ctas_c;
-        const int nc = p == 0 ? 7 : p == 3 ? 3 : 4;
+    for (int p = 0; p < 5 && err == DDGI_OK; ++p) {
+        const uint32_t* cand = p == 0 ? width_c : p == 1 ? rpw_c : p == 2 ? split_c : p == 3 ? refill_c : ctas_c;
+        const int nc = p == 0 ? 2 : p == 1 ? 7 : p == 4 ? 3 : 4;
         for (int i = 0; i < nc && err == DDGI_OK; ++i) {
             ddgi_batch_tuning t = best;
-            uint32_t* field = p == 0 ? &t.rays_per_warp : p == 1 ? &t.smem_stack : p == 2 ? &t.refill_lanes
-                                                                                        : &t.trace_ctas_per_sm;
+            uint32_t* field = p == 0 ? &t.node_width : p == 1 ? &t.rays_per_warp : p == 2 ? &t.smem_stack
+                              : p == 3 ? &t.refill_lanes : &t.trace_ctas_per_sm;
             if (*field == cand[i]) continue;
-            if (p == 1 && cand[i] != 0 && (int)cand[i] >= b->stack_cap) continue;
+            const int cap = t.node_width == 4 && b->wstack_cap > 0 ? b->wstack_cap : b->stack_cap;
+            if (p == 2 && cand[i] != 0 && (int)cand[i] >= cap) continue;
             *field = cand[i];
             float tt = 0.0f;
             err = measure(t, 0, &tt);

@@ -67,6 +67,16 @@ struct __align__(16) GpuInstance {
     uint32_t id;        // index in the caller's instance array
 };
 
+// Four-wide node, 128 bytes, collapsed from the binary trees: the boxes of
+// up to four children as structure-of-arrays (lane k = child k) and their
+// references (>= 0: wide node, < 0: leaf as in BvhNode, kNone: no child).
+struct __align__(16) WideNode {
+    float4 lox, hix, loy, hiy, loz, hiz;
+    int4 ref;
+    int4 unused;
+};
+static_assert(sizeof(WideNode) == 128, "wide node is 128 bytes");
+
 struct DeviceScene {
     const BvhNode* nodes;
     const BvhTri* tris;
@@ -79,6 +89,12 @@ struct DeviceScene {
     int32_t tlas_root;      // -1: empty scene
     uint32_t vertex_count, index_count, offset_count, material_count;
     uint32_t node_count, tri_count, instance_count;  // bounds of the references above
+    // the same trees as four-wide nodes; instances (leaf order) whose
+    // blas_root is a wide-node index
+    const WideNode* wnodes;
+    const GpuInstance* winstances;
+    int32_t wtlas_root;
+    uint32_t wnode_count;
 };
 
 struct DeviceGrid {

@@ -14,7 +14,7 @@
 
 namespace ddgi {
 
-constexpr int kBlasLeafMax = 4;
+constexpr int kBlasLeafMax = 2;  // default; measured best of 1, 2, 4, 8 on the 1M-triangle scene
 constexpr int kTlasLeafMax = 1;
 // deepest traversal stack of the wavefront kernels (entries per thread in
 // shared memory: 96 x 128 threads x 4 bytes = 48 KB per block)
@@ -49,6 +49,14 @@ struct SceneBuffers {
     uint32_t* refit_flags = nullptr;
     float4* sub_lo = nullptr;
     float4* sub_hi = nullptr;
+    // four-wide copy of the trees: [mesh trees | top level, with room for
+    // a rebuilt top level]; instances in leaf order with wide mesh roots
+    WideNode* wnodes = nullptr;
+    GpuInstance* winst_leaf = nullptr;
+    uint32_t wnode_count = 0, wide_tlas_start = 0, wide_cap = 0, wlevels_blas = 0;
+    int32_t wtlas_root = -1;
+    int wstack_cap = 0;  // 0: no wide trees (too deep for the stack)
+    std::vector<int32_t> wide_root_of_mesh;
 };
 
 }  // namespace ddgi
@@ -108,7 +116,8 @@ struct ddgi_ctx {
     // index, selected count}; probe classification scratch
     uint32_t* sched = nullptr;
     // traversal launch tuning; probes in Morton order of the grid (grouped warps)
-    ddgi_trace_tuning tune{0, 8, 0, 0};
+    ddgi_trace_tuning tune{0, 8, 0, 0, 2};
+    int blas_leaf_max = ddgi::kBlasLeafMax;  // triangles per mesh-tree leaf (scene build option)
     uint32_t* probe_perm = nullptr;
     float4* init_dirs = nullptr;
     uint32_t* init_back = nullptr;
@@ -190,6 +199,10 @@ inline DeviceScene device_scene(const ddgi_ctx* c) {
     s.node_count = (uint32_t)c->scene.node_count;
     s.tri_count = (uint32_t)c->scene.tri_count;
     s.instance_count = c->scene.instance_count;
+    s.wnodes = c->scene.wstack_cap > 0 ? c->scene.wnodes : nullptr;
+    s.winstances = c->scene.wstack_cap > 0 ? c->scene.winst_leaf : nullptr;
+    s.wtlas_root = c->scene.wtlas_root;
+    s.wnode_count = c->scene.wnode_count;
     return s;
 }
 

@@ -28,6 +28,7 @@
 #include "ctx.h"
 #include "kernels.h"
 #include "lbvh.h"
+#include "wide.h"
 
 using namespace ddgi;
 
@@ -136,6 +137,8 @@ size_t atlas_bytes(const DeviceGrid& d, ddgi_atlas_kind k, bool fp16) {
 }
 
 void free_scene(SceneBuffers& s) {
+    dfree(s.wnodes);
+    dfree(s.winst_leaf);
     dfree(s.leaf_lo);
     dfree(s.leaf_hi);
     dfree(s.leaf_parent);
@@ -499,6 +502,93 @@ ddgi_status build_top_level(ddgi_ctx* ctx, uint64_t node_base, void* scratch, fl
     return DDGI_OK;
 }
 
+// Instances in leaf order with the mesh roots of the wide trees.
+ddgi_status upload_wide_instances(ddgi_ctx* ctx, cudaStream_t st) {
+    SceneBuffers& S = ctx->scene;
+    const uint32_t ni = (uint32_t)S.host_inst.size();
+    if (ni == 0) return DDGI_OK;
+    std::vector<GpuInstance> leaf(ni);
+    for (uint32_t id = 0; id < ni; ++id) {
+        GpuInstance g = S.host_inst[id];
+        g.blas_root = g.blas_root >= 0 ? S.wide_root_of_mesh[S.mesh_of_inst[id]] : -1;
+        leaf[S.leaf_of_id[id]] = g;
+    }
+    CK(cudaMemcpyAsync(S.winst_leaf, leaf.data(), sizeof(GpuInstance) * ni, cudaMemcpyHostToDevice, st), "upload");
+    return DDGI_OK;
+}
+
+// Top level of the wide trees again (after a refit or rebuild of the
+// binary top level): collapsed from the binary top-level nodes, placed at
+// wide_tlas_start.
+ddgi_status refresh_wide_top(ddgi_ctx* ctx, cudaStream_t st) {
+    SceneBuffers& S = ctx->scene;
+    if (!S.wnodes) return DDGI_OK;
+    const uint32_t ni = (uint32_t)S.host_inst.size();
+    const uint32_t inner = ni > 1 ? ni - 1 : 1;
+    std::vector<BvhNode> top(inner);
+    CK(cudaMemcpyAsync(top.data(), S.nodes + S.tlas_root, sizeof(BvhNode) * inner, cudaMemcpyDeviceToHost, st),
+       "read top level");
+    CK(cudaStreamSynchronize(st), "read top level");
+    for (auto& n : top) {  // references relative to the top level's first node
+        if (n.d.x >= 0) n.d.x -= S.tlas_root;
+        if (n.d.y >= 0) n.d.y -= S.tlas_root;
+    }
+    std::vector<WideNode> w;
+    uint32_t lt = 0;
+    bool ok = true;
+    collapse_wide(top, 0, w, &lt, &ok);
+    if (!ok || S.wide_tlas_start + w.size() > S.wide_cap) return fail(ctx, DDGI_ERR_DEVICE, "wide top level");
+    for (auto& n : w) {
+        int* r = &n.ref.x;
+        for (int k = 0; k < 4; ++k)
+            if (r[k] >= 0) r[k] += (int)S.wide_tlas_start;
+    }
+    CK(cudaMemcpyAsync(S.wnodes + S.wide_tlas_start, w.data(), sizeof(WideNode) * w.size(), cudaMemcpyHostToDevice, st),
+       "upload wide top level");
+    S.wtlas_root = (int32_t)S.wide_tlas_start;
+    S.wnode_count = S.wide_tlas_start + (uint32_t)w.size();
+    const int cap = (int)(3 * S.wlevels_blas + 3 * lt + 4);
+    S.wstack_cap = cap <= kMaxStack ? cap : 0;
+    return upload_wide_instances(ctx, st);
+}
+
+// Four-wide copies of every mesh tree and of the top level.
+ddgi_status build_wide(ddgi_ctx* ctx, const std::vector<int32_t>& mesh_root, cudaStream_t st) {
+    SceneBuffers& S = ctx->scene;
+    S.wstack_cap = 0;
+    if (S.node_count == 0) return DDGI_OK;
+    std::vector<BvhNode> bin(S.node_count);
+    CK(cudaMemcpyAsync(bin.data(), S.nodes, sizeof(BvhNode) * S.node_count, cudaMemcpyDeviceToHost, st),
+       "read trees");
+    CK(cudaStreamSynchronize(st), "read trees");
+    std::vector<WideNode> w;
+    bool ok = true;
+    uint32_t lb = 0;
+    S.wide_root_of_mesh.assign(mesh_root.size(), -1);
+    for (size_t m = 0; m < mesh_root.size(); ++m) {
+        if (mesh_root[m] < 0) continue;
+        uint32_t lv = 0;
+        S.wide_root_of_mesh[m] = collapse_wide(bin, mesh_root[m], w, &lv, &ok);
+        lb = std::max(lb, lv);
+    }
+    if (!ok) return fail(ctx, DDGI_ERR_DEVICE, "malformed mesh tree");
+    const uint32_t ni = (uint32_t)S.host_inst.size();
+    S.wide_tlas_start = (uint32_t)w.size();
+    S.wide_cap = S.wide_tlas_start + (ni > 1 ? ni - 1 : 1);
+    S.wlevels_blas = lb;
+    CK(cudaMalloc(&S.wnodes, sizeof(WideNode) * std::max<uint32_t>(S.wide_cap, 1)), "alloc wide nodes");
+    CK(cudaMalloc(&S.winst_leaf, sizeof(GpuInstance) * std::max<uint32_t>(ni, 1)), "alloc wide instances");
+    if (!w.empty())
+        CK(cudaMemcpyAsync(S.wnodes, w.data(), sizeof(WideNode) * w.size(), cudaMemcpyHostToDevice, st), "upload");
+    S.wnode_count = (uint32_t)w.size();
+    S.wtlas_root = -1;
+    if (S.tlas_root < 0) {
+        S.wstack_cap = (int)(3 * lb + 4);
+        return DDGI_OK;
+    }
+    return refresh_wide_top(ctx, st);
+}
+
 }  // namespace
 
 ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_stream stream) {
@@ -654,7 +744,7 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
                 }
             }
         }
-        CKB(build_mesh_blas(dpos, S.indices, me.vertex_offset, me.vertex_count, me.index_offset, nt, kBlasLeafMax,
+        CKB(build_mesh_blas(dpos, S.indices, me.vertex_offset, me.vertex_count, me.index_offset, nt, ctx->blas_leaf_max,
                             S.nodes, (int)node_base, S.tris, (int)tri_base, box_lo, box_hi, sorted, scratch, ctx->err,
                             depth, st),
             "bottom-level build");
@@ -713,6 +803,13 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
     S.instance_count = ni;
     S.node_count = total_nodes + tlas_nodes;
     S.tri_count = total_tris;
+    {
+        ddgi_status ws = build_wide(ctx, mesh_root, st);
+        if (ws != DDGI_OK) {
+            free_scene(ctx->scene);
+            return ws;
+        }
+    }
     S.build_id = next_build_id();
     S.built = true;
     return check_device_error(ctx);
@@ -809,6 +906,10 @@ ddgi_status ddgi_update_instances(ddgi_ctx* ctx, const uint32_t* ids, const floa
            "top-level refit");
         // the host vectors above are staged by the copies before they return
     }
+    {
+        ddgi_status ws = refresh_wide_top(ctx, st);
+        if (ws != DDGI_OK) return ws;
+    }
     S.build_id = next_build_id();  // batches made from the old top level are stale
     return DDGI_OK;
 }
@@ -864,6 +965,7 @@ TraceTuning trace_tuning(const ddgi_ctx* ctx) {
     t.refill = ctx->tune.refill_lanes;
     t.split = ctx->tune.smem_stack;
     t.rays_per_warp = ctx->tune.rays_per_warp;
+    t.wide = ctx->tune.node_width == 4 ? 1u : 0u;
     return t;
 }
 
@@ -923,8 +1025,8 @@ ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_
         ShadowQueue q{ctx->q_idx, ctx->q_pos, ctx->q_sun, nullptr};
         CK(launch_wavefront(sc, ctx->dg, ctx->dl, dlist, n, ctx->dirs, ctx->ray_order, ctx->states, ctx->color,
                             ctx->depth, ctx->fp16, wh, q, ctx->counters, ctx->rays, hits_out, ctx->scene.stack_cap,
-                            ctx->err, st, ctx->timing ? ctx->ev[3] : nullptr, nullptr, trace_tuning(ctx),
-                            ctx->probe_perm),
+                            ctx->scene.wstack_cap, ctx->err, st, ctx->timing ? ctx->ev[3] : nullptr, nullptr,
+                            trace_tuning(ctx), ctx->probe_perm),
            "wavefront trace launch");
     }
     if (ctx->timing) CK(cudaEventRecord(ctx->ev[1], st), "event");
@@ -982,8 +1084,8 @@ ddgi_status ddgi_update_scheduled(ddgi_ctx* ctx, const float orientation[9], uin
     ddgi_hit* hits_out = ctx->record_hits ? ctx->hits : nullptr;
     CK(launch_wavefront(device_scene(ctx), ctx->dg, ctx->dl, ctx->probe_list, P, ctx->dirs, ctx->ray_order,
                         ctx->states, ctx->color, ctx->depth, ctx->fp16, wh, q, ctx->counters, ctx->rays, hits_out,
-                        ctx->scene.stack_cap, ctx->err, st, ctx->timing ? ctx->ev[3] : nullptr, dcount,
-                        trace_tuning(ctx), nullptr),
+                        ctx->scene.stack_cap, ctx->scene.wstack_cap, ctx->err, st,
+                        ctx->timing ? ctx->ev[3] : nullptr, dcount, trace_tuning(ctx), nullptr),
        "wavefront trace launch");
     if (ctx->timing) CK(cudaEventRecord(ctx->ev[1], st), "event");
     if (ctx->fp16)
@@ -1079,7 +1181,17 @@ ddgi_status ddgi_set_trace_tuning(ddgi_ctx* ctx, const ddgi_trace_tuning* t) {
         return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "refill_lanes = %u outside [1, 32]", t->refill_lanes);
     if (t->smem_stack > (uint32_t)kMaxStack || t->ctas_per_sm > 32)
         return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "smem_stack or ctas_per_sm out of range");
+    if (t->node_width != 2 && t->node_width != 4)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "node_width = %u: want 2 or 4", t->node_width);
     ctx->tune = *t;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_set_leaf_size(ddgi_ctx* ctx, uint32_t max_triangles) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    if (max_triangles < 1 || max_triangles > 8)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "leaf size %u outside [1, 8]", max_triangles);
+    ctx->blas_leaf_max = (int)max_triangles;
     return DDGI_OK;
 }
 
@@ -1146,20 +1258,22 @@ ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t re
     float best_t = 0.0f;
     ddgi_status err = measure(best, &best_t);
     const uint32_t R = ctx->grid.rays_per_probe;
+    const uint32_t width_c[] = {4u, 2u};
     const uint32_t rpw_c[] = {0u, 32u, 16u, 8u, 4u, 2u, 1u};
     const uint32_t refill_c[] = {4u, 8u, 16u, 24u};
     const uint32_t split_c[] = {0u, 32u, 24u, 16u};
     const uint32_t ctas_c[] = {0u, 6u, 4u};
-    for (int p = 0; p < 4 && err == DDGI_OK; ++p) {
-        const uint32_t* cand = p == 0 ? rpw_c : p == 1 ? refill_c : p == 2 ? split_c : ctas_c;
-        const int nc = p == 0 ? 7 : p == 3 ? 3 : 4;
+    for (int p = 0; p < 5 && err == DDGI_OK; ++p) {
+        const uint32_t* cand = p == 0 ? width_c : p == 1 ? rpw_c : p == 2 ? refill_c : p == 3 ? split_c : ctas_c;
+        const int nc = p == 0 ? 2 : p == 1 ? 7 : p == 4 ? 3 : 4;
         for (int i = 0; i < nc && err == DDGI_OK; ++i) {
             ddgi_trace_tuning t = best;
-            uint32_t* field = p == 0 ? &t.rays_per_warp : p == 1 ? &t.refill_lanes : p == 2 ? &t.smem_stack
-                                                                                      : &t.ctas_per_sm;
+            uint32_t* field = p == 0 ? &t.node_width : p == 1 ? &t.rays_per_warp : p == 2 ? &t.refill_lanes
+                              : p == 3 ? &t.smem_stack : &t.ctas_per_sm;
             if (*field == cand[i]) continue;
-            if (p == 0 && grouped_rays_per_warp(cand[i], R) != cand[i]) continue;
-            if (p == 2 && cand[i] != 0 && (int)cand[i] >= ctx->scene.stack_cap) continue;
+            if (p == 1 && grouped_rays_per_warp(cand[i], R) != cand[i]) continue;
+            const int cap = t.node_width == 4 && ctx->scene.wstack_cap > 0 ? ctx->scene.wstack_cap : ctx->scene.stack_cap;
+            if (p == 3 && cand[i] != 0 && (int)cand[i] >= cap) continue;
             *field = cand[i];
             float tt = 0.0f;
             err = measure(t, &tt);
@@ -1181,7 +1295,7 @@ ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t re
 }
 
 ddgi_status ddgi_count_fetches(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
-                               uint32_t probe_count, uint64_t out[9], ddgi_stream stream) {
+                               uint32_t probe_count, uint64_t out[11], ddgi_stream stream) {
     if (!ctx || !orientation || !out) return DDGI_ERR_INVALID_ARGUMENT;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const uint32_t* dlist = nullptr;
@@ -1189,17 +1303,17 @@ ddgi_status ddgi_count_fetches(ddgi_ctx* ctx, const float orientation[9], const 
     ddgi_status s = prepare_update(ctx, orientation, probe_list, probe_count, st, &dlist, &n);
     if (s != DDGI_OK) return s;
     unsigned long long* dc = nullptr;
-    CK(cudaMalloc(&dc, 9 * sizeof(unsigned long long)), "alloc counters");
-    cudaError_t e = cudaMemsetAsync(dc, 0, 9 * sizeof(unsigned long long), st);
+    CK(cudaMalloc(&dc, 11 * sizeof(unsigned long long)), "alloc counters");
+    cudaError_t e = cudaMemsetAsync(dc, 0, 11 * sizeof(unsigned long long), st);
     if (e == cudaSuccess)
         e = launch_trace_shade(device_scene(ctx), ctx->dg, ctx->dl, dlist, n, ctx->dirs, ctx->ray_order, ctx->states,
                                ctx->color, ctx->depth, ctx->fp16, ctx->rays, nullptr, ctx->err, st, dc);
-    unsigned long long h[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long h[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(h, dc, sizeof(h), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     cudaFree(dc);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "count fetches");
-    for (int k = 0; k < 9; ++k) out[k] = h[k];
+    for (int k = 0; k < 11; ++k) out[k] = h[k];
     ctx->last_count = n;
     ctx->last_rays = ctx->grid.rays_per_probe;
     return check_device_error(ctx);

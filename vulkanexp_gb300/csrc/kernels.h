@@ -35,6 +35,7 @@ struct TraceTuning {
     uint32_t refill;         // idle lanes that trigger a warp's work request
     uint32_t split;          // stack entries in shared memory (0 or >= cap: all)
     uint32_t rays_per_warp;  // 0: a warp per probe in slot order; 1..32: grouped order (see below)
+    uint32_t wide;           // 1: four-wide nodes (when the scene has them), 0: binary nodes
 };
 // Grouped order: lane groups of rays_per_warp consecutive directions (of the
 // octant-binned ray order) from 32 / rays_per_warp probes taken in `perm`
@@ -50,7 +51,7 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
                              const uint32_t* probe_list, uint32_t nprobes, const float4* dirs,
                              const uint32_t* ray_order, const uint32_t* states, const void* color, const void* depth,
                              bool fp16_atlas, WaveHits hits, ShadowQueue q, uint32_t* counters, float4* rays_out,
-                             ddgi_hit* hits_out, int stack_cap, uint32_t* err, cudaStream_t st,
+                             ddgi_hit* hits_out, int stack_cap, int wstack_cap, uint32_t* err, cudaStream_t st,
                              cudaEvent_t after_primary, const uint32_t* dev_count, const TraceTuning& tune,
                              const uint32_t* perm);
 // Probe classification (probesInit): kInitRays rays per probe.
@@ -89,6 +90,7 @@ struct BatchVolume {
     float* rowsum;
     const uint32_t* perm;  // probe order of grouped warps (NULL: a warp per probe)
     uint32_t rays_per_warp;
+    int32_t wroot;  // top-level root among the arena's wide nodes (-1: empty)
 };
 
 struct BatchTables {
@@ -112,7 +114,7 @@ struct BatchBlendList {
 
 // wavefront.cu: primary trace, shading and shadow rays of all volumes
 cudaError_t launch_batch_trace(const DeviceScene& arena, const BatchTables& bt, uint32_t total, WaveHits hits,
-                               ShadowQueue q, uint32_t* counters, float4* rays_out, int stack_cap,
+                               ShadowQueue q, uint32_t* counters, float4* rays_out, int stack_cap, int wstack_cap,
                                const TraceTuning& tune, cudaStream_t st, cudaEvent_t after_primary,
                                cudaEvent_t after_shade);
 // blend.cu

@@ -44,10 +44,10 @@ __device__ float3 shade_front(const DeviceScene& sc, const DeviceGrid& g, const 
 }
 
 __device__ __forceinline__ void flush_counters(const Fetches& fc, unsigned long long* c) {
-    unsigned long long v[9] = {fc.nodes[0], fc.tris[0], fc.insts[0], fc.rays[0], fc.shade_bytes,
-                               fc.nodes[1], fc.tris[1], fc.insts[1], fc.rays[1]};
+    unsigned long long v[11] = {fc.nodes[0], fc.tris[0], fc.insts[0], fc.rays[0], fc.shade_bytes,
+                                fc.nodes[1], fc.tris[1], fc.insts[1], fc.rays[1], fc.top_nodes[0], fc.top_nodes[1]};
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
+    for (int k = 0; k < 11; ++k) {
         unsigned long long x = v[k];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
         if ((threadIdx.x & 31) == 0 && x) atomicAdd(c + k, x);

@@ -128,7 +128,7 @@ struct SpillArea<SplitStack> {
 // Persistent traversal loop with per-lane refill.  A warp refills when at
 // least `refill` of its lanes are idle (or all are), taking as many rays as
 // it has idle lanes with one atomic.
-template <bool ANY, class Stack, class Job>
+template <bool ANY, class Stack, template <bool, class> class Walker, class Job>
 __device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job& job, uint32_t total,
                                                 uint32_t* counter, int stack_cap, int split, int refill,
                                                 uint32_t* err) {
@@ -136,7 +136,7 @@ __device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     SpillArea<Stack> spill;
-    WarpWalker<ANY, Stack> w;
+    Walker<ANY, Stack> w;
     init_stack(w.stk, s_stack + threadIdx.x, blockDim.x, split, spill.ptr());
     w.cap = stack_cap;
     w.ref = kNone;
@@ -173,18 +173,18 @@ __device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job
     }
 }
 
-template <class Stack>
+template <class Stack, template <bool, class> class Walker>
 __global__ void __launch_bounds__(kPersistThreads, 8) k_primary(DeviceScene sc, PrimaryJob job, uint32_t* counter,
                                                                 int stack_cap, int split, int refill, uint32_t* err) {
     const uint32_t total = job.dev_count ? *job.dev_count * job.g.rays : job.total;
-    persistent_walk<false, Stack>(sc, job, total, counter, stack_cap, split, refill, err);
+    persistent_walk<false, Stack, Walker>(sc, job, total, counter, stack_cap, split, refill, err);
 }
 
-template <class Stack>
+template <class Stack, template <bool, class> class Walker>
 __global__ void __launch_bounds__(kPersistThreads, 8) k_shadow(DeviceScene sc, ShadowJob job, const uint32_t* qcount,
                                                                uint32_t* counter, int stack_cap, int split, int refill,
                                                                uint32_t* err) {
-    persistent_walk<true, Stack>(sc, job, *qcount, counter, stack_cap, split, refill, err);
+    persistent_walk<true, Stack, Walker>(sc, job, *qcount, counter, stack_cap, split, refill, err);
 }
 
 template <class AV>
@@ -282,7 +282,7 @@ struct InitJob {
 
 __global__ void __launch_bounds__(kPersistThreads) k_init_probes(DeviceScene sc, InitJob job, uint32_t total,
                                                                  uint32_t* counter, int stack_cap, uint32_t* err) {
-    persistent_walk<false, SmemStack>(sc, job, total, counter, stack_cap, stack_cap, 8, err);
+    persistent_walk<false, SmemStack, WarpWalker>(sc, job, total, counter, stack_cap, stack_cap, 8, err);
 }
 
 // State per probe: OFF (0) when more than half of raysPerProbe back-face
@@ -329,8 +329,8 @@ struct BatchPrimaryJob {
         const uint32_t ray = __ldg(bt.ray_order + vol.dir_base + j);
         *out = base + slot * R + ray;
         float4 d4 = __ldg(bt.dirs + vol.dir_base + ray);
-        return w.start_at(sc, vol.root, probe_origin_exact(vol.g, slot), f3(d4.x, d4.y, d4.z), 0.01f, vol.g.tmax,
-                          0x3u);
+        return w.start_at(sc, W::kWide ? vol.wroot : vol.root, probe_origin_exact(vol.g, slot), f3(d4.x, d4.y, d4.z),
+                          0.01f, vol.g.tmax, 0x3u);
     }
     template <class W>
     __device__ __forceinline__ void finish(const W& w, uint32_t out) const {
@@ -356,8 +356,8 @@ struct BatchShadowJob {
             v = 0;
         }
         const BatchVolume& vol = bt.vols[v];
-        return w.start_at(sc, vol.root, f3(p.x, p.y, p.z), f3(vol.L.dir[0], vol.L.dir[1], vol.L.dir[2]), 0.1f,
-                          10000.0f, 0xFFu);
+        return w.start_at(sc, W::kWide ? vol.wroot : vol.root, f3(p.x, p.y, p.z),
+                          f3(vol.L.dir[0], vol.L.dir[1], vol.L.dir[2]), 0.1f, 10000.0f, 0xFFu);
     }
     template <class W>
     __device__ __forceinline__ void finish(const W& w, uint32_t id) const {
@@ -373,18 +373,18 @@ struct BatchShadowJob {
     }
 };
 
-template <class Stack>
+template <class Stack, template <bool, class> class Walker>
 __global__ void __launch_bounds__(kPersistThreads, 8) k_batch_primary(DeviceScene arena, BatchPrimaryJob job,
                                                                    uint32_t total, uint32_t* counter, int stack_cap,
                                                                    int split, int refill) {
-    persistent_walk<false, Stack>(arena, job, total, counter, stack_cap, split, refill, job.bt.err);
+    persistent_walk<false, Stack, Walker>(arena, job, total, counter, stack_cap, split, refill, job.bt.err);
 }
 
-template <class Stack>
+template <class Stack, template <bool, class> class Walker>
 __global__ void __launch_bounds__(kPersistThreads, 8) k_batch_shadow(DeviceScene arena, BatchShadowJob job,
                                                                   const uint32_t* qcount, uint32_t* counter,
                                                                   int stack_cap, int split, int refill) {
-    persistent_walk<true, Stack>(arena, job, *qcount, counter, stack_cap, split, refill, job.bt.err);
+    persistent_walk<true, Stack, Walker>(arena, job, *qcount, counter, stack_cap, split, refill, job.bt.err);
 }
 
 // Shading of every record of the batch (the per-volume k_shade, with the
@@ -464,7 +464,7 @@ uint32_t persistent_blocks(const void* kernel, size_t smem, uint32_t cap_per_sm 
 
 namespace {
 
-template <class Stack>
+template <class Stack, template <bool, class> class Walker>
 cudaError_t wavefront_kernels(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L,
                               const uint32_t* probe_list, uint32_t total, const float4* dirs, const uint32_t* states,
                               const void* color, const void* depth, bool fp16_atlas, WaveHits hits, ShadowQueue q,
@@ -473,8 +473,8 @@ cudaError_t wavefront_kernels(const DeviceScene& sc, const DeviceGrid& g, const 
                               const TraceTuning& tune, const PrimaryJob& pj) {
     const size_t smem = (size_t)split * kPersistThreads * sizeof(int);
     const int refill = (int)(tune.refill < 1 ? 1 : (tune.refill > 32 ? 32 : tune.refill));
-    k_primary<Stack><<<persistent_blocks((const void*)k_primary<Stack>, smem, tune.ctas_per_sm), kPersistThreads,
-                       smem, st>>>(sc, pj, counters, stack_cap, split, refill, err);
+    k_primary<Stack, Walker><<<persistent_blocks((const void*)k_primary<Stack, Walker>, smem, tune.ctas_per_sm),
+                               kPersistThreads, smem, st>>>(sc, pj, counters, stack_cap, split, refill, err);
     if (after_primary) cudaEventRecord(after_primary, st);
     ShadowQueue qq = q;
     qq.count = counters + 1;
@@ -491,8 +491,9 @@ cudaError_t wavefront_kernels(const DeviceScene& sc, const DeviceGrid& g, const 
                                         dev_count, err);
     }
     ShadowJob sj{qq, make_float3(L.dir[0], L.dir[1], L.dir[2]), rays_out, hits.prim, 0};
-    k_shadow<Stack><<<persistent_blocks((const void*)k_shadow<Stack>, smem, tune.ctas_per_sm), kPersistThreads, smem,
-                      st>>>(sc, sj, counters + 1, counters + 2, stack_cap, split, refill, err);
+    k_shadow<Stack, Walker><<<persistent_blocks((const void*)k_shadow<Stack, Walker>, smem, tune.ctas_per_sm),
+                              kPersistThreads, smem, st>>>(sc, sj, counters + 1, counters + 2, stack_cap, split, refill,
+                                                           err);
     return cudaGetLastError();
 }
 
@@ -502,7 +503,7 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
                              const uint32_t* probe_list, uint32_t nprobes, const float4* dirs,
                              const uint32_t* ray_order, const uint32_t* states, const void* color, const void* depth,
                              bool fp16_atlas, WaveHits hits, ShadowQueue q, uint32_t* counters, float4* rays_out,
-                             ddgi_hit* hits_out, int stack_cap, uint32_t* err, cudaStream_t st,
+                             ddgi_hit* hits_out, int stack_cap, int wstack_cap, uint32_t* err, cudaStream_t st,
                              cudaEvent_t after_primary, const uint32_t* dev_count, const TraceTuning& tune,
                              const uint32_t* perm) {
     uint32_t total = nprobes * g.rays;
@@ -514,18 +515,26 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
     // the grouped order covers all probes in perm order: no list, no device count
     const uint32_t* pm = (perm && !probe_list && !dev_count && rpw != 0u) ? perm : nullptr;
     PrimaryJob pj{g, probe_list, dirs, ray_order, hits, total, dev_count, pm, rpw, nprobes};
-    if (tune.split == 0 || (int)tune.split >= stack_cap)
-        return wavefront_kernels<SmemStack>(sc, g, L, probe_list, total, dirs, states, color, depth, fp16_atlas, hits,
-                                            q, counters, rays_out, hits_out, stack_cap, stack_cap, err, st,
-                                            after_primary, dev_count, tune, pj);
-    return wavefront_kernels<SplitStack>(sc, g, L, probe_list, total, dirs, states, color, depth, fp16_atlas, hits, q,
-                                         counters, rays_out, hits_out, stack_cap, (int)tune.split, err, st,
-                                         after_primary, dev_count, tune, pj);
+    const bool wide = tune.wide && sc.wnodes && sc.winstances && wstack_cap > 0;
+    const int cap = wide ? wstack_cap : stack_cap;
+    const bool split = !(tune.split == 0 || (int)tune.split >= cap);
+    const int sp = split ? (int)tune.split : cap;
+#define DDGI_WAVE(STACK, WALKER)                                                                                       \
+    return wavefront_kernels<STACK, WALKER>(sc, g, L, probe_list, total, dirs, states, color, depth, fp16_atlas, hits, \
+                                            q, counters, rays_out, hits_out, cap, sp, err, st, after_primary,         \
+                                            dev_count, tune, pj)
+    if (wide) {
+        if (split) DDGI_WAVE(SplitStack, WideWalker);
+        DDGI_WAVE(SmemStack, WideWalker);
+    }
+    if (split) DDGI_WAVE(SplitStack, WarpWalker);
+    DDGI_WAVE(SmemStack, WarpWalker);
+#undef DDGI_WAVE
 }
 
 namespace {
 
-template <class Stack>
+template <class Stack, template <bool, class> class Walker>
 cudaError_t batch_trace_kernels(const DeviceScene& arena, const BatchTables& bt, uint32_t total, WaveHits hits,
                                 ShadowQueue q, uint32_t* counters, float4* rays_out, int stack_cap, int split,
                                 const TraceTuning& tune, cudaStream_t st, cudaEvent_t after_primary,
@@ -533,17 +542,18 @@ cudaError_t batch_trace_kernels(const DeviceScene& arena, const BatchTables& bt,
     const size_t smem = (size_t)split * kPersistThreads * sizeof(int);
     const int refill = (int)(tune.refill < 1 ? 1 : (tune.refill > 32 ? 32 : tune.refill));
     BatchPrimaryJob pj{bt, hits};
-    k_batch_primary<Stack><<<persistent_blocks((const void*)k_batch_primary<Stack>, smem, tune.ctas_per_sm),
-                             kPersistThreads, smem, st>>>(arena, pj, total, counters, stack_cap, split, refill);
+    k_batch_primary<Stack, Walker>
+        <<<persistent_blocks((const void*)k_batch_primary<Stack, Walker>, smem, tune.ctas_per_sm), kPersistThreads,
+           smem, st>>>(arena, pj, total, counters, stack_cap, split, refill);
     if (after_primary) cudaEventRecord(after_primary, st);
     ShadowQueue qq = q;
     qq.count = counters + 1;
     k_batch_shade<<<(total + 127) / 128, 128, 0, st>>>(bt, total, hits, rays_out, qq);
     if (after_shade) cudaEventRecord(after_shade, st);
     BatchShadowJob sj{qq, bt, rays_out, hits.prim};
-    k_batch_shadow<Stack><<<persistent_blocks((const void*)k_batch_shadow<Stack>, smem, tune.ctas_per_sm),
-                            kPersistThreads, smem, st>>>(arena, sj, counters + 1, counters + 2, stack_cap, split,
-                                                         refill);
+    k_batch_shadow<Stack, Walker>
+        <<<persistent_blocks((const void*)k_batch_shadow<Stack, Walker>, smem, tune.ctas_per_sm), kPersistThreads,
+           smem, st>>>(arena, sj, counters + 1, counters + 2, stack_cap, split, refill);
     return cudaGetLastError();
 }
 
@@ -552,15 +562,24 @@ cudaError_t batch_trace_kernels(const DeviceScene& arena, const BatchTables& bt,
 // counters[0..2] (primary work, shadow queue length, shadow work) must be
 // zero when the launch sequence starts.
 cudaError_t launch_batch_trace(const DeviceScene& arena, const BatchTables& bt, uint32_t total, WaveHits hits,
-                               ShadowQueue q, uint32_t* counters, float4* rays_out, int stack_cap,
+                               ShadowQueue q, uint32_t* counters, float4* rays_out, int stack_cap, int wstack_cap,
                                const TraceTuning& tune, cudaStream_t st, cudaEvent_t after_primary,
                                cudaEvent_t after_shade) {
     if (total == 0) return cudaSuccess;
-    if (tune.split == 0 || (int)tune.split >= stack_cap)
-        return batch_trace_kernels<SmemStack>(arena, bt, total, hits, q, counters, rays_out, stack_cap, stack_cap,
-                                              tune, st, after_primary, after_shade);
-    return batch_trace_kernels<SplitStack>(arena, bt, total, hits, q, counters, rays_out, stack_cap, (int)tune.split,
-                                           tune, st, after_primary, after_shade);
+    const bool wide = tune.wide && arena.wnodes && arena.winstances && wstack_cap > 0;
+    const int cap = wide ? wstack_cap : stack_cap;
+    const bool split = !(tune.split == 0 || (int)tune.split >= cap);
+    const int sp = split ? (int)tune.split : cap;
+#define DDGI_BATCH(STACK, WALKER)                                                                            \
+    return batch_trace_kernels<STACK, WALKER>(arena, bt, total, hits, q, counters, rays_out, cap, sp, tune, \
+                                              st, after_primary, after_shade)
+    if (wide) {
+        if (split) DDGI_BATCH(SplitStack, WideWalker);
+        DDGI_BATCH(SmemStack, WideWalker);
+    }
+    if (split) DDGI_BATCH(SplitStack, WarpWalker);
+    DDGI_BATCH(SmemStack, WarpWalker);
+#undef DDGI_BATCH
 }
 
 // Probe classification of all P probes into `states`.  `dirs` holds the

@@ -71,6 +71,7 @@ _SIGNATURES = [
     ("ddgi_update_instances", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]),
     ("ddgi_final_gather", C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ddgi_set_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
+    ("ddgi_set_leaf_size", C.c_int, [C.c_void_p, C.c_uint32]),
     ("ddgi_get_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_autotune", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_init_probes", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -230,6 +231,10 @@ class Context:
         self._check(self.lib.ddgi_final_gather(self.h, C.byref(gb), _ptr(o), C.c_void_p(out.data_ptr()),
                                                _stream_ptr(stream)))
 
+    def set_leaf_size(self, max_triangles):
+        """Triangles per mesh-tree leaf for the next build_scene."""
+        self._check(self.lib.ddgi_set_leaf_size(self.h, int(max_triangles)))
+
     def trace_tuning(self):
         t = TraceTuning()
         self._check(self.lib.ddgi_get_trace_tuning(self.h, C.byref(t)))
@@ -278,11 +283,11 @@ class Context:
         """Fetch counters of one trace + shade pass (see ddgi_count_fetches)."""
         o = np.ascontiguousarray(orientation, np.float32).reshape(9)
         pl = None if probe_list is None else np.ascontiguousarray(probe_list, np.uint32)
-        out = np.zeros(9, np.uint64)
+        out = np.zeros(11, np.uint64)
         self._check(self.lib.ddgi_count_fetches(self.h, _ptr(o), _ptr(pl), 0 if pl is None else len(pl), _ptr(out),
                                                 _stream_ptr(stream)))
         keys = ("nodes", "tris", "instances", "rays", "shade_bytes", "shadow_nodes", "shadow_tris",
-                "shadow_instances", "shadow_rays")
+                "shadow_instances", "shadow_rays", "top_nodes", "shadow_top_nodes")
         return {k: int(v) for k, v in zip(keys, out)}
 
     def blend_records(self, orientation, records, probe_list=None, stream=None):
