@@ -369,6 +369,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only", default=None, choices=["batching"],
                     help="run one sub-measurement alone and print it")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="the three update forms, e2e and rooflines only (no differentiation, batching, final "
+                         "gather or CPU baseline): the profiling command for the launch list")
     ap.add_argument("--profile", action="store_true",
                     help="profiling target: scene build, then two BF16 wavefront updates and two FP32 ones, no timing")
     args = ap.parse_args()
@@ -395,13 +398,16 @@ def main():
     P, R = w.grid.probe_count(), w.grid.rays_per_probe
 
     if args.profile:
+        flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
         for prec in (abi.PRECISION_BF16, abi.PRECISION_FP32):
             ctx, _ = build_context(w, prec, abi.PIPELINE_WAVEFRONT, stream)
             for k in range(2):
                 ctx.update(w.orientation(k), stream=stream)
             ctx.synchronize(stream)
+            if prec == abi.PRECISION_BF16:  # one final gather over the BF16 atlas
+                measure_final_gather(ctx, w, stream, flush, reps=1)
             ctx.close()
-        print(json.dumps({"profile_target": w.name, "updates": 4}), flush=True)
+        print(json.dumps({"profile_target": w.name, "updates": 4, "final_gathers": 4}), flush=True)
         return
 
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -484,11 +490,13 @@ def main():
             "roofline_blend": roofline_blend,
             "e2e": {"value": e2e_val, "unit": UNIT, "ms_per_step": float(np.mean(e2e_ms)),
                     "h2d_bytes_per_step": R * 20, "d2h_bytes_per_step": int(host_c.nbytes + host_d.nbytes)}}
-    line["final_gather"] = measure_final_gather(ctx, w, stream, flush)
+    if not args.headline_only:
+        line["final_gather"] = measure_final_gather(ctx, w, stream, flush)
     ctx.close()
-    line["differentiation"] = measure_differentiation(stream)
-    line["batching"] = measure_batching(stream, args.steps, args.warmup, flush)
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if not args.headline_only:
+        line["differentiation"] = measure_differentiation(stream)
+        line["batching"] = measure_batching(stream, args.steps, args.warmup, flush)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.headline_only:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_probes)
     if rank == 0:
         print(json.dumps(line), flush=True)

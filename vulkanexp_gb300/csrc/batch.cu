@@ -63,6 +63,7 @@ struct ddgi_batch {
     uint32_t total = 0;
     float4* thit = nullptr;
     uint32_t* prim = nullptr;
+    uint32_t* front = nullptr;
     float4* rays = nullptr;
     uint32_t* q_idx = nullptr;
     float4* q_pos = nullptr;
@@ -168,7 +169,7 @@ __global__ void k_batch_begin(uint32_t* counters, uint32_t* done, unsigned long 
         done[i] = 0u;
         clock[1 + i] = 0ull;
     }
-    if (threadIdx.x < 3) counters[threadIdx.x] = 0u;
+    if (threadIdx.x < 4) counters[threadIdx.x] = 0u;
     if (threadIdx.x == 0) clock[0] = globaltimer_ns();
 }
 
@@ -309,7 +310,7 @@ cudaError_t enqueue(ddgi_batch* b, cudaStream_t st, bool timed) {
     tt.split = b->tuning.smem_stack;
     tt.rays_per_warp = b->tuning.rays_per_warp;  // applied per volume through the volume table
     tt.wide = b->tuning.node_width == 4 ? 1u : 0u;
-    WaveHits wh{b->thit, b->prim};
+    WaveHits wh{b->thit, b->prim, b->front};
     ShadowQueue q{b->q_idx, b->q_pos, b->q_sun, nullptr};
     e = launch_batch_trace(arena_scene(b), bt, b->total, wh, q, b->counters, b->rays, b->stack_cap, b->wstack_cap,
                            tt, st, timed ? b->ev[1] : nullptr, timed ? b->ev[2] : nullptr);
@@ -466,6 +467,7 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
         cudaMalloc(&b->winsts, sizeof(GpuInstance) * std::max<uint64_t>(insts, 1)) != cudaSuccess ||
         cudaMalloc(&b->thit, sizeof(float4) * N) != cudaSuccess ||
         cudaMalloc(&b->prim, sizeof(uint32_t) * N) != cudaSuccess ||
+        cudaMalloc(&b->front, sizeof(uint32_t) * N) != cudaSuccess ||
         cudaMalloc(&b->rays, sizeof(float4) * N) != cudaSuccess ||
         cudaMalloc(&b->q_idx, sizeof(uint32_t) * N) != cudaSuccess ||
         cudaMalloc(&b->q_pos, sizeof(float4) * N) != cudaSuccess ||
@@ -565,6 +567,7 @@ ddgi_status ddgi_batch_destroy(ddgi_batch* b) {
     bfree(b->winsts);
     bfree(b->thit);
     bfree(b->prim);
+    bfree(b->front);
     bfree(b->rays);
     bfree(b->q_idx);
     bfree(b->q_pos);

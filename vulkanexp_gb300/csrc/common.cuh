@@ -169,6 +169,19 @@ __device__ __forceinline__ void xform_exact(const float4 w[3], float3 o, float3 
     *od = make_float3(s[0], s[1], s[2]);
 }
 
+// Three-input min / max (PTX min.f32 / max.f32 with three sources, sm_100
+// and later): exact, like the two-input forms, in one instruction.
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 // Watertight ray/triangle test (Woop, Benthin, Wald 2013), every operation
 // rounded separately.  Accepts t in [tmin, tmax].
 __device__ __forceinline__ bool tri_hit_exact(const Ray& r, float3 v0, float3 v1, float3 v2, float tmin, float tmax,
@@ -186,7 +199,8 @@ __device__ __forceinline__ bool tri_hit_exact(const Ray& r, float3 v0, float3 v1
     float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
     float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
     float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
-    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    // edge functions of mixed signs: outside (U, V, W are finite here)
+    if (fmin3(U, V, W) < 0.0f && fmax3(U, V, W) > 0.0f) return false;
     float det = __fadd_rn(__fadd_rn(U, V), W);
     if (det == 0.0f) return false;
     float Az = __fmul_rn(r.Sz, Akz), Bz = __fmul_rn(r.Sz, Bkz), Cz = __fmul_rn(r.Sz, Ckz);
@@ -208,13 +222,13 @@ __device__ __forceinline__ void node_hit(const Ray& r, const BvhNode& n, float t
     float a0 = (n.a.x - ox) * ix, a1 = (n.a.y - ox) * ix;
     float a2 = (n.a.z - oy) * iy, a3 = (n.a.w - oy) * iy;
     float a4 = (n.c.x - oz) * iz, a5 = (n.c.y - oz) * iz;
-    float n0 = fmaxf(fmaxf(fminf(a0, a1), fminf(a2, a3)), fmaxf(fminf(a4, a5), tmin));
-    float f0 = fminf(fminf(fmaxf(a0, a1), fmaxf(a2, a3)), fminf(fmaxf(a4, a5), tmax));
+    float n0 = fmax3(fminf(a0, a1), fminf(a2, a3), fmaxf(fminf(a4, a5), tmin));
+    float f0 = fmin3(fmaxf(a0, a1), fmaxf(a2, a3), fminf(fmaxf(a4, a5), tmax));
     float b0 = (n.b.x - ox) * ix, b1 = (n.b.y - ox) * ix;
     float b2 = (n.b.z - oy) * iy, b3 = (n.b.w - oy) * iy;
     float b4 = (n.c.z - oz) * iz, b5 = (n.c.w - oz) * iz;
-    float n1 = fmaxf(fmaxf(fminf(b0, b1), fminf(b2, b3)), fmaxf(fminf(b4, b5), tmin));
-    float f1 = fminf(fminf(fmaxf(b0, b1), fmaxf(b2, b3)), fminf(fmaxf(b4, b5), tmax));
+    float n1 = fmax3(fminf(b0, b1), fminf(b2, b3), fmaxf(fminf(b4, b5), tmin));
+    float f1 = fmin3(fmaxf(b0, b1), fmaxf(b2, b3), fminf(fmaxf(b4, b5), tmax));
     *h0 = n0 <= f0;
     *h1 = n1 <= f1;
     *t0 = n0;

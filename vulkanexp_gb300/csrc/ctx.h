@@ -75,6 +75,7 @@ struct ddgi_ctx {
     // wavefront pipeline: hit buffer, shadow-ray queue, work counters
     float4* wave_thit = nullptr;
     uint32_t* wave_prim = nullptr;
+    uint32_t* wave_front = nullptr;  // compacted front-face hits
     uint32_t* q_idx = nullptr;
     float4* q_pos = nullptr;
     float4* q_sun = nullptr;

@@ -162,6 +162,7 @@ ddgi_status ensure_ray_capacity(ddgi_ctx* ctx, size_t records) {
         dfree(ctx->rays);
         dfree(ctx->wave_thit);
         dfree(ctx->wave_prim);
+        dfree(ctx->wave_front);
         dfree(ctx->q_idx);
         dfree(ctx->q_pos);
         dfree(ctx->q_sun);
@@ -169,6 +170,7 @@ ddgi_status ensure_ray_capacity(ddgi_ctx* ctx, size_t records) {
         CK(cudaMalloc(&ctx->rays, records * sizeof(float4)), "cudaMalloc ray records");
         CK(cudaMalloc(&ctx->wave_thit, records * sizeof(float4)), "cudaMalloc hit buffer");
         CK(cudaMalloc(&ctx->wave_prim, records * sizeof(uint32_t)), "cudaMalloc hit buffer");
+        CK(cudaMalloc(&ctx->wave_front, records * sizeof(uint32_t)), "cudaMalloc front-hit queue");
         CK(cudaMalloc(&ctx->q_idx, records * sizeof(uint32_t)), "cudaMalloc shadow queue");
         CK(cudaMalloc(&ctx->q_pos, records * sizeof(float4)), "cudaMalloc shadow queue");
         CK(cudaMalloc(&ctx->q_sun, records * sizeof(float4)), "cudaMalloc shadow queue");
@@ -300,6 +302,7 @@ ddgi_status ddgi_destroy(ddgi_ctx* ctx) {
     dfree(ctx->rays);
     dfree(ctx->wave_thit);
     dfree(ctx->wave_prim);
+    dfree(ctx->wave_front);
     dfree(ctx->q_idx);
     dfree(ctx->q_pos);
     dfree(ctx->q_sun);
@@ -1021,7 +1024,7 @@ ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_
            "trace launch");
         if (ctx->timing) CK(cudaEventRecord(ctx->ev[3], st), "event");
     } else {
-        WaveHits wh{ctx->wave_thit, ctx->wave_prim};
+        WaveHits wh{ctx->wave_thit, ctx->wave_prim, ctx->wave_front};
         ShadowQueue q{ctx->q_idx, ctx->q_pos, ctx->q_sun, nullptr};
         CK(launch_wavefront(sc, ctx->dg, ctx->dl, dlist, n, ctx->dirs, ctx->ray_order, ctx->states, ctx->color,
                             ctx->depth, ctx->fp16, wh, q, ctx->counters, ctx->rays, hits_out, ctx->scene.stack_cap,
@@ -1079,7 +1082,7 @@ ddgi_status ddgi_update_scheduled(ddgi_ctx* ctx, const float orientation[9], uin
     uint32_t* dcount = ctx->sched + 2;
     if (ctx->timing) CK(cudaEventRecord(ctx->ev[0], st), "event");
     CK(launch_select_probes(ctx->states, P, max_probes, ctx->sched, ctx->probe_list, st), "schedule launch");
-    WaveHits wh{ctx->wave_thit, ctx->wave_prim};
+    WaveHits wh{ctx->wave_thit, ctx->wave_prim, ctx->wave_front};
     ShadowQueue q{ctx->q_idx, ctx->q_pos, ctx->q_sun, nullptr};
     ddgi_hit* hits_out = ctx->record_hits ? ctx->hits : nullptr;
     CK(launch_wavefront(device_scene(ctx), ctx->dg, ctx->dl, ctx->probe_list, P, ctx->dirs, ctx->ray_order,

@@ -20,8 +20,9 @@ cudaError_t launch_trace_rays(const DeviceScene& sc, const float* origins, const
 
 // wavefront.cu
 struct WaveHits {
-    float4* thit;    // (t, b1, b2, instance bits) per ray
-    uint32_t* prim;  // primitive | backface << 31
+    float4* thit;     // (t, b1, b2, instance bits) per ray
+    uint32_t* prim;   // primitive | backface << 31
+    uint32_t* front;  // compacted queue of front-face hits (record indices)
 };
 struct ShadowQueue {
     uint32_t* idx;   // ray record index

@@ -266,7 +266,10 @@ struct WarpWalker {
         int leaf = kNone;
         bool searching = active && ref != kNone;
         bool failed = false;
-        while (__any_sync(0xffffffffu, searching)) {
+        const float blo = tmin * kBoxLo, bhi = tcur * kBoxHi;  // tcur is fixed until the leaf phase
+        // step until no lane is still searching for its first leaf (one vote
+        // per step; lanes already holding a leaf walk on speculatively)
+        while (__any_sync(0xffffffffu, searching && leaf == kNone)) {
             if (searching) {
                 if (ref >= 0) {
                     if (++steps > max_steps || (uint32_t)ref >= sc.node_count) {
@@ -277,7 +280,7 @@ struct WarpWalker {
                         BvhNode n = load_node(sc.nodes, ref);
                         bool h0, h1;
                         float t0, t1;
-                        node_hit(r, n, tmin * kBoxLo, tcur * kBoxHi, &h0, &h1, &t0, &t1);
+                        node_hit(r, n, blo, bhi, &h0, &h1, &t0, &t1);
                         if (h0 && h1) {
                             int nearr = n.d.x, farr = n.d.y;
                             if (t1 < t0) {
@@ -305,7 +308,6 @@ struct WarpWalker {
                 }
                 if (ref == kNone) searching = false;
             }
-            if (__all_sync(0xffffffffu, !searching || leaf != kNone)) break;
         }
         if (!active) return false;
         if (failed) return true;
@@ -515,7 +517,7 @@ struct WideWalker {
         int leaf = kNone;
         bool searching = active && ref != kNone;
         bool failed = false;
-        while (__any_sync(0xffffffffu, searching)) {
+        while (__any_sync(0xffffffffu, searching && leaf == kNone)) {
             if (searching) {
                 if (ref >= 0) {
                     if (++steps > max_steps || (uint32_t)ref >= sc.wnode_count) {
@@ -534,7 +536,6 @@ struct WideWalker {
                 }
                 if (ref == kNone) searching = false;
             }
-            if (__all_sync(0xffffffffu, !searching || leaf != kNone)) break;
         }
         if (!active) return false;
         if (failed) return true;

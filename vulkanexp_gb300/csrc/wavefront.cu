@@ -140,29 +140,29 @@ __device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job
     init_stack(w.stk, s_stack + threadIdx.x, blockDim.x, split, spill.ptr());
     w.cap = stack_cap;
     w.ref = kNone;
-    bool active = false, exhausted = false;
+    bool active = false;
+    bool drained = false;  // warp-uniform: the work counter has passed `total`
     uint32_t out = 0;
     for (;;) {
-        unsigned idle = __ballot_sync(kFull, !active && !exhausted);
         unsigned busy = __ballot_sync(kFull, active);
-        if (idle && (__popc(idle) >= refill || busy == 0)) {
+        const unsigned idle = ~busy;
+        if (!drained && (__popc(idle) >= refill || busy == 0)) {
             int leader = __ffs(idle) - 1;
             uint32_t base = 0;
             if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(idle));
             base = __shfl_sync(kFull, base, leader);
-            if (!active && !exhausted) {
+            drained = base >= total;  // the counter only grows: every later request fails too
+            if (!active) {
                 uint32_t id = base + (uint32_t)__popc(idle & lt);
                 if (id < total) {
                     if (job.start(w, sc, id, &out)) active = true;
                     else job.finish(w, out);  // empty scene: immediate miss
-                } else {
-                    exhausted = true;
                 }
             }
             busy = __ballot_sync(kFull, active);
         }
         if (busy == 0) {
-            if (__all_sync(kFull, exhausted)) break;
+            if (drained) break;
             continue;
         }
         bool fin = w.advance(sc, err, active);  // every lane takes part (warp votes)
@@ -187,39 +187,35 @@ __global__ void __launch_bounds__(kPersistThreads, 8) k_shadow(DeviceScene sc, S
     persistent_walk<true, Stack, Walker>(sc, job, *qcount, counter, stack_cap, split, refill, err);
 }
 
-template <class AV>
-__global__ void __launch_bounds__(128) k_shade(DeviceScene sc, DeviceGrid g, DeviceLight L,
-                                               const uint32_t* __restrict__ probe_list, uint32_t total,
-                                               const float4* __restrict__ dirs, const uint32_t* __restrict__ states,
-                                               AV at, WaveHits hits, float4* rays_out, ddgi_hit* hits_out,
-                                               ShadowQueue q, const uint32_t* dev_count, uint32_t* err) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
-    bool enqueue = false;
-    SurfaceShade s;
+// Warp-aggregated append: the lanes with `flag` get consecutive slots of a
+// queue whose length is *count; returns this lane's slot (valid if flag).
+__device__ __forceinline__ uint32_t warp_append(bool flag, uint32_t* count) {
+    const unsigned m = __ballot_sync(kFull, flag);
+    if (!m) return 0;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(kFull, base, leader);
+    return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+}
+
+// Shading, pass 1, one thread per record: a miss gets the sky radiance
+// (miss.rmiss:17-23), a back face (0, 0, 0, 0.8 t) (closesthit.glsl:137-141);
+// front faces go to a compacted queue so that pass 2 runs in full warps.
+__global__ void __launch_bounds__(128) k_shade_classify(DeviceGrid g, DeviceLight L, uint32_t total, WaveHits hits,
+                                                        float4* rays_out, ddgi_hit* hits_out, uint32_t* front_count,
+                                                        const uint32_t* dev_count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (dev_count) total = *dev_count * g.rays;
+    bool is_front = false;
     if (i < total) {
-        uint32_t R = g.rays;
-        uint32_t slot = i / R, ray = i - slot * R;
-        float4 th = hits.thit[i];
-        uint32_t pb = hits.prim[i];
-        uint32_t inst = __float_as_uint(th.w), prim = pb & 0x0fffffffu;
-        bool back = (pb >> 31) != 0;
-        float4 rec;
-        if (inst == kNoHit) {
-            rec = make_float4(L.sky[0], L.sky[1], L.sky[2], -1.0f);  // miss.rmiss:17-23
-        } else if (back) {
-            rec = make_float4(0.0f, 0.0f, 0.0f, th.x * 0.80f);  // closesthit.glsl:137-141
-        } else {
-            uint32_t probe = probe_list ? __ldg(probe_list + slot) : slot;
-            float4 d4 = __ldg(dirs + ray);
-            float3 d = f3(d4.x, d4.y, d4.z);
-            if (shade_surface(sc, g, L, states, at, probe_origin_exact(g, probe), d, th.x, th.y, th.z, inst, prim, &s,
-                              err))
-                enqueue = true;
-            rec = make_float4(s.base.x, s.base.y, s.base.z, th.x);
-        }
-        rays_out[i] = rec;
+        const float4 th = hits.thit[i];
+        const uint32_t pb = hits.prim[i];
+        const uint32_t inst = __float_as_uint(th.w), prim = pb & 0x0fffffffu;
+        const bool back = (pb >> 31) != 0;
+        if (inst == kNoHit) rays_out[i] = make_float4(L.sky[0], L.sky[1], L.sky[2], -1.0f);
+        else if (back) rays_out[i] = make_float4(0.0f, 0.0f, 0.0f, th.x * 0.80f);
+        else is_front = true;
         if (hits_out) {
             ddgi_hit hr;
             hr.instance = inst;
@@ -229,18 +225,45 @@ __global__ void __launch_bounds__(128) k_shade(DeviceScene sc, DeviceGrid g, Dev
             hits_out[i] = hr;
         }
     }
-    unsigned m = __ballot_sync(kFull, enqueue);
-    if (m) {
-        int leader = __ffs(m) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(q.count, (uint32_t)__popc(m));
-        base = __shfl_sync(kFull, base, leader);
-        if (enqueue) {
-            uint32_t k = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
-            q.idx[k] = i;
-            q.pos[k] = make_float4(s.position.x, s.position.y, s.position.z, 0.0f);
-            q.sun[k] = make_float4(s.sun.x, s.sun.y, s.sun.z, s.fade);
-        }
+    const uint32_t k = warp_append(is_front, front_count);
+    if (is_front) hits.front[k] = i;
+}
+
+// Shading, pass 2, one thread per queued front hit: closesthit.glsl
+// (NO_REFLECTION) up to the shadow query, whose rays are appended to the
+// shadow queue (an unshadowed ray later adds the sun term).
+// 80 registers at most: six resident blocks per SM without spills.
+template <class AV>
+__global__ void __launch_bounds__(128, 6) k_shade_front(DeviceScene sc, DeviceGrid g, DeviceLight L,
+                                                        const uint32_t* __restrict__ probe_list,
+                                                        const float4* __restrict__ dirs,
+                                                        const uint32_t* __restrict__ states, AV at, WaveHits hits,
+                                                        const uint32_t* front_count, float4* rays_out, ShadowQueue q,
+                                                        uint32_t* err) {
+    const uint32_t n = *front_count;
+    if (blockIdx.x * blockDim.x >= n) return;  // whole block
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    bool enqueue = false;
+    SurfaceShade s;
+    uint32_t i = 0;
+    if (k < n) {
+        i = hits.front[k];
+        const uint32_t R = g.rays;
+        const uint32_t slot = i / R, ray = i - slot * R;
+        const float4 th = hits.thit[i];
+        const uint32_t inst = __float_as_uint(th.w), prim = hits.prim[i] & 0x0fffffffu;
+        const uint32_t probe = probe_list ? __ldg(probe_list + slot) : slot;
+        const float4 d4 = __ldg(dirs + ray);
+        if (shade_surface(sc, g, L, states, at, probe_origin_exact(g, probe), f3(d4.x, d4.y, d4.z), th.x, th.y, th.z,
+                          inst, prim, &s, err))
+            enqueue = true;
+        rays_out[i] = make_float4(s.base.x, s.base.y, s.base.z, th.x);
+    }
+    const uint32_t qk = warp_append(enqueue, q.count);
+    if (enqueue) {
+        q.idx[qk] = i;
+        q.pos[qk] = make_float4(s.position.x, s.position.y, s.position.z, 0.0f);
+        q.sun[qk] = make_float4(s.sun.x, s.sun.y, s.sun.z, s.fade);
     }
 }
 
@@ -387,61 +410,70 @@ __global__ void __launch_bounds__(kPersistThreads, 8) k_batch_shadow(DeviceScene
     persistent_walk<true, Stack, Walker>(arena, job, *qcount, counter, stack_cap, split, refill, job.bt.err);
 }
 
-// Shading of every record of the batch (the per-volume k_shade, with the
-// volume's scene, grid, light, states and atlas looked up per record).
-__global__ void __launch_bounds__(128) k_batch_shade(BatchTables bt, uint32_t total, WaveHits hits,
-                                                     float4* rays_out, ShadowQueue q) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
+// Batched shading, pass 1 (k_shade_classify with the record's volume).
+__global__ void __launch_bounds__(128) k_batch_classify(BatchTables bt, uint32_t total, WaveHits hits,
+                                                        float4* rays_out, uint32_t* front_count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool is_front = false;
+    if (i < total) {
+        const float4 th = hits.thit[i];
+        const uint32_t pb = hits.prim[i];
+        const uint32_t inst = __float_as_uint(th.w);
+        const bool back = (pb >> 31) != 0;
+        if (inst == kNoHit) {
+            const BatchVolume& vol = bt.vols[batch_volume(bt, i)];
+            rays_out[i] = make_float4(vol.L.sky[0], vol.L.sky[1], vol.L.sky[2], -1.0f);
+        } else if (back) {
+            rays_out[i] = make_float4(0.0f, 0.0f, 0.0f, th.x * 0.80f);
+        } else {
+            is_front = true;
+        }
+    }
+    const uint32_t k = warp_append(is_front, front_count);
+    if (is_front) hits.front[k] = i;
+}
+
+// Batched shading, pass 2 (k_shade_front with the volume's scene, grid,
+// light, states and atlas; the shadow-queue entry carries the volume).
+__global__ void __launch_bounds__(128, 6) k_batch_shade_front(BatchTables bt, WaveHits hits,
+                                                              const uint32_t* front_count, float4* rays_out,
+                                                              ShadowQueue q) {
+    const uint32_t n = *front_count;
+    if (blockIdx.x * blockDim.x >= n) return;  // whole block
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     bool enqueue = false;
     SurfaceShade s;
-    uint32_t v = 0;
-    if (i < total) {
+    uint32_t i = 0, v = 0;
+    if (k < n) {
+        i = hits.front[k];
         v = batch_volume(bt, i);
         const BatchVolume& vol = bt.vols[v];
         const uint32_t R = vol.g.rays;
         const uint32_t local = i - __ldg(bt.ray_base + v);
         const uint32_t slot = local / R, ray = local - slot * R;
-        float4 th = hits.thit[i];
-        uint32_t pb = hits.prim[i];
-        uint32_t inst = __float_as_uint(th.w), prim = pb & 0x0fffffffu;
-        bool back = (pb >> 31) != 0;
-        float4 rec;
-        if (inst == kNoHit) {
-            rec = make_float4(vol.L.sky[0], vol.L.sky[1], vol.L.sky[2], -1.0f);
-        } else if (back) {
-            rec = make_float4(0.0f, 0.0f, 0.0f, th.x * 0.80f);
+        const float4 th = hits.thit[i];
+        const uint32_t inst = __float_as_uint(th.w), prim = hits.prim[i] & 0x0fffffffu;
+        const float4 d4 = __ldg(bt.dirs + vol.dir_base + ray);
+        const float3 d = f3(d4.x, d4.y, d4.z);
+        const float3 o = probe_origin_exact(vol.g, slot);
+        if (vol.fp16) {
+            AtlasView<ColorTexF16, DepthTexF16> at{{static_cast<const uint2*>(vol.color)},
+                                                   {static_cast<const uint32_t*>(vol.depth)}};
+            enqueue = shade_surface(vol.sc, vol.g, vol.L, vol.states, at, o, d, th.x, th.y, th.z, inst, prim, &s,
+                                    bt.err);
         } else {
-            float4 d4 = __ldg(bt.dirs + vol.dir_base + ray);
-            float3 d = f3(d4.x, d4.y, d4.z);
-            float3 o = probe_origin_exact(vol.g, slot);
-            if (vol.fp16) {
-                AtlasView<ColorTexF16, DepthTexF16> at{{static_cast<const uint2*>(vol.color)},
-                                                       {static_cast<const uint32_t*>(vol.depth)}};
-                enqueue = shade_surface(vol.sc, vol.g, vol.L, vol.states, at, o, d, th.x, th.y, th.z, inst, prim, &s,
-                                        bt.err);
-            } else {
-                AtlasView<ColorTexF32, DepthTexF32> at{{static_cast<const float4*>(vol.color)},
-                                                       {static_cast<const float2*>(vol.depth)}};
-                enqueue = shade_surface(vol.sc, vol.g, vol.L, vol.states, at, o, d, th.x, th.y, th.z, inst, prim, &s,
-                                        bt.err);
-            }
-            rec = make_float4(s.base.x, s.base.y, s.base.z, th.x);
+            AtlasView<ColorTexF32, DepthTexF32> at{{static_cast<const float4*>(vol.color)},
+                                                   {static_cast<const float2*>(vol.depth)}};
+            enqueue = shade_surface(vol.sc, vol.g, vol.L, vol.states, at, o, d, th.x, th.y, th.z, inst, prim, &s,
+                                    bt.err);
         }
-        rays_out[i] = rec;
+        rays_out[i] = make_float4(s.base.x, s.base.y, s.base.z, th.x);
     }
-    unsigned m = __ballot_sync(kFull, enqueue);
-    if (m) {
-        int leader = __ffs(m) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(q.count, (uint32_t)__popc(m));
-        base = __shfl_sync(kFull, base, leader);
-        if (enqueue) {
-            uint32_t k = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
-            q.idx[k] = i;
-            q.pos[k] = make_float4(s.position.x, s.position.y, s.position.z, __uint_as_float(v));
-            q.sun[k] = make_float4(s.sun.x, s.sun.y, s.sun.z, s.fade);
-        }
+    const uint32_t qk = warp_append(enqueue, q.count);
+    if (enqueue) {
+        q.idx[qk] = i;
+        q.pos[qk] = make_float4(s.position.x, s.position.y, s.position.z, __uint_as_float(v));
+        q.sun[qk] = make_float4(s.sun.x, s.sun.y, s.sun.z, s.fade);
     }
 }
 
@@ -479,16 +511,17 @@ cudaError_t wavefront_kernels(const DeviceScene& sc, const DeviceGrid& g, const 
     ShadowQueue qq = q;
     qq.count = counters + 1;
     uint32_t blocks = (total + 127) / 128;
+    k_shade_classify<<<blocks, 128, 0, st>>>(g, L, total, hits, rays_out, hits_out, counters + 3, dev_count);
     if (fp16_atlas) {
         AtlasView<ColorTexF16, DepthTexF16> at{{static_cast<const uint2*>(color)},
                                                {static_cast<const uint32_t*>(depth)}};
-        k_shade<<<blocks, 128, 0, st>>>(sc, g, L, probe_list, total, dirs, states, at, hits, rays_out, hits_out, qq,
-                                        dev_count, err);
+        k_shade_front<<<blocks, 128, 0, st>>>(sc, g, L, probe_list, dirs, states, at, hits, counters + 3, rays_out, qq,
+                                              err);
     } else {
         AtlasView<ColorTexF32, DepthTexF32> at{{static_cast<const float4*>(color)},
                                                {static_cast<const float2*>(depth)}};
-        k_shade<<<blocks, 128, 0, st>>>(sc, g, L, probe_list, total, dirs, states, at, hits, rays_out, hits_out, qq,
-                                        dev_count, err);
+        k_shade_front<<<blocks, 128, 0, st>>>(sc, g, L, probe_list, dirs, states, at, hits, counters + 3, rays_out, qq,
+                                              err);
     }
     ShadowJob sj{qq, make_float3(L.dir[0], L.dir[1], L.dir[2]), rays_out, hits.prim, 0};
     k_shadow<Stack, Walker><<<persistent_blocks((const void*)k_shadow<Stack, Walker>, smem, tune.ctas_per_sm),
@@ -508,8 +541,8 @@ cudaError_t launch_wavefront(const DeviceScene& sc, const DeviceGrid& g, const D
                              const uint32_t* perm) {
     uint32_t total = nprobes * g.rays;
     if (total == 0) return cudaSuccess;
-    // counters[0]: primary work, counters[1]: shadow queue length, counters[2]: shadow work
-    cudaError_t e = cudaMemsetAsync(counters, 0, 3 * sizeof(uint32_t), st);
+    // counters[0]: primary work, [1]: shadow queue length, [2]: shadow work, [3]: front-hit queue length
+    cudaError_t e = cudaMemsetAsync(counters, 0, 4 * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     const uint32_t rpw = grouped_rays_per_warp(tune.rays_per_warp, g.rays);
     // the grouped order covers all probes in perm order: no list, no device count
@@ -548,7 +581,8 @@ cudaError_t batch_trace_kernels(const DeviceScene& arena, const BatchTables& bt,
     if (after_primary) cudaEventRecord(after_primary, st);
     ShadowQueue qq = q;
     qq.count = counters + 1;
-    k_batch_shade<<<(total + 127) / 128, 128, 0, st>>>(bt, total, hits, rays_out, qq);
+    k_batch_classify<<<(total + 127) / 128, 128, 0, st>>>(bt, total, hits, rays_out, counters + 3);
+    k_batch_shade_front<<<(total + 127) / 128, 128, 0, st>>>(bt, hits, counters + 3, rays_out, qq);
     if (after_shade) cudaEventRecord(after_shade, st);
     BatchShadowJob sj{qq, bt, rays_out, hits.prim};
     k_batch_shadow<Stack, Walker>
@@ -559,8 +593,8 @@ cudaError_t batch_trace_kernels(const DeviceScene& arena, const BatchTables& bt,
 
 }  // namespace
 
-// counters[0..2] (primary work, shadow queue length, shadow work) must be
-// zero when the launch sequence starts.
+// counters[0..3] (primary work, shadow queue length, shadow work, front-hit
+// queue length) must be zero when the launch sequence starts.
 cudaError_t launch_batch_trace(const DeviceScene& arena, const BatchTables& bt, uint32_t total, WaveHits hits,
                                ShadowQueue q, uint32_t* counters, float4* rays_out, int stack_cap, int wstack_cap,
                                const TraceTuning& tune, cudaStream_t st, cudaEvent_t after_primary,
