@@ -227,6 +227,7 @@ DeviceScene arena_scene(const ddgi_batch* b) {
     s.winstances = b->wstack_cap > 0 ? b->winsts : nullptr;
     s.wtlas_root = -1;
     s.wnode_count = (uint32_t)b->wnode_count;
+    set_step_limits(s);
     return s;
 }
 

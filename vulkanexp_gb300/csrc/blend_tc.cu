@@ -107,11 +107,14 @@ __device__ __forceinline__ uint2 float4_to_half4(float a, float b, float c, floa
 }
 
 // Row `row` of the weight matrices of one update in the B-operand layout
-// (depth rows first, then colour rows), plus its row sum.
-__device__ __forceinline__ void tc_weight_row(uint32_t row, const float4* dirs, uint32_t R, uint32_t nc, uint32_t nd,
-                                              float sharp, uint32_t Nc, uint32_t Nd, uint32_t nchunks, uint8_t* wout,
-                                              float* rowsum) {
-    if (row >= Nd + Nc) return;
+// (depth rows first, then colour rows), plus its row sum; one warp per row.
+// Lane g builds the 16-byte core-matrix rows of 8-ray groups g, g + 32, ...
+// (high and low BF16 parts); the row sum adds the parts group by group and
+// then across lanes in a fixed shuffle order, so it is deterministic.
+__device__ __forceinline__ void tc_weight_row(uint32_t row, uint32_t lane, const float4* dirs, uint32_t R,
+                                              uint32_t nc, uint32_t nd, float sharp, uint32_t Nc, uint32_t Nd,
+                                              uint32_t nchunks, uint8_t* wout, float* rowsum) {
+    if (row >= Nd + Nc) return;  // warp-uniform
     const bool colour = row >= Nd;
     const uint32_t t = colour ? row - Nd : row;
     const uint32_t n = colour ? nc : nd;
@@ -122,29 +125,49 @@ __device__ __forceinline__ void tc_weight_row(uint32_t row, const float4* dirs, 
         td = oct_decode(sc * ((float)(t % n) - ce), sc * ((float)(t / n) - ce));
     }
     const size_t part_bytes = (size_t)(Nd + Nc) * 128;  // one chunk of one part
+    const uint32_t groups = nchunks * (kKChunk / 8);
     float sum = 0.0f;
-    for (uint32_t r = 0; r < nchunks * kKChunk; ++r) {
-        float w = 0.0f;
-        if (valid && r < R) {
-            float4 d = dirs[r];
-            float c = fmaxf(0.0f, td.x * d.x + td.y * d.y + td.z * d.z);
-            w = colour ? c : powf(c, sharp);
+    for (uint32_t gidx = lane; gidx < groups; gidx += 32) {
+        uint32_t hw[4], lw[4];
+        float part = 0.0f;
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+            float w2[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t r = gidx * 8 + e + h;
+                float w = 0.0f;
+                if (valid && r < R) {
+                    float4 d = dirs[r];
+                    float c = fmaxf(0.0f, td.x * d.x + td.y * d.y + td.z * d.z);
+                    w = colour ? c : powf(c, sharp);
+                }
+                w2[h] = w;
+            }
+            __nv_bfloat162 hi = __floats2bfloat162_rn(w2[0], w2[1]);
+            float2 hf = __bfloat1622float2(hi);
+            __nv_bfloat162 lo = __floats2bfloat162_rn(w2[0] - hf.x, w2[1] - hf.y);
+            float2 lf = __bfloat1622float2(lo);
+            part += hf.x + lf.x;
+            part += hf.y + lf.y;
+            hw[e / 2] = *reinterpret_cast<uint32_t*>(&hi);
+            lw[e / 2] = *reinterpret_cast<uint32_t*>(&lo);
         }
-        __nv_bfloat16 hi = __float2bfloat16_rn(w);
-        __nv_bfloat16 lo = __float2bfloat16_rn(w - __bfloat162float(hi));
-        sum += __bfloat162float(hi) + __bfloat162float(lo);
-        uint32_t k = r % kKChunk;
-        size_t off = (size_t)(r / kKChunk) * 2 * part_bytes + (colour ? (size_t)Nd * 128 : 0) + canon_off(t, k / 8) +
-                     (k % 8) * 2;
-        *reinterpret_cast<__nv_bfloat16*>(wout + off) = hi;
-        *reinterpret_cast<__nv_bfloat16*>(wout + off + part_bytes) = lo;
+        sum += part;
+        const uint32_t c = gidx / (kKChunk / 8), kg = gidx % (kKChunk / 8);
+        const size_t off = (size_t)c * 2 * part_bytes + (colour ? (size_t)Nd * 128 : 0) + canon_off(t, kg);
+        *reinterpret_cast<uint4*>(wout + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        *reinterpret_cast<uint4*>(wout + off + part_bytes) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
     }
-    rowsum[row] = sum;
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) rowsum[row] = sum;
 }
 
+// One warp per row, four rows per block.
 __global__ void k_tc_weights(const float4* dirs, uint32_t R, uint32_t nc, uint32_t nd, float sharp, uint32_t Nc,
                              uint32_t Nd, uint32_t nchunks, uint8_t* wout, float* rowsum) {
-    tc_weight_row(blockIdx.x * blockDim.x + threadIdx.x, dirs, R, nc, nd, sharp, Nc, Nd, nchunks, wout, rowsum);
+    tc_weight_row(blockIdx.x * 4 + (threadIdx.x >> 5), threadIdx.x & 31, dirs, R, nc, nd, sharp, Nc, Nd, nchunks,
+                  wout, rowsum);
 }
 
 // Blend of the 32-probe tile starting at probe slot p0 (< nprobes) by the
@@ -453,8 +476,8 @@ __host__ __device__ __forceinline__ TcShape tc_shape(const DeviceGrid& g) {
 __global__ void k_batch_tc_weights(BatchTables bt, BatchBlendList bl) {
     const BatchVolume& vol = bt.vols[__ldg(bl.list + blockIdx.y)];
     const TcShape t = tc_shape(vol.g);
-    tc_weight_row(blockIdx.x * blockDim.x + threadIdx.x, bt.dirs + vol.dir_base, vol.g.rays, t.nc, t.nd, vol.g.sharp,
-                  t.Nc, t.Nd, t.nchunks, vol.wbuf, vol.rowsum);
+    tc_weight_row(blockIdx.x * 4 + (threadIdx.x >> 5), threadIdx.x & 31, bt.dirs + vol.dir_base, vol.g.rays, t.nc,
+                  t.nd, vol.g.sharp, t.Nc, t.Nd, t.nchunks, vol.wbuf, vol.rowsum);
 }
 
 // Batched blend: CTA b takes tile (b - tile_base[i]) of volume list[i]; the
@@ -538,7 +561,7 @@ cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uin
     const uint32_t nc = g.color_res - 2, nd = g.depth_res - 2;
     const uint32_t Nc = (nc * nc + 15) / 16 * 16, Nd = (nd * nd + 15) / 16 * 16;
     const uint32_t nchunks = (g.rays + kKChunk - 1) / kKChunk;
-    k_tc_weights<<<(Nd + Nc + 127) / 128, 128, 0, st>>>(dirs, g.rays, nc, nd, g.sharp, Nc, Nd, nchunks, wbuf, rowsum);
+    k_tc_weights<<<(Nd + Nc + 3) / 4, 128, 0, st>>>(dirs, g.rays, nc, nd, g.sharp, Nc, Nd, nchunks, wbuf, rowsum);
     TcArgs a;
     a.g = g;
     a.probe_list = probe_list;
@@ -586,7 +609,7 @@ size_t batch_tc_smem(uint32_t color_res, uint32_t depth_res) {
 cudaError_t launch_batch_tc_weights(const BatchTables& bt, const BatchBlendList& bl, uint32_t max_rows,
                                     cudaStream_t st) {
     if (bl.n == 0) return cudaSuccess;
-    k_batch_tc_weights<<<dim3((max_rows + 127) / 128, bl.n), 128, 0, st>>>(bt, bl);
+    k_batch_tc_weights<<<dim3((max_rows + 3) / 4, bl.n), 128, 0, st>>>(bt, bl);
     return cudaGetLastError();
 }
 

@@ -95,7 +95,15 @@ struct DeviceScene {
     const GpuInstance* winstances;
     int32_t wtlas_root;
     uint32_t wnode_count;
+    // traversal step limits: a well-formed tree visits each node at most
+    // once per ray (4 x (nodes + triangles + instances) + 64, binary / wide)
+    uint32_t max_steps, wmax_steps;
 };
+
+inline void set_step_limits(DeviceScene& s) {
+    s.max_steps = 4u * (s.node_count + s.tri_count + s.instance_count) + 64u;
+    s.wmax_steps = 4u * (s.wnode_count + s.tri_count + s.instance_count) + 64u;
+}
 
 struct DeviceGrid {
     float mn[3], mx[3];

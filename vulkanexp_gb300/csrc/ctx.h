@@ -204,6 +204,7 @@ inline DeviceScene device_scene(const ddgi_ctx* c) {
     s.winstances = c->scene.wstack_cap > 0 ? c->scene.winst_leaf : nullptr;
     s.wtlas_root = c->scene.wtlas_root;
     s.wnode_count = c->scene.wnode_count;
+    set_step_limits(s);
     return s;
 }
 

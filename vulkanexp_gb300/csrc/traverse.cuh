@@ -200,13 +200,16 @@ struct SplitStack {
 template <bool ANY, class Stack = SmemStack>
 struct WarpWalker {
     static constexpr bool kWide = false;
+    static constexpr int kMinBlocks = 8;  // resident 128-thread blocks per SM the kernels are built for
     Ray wr, r;  // world ray, current ray (world or object space)
     Stack stk;
     int sp, cap, ref;
     bool in_blas;
-    uint32_t inst_id, steps, max_steps, mask;
+    uint32_t inst_id, steps, mask;
     float tmin, tcur;
     HitRec best;
+
+
 
     __device__ __forceinline__ bool start(const DeviceScene& sc, float3 o, float3 d, float tmin_, float tmax_,
                                           uint32_t mask_) {
@@ -229,7 +232,6 @@ struct WarpWalker {
         in_blas = false;
         inst_id = 0;
         steps = 0;
-        max_steps = 4u * (sc.node_count + sc.tri_count + sc.instance_count) + 64u;
         ref = root >= 0 ? root : kNone;
         return ref != kNone;
     }
@@ -272,7 +274,7 @@ struct WarpWalker {
         while (__any_sync(0xffffffffu, searching && leaf == kNone)) {
             if (searching) {
                 if (ref >= 0) {
-                    if (++steps > max_steps || (uint32_t)ref >= sc.node_count) {
+                    if (++steps > sc.max_steps || (uint32_t)ref >= sc.node_count) {
                         raise_error(err, DEV_BAD_INDEX);
                         failed = true;
                         searching = false;
@@ -401,11 +403,12 @@ __device__ __forceinline__ float slab_near(float lx, float hx, float ly, float h
 template <bool ANY, class Stack = SmemStack>
 struct WideWalker {
     static constexpr bool kWide = true;
+    static constexpr int kMinBlocks = 7;
     Ray wr, r;
     Stack stk;
     int sp, cap, ref;
     bool in_blas;
-    uint32_t inst_id, steps, max_steps, mask;
+    uint32_t inst_id, steps, mask;
     float tmin, tcur;
     HitRec best;
 
@@ -429,7 +432,6 @@ struct WideWalker {
         in_blas = false;
         inst_id = 0;
         steps = 0;
-        max_steps = 4u * (sc.wnode_count + sc.tri_count + sc.instance_count) + 64u;
         ref = root >= 0 ? root : kNone;
         return ref != kNone;
     }
@@ -520,7 +522,7 @@ struct WideWalker {
         while (__any_sync(0xffffffffu, searching && leaf == kNone)) {
             if (searching) {
                 if (ref >= 0) {
-                    if (++steps > max_steps || (uint32_t)ref >= sc.wnode_count) {
+                    if (++steps > sc.wmax_steps || (uint32_t)ref >= sc.wnode_count) {
                         raise_error(err, DEV_BAD_INDEX);
                         failed = true;
                         searching = false;

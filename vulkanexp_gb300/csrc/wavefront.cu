@@ -174,14 +174,14 @@ __device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job
 }
 
 template <class Stack, template <bool, class> class Walker>
-__global__ void __launch_bounds__(kPersistThreads, 8) k_primary(DeviceScene sc, PrimaryJob job, uint32_t* counter,
+__global__ void __launch_bounds__(kPersistThreads, Walker<false, Stack>::kMinBlocks) k_primary(DeviceScene sc, PrimaryJob job, uint32_t* counter,
                                                                 int stack_cap, int split, int refill, uint32_t* err) {
     const uint32_t total = job.dev_count ? *job.dev_count * job.g.rays : job.total;
     persistent_walk<false, Stack, Walker>(sc, job, total, counter, stack_cap, split, refill, err);
 }
 
 template <class Stack, template <bool, class> class Walker>
-__global__ void __launch_bounds__(kPersistThreads, 8) k_shadow(DeviceScene sc, ShadowJob job, const uint32_t* qcount,
+__global__ void __launch_bounds__(kPersistThreads, Walker<false, Stack>::kMinBlocks) k_shadow(DeviceScene sc, ShadowJob job, const uint32_t* qcount,
                                                                uint32_t* counter, int stack_cap, int split, int refill,
                                                                uint32_t* err) {
     persistent_walk<true, Stack, Walker>(sc, job, *qcount, counter, stack_cap, split, refill, err);
@@ -397,14 +397,14 @@ struct BatchShadowJob {
 };
 
 template <class Stack, template <bool, class> class Walker>
-__global__ void __launch_bounds__(kPersistThreads, 8) k_batch_primary(DeviceScene arena, BatchPrimaryJob job,
+__global__ void __launch_bounds__(kPersistThreads, Walker<false, Stack>::kMinBlocks) k_batch_primary(DeviceScene arena, BatchPrimaryJob job,
                                                                    uint32_t total, uint32_t* counter, int stack_cap,
                                                                    int split, int refill) {
     persistent_walk<false, Stack, Walker>(arena, job, total, counter, stack_cap, split, refill, job.bt.err);
 }
 
 template <class Stack, template <bool, class> class Walker>
-__global__ void __launch_bounds__(kPersistThreads, 8) k_batch_shadow(DeviceScene arena, BatchShadowJob job,
+__global__ void __launch_bounds__(kPersistThreads, Walker<false, Stack>::kMinBlocks) k_batch_shadow(DeviceScene arena, BatchShadowJob job,
                                                                   const uint32_t* qcount, uint32_t* counter,
                                                                   int stack_cap, int split, int refill) {
     persistent_walk<true, Stack, Walker>(arena, job, *qcount, counter, stack_cap, split, refill, job.bt.err);
