@@ -555,7 +555,44 @@ ddgi_status refresh_wide_top(ddgi_ctx* ctx, cudaStream_t st) {
     return upload_wide_instances(ctx, st);
 }
 
-// Four-wide copies of every mesh tree and of the top level.
+// Mesh tree in nodes[b, e) (root at b) laid out depth first: every node is
+// followed by its first child's subtree, then its second child's, so that a
+// walk down the tree mostly moves to the adjacent node (the same 128-byte
+// cache line).  The root keeps index b, leaf references are unchanged, and
+// the nodes a collapsed leaf made unreachable keep their slots after the
+// reachable ones.  Returns false (nodes untouched) on a malformed tree.
+bool depth_first_layout(std::vector<BvhNode>& nodes, uint32_t b, uint32_t e) {
+    const uint32_t n = e - b;
+    std::vector<int32_t> newidx(n, -1);
+    std::vector<uint32_t> order;
+    order.reserve(n);
+    std::vector<uint32_t> stack{b};
+    while (!stack.empty()) {
+        const uint32_t k = stack.back();
+        stack.pop_back();
+        if (k < b || k >= e || newidx[k - b] >= 0) return false;
+        newidx[k - b] = (int32_t)(b + order.size());
+        order.push_back(k);
+        const int4 d = nodes[k].d;
+        if (d.y >= 0) stack.push_back((uint32_t)d.y);  // second child after the first one's subtree
+        if (d.x >= 0 && d.x != d.y) stack.push_back((uint32_t)d.x);
+    }
+    std::vector<BvhNode> out(nodes.begin() + b, nodes.begin() + e);
+    uint32_t pos = (uint32_t)order.size();
+    for (uint32_t k = 0; k < n; ++k)
+        if (newidx[k] < 0) out[pos++] = nodes[b + k];  // unreachable: kept, never referenced
+    for (size_t i = 0; i < order.size(); ++i) {
+        BvhNode nd = nodes[order[i]];
+        if (nd.d.x >= 0) nd.d.x = newidx[nd.d.x - (int)b];
+        if (nd.d.y >= 0) nd.d.y = newidx[nd.d.y - (int)b];
+        out[i] = nd;
+    }
+    std::copy(out.begin(), out.end(), nodes.begin() + b);
+    return true;
+}
+
+// Depth-first layout of every mesh tree, then four-wide copies of every mesh
+// tree and of the top level.
 ddgi_status build_wide(ddgi_ctx* ctx, const std::vector<int32_t>& mesh_root, cudaStream_t st) {
     SceneBuffers& S = ctx->scene;
     S.wstack_cap = 0;
@@ -564,6 +601,20 @@ ddgi_status build_wide(ddgi_ctx* ctx, const std::vector<int32_t>& mesh_root, cud
     CK(cudaMemcpyAsync(bin.data(), S.nodes, sizeof(BvhNode) * S.node_count, cudaMemcpyDeviceToHost, st),
        "read trees");
     CK(cudaStreamSynchronize(st), "read trees");
+    {
+        // mesh trees occupy consecutive ranges in mesh order, the top level follows
+        std::vector<uint32_t> roots;
+        for (int32_t r : mesh_root)
+            if (r >= 0) roots.push_back((uint32_t)r);
+        const uint32_t blas_end = S.tlas_root >= 0 ? (uint32_t)S.tlas_root : (uint32_t)S.node_count;
+        for (size_t i = 0; i < roots.size(); ++i) {
+            const uint32_t e = i + 1 < roots.size() ? roots[i + 1] : blas_end;
+            if (roots[i] < e && e <= S.node_count) depth_first_layout(bin, roots[i], e);
+        }
+        if (blas_end > 0)
+            CK(cudaMemcpyAsync(S.nodes, bin.data(), sizeof(BvhNode) * blas_end, cudaMemcpyHostToDevice, st),
+               "upload mesh trees");
+    }
     std::vector<WideNode> w;
     bool ok = true;
     uint32_t lb = 0;
