@@ -314,6 +314,20 @@ def measure_batching(stream, steps, warmup, flush):
     return out
 
 
+def profiled_traffic(summary):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum of
+    one ncu capture of the same workload) from the committed summary under
+    profiles/, or None."""
+    import re
+
+    try:
+        with open(os.path.join(ROOT, "profiles", summary)) as f:
+            m = re.search(r"traffic_bytes_per_launch:\s*(\d+)", f.read())
+    except OSError:
+        return None
+    return int(m.group(1)) if m else None
+
+
 def measure_final_gather(ctx, w, stream, flush, reps=10, width=1920, height=1080):
     """The atlas consumer: FinalGather.frag over a seeded 1920x1080 G-buffer
     (positions inside the probe grid, random normals and materials, 10% sky
@@ -464,7 +478,9 @@ def main():
     alg_bytes = fetches["nodes"] * 64 + fetches["tris"] * 48 + fetches["instances"] * 64
     achieved = alg_bytes / (prim_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "kernel": "k_primary", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "peak_source": peak_kind, "traffic": None,
+                "frac": achieved / hbm, "peak_source": peak_kind,
+                "traffic": profiled_traffic("k_primary_terrain_32x16x32_r256.md"),
+                "traffic_source": "ncu capture, profiles/k_primary_terrain_32x16x32_r256.md",
                 "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": prim_ms,
                 "note": "fetch-counted node/triangle/instance bytes of the primary rays; they are served mostly by "
                         "L1/L2, so frac > 1 is cache reuse, not DRAM traffic",
@@ -477,7 +493,9 @@ def main():
     roofline_blend = {"kernel": "k_blend_tc (+ k_tc_weights)", "bound": "hbm", "kernel_ms": blend_ms,
                       "algorithmic_bytes": blend_bytes, "achieved_gbs": blend_bytes / (blend_ms * 1e-3) / 1e9,
                       "frac_hbm": blend_bytes / (blend_ms * 1e-3) / 1e9 / hbm,
-                      "useful_tflops": blend_flop / (blend_ms * 1e-3) / 1e12, "peak_bf16_tflops": bf16_peak}
+                      "useful_tflops": blend_flop / (blend_ms * 1e-3) / 1e12, "peak_bf16_tflops": bf16_peak,
+                      "traffic": profiled_traffic("k_blend_tc_terrain_32x16x32_r256.md"),
+                      "traffic_source": "ncu capture, profiles/k_blend_tc_terrain_32x16x32_r256.md"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 trace / bf16 blend", "data": "synthetic (seeded)",
