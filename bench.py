@@ -105,41 +105,57 @@ class ClockSampler:
         return out
 
 
-def cpu_baseline(w, sample_probes, threads=None):
-    """Times the CPU oracle on a bounded sample of probes of the workload."""
+def cpu_baseline(w, sample_probes, threads=None, oracle=None, orientation=0):
+    """Times the CPU oracle on `sample_probes` probes of the workload (0 or
+    more than the grid: all of them), one update from a zero atlas, on
+    `threads` host threads (default: all cores)."""
     from oracle.oracle import Oracle, zero_atlas
 
     threads = threads or os.cpu_count()
+    own = oracle is None
     t0 = time.perf_counter()
-    o = Oracle(w.scene, threads=threads)
+    o = oracle or Oracle(w.scene, threads=threads)
     build_s = time.perf_counter() - t0
-    rng = np.random.default_rng(5)
-    plist = np.sort(rng.permutation(w.grid.probe_count())[:sample_probes]).astype(np.uint32)
+    P = w.grid.probe_count()
+    n = P if sample_probes <= 0 or sample_probes >= P else sample_probes
+    plist = None
+    if n < P:
+        rng = np.random.default_rng(5 + orientation)
+        plist = np.sort(rng.permutation(P)[:n]).astype(np.uint32)
     c, d = zero_atlas(w.grid)
-    st = np.ones(w.grid.probe_count(), np.uint32)
+    st = np.ones(P, np.uint32)
     t0 = time.perf_counter()
-    o.update(w.grid, w.light, w.orientation(0), c, d, st, plist)
+    o.update(w.grid, w.light, w.orientation(orientation), c, d, st, plist)
     dt = time.perf_counter() - t0
-    rays = len(plist) * w.grid.rays_per_probe
-    o.close()
-    return {"value": rays / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d of %d probes x %d rays, 1 update from a zero atlas (%.1f s; BVH build %.1f s untimed)"
-                      % (len(plist), w.grid.probe_count(), w.grid.rays_per_probe, dt, build_s),
-            "ms_per_update_extrapolated": dt * 1e3 * w.grid.probe_count() / len(plist)}
+    rays = n * w.grid.rays_per_probe
+    if own:
+        o.close()
+    probes = "all %d probes" % P if n == P else "%d of %d probes" % (n, P)
+    sample = "%s x %d rays, 1 update from a zero atlas (%.1f s%s)" % (
+        probes, w.grid.rays_per_probe, dt, "; BVH build %.1f s untimed" % build_s if own else "")
+    return {"value": rays / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+            "ms_per_update_extrapolated": dt * 1e3 * P / n}
 
 
 def run_reference(args, w):
+    """The reference arm: the CPU restatement of the reference's probe-update
+    shaders on all host cores (the reference itself is Vulkan/GLSL), each
+    step one update of a bounded probe sample (--ref-probes) with a new
+    ray-set rotation; the median over the timed steps."""
+    from oracle.oracle import Oracle
+
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    probes = args.cpu_probes
+    o = Oracle(w.scene, threads=os.cpu_count())
     vals = []
-    for _ in range(args.warmup):
-        cpu_baseline(w, probes)
+    for k in range(args.warmup):
+        cpu_baseline(w, args.ref_probes, oracle=o, orientation=k)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(w, probes))
+    for k in range(args.steps):
+        vals.append(cpu_baseline(w, args.ref_probes, oracle=o, orientation=args.warmup + k))
     wall = time.perf_counter() - t0
+    o.close()
     v = statistics.median(x["value"] for x in vals)
     cb = dict(vals[0])
     cb["value"] = v
@@ -379,7 +395,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=1)
-    ap.add_argument("--cpu-probes", type=int, default=1024)
+    ap.add_argument("--cpu-probes", type=int, default=0,
+                    help="probes of the CPU-baseline sample (0: the whole grid, one full update)")
+    ap.add_argument("--ref-probes", type=int, default=4096,
+                    help="probes per step of the reference arm's sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only", default=None, choices=["batching"],
                     help="run one sub-measurement alone and print it")

@@ -76,6 +76,8 @@ struct ddgi_ctx {
     float4* wave_thit = nullptr;
     uint32_t* wave_prim = nullptr;
     uint32_t* wave_front = nullptr;  // compacted front-face hits
+    float* xfer = nullptr;           // FP32 staging of an FP16 atlas being read back
+    size_t xfer_cap = 0;             // in floats
     uint32_t* q_idx = nullptr;
     float4* q_pos = nullptr;
     float4* q_sun = nullptr;

@@ -303,6 +303,7 @@ ddgi_status ddgi_destroy(ddgi_ctx* ctx) {
     dfree(ctx->wave_thit);
     dfree(ctx->wave_prim);
     dfree(ctx->wave_front);
+    dfree(ctx->xfer);
     dfree(ctx->q_idx);
     dfree(ctx->q_pos);
     dfree(ctx->q_sun);
@@ -1419,6 +1420,15 @@ ddgi_status ddgi_atlas_dims(const ddgi_ctx* ctx, ddgi_atlas_kind kind, uint32_t*
     return DDGI_OK;
 }
 
+namespace {
+
+__global__ void k_half_to_float(const __half* __restrict__ in, float* __restrict__ out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = __half2float(in[i]);
+}
+
+}  // namespace
+
 ddgi_status ddgi_get_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, float* dst, size_t bytes, ddgi_stream stream) {
     if (!ctx || !dst || (kind != DDGI_ATLAS_COLOR && kind != DDGI_ATLAS_DEPTH)) return DDGI_ERR_INVALID_ARGUMENT;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -1431,10 +1441,17 @@ ddgi_status ddgi_get_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, float* dst, size
         CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st), "atlas download");
         CK(cudaStreamSynchronize(st), "atlas download");
     } else {
-        std::vector<__half> tmp(count);
-        CK(cudaMemcpyAsync(tmp.data(), src, count * sizeof(__half), cudaMemcpyDeviceToHost, st), "atlas download");
+        // widen on the device, then one copy into the caller's buffer
+        if (ctx->xfer_cap < count) {
+            dfree(ctx->xfer);
+            ctx->xfer_cap = 0;
+            CK(cudaMalloc(&ctx->xfer, count * sizeof(float)), "alloc atlas staging");
+            ctx->xfer_cap = count;
+        }
+        k_half_to_float<<<1216, 256, 0, st>>>(static_cast<const __half*>(src), ctx->xfer, count);
+        CK(cudaGetLastError(), "atlas widen");
+        CK(cudaMemcpyAsync(dst, ctx->xfer, bytes, cudaMemcpyDeviceToHost, st), "atlas download");
         CK(cudaStreamSynchronize(st), "atlas download");
-        for (size_t i = 0; i < count; ++i) dst[i] = __half2float(tmp[i]);
     }
     return check_device_error(ctx);
 }
