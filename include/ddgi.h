@@ -401,6 +401,18 @@ ddgi_status ddgi_set_trace_tuning(ddgi_ctx* ctx, const ddgi_trace_tuning* tuning
 /* Most triangles per leaf of the mesh trees built by the next
  * ddgi_scene_build (1..8, default 2). */
 ddgi_status ddgi_set_leaf_size(ddgi_ctx* ctx, uint32_t max_triangles);
+/* Tree builder of the next ddgi_scene_build (mesh trees and top level) and
+ * of ddgi_update_instances' top-level rebuilds.  Hits do not depend on it.
+ *   DDGI_BUILD_FAST_TRACE (default): surface-area-heuristic trees built on
+ *     the host (the reference's PREFER_FAST_TRACE structures,
+ *     src/Renderer.cpp:334);
+ *   DDGI_BUILD_FAST_BUILD: linear BVHs built on the GPU (PREFER_FAST_BUILD,
+ *     src/Renderer.cpp:364). */
+typedef enum ddgi_build_mode {
+    DDGI_BUILD_FAST_TRACE = 0,
+    DDGI_BUILD_FAST_BUILD = 1
+} ddgi_build_mode;
+ddgi_status ddgi_set_build_mode(ddgi_ctx* ctx, ddgi_build_mode mode);
 ddgi_status ddgi_get_trace_tuning(const ddgi_ctx* ctx, ddgi_trace_tuning* out);
 /* Times candidate tunings on updates of all probes with the given
  * orientation (`reps` timed updates each, coordinate descent), keeps the

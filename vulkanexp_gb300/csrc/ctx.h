@@ -35,6 +35,7 @@ struct SceneBuffers {
     uint32_t vertex_count = 0, index_count = 0, offset_count = 0, material_count = 0, instance_count = 0;
     uint64_t node_count = 0, tri_count = 0;
     uint64_t build_id = 0;  // distinct for every successful build or instance update in the process
+    ddgi_build_mode build_mode = DDGI_BUILD_FAST_BUILD;  // builder of these trees
     bool built = false;
     // top level, kept for instance updates (refit / rebuild)
     std::vector<GpuInstance> host_inst;      // caller order
@@ -121,6 +122,7 @@ struct ddgi_ctx {
     // traversal launch tuning; probes in Morton order of the grid (grouped warps)
     ddgi_trace_tuning tune{0, 8, 0, 0, 2};
     int blas_leaf_max = ddgi::kBlasLeafMax;  // triangles per mesh-tree leaf (scene build option)
+    ddgi_build_mode build_mode = DDGI_BUILD_FAST_TRACE;  // tree builder (scene build option)
     uint32_t* probe_perm = nullptr;
     float4* init_dirs = nullptr;
     uint32_t* init_back = nullptr;

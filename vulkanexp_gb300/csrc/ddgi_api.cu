@@ -28,6 +28,7 @@
 #include "ctx.h"
 #include "kernels.h"
 #include "lbvh.h"
+#include "sah.h"
 #include "wide.h"
 
 using namespace ddgi;
@@ -404,6 +405,11 @@ ddgi_status ddgi_enable_timing(ddgi_ctx* ctx, int enable) {
 // ---------------------------------------------------------------------------
 namespace {
 
+unsigned host_threads() {
+    const unsigned n = std::thread::hardware_concurrency();
+    return n ? std::min(n, 64u) : 1u;
+}
+
 uint64_t next_build_id() {
     static std::atomic<uint64_t> builds{0};
     return ++builds;
@@ -457,17 +463,27 @@ ddgi_status build_top_level(ddgi_ctx* ctx, uint64_t node_base, void* scratch, fl
         CK(cudaMalloc(&S.sub_lo, sizeof(float4) * 2 * inner), "alloc top level");
         CK(cudaMalloc(&S.sub_hi, sizeof(float4) * 2 * inner), "alloc top level");
     }
-    CK(cudaMemcpyAsync(box_lo, S.inst_lo.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
-    CK(cudaMemcpyAsync(box_hi, S.inst_hi.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
-    CK(lbvh_build(box_lo, box_hi, ni, kTlasLeafMax, S.nodes, (int)node_base, 0, sorted, scratch, ctx->err, depth_dev,
-                  st),
-       "top-level build");
     std::vector<uint32_t> order(ni);
     std::vector<BvhNode> top(inner);
-    CK(cudaMemcpyAsync(order.data(), sorted, sizeof(uint32_t) * ni, cudaMemcpyDeviceToHost, st), "read order");
-    CK(cudaMemcpyAsync(top.data(), S.nodes + node_base, sizeof(BvhNode) * inner, cudaMemcpyDeviceToHost, st),
-       "read top level");
-    CK(cudaStreamSynchronize(st), "top-level build");
+    if (S.build_mode == DDGI_BUILD_FAST_TRACE) {
+        uint32_t d = 1;
+        sah_build(S.inst_lo.data(), S.inst_hi.data(), ni, kTlasLeafMax, (int)node_base, 0, top.data(), order.data(), &d,
+                  host_threads());
+        CK(cudaMemcpyAsync(S.nodes + node_base, top.data(), sizeof(BvhNode) * inner, cudaMemcpyHostToDevice, st),
+           "upload top level");
+        CK(cudaMemcpyAsync(depth_dev, &d, sizeof(d), cudaMemcpyHostToDevice, st), "upload depth");
+        CK(cudaStreamSynchronize(st), "top-level build");
+    } else {
+        CK(cudaMemcpyAsync(box_lo, S.inst_lo.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
+        CK(cudaMemcpyAsync(box_hi, S.inst_hi.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
+        CK(lbvh_build(box_lo, box_hi, ni, kTlasLeafMax, S.nodes, (int)node_base, 0, sorted, scratch, ctx->err,
+                      depth_dev, st),
+           "top-level build");
+        CK(cudaMemcpyAsync(order.data(), sorted, sizeof(uint32_t) * ni, cudaMemcpyDeviceToHost, st), "read order");
+        CK(cudaMemcpyAsync(top.data(), S.nodes + node_base, sizeof(BvhNode) * inner, cudaMemcpyDeviceToHost, st),
+           "read top level");
+        CK(cudaStreamSynchronize(st), "top-level build");
+    }
     std::vector<GpuInstance> leaf(ni);
     std::vector<float4> llo(ni), lhi(ni);
     S.leaf_of_id.assign(ni, 0);
@@ -781,7 +797,9 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
                             st),
             "upload");
 
-    // ---- bottom level: one LBVH per mesh ----
+    // ---- bottom level: one tree per mesh ----
+    S.build_mode = ctx->build_mode;
+    uint32_t host_blas_depth = 1;
     std::vector<int32_t> mesh_root(d->mesh_count, -1);
     std::vector<float> mesh_lo((size_t)d->mesh_count * 3, INFINITY), mesh_hi((size_t)d->mesh_count * 3, -INFINITY);
     uint64_t node_base = 0, tri_base = 0;
@@ -799,10 +817,37 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
                 }
             }
         }
-        CKB(build_mesh_blas(dpos, S.indices, me.vertex_offset, me.vertex_count, me.index_offset, nt, ctx->blas_leaf_max,
-                            S.nodes, (int)node_base, S.tris, (int)tri_base, box_lo, box_hi, sorted, scratch, ctx->err,
-                            depth, st),
-            "bottom-level build");
+        if (S.build_mode == DDGI_BUILD_FAST_TRACE) {
+            std::vector<float4> tlo(nt), thi(nt);
+            for (uint32_t t = 0; t < nt; ++t) {
+                const float4* v[3];
+                for (int k = 0; k < 3; ++k) v[k] = &pos[me.vertex_offset + d->indices[me.index_offset + 3 * t + k]];
+                tlo[t] = make_float4(fminf(fminf(v[0]->x, v[1]->x), v[2]->x), fminf(fminf(v[0]->y, v[1]->y), v[2]->y),
+                                     fminf(fminf(v[0]->z, v[1]->z), v[2]->z), 0.0f);
+                thi[t] = make_float4(fmaxf(fmaxf(v[0]->x, v[1]->x), v[2]->x), fmaxf(fmaxf(v[0]->y, v[1]->y), v[2]->y),
+                                     fmaxf(fmaxf(v[0]->z, v[1]->z), v[2]->z), 0.0f);
+            }
+            std::vector<BvhNode> tree(nt > 1 ? nt - 1 : 1);
+            std::vector<uint32_t> order(nt);
+            uint32_t dm = 1;
+            sah_build(tlo.data(), thi.data(), nt, ctx->blas_leaf_max, (int)node_base, (int)tri_base, tree.data(),
+                      order.data(), &dm, host_threads());
+            host_blas_depth = std::max(host_blas_depth, dm);
+            // pageable sources: both copies have read them when they return
+            CKB(cudaMemcpyAsync(S.nodes + node_base, tree.data(), sizeof(BvhNode) * tree.size(), cudaMemcpyHostToDevice,
+                                st),
+                "upload mesh tree");
+            CKB(cudaMemcpyAsync(sorted, order.data(), sizeof(uint32_t) * nt, cudaMemcpyHostToDevice, st),
+                "upload leaf order");
+            CKB(gather_mesh_tris(dpos, S.indices, me.vertex_offset, me.vertex_count, me.index_offset, nt, sorted,
+                                 S.tris + tri_base, st),
+                "gather triangles");
+        } else {
+            CKB(build_mesh_blas(dpos, S.indices, me.vertex_offset, me.vertex_count, me.index_offset, nt,
+                                ctx->blas_leaf_max, S.nodes, (int)node_base, S.tris, (int)tri_base, box_lo, box_hi,
+                                sorted, scratch, ctx->err, depth, st),
+                "bottom-level build");
+        }
         mesh_root[m] = (int32_t)node_base;
         node_base += nt > 1 ? nt - 1 : 1;
         tri_base += nt;
@@ -841,6 +886,7 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
     CKB(cudaStreamSynchronize(st), "scene build");
     cleanup();
 #undef CKB
+    depths[0] = std::max(depths[0], host_blas_depth);
     // traversal stack: one entry per inner node on a root-to-leaf path in each
     // level, plus the resume node and the EXIT marker of an instance entry
     S.stack_cap = (int)(depths[0] + depths[1] + 4);
@@ -1247,6 +1293,14 @@ ddgi_status ddgi_set_leaf_size(ddgi_ctx* ctx, uint32_t max_triangles) {
     if (max_triangles < 1 || max_triangles > 8)
         return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "leaf size %u outside [1, 8]", max_triangles);
     ctx->blas_leaf_max = (int)max_triangles;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_set_build_mode(ddgi_ctx* ctx, ddgi_build_mode mode) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    if (mode != DDGI_BUILD_FAST_TRACE && mode != DDGI_BUILD_FAST_BUILD)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "unknown build mode %d", (int)mode);
+    ctx->build_mode = mode;
     return DDGI_OK;
 }
 

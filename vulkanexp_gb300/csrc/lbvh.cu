@@ -542,4 +542,12 @@ cudaError_t build_mesh_blas(const float4* pos, const uint32_t* indices, uint32_t
     return cudaGetLastError();
 }
 
+cudaError_t gather_mesh_tris(const float4* pos, const uint32_t* indices, uint32_t vbase, uint32_t vcount,
+                             uint32_t ibase, uint32_t ntri, const uint32_t* sorted_ids, BvhTri* tris, cudaStream_t st) {
+    if (ntri == 0) return cudaSuccess;
+    const int T = 256;
+    k_gather_tris<<<div_up(ntri, T), T, 0, st>>>(pos, indices, vbase, ibase, ntri, vcount, sorted_ids, tris);
+    return cudaGetLastError();
+}
+
 }  // namespace ddgi

@@ -27,6 +27,11 @@ cudaError_t build_mesh_blas(const float4* pos, const uint32_t* indices, uint32_t
                             int tri_base, float4* box_lo, float4* box_hi, uint32_t* sorted_ids, void* scratch,
                             uint32_t* err, uint32_t* depth, cudaStream_t st);
 
+// Triangles of one mesh gathered in leaf order (sorted_ids[s] = triangle of
+// leaf position s) at tris[0, ntri), for a tree built elsewhere.
+cudaError_t gather_mesh_tris(const float4* pos, const uint32_t* indices, uint32_t vbase, uint32_t vcount,
+                             uint32_t ibase, uint32_t ntri, const uint32_t* sorted_ids, BvhTri* tris, cudaStream_t st);
+
 // Refit of a top-level tree whose topology is kept: new boxes for its n
 // leaf slots (leaf order); leaf_parent[s] / node_parent[k] = parent node
 // (relative to node_base) << 1 | side, 0xFFFFFFFF for the root; flags

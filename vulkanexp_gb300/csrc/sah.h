@@ -1,0 +1,21 @@
+// sah.h — surface-area-heuristic trees built on the host (see sah.cu).
+#pragma once
+
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace ddgi {
+
+// Binary tree over n primitive boxes (xyz of lo/hi) split by the surface-area
+// heuristic; every subtree of at most leaf_max primitives becomes a leaf.
+// Writes max(n - 1, 1) nodes: the tree depth first from nodes[0] (inner
+// references node_base + index, leaf references prim_base + leaf position,
+// every box enlarged like the GPU builder's), then never-hit filler nodes.
+// order[s] = primitive at leaf position s; *depth = inner nodes on the
+// longest root-to-leaf path.  Uses up to `threads` host threads.  Returns
+// false when n == 0.
+bool sah_build(const float4* lo, const float4* hi, uint32_t n, int leaf_max, int node_base, int prim_base,
+               BvhNode* nodes, uint32_t* order, uint32_t* depth, unsigned threads);
+
+}  // namespace ddgi

@@ -72,6 +72,7 @@ _SIGNATURES = [
     ("ddgi_final_gather", C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ddgi_set_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_set_leaf_size", C.c_int, [C.c_void_p, C.c_uint32]),
+    ("ddgi_set_build_mode", C.c_int, [C.c_void_p, C.c_int]),
     ("ddgi_get_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_autotune", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_init_probes", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -234,6 +235,14 @@ class Context:
     def set_leaf_size(self, max_triangles):
         """Triangles per mesh-tree leaf for the next build_scene."""
         self._check(self.lib.ddgi_set_leaf_size(self.h, int(max_triangles)))
+
+    def set_build_mode(self, mode):
+        """Tree builder for the next build_scene: "fast_trace" (host SAH
+        trees) or "fast_build" (GPU linear BVHs)."""
+        modes = {"fast_trace": 0, "fast_build": 1}
+        if mode not in modes:
+            raise ValueError("build mode %r: want one of %s" % (mode, sorted(modes)))
+        self._check(self.lib.ddgi_set_build_mode(self.h, modes[mode]))
 
     def trace_tuning(self):
         t = TraceTuning()
