@@ -522,11 +522,13 @@ def main():
             "form": "wavefront trace (persistent traversal) + BF16 tcgen05 blend, FP16 atlas",
             "forms": forms,
             "speedup_vs_plain_fp32": forms["plain_fp32"]["ms_per_update"] / head["ms_per_update"],
-            # per update: k_primary, k_shade, k_shadow, k_tc_weights, k_blend_tc
-            "gpu_launches": 5 * args.steps, "clocks": clocks, "roofline": roofline,
+            # per update: k_primary, k_shade_classify, k_shade_front, k_shadow, k_tc_weights, k_blend_tc
+            "gpu_launches": 6 * args.steps, "clocks": clocks, "roofline": roofline,
             "roofline_blend": roofline_blend,
             "e2e": {"value": e2e_val, "unit": UNIT, "ms_per_step": float(np.mean(e2e_ms)),
-                    "h2d_bytes_per_step": R * 20, "d2h_bytes_per_step": int(host_c.nbytes + host_d.nbytes)}}
+                    "h2d_bytes_per_step": R * 20, "d2h_bytes_per_step": int(host_c.nbytes + host_d.nbytes)},
+            # sanity of the last e2e step's result as read back
+            "atlas_finite": bool(np.isfinite(host_c).all() and np.isfinite(host_d).all())}
     if not args.headline_only:
         line["final_gather"] = measure_final_gather(ctx, w, stream, flush)
     ctx.close()

@@ -82,6 +82,32 @@ def test_blend_bf16_error_vs_fp64(gpu_lib, rays, color_res, depth_res):
     ctx.close()
 
 
+def test_blend_bf16_tiny_and_zero_radiance(gpu_lib):
+    """Probes whose largest radiance is zero, denormal or tiny: the per-probe
+    scale of the BF16 operands stays finite, so the atlas has no NaN (an
+    infinite reciprocal once turned 0 x inf into NaN for such a probe)."""
+    g = grid_for(abi.PRECISION_BF16, 256)
+    rng = np.random.default_rng(4)
+    ctx = Context(g)
+    c, d = zero_atlas(g, fp64=True)
+    st = np.ones(g.probe_count(), np.uint32)
+    rec = synthetic_records(rng, g.probe_count(), 256, cell_len(g))
+    rec[0, :, :3] = 0.0
+    rec[0, 7, 1] = 1e-39   # denormal maximum
+    rec[1, :, :3] = 0.0
+    rec[1, 3, 0] = 3e-36   # below the smallest scale
+    rec[2, :, :3] = 0.0    # all zero
+    rec[3, :, :3] *= 1e-20  # tiny but scaled
+    o = scenes.random_orientation(29, 0)
+    ctx.blend_records(o, rec)
+    Oracle.blend(g, o, rec, c, d, st)
+    gc = ctx.get_atlas(abi.ATLAS_COLOR)
+    gd = ctx.get_atlas(abi.ATLAS_DEPTH)
+    assert np.isfinite(gc).all() and np.isfinite(gd).all()
+    assert rel_err(gc[..., :3], c[..., :3], FLOOR).max() <= BF16_MAX
+    ctx.close()
+
+
 def test_update_bf16_room_vs_fp64(gpu_lib):
     """Whole update in the BF16 form: hit IDs stay bit-exact (geometry is
     FP32), the atlas after three updates stays within the BF16 bars."""
@@ -105,3 +131,30 @@ def test_update_bf16_room_vs_fp64(gpu_lib):
           % (ec.max(), np.sqrt((ec ** 2).mean()), ed.max(), np.sqrt((ed ** 2).mean())))
     assert ec.max() <= BF16_MAX and ed.max() <= BF16_MAX
     ctx.close()
+
+
+def test_update_bf16_terrain_full_size_finite(gpu_lib):
+    """The 32x16x32-probe, 256-ray terrain update at full size in the BF16
+    form: four updates keep every atlas texel finite, and the atlas stays
+    close to the FP32 form's (both trace the same hits; the BF16 form's
+    shading samples the FP16 atlas)."""
+    w = scenes.workload(1)
+    atl = {}
+    for prec in (abi.PRECISION_BF16, abi.PRECISION_FP32):
+        g = w.grid.copy()
+        g.precision = prec
+        ctx = Context(g)
+        ctx.set_pipeline(abi.PIPELINE_WAVEFRONT)
+        ctx.build_scene(w.scene)
+        ctx.set_light(w.light)
+        for k in range(4):
+            ctx.update(w.orientation(k))
+        atl[prec] = (ctx.get_atlas(abi.ATLAS_COLOR), ctx.get_atlas(abi.ATLAS_DEPTH))
+        ctx.close()
+    bc, bd = atl[abi.PRECISION_BF16]
+    fc, fd = atl[abi.PRECISION_FP32]
+    assert np.isfinite(bc).all() and np.isfinite(bd).all()
+    ec, ed = rel_err(bc[..., :3], fc[..., :3], FLOOR), rel_err(bd, fd, FLOOR)
+    print("terrain bf16 vs fp32 after 4 updates: colour max %.2e rms %.2e, depth max %.2e rms %.2e"
+          % (ec.max(), np.sqrt((ec ** 2).mean()), ed.max(), np.sqrt((ed ** 2).mean())))
+    assert np.sqrt((ec ** 2).mean()) <= 1e-3 and np.sqrt((ed ** 2).mean()) <= 1e-3

@@ -172,6 +172,18 @@ __global__ void k_tc_weights(const float4* dirs, uint32_t R, uint32_t nc, uint32
 
 // Blend of the 32-probe tile starting at probe slot p0 (< nprobes) by the
 // whole CTA.
+// Scale of a probe's colour records before the BF16 split: the power of two
+// 2^e >= the largest radiance (so scaled records are <= 1 and the scaling
+// is exact), e clamped to [-100, 100]; a probe whose largest radiance is
+// below 2^-100 (zero, denormal) keeps scale 1, so the reciprocal is always
+// finite and a zero record never meets an infinite one (0 x inf = NaN).
+__device__ __forceinline__ float radiance_scale(float mx) {
+    if (!(mx >= 0x1p-100f)) return 1.0f;  // also NaN
+    int e = 100;
+    if (mx < 0x1p100f) frexpf(mx, &e);
+    return ldexpf(1.0f, e);
+}
+
 __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0, const uint32_t nprobes) {
     extern __shared__ __align__(1024) uint8_t smem[];
     // A operands (128 x 64 BF16 = 16 KB each): colour hi/lo, depth hi/lo;
@@ -183,7 +195,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
     uint8_t* sB = smem + 65536;
     __shared__ uint64_t s_bar;
     __shared__ uint32_t s_tmem;
-    __shared__ float s_max[kTileProbes];
+    __shared__ float s_max[kTileProbes];  // per-probe colour scale (radiance_scale)
     __shared__ uint32_t s_oor[kTileProbes], s_maxc[kTileProbes];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -217,7 +229,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
             oor += __shfl_xor_sync(0xffffffffu, oor, o);
         }
         if (lane == 0) {
-            s_max[pl] = mx;
+            s_max[pl] = radiance_scale(mx);
             s_oor[pl] = oor;
         }
     }
@@ -230,7 +242,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
     for (uint32_t c = 0; c < a.nchunks; ++c) {
         {   // A: thread = (probe, group of 8 rays); one 16-byte core-matrix row per operand row
             const uint32_t pl = (uint32_t)tid >> 3, j = (uint32_t)tid & 7u;
-            const float inv = s_max[pl] > 0.0f ? 1.0f / s_max[pl] : 1.0f;
+            const float inv = 1.0f / s_max[pl];  // a power of two: exact
             const float cinv = 1.0f / cell;
             // [row][hi/lo][4 words of 2 BF16]: rows r, g, b (colour), d, d^2 (depth)
             uint32_t w[5][2][4];
@@ -323,8 +335,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
         const uint32_t row = quarter * 32u + (uint32_t)lane;
         const uint32_t pl = row >> 2, ch = row & 3u;
         const uint32_t lane_base = tmem + ((quarter * 32u) << 16);
-        const float pmax = s_max[pl];
-        const float scale_c = pmax > 0.0f ? pmax : 1.0f;
+        const float scale_c = s_max[pl];
         if (warp < 4) {
             const uint32_t ntex = a.nc * a.nc;
             for (uint32_t col0 = 0; col0 < a.Nc; col0 += 16) {
