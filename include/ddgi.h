@@ -38,7 +38,8 @@ typedef enum ddgi_status {
     DDGI_ERR_NO_SCENE = 4,         /* update/init before ddgi_scene_build */
     DDGI_ERR_TIMEOUT = 5,          /* ddgi_synchronize gave up waiting */
     DDGI_ERR_DEVICE = 6,           /* a kernel raised its error word (stack overflow, bad index) */
-    DDGI_ERR_UNSUPPORTED = 7       /* valid request this build does not implement */
+    DDGI_ERR_UNSUPPORTED = 7,      /* valid request this build does not implement */
+    DDGI_ERR_IO = 8                /* a checkpoint file cannot be written / read, or does not fit the context */
 } ddgi_status;
 
 /* Blend precision of ddgi_update. */
@@ -256,6 +257,17 @@ ddgi_status ddgi_get_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, float* dst, size
 /* Replaces an atlas from host FP32 data of the same shape (checkpoint load). */
 ddgi_status ddgi_set_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, const float* src, size_t bytes,
                            ddgi_stream stream);
+/* Atlas checkpoints (no counterpart in the reference, whose atlases live
+ * only in GPU images): the context's atlases, for an FP16 (BF16-blend)
+ * context also its FP32 hysteresis accumulators, and the probe states,
+ * written to / read from a file with a header holding the grid.  Loading
+ * needs the same probe resolution, tile sides and precision.  Both wait for
+ * `stream`.  File format, little-endian: "DDGIATL1", u32 version (1), u32
+ * fp16, the 64-byte ddgi_grid_desc, u32 colour w, h, depth w, h, probe
+ * count, 3 reserved words; then colour atlas, depth atlas (FP32 or FP16
+ * texels, row-major), [FP32 colour and depth accumulators], u32 states. */
+ddgi_status ddgi_atlas_save(ddgi_ctx* ctx, const char* path, ddgi_stream stream);
+ddgi_status ddgi_atlas_load(ddgi_ctx* ctx, const char* path, ddgi_stream stream);
 ddgi_status ddgi_atlas_dims(const ddgi_ctx* ctx, ddgi_atlas_kind kind, uint32_t* width,
                             uint32_t* height, uint32_t* channels);
 
@@ -413,6 +425,17 @@ typedef enum ddgi_build_mode {
     DDGI_BUILD_FAST_BUILD = 1
 } ddgi_build_mode;
 ddgi_status ddgi_set_build_mode(ddgi_ctx* ctx, ddgi_build_mode mode);
+
+/* ---- Failure-detection test hooks ---------------------------------------
+ * No counterpart in the reference (its fence waits use UINT64_MAX).  Every
+ * device-side wait of this library is bounded: the tensor-core blend gives
+ * up on a completion that does not come within 0.5 s, releases its tensor
+ * memory, and the next ddgi_synchronize / ddgi_get_* call returns
+ * DDGI_ERR_DEVICE ("device wait timed out"); the context stays usable.
+ * DDGI_FAULT_STALL_TENSOR_WAIT makes the next BF16 blend issue no
+ * tensor-core work, so its completion wait runs out (one-shot). */
+enum { DDGI_FAULT_STALL_TENSOR_WAIT = 1u };
+ddgi_status ddgi_inject_fault(ddgi_ctx* ctx, uint32_t faults);
 ddgi_status ddgi_get_trace_tuning(const ddgi_ctx* ctx, ddgi_trace_tuning* out);
 /* Times candidate tunings on updates of all probes with the given
  * orientation (`reps` timed updates each, coordinate descent), keeps the

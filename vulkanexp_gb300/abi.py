@@ -50,7 +50,11 @@ STATUS_NAMES = {
     5: "DDGI_ERR_TIMEOUT",
     6: "DDGI_ERR_DEVICE",
     7: "DDGI_ERR_UNSUPPORTED",
+    8: "DDGI_ERR_IO",
 }
+ERR_DEVICE = 6
+ERR_IO = 8
+FAULT_STALL_TENSOR_WAIT = 1
 
 
 class GridDesc(C.Structure):

@@ -70,7 +70,12 @@ struct TcArgs {
     float2* acc_depth;
     uint32_t* err;
     const uint32_t* dev_count;  // listed probes, read on the device (NULL: nprobes)
+    uint32_t stall;             // test hook: issue no MMA and no commit, so the completion wait runs out
 };
+
+// Limit of one tensor-core completion wait (the MMAs of a chunk take
+// microseconds).
+constexpr uint64_t kWaitLimitNs = 500ull * 1000 * 1000;
 
 // Byte offset of (row, 8-element K group) in a K-chunk operand.
 __host__ __device__ __forceinline__ uint32_t canon_off(uint32_t row, uint32_t kgroup) {
@@ -290,7 +295,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
         }
         tc::fence_proxy_async();
         __syncthreads();
-        if (tid == 0) {
+        if (tid == 0 && !a.stall) {
             tc::fence_after_sync();
             const uint32_t part = (a.Nd + a.Nc) * 128;
             const uint32_t aC = tc::smem_u32(sA_c), aCl = tc::smem_u32(sA_cl);
@@ -313,7 +318,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
             tc::commit(&s_bar);
         }
         __syncwarp();
-        bool done = tc::mbar_wait(&s_bar, phase, 1u << 20);
+        bool done = tc::mbar_wait(&s_bar, phase, kWaitLimitNs);
         phase ^= 1u;
         tc::fence_after_sync();
         if (!__syncthreads_and(done)) {
@@ -326,7 +331,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
         // the MMAs did not complete in time: record it, give them one more
         // bounded wait, then release the tensor memory
         if (tid == 0) raise_error(a.err, DEV_WAIT_TIMEOUT);
-        tc::mbar_wait(&s_bar, phase ^ 1u, 1u << 20);
+        tc::mbar_wait(&s_bar, phase ^ 1u, kWaitLimitNs);
     } else {
         // epilogue 1: accumulators -> shared staging (the operand buffers are free now)
         float* S_c = reinterpret_cast<float*>(smem);                        // [32][nc*nc][3]
@@ -527,6 +532,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_blend_tc(BatchTables bt, Bat
         a.acc_depth = vol.acc_depth;
         a.err = bt.err;
         a.dev_count = nullptr;
+        a.stall = 0;
         s_v = v;
         s_tile = b - __ldg(bl.tile_base + lo);
         s_items = __ldg(bl.tile_base + lo + 1) - __ldg(bl.tile_base + lo);
@@ -567,7 +573,7 @@ bool tc_blend_supported(uint32_t color_res, uint32_t depth_res) {
 cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
                             const float4* dirs, uint8_t* wbuf, float* rowsum, uint32_t* states, void* color,
                             void* depth, float4* acc_color, float2* acc_depth, uint32_t* err, cudaStream_t st,
-                            const uint32_t* dev_count) {
+                            const uint32_t* dev_count, bool stall) {
     if (nprobes == 0) return cudaSuccess;
     const uint32_t nc = g.color_res - 2, nd = g.depth_res - 2;
     const uint32_t Nc = (nc * nc + 15) / 16 * 16, Nd = (nd * nd + 15) / 16 * 16;
@@ -592,6 +598,7 @@ cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uin
     a.acc_depth = acc_depth;
     a.err = err;
     a.dev_count = dev_count;
+    a.stall = stall ? 1u : 0u;
     // operand stage (A 64 KB + B up to 128 KB), reused by the epilogue staging
     size_t stage = 65536 + 2 * (size_t)(Nd + Nc) * 128;
     size_t staging = (size_t)kTileProbes * (nc * nc * 3 + nd * nd * 2) * sizeof(float);

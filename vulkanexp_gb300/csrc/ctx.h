@@ -123,6 +123,7 @@ struct ddgi_ctx {
     ddgi_trace_tuning tune{0, 8, 0, 0, 2};
     int blas_leaf_max = ddgi::kBlasLeafMax;  // triangles per mesh-tree leaf (scene build option)
     ddgi_build_mode build_mode = DDGI_BUILD_FAST_TRACE;  // tree builder (scene build option)
+    uint32_t inject = 0;  // one-shot test hooks (DDGI_FAULT_*), cleared by the launch that uses them
     uint32_t* probe_perm = nullptr;
     float4* init_dirs = nullptr;
     uint32_t* init_back = nullptr;

@@ -213,6 +213,7 @@ const char* ddgi_status_string(ddgi_status s) {
         case DDGI_ERR_TIMEOUT: return "DDGI_ERR_TIMEOUT";
         case DDGI_ERR_DEVICE: return "DDGI_ERR_DEVICE";
         case DDGI_ERR_UNSUPPORTED: return "DDGI_ERR_UNSUPPORTED";
+        case DDGI_ERR_IO: return "DDGI_ERR_IO";
     }
     return "DDGI_ERR_UNKNOWN";
 }
@@ -676,9 +677,14 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
         if ((uint64_t)me.index_offset + me.index_count > d->index_count ||
             (uint64_t)me.vertex_offset + me.vertex_count > d->vertex_count)
             return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "mesh %u: range outside the vertex/index arrays", m);
-        for (uint32_t i = 0; i < me.index_count; ++i)
-            if (d->indices[me.index_offset + i] >= me.vertex_count)
+        for (uint32_t i = 0; i < me.index_count; ++i) {
+            const uint32_t v = d->indices[me.index_offset + i];
+            if (v >= me.vertex_count)
                 return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "mesh %u: index %u out of range", m, i);
+            const float* p = d->vertices[me.vertex_offset + v].pos;
+            if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(p[2]))
+                return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "mesh %u: vertex %u of a triangle is not finite", m, v);
+        }
         if ((uint64_t)me.index_count / 3 >= (1ull << 28))
             return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "mesh %u: too many triangles", m);
     }
@@ -1072,10 +1078,18 @@ TraceTuning trace_tuning(const ddgi_ctx* ctx) {
 
 // Blend + border copy of the ray records in ctx->rays: the FP32 SIMT kernel or
 // the BF16 tensor-core kernel, by the context's precision.
+// One-shot test hook: true once after ddgi_inject_fault(DDGI_FAULT_STALL_TENSOR_WAIT).
+bool take_stall(ddgi_ctx* ctx) {
+    const bool s = (ctx->inject & DDGI_FAULT_STALL_TENSOR_WAIT) != 0;
+    ctx->inject &= ~(uint32_t)DDGI_FAULT_STALL_TENSOR_WAIT;
+    return s;
+}
+
 cudaError_t launch_blend(ddgi_ctx* ctx, const uint32_t* dlist, uint32_t n, cudaStream_t st) {
     if (ctx->fp16)
         return launch_blend_tc(ctx->dg, dlist, n, ctx->rays, ctx->dirs, ctx->tc_weights, ctx->tc_rowsum, ctx->states,
-                               ctx->color, ctx->depth, ctx->acc_color, ctx->acc_depth, ctx->err, st);
+                               ctx->color, ctx->depth, ctx->acc_color, ctx->acc_depth, ctx->err, st, nullptr,
+                               take_stall(ctx));
     return launch_blend_fp32(ctx->dg, dlist, n, ctx->rays, ctx->dirs, ctx->states, static_cast<float4*>(ctx->color),
                              static_cast<float2*>(ctx->depth), st);
 }
@@ -1191,7 +1205,8 @@ ddgi_status ddgi_update_scheduled(ddgi_ctx* ctx, const float orientation[9], uin
     if (ctx->timing) CK(cudaEventRecord(ctx->ev[1], st), "event");
     if (ctx->fp16)
         CK(launch_blend_tc(ctx->dg, ctx->probe_list, P, ctx->rays, ctx->dirs, ctx->tc_weights, ctx->tc_rowsum,
-                           ctx->states, ctx->color, ctx->depth, ctx->acc_color, ctx->acc_depth, ctx->err, st, dcount),
+                           ctx->states, ctx->color, ctx->depth, ctx->acc_color, ctx->acc_depth, ctx->err, st, dcount,
+                           take_stall(ctx)),
            "blend launch");
     else
         CK(launch_blend_fp32(ctx->dg, ctx->probe_list, P, ctx->rays, ctx->dirs, ctx->states,
@@ -1293,6 +1308,14 @@ ddgi_status ddgi_set_leaf_size(ddgi_ctx* ctx, uint32_t max_triangles) {
     if (max_triangles < 1 || max_triangles > 8)
         return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "leaf size %u outside [1, 8]", max_triangles);
     ctx->blas_leaf_max = (int)max_triangles;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_inject_fault(ddgi_ctx* ctx, uint32_t faults) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    if (faults & ~(uint32_t)DDGI_FAULT_STALL_TENSOR_WAIT)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "unknown fault bits 0x%x", faults);
+    ctx->inject |= faults;
     return DDGI_OK;
 }
 
@@ -1530,6 +1553,103 @@ ddgi_status ddgi_set_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, const float* src
         CK(cudaMemcpyAsync(acc, src, bytes, cudaMemcpyHostToDevice, st), "atlas upload");
         CK(cudaStreamSynchronize(st), "atlas upload");
     }
+    return DDGI_OK;
+}
+
+namespace {
+
+struct AtlasFileHeader {
+    char magic[8];
+    uint32_t version, fp16;
+    ddgi_grid_desc grid;
+    uint32_t color_w, color_h, depth_w, depth_h, probes;
+    uint32_t reserved[3];
+};
+static_assert(sizeof(AtlasFileHeader) == 112, "checkpoint header is 112 bytes");
+constexpr char kAtlasMagic[8] = {'D', 'D', 'G', 'I', 'A', 'T', 'L', '1'};
+
+struct FileCloser {
+    FILE* f;
+    ~FileCloser() {
+        if (f) fclose(f);
+    }
+};
+
+// The device buffers of a checkpoint in file order, with their sizes.
+std::vector<std::pair<void*, size_t>> checkpoint_parts(ddgi_ctx* ctx) {
+    std::vector<std::pair<void*, size_t>> parts = {
+        {ctx->color, atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, ctx->fp16)},
+        {ctx->depth, atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, ctx->fp16)}};
+    if (ctx->fp16) {
+        parts.push_back({ctx->acc_color, atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, false)});
+        parts.push_back({ctx->acc_depth, atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, false)});
+    }
+    parts.push_back({ctx->states, sizeof(uint32_t) * (size_t)probe_count_of(ctx->grid)});
+    return parts;
+}
+
+AtlasFileHeader checkpoint_header(const ddgi_ctx* ctx) {
+    AtlasFileHeader h{};
+    std::memcpy(h.magic, kAtlasMagic, 8);
+    h.version = 1;
+    h.fp16 = ctx->fp16 ? 1u : 0u;
+    h.grid = ctx->grid;
+    uint32_t ch;
+    ddgi_atlas_dims(ctx, DDGI_ATLAS_COLOR, &h.color_w, &h.color_h, &ch);
+    ddgi_atlas_dims(ctx, DDGI_ATLAS_DEPTH, &h.depth_w, &h.depth_h, &ch);
+    h.probes = probe_count_of(ctx->grid);
+    return h;
+}
+
+}  // namespace
+
+ddgi_status ddgi_atlas_save(ddgi_ctx* ctx, const char* path, ddgi_stream stream) {
+    if (!ctx || !path) return DDGI_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaStreamSynchronize(st), "checkpoint");
+    ddgi_status s = check_device_error(ctx);
+    if (s != DDGI_OK) return s;
+    const AtlasFileHeader h = checkpoint_header(ctx);
+    FileCloser fc{fopen(path, "wb")};
+    if (!fc.f) return fail(ctx, DDGI_ERR_IO, "cannot open %s for writing", path);
+    if (fwrite(&h, sizeof(h), 1, fc.f) != 1) return fail(ctx, DDGI_ERR_IO, "write failed: %s", path);
+    std::vector<uint8_t> buf;
+    for (const auto& part : checkpoint_parts(ctx)) {
+        buf.resize(part.second);
+        CK(cudaMemcpy(buf.data(), part.first, part.second, cudaMemcpyDeviceToHost), "checkpoint read");
+        if (fwrite(buf.data(), 1, part.second, fc.f) != part.second)
+            return fail(ctx, DDGI_ERR_IO, "write failed: %s", path);
+    }
+    if (fflush(fc.f) != 0) return fail(ctx, DDGI_ERR_IO, "write failed: %s", path);
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_atlas_load(ddgi_ctx* ctx, const char* path, ddgi_stream stream) {
+    if (!ctx || !path) return DDGI_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    FileCloser fc{fopen(path, "rb")};
+    if (!fc.f) return fail(ctx, DDGI_ERR_IO, "cannot open %s", path);
+    AtlasFileHeader h{};
+    if (fread(&h, sizeof(h), 1, fc.f) != 1 || std::memcmp(h.magic, kAtlasMagic, 8) != 0 || h.version != 1)
+        return fail(ctx, DDGI_ERR_IO, "%s is not an atlas checkpoint", path);
+    const AtlasFileHeader mine = checkpoint_header(ctx);
+    if (h.fp16 != mine.fp16 || h.color_w != mine.color_w || h.color_h != mine.color_h ||
+        h.depth_w != mine.depth_w || h.depth_h != mine.depth_h || h.probes != mine.probes ||
+        h.grid.color_res != mine.grid.color_res || h.grid.depth_res != mine.grid.depth_res ||
+        std::memcmp(h.grid.resolution, mine.grid.resolution, sizeof(h.grid.resolution)) != 0)
+        return fail(ctx, DDGI_ERR_IO, "%s: grid or precision differs from the context's", path);
+    // read everything before changing anything
+    const auto parts = checkpoint_parts(ctx);
+    std::vector<std::vector<uint8_t>> data(parts.size());
+    for (size_t i = 0; i < parts.size(); ++i) {
+        data[i].resize(parts[i].second);
+        if (fread(data[i].data(), 1, parts[i].second, fc.f) != parts[i].second)
+            return fail(ctx, DDGI_ERR_IO, "%s is truncated", path);
+    }
+    if (fgetc(fc.f) != EOF) return fail(ctx, DDGI_ERR_IO, "%s has trailing data", path);
+    CK(cudaStreamSynchronize(st), "checkpoint");
+    for (size_t i = 0; i < parts.size(); ++i)
+        CK(cudaMemcpy(parts[i].first, data[i].data(), parts[i].second, cudaMemcpyHostToDevice), "checkpoint write");
     return DDGI_OK;
 }
 

@@ -163,7 +163,7 @@ bool tc_blend_supported(uint32_t color_res, uint32_t depth_res);
 cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
                             const float4* dirs, uint8_t* wbuf, float* rowsum, uint32_t* states, void* color,
                             void* depth, float4* acc_color, float2* acc_depth, uint32_t* err, cudaStream_t st,
-                            const uint32_t* dev_count = nullptr);
+                            const uint32_t* dev_count = nullptr, bool stall = false);
 
 // blend.cu
 cudaError_t launch_blend_fp32(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,

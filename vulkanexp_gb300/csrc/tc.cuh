@@ -86,9 +86,20 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 }
 
 // Bounded wait on an mbarrier phase; false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_iters) {
-    uint32_t addr = smem_u32(bar);
-    for (uint32_t i = 0; i < max_iters; ++i) {
+// Nanoseconds of the GPU's global timer.
+__device__ __forceinline__ uint64_t timer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for phase `parity` of a shared-memory mbarrier to complete; gives
+// up (returns false) after `limit_ns` of global time, or after 2^26 polls
+// should the timer not advance, so a wait that nothing will end still ends.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+    const uint32_t addr = smem_u32(bar);
+    uint64_t t0 = 0;
+    for (uint32_t i = 0; i < (1u << 26); ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -99,6 +110,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
             : "r"(addr), "r"(parity)
             : "memory");
         if (done) return true;
+        if ((i & 255u) == 255u) {
+            const uint64_t now = timer_ns();
+            if (t0 == 0) t0 = now;
+            else if (now - t0 > limit_ns) return false;
+        }
     }
     return false;
 }

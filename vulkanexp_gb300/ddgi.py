@@ -73,6 +73,9 @@ _SIGNATURES = [
     ("ddgi_set_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_set_leaf_size", C.c_int, [C.c_void_p, C.c_uint32]),
     ("ddgi_set_build_mode", C.c_int, [C.c_void_p, C.c_int]),
+    ("ddgi_inject_fault", C.c_int, [C.c_void_p, C.c_uint32]),
+    ("ddgi_atlas_save", C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
+    ("ddgi_atlas_load", C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
     ("ddgi_get_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_autotune", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_init_probes", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -345,6 +348,18 @@ class Context:
         assert out.shape == shape and out.dtype == np.float32 and out.flags.c_contiguous
         self._check(self.lib.ddgi_get_atlas(self.h, kind, _ptr(out), out.nbytes, _stream_ptr(stream)))
         return out
+
+    def save_atlas(self, path, stream=None):
+        """Checkpoint of the atlases (and accumulators, probe states) to a file."""
+        self._check(self.lib.ddgi_atlas_save(self.h, os.fsencode(path), _stream_ptr(stream)))
+
+    def load_atlas(self, path, stream=None):
+        """Restores a checkpoint written by save_atlas for the same grid."""
+        self._check(self.lib.ddgi_atlas_load(self.h, os.fsencode(path), _stream_ptr(stream)))
+
+    def inject_fault(self, faults):
+        """One-shot failure-detection test hooks (abi.FAULT_*)."""
+        self._check(self.lib.ddgi_inject_fault(self.h, int(faults)))
 
     def set_atlas(self, kind, data, stream=None):
         data = np.ascontiguousarray(data, np.float32)
