@@ -69,7 +69,8 @@ class Oracle:
     @classmethod
     def lib(cls):
         if cls._lib is None:
-            lib = C.CDLL(build_oracle())
+            # DDGI_ORACLE_LIB: a differently built checker (the sanitizer test)
+            lib = C.CDLL(os.environ.get("DDGI_ORACLE_LIB") or build_oracle())
             lib.oracle_scene_create.restype = C.c_void_p
             lib.oracle_scene_create.argtypes = [C.POINTER(SceneDesc), C.c_int]
             lib.oracle_scene_destroy.argtypes = [C.c_void_p]

@@ -1,0 +1,100 @@
+"""Host code under AddressSanitizer and UndefinedBehaviorSanitizer, no GPU:
+
+* the SAH tree builder (vulkanexp_gb300/csrc/sah.cu) through a structural
+  check (tests/native/sah_check.cu) over random, coincident, flat and
+  NaN/infinite primitive boxes, every leaf size;
+* the CPU checker (oracle/ddgi_oracle.cpp) on a small room: trace, update
+  (FP32 and FP64), probe classification and final gather, loaded into a
+  Python process with the ASan runtime preloaded.
+
+Any sanitizer report aborts the child process, which fails the test."""
+import os
+import subprocess
+import sys
+import textwrap
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SAN = ["-fsanitize=address", "-fsanitize=undefined", "-fno-sanitize-recover=all", "-fno-omit-frame-pointer", "-g",
+       "-O1"]
+ENV = {"ASAN_OPTIONS": "detect_leaks=0:abort_on_error=1", "UBSAN_OPTIONS": "halt_on_error=1:print_stacktrace=1"}
+
+
+def _have(tool):
+    return subprocess.run(["which", tool], capture_output=True).returncode == 0
+
+
+def _runtime(name):
+    p = subprocess.run(["gcc", "-print-file-name=%s" % name], capture_output=True, text=True).stdout.strip()
+    return p if os.path.isabs(p) and os.path.exists(p) else None
+
+
+def test_sah_builder_under_sanitizers(tmp_path):
+    from vulkanexp_gb300 import build
+
+    nvcc = build.nvcc()
+    if not (os.path.exists(nvcc) or _have(nvcc)) or _runtime("libasan.so") is None:
+        pytest.skip("nvcc or the ASan runtime is missing")
+    flags = ["-std=c++17"] + build.ARCH + ["--expt-relaxed-constexpr"]
+    for f in SAN[:4] + ["-ffp-contract=off"]:
+        flags += ["-Xcompiler", f]
+    flags += ["-g", "-O1"]
+    objs = []
+    for src in ("tests/native/sah_check.cu", "vulkanexp_gb300/csrc/sah.cu"):
+        o = str(tmp_path / (os.path.basename(src) + ".o"))
+        subprocess.check_call([nvcc] + flags + ["-c", os.path.join(ROOT, src), "-o", o])
+        objs.append(o)
+    exe = str(tmp_path / "sah_check")
+    cudart = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "lib64")
+    subprocess.check_call(["g++", "-fsanitize=address", "-fsanitize=undefined"] + objs +
+                          ["-L" + cudart, "-lcudart_static", "-ldl", "-lrt", "-pthread", "-o", exe])
+    r = subprocess.run([exe], capture_output=True, text=True, env=dict(os.environ, **ENV), timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "all ok" in r.stdout
+
+
+SCRIPT = textwrap.dedent("""
+    import numpy as np
+    from oracle.oracle import Oracle, zero_atlas
+    from vulkanexp_gb300 import abi, scenes
+    w = scenes.room_workload(61, n_boxes=30, resolution=(3, 3, 3), rays=32)
+    o = Oracle(w.scene)
+    rng = np.random.default_rng(2)
+    orig = rng.uniform(-1, 11, size=(500, 3)).astype(np.float32)
+    d = rng.normal(size=(500, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    for any_hit in (False, True):
+        o.trace(orig, d, 0.01, 100.0, 0xFF, any_hit)
+    st = np.ones(w.grid.probe_count(), np.uint32)
+    for fp64 in (False, True):
+        c, dd = zero_atlas(w.grid, fp64=fp64)
+        o.update(w.grid, w.light, w.orientation(0), c, dd, st, fp64=fp64)
+        o.update(w.grid, w.light, w.orientation(1), c, dd, st, fp64=fp64)
+    o.init_probes(w.grid, w.orientation(0))
+    c, dd = zero_atlas(w.grid)
+    o.update(w.grid, w.light, w.orientation(0), c, dd, st)
+    n = 64
+    gb = {"position_depth": np.column_stack([rng.uniform(0, 10, (n, 3)), np.ones(n)]),
+          "normal_metalness": np.column_stack([rng.normal(size=(n, 3)), rng.uniform(0, 1, n)]),
+          "albedo_roughness": np.column_stack([rng.uniform(0, 1, (n, 3)), rng.uniform(0.1, 1, n)]),
+          "emissive": np.zeros((n, 4)), "direct_light": np.ones(n), "reflection": None}
+    gb = {k: None if v is None else v.astype(np.float32) for k, v in gb.items()}
+    Oracle.final_gather(w.grid, w.light, st, c, dd, gb, (5, 3, 12))
+    print("oracle ok")
+""")
+
+
+def test_oracle_under_sanitizers(tmp_path):
+    asan = _runtime("libasan.so")
+    if asan is None:
+        pytest.skip("the ASan runtime is missing")
+    lib = str(tmp_path / "libddgi_oracle_san.so")
+    subprocess.check_call(["g++", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread"] +
+                          SAN + ["-o", lib, os.path.join(ROOT, "oracle", "ddgi_oracle.cpp")])
+    env = dict(os.environ, **ENV)
+    env.update({"LD_PRELOAD": asan, "DDGI_ORACLE_LIB": lib, "PYTHONPATH": ROOT})
+    r = subprocess.run([sys.executable, "-c", SCRIPT], capture_output=True, text=True, env=env, cwd=ROOT,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "oracle ok" in r.stdout

@@ -239,7 +239,10 @@ class SahBuilder {
             for (uint32_t i = 1; i < cnt; ++i) {
                 acc.grow(refs_[b + i - 1].box);
                 const float cost = acc.half_area() * (float)i + suffix[i] * (float)(cnt - i);
-                if (cost < best) {
+                // equal costs (coincident boxes): the more balanced split keeps the tree shallow
+                const uint32_t off = i > cnt / 2 ? i - cnt / 2 : cnt / 2 - i;
+                const uint32_t best_off = best_pos > cnt / 2 ? best_pos - cnt / 2 : cnt / 2 - best_pos;
+                if (cost < best || (cost == best && off < best_off)) {
                     best = cost;
                     best_axis = k;
                     best_pos = i;
