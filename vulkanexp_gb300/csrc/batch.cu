@@ -36,6 +36,7 @@
 #include "common.cuh"
 #include "ctx.h"
 #include "kernels.h"
+#include "nvtx.h"
 #include "traverse.cuh"
 #include "wide.h"
 
@@ -630,6 +631,7 @@ ddgi_status ddgi_batch_use_graph(ddgi_batch* b, int enable) {
 }
 
 ddgi_status ddgi_batch_update(ddgi_batch* b, const float* orientations, ddgi_stream stream) {
+    ddgi::NvtxRange nvtx_range("ddgi_batch_update");
     if (!b || !orientations) return DDGI_ERR_INVALID_ARGUMENT;
     return run_update(b, orientations, reinterpret_cast<cudaStream_t>(stream), false);
 }

@@ -28,6 +28,7 @@
 #include "ctx.h"
 #include "kernels.h"
 #include "lbvh.h"
+#include "nvtx.h"
 #include "sah.h"
 #include "wide.h"
 
@@ -664,6 +665,7 @@ ddgi_status build_wide(ddgi_ctx* ctx, const std::vector<int32_t>& mesh_root, cud
 }  // namespace
 
 ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_stream stream) {
+    ddgi::NvtxRange nvtx_range("ddgi_scene_build");
     if (!ctx || !d) return DDGI_ERR_INVALID_ARGUMENT;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     // ---- validation (the reference would fault on any of these) ----
@@ -928,6 +930,7 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
 // ---------------------------------------------------------------------------
 ddgi_status ddgi_update_instances(ddgi_ctx* ctx, const uint32_t* ids, const float* transforms, uint32_t count,
                                   int rebuild, ddgi_stream stream) {
+    ddgi::NvtxRange nvtx_range("ddgi_update_instances");
     if (!ctx || (count && !transforms)) return DDGI_ERR_INVALID_ARGUMENT;
     SceneBuffers& S = ctx->scene;
     if (!S.built) return fail(ctx, DDGI_ERR_NO_SCENE, "ddgi_update_instances before ddgi_scene_build");
@@ -1121,6 +1124,7 @@ ddgi_status ddgi_blend_records(ddgi_ctx* ctx, const float orientation[9], const 
 
 ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list, uint32_t probe_count,
                         ddgi_stream stream) {
+    ddgi::NvtxRange nvtx_range("ddgi_update");
     if (!ctx || !orientation) return DDGI_ERR_INVALID_ARGUMENT;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const uint32_t* dlist = nullptr;
@@ -1160,6 +1164,7 @@ ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_
 // src/IrradianceProbes.cpp:357-394, and selectProbesToUpdate, :396-424)
 // ---------------------------------------------------------------------------
 ddgi_status ddgi_init_probes(ddgi_ctx* ctx, const float orientation[9], ddgi_stream stream) {
+    ddgi::NvtxRange nvtx_range("ddgi_init_probes");
     if (!ctx || !orientation) return DDGI_ERR_INVALID_ARGUMENT;
     if (!ctx->scene.built) return fail(ctx, DDGI_ERR_NO_SCENE, "ddgi_init_probes before ddgi_scene_build");
     for (int k = 0; k < 9; ++k)
@@ -1185,6 +1190,7 @@ ddgi_status ddgi_init_probes(ddgi_ctx* ctx, const float orientation[9], ddgi_str
 }
 
 ddgi_status ddgi_update_scheduled(ddgi_ctx* ctx, const float orientation[9], uint32_t max_probes, ddgi_stream stream) {
+    ddgi::NvtxRange nvtx_range("ddgi_update_scheduled");
     if (!ctx || !orientation) return DDGI_ERR_INVALID_ARGUMENT;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const uint32_t* unused = nullptr;
@@ -1255,6 +1261,7 @@ ddgi_status ddgi_set_schedule(ddgi_ctx* ctx, uint32_t offset, uint32_t loop, ddg
 // ---------------------------------------------------------------------------
 ddgi_status ddgi_final_gather(ddgi_ctx* ctx, const ddgi_gbuffer* gb, const float camera_origin[3], float* color_out,
                               ddgi_stream stream) {
+    ddgi::NvtxRange nvtx_range("ddgi_final_gather");
     if (!ctx || !gb || !camera_origin || !color_out) return DDGI_ERR_INVALID_ARGUMENT;
     const uint64_t px = (uint64_t)gb->width * gb->height;
     if (px == 0) return DDGI_OK;
@@ -1808,6 +1815,7 @@ ddgi_status upload_dirs(ddgi_ctx* ctx, const float* orientation, cudaStream_t st
 
 ddgi_status ddgi_forward_record(ddgi_ctx* ctx, uint32_t K, const float* orientations, uint32_t checkpoint_every,
                                 ddgi_stream stream) {
+    ddgi::NvtxRange nvtx_range("ddgi_forward_record");
     if (!ctx || !orientations || K == 0 || checkpoint_every == 0) return DDGI_ERR_INVALID_ARGUMENT;
     if (ctx->fp16) return fail(ctx, DDGI_ERR_UNSUPPORTED, "gradients need the FP32 form");
     if (!ctx->scene.built) return fail(ctx, DDGI_ERR_NO_SCENE, "no scene");
@@ -1849,6 +1857,7 @@ ddgi_status ddgi_forward_record(ddgi_ctx* ctx, uint32_t K, const float* orientat
 
 ddgi_status ddgi_backward(ddgi_ctx* ctx, const float* dL_dcolor, size_t bytes, float* grad_albedo, float grad_sun[3],
                           float grad_sky[3], ddgi_stream stream) {
+    ddgi::NvtxRange nvtx_range("ddgi_backward");
     if (!ctx || !dL_dcolor || !grad_albedo || !grad_sun || !grad_sky) return DDGI_ERR_INVALID_ARGUMENT;
     if (ctx->rec_K == 0) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "ddgi_backward without ddgi_forward_record");
     const size_t cb = atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, false), db = atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, false);
