@@ -408,6 +408,9 @@ typedef struct ddgi_trace_tuning {
                                memory; 0 = the whole stack in shared memory (default) */
     uint32_t ctas_per_sm;   /* persistent CTAs per SM; 0 = as many as fit (default) */
     uint32_t node_width;    /* 2: binary nodes (default), 4: four-wide nodes collapsed from the binary trees */
+    uint32_t straggler_lanes; /* a warp leaves its node-search loop to test the leaves its lanes hold once at
+                                 most this many lanes still search for one (0..31, default 8; 0: wait for
+                                 every lane, the plain while-while traversal) */
 } ddgi_trace_tuning;
 ddgi_status ddgi_set_trace_tuning(ddgi_ctx* ctx, const ddgi_trace_tuning* tuning);
 /* Most triangles per leaf of the mesh trees built by the next
@@ -474,6 +477,7 @@ typedef struct ddgi_batch_tuning {
     uint32_t rays_per_warp;     /* as in ddgi_trace_tuning, per volume (values a volume's ray count
                                    does not allow fall back to 0 for that volume) */
     uint32_t node_width;        /* as in ddgi_trace_tuning */
+    uint32_t straggler_lanes;   /* as in ddgi_trace_tuning */
 } ddgi_batch_tuning;
 
 ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_stream stream, ddgi_batch** out);

@@ -119,7 +119,8 @@ class Timings(C.Structure):
 class BatchTuning(C.Structure):
     """ddgi_batch_tuning: launch parameters of a batch."""
     _fields_ = [("trace_ctas_per_sm", C.c_uint32), ("refill_lanes", C.c_uint32), ("smem_stack", C.c_uint32),
-                ("blend_threads", C.c_uint32), ("rays_per_warp", C.c_uint32), ("node_width", C.c_uint32)]
+                ("blend_threads", C.c_uint32), ("rays_per_warp", C.c_uint32), ("node_width", C.c_uint32),
+                ("straggler_lanes", C.c_uint32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -135,7 +136,7 @@ class GBuffer(C.Structure):
 class TraceTuning(C.Structure):
     """ddgi_trace_tuning: launch parameters of a context's traversals."""
     _fields_ = [("rays_per_warp", C.c_uint32), ("refill_lanes", C.c_uint32), ("smem_stack", C.c_uint32),
-                ("ctas_per_sm", C.c_uint32), ("node_width", C.c_uint32)]
+                ("ctas_per_sm", C.c_uint32), ("node_width", C.c_uint32), ("straggler_lanes", C.c_uint32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

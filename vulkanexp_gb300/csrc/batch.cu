@@ -87,7 +87,7 @@ struct ddgi_batch {
     uint8_t* d_stage = nullptr;
     size_t stage_bytes = 0, off_order = 0, off_vols = 0;
     // launch state
-    ddgi_batch_tuning tuning{0, 8, 0, 256, 0, 2};
+    ddgi_batch_tuning tuning{0, 8, 0, 256, 0, 2, kDefaultWait};
     bool use_graph = true;
     cudaStream_t cap = nullptr, side = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr, done_ev = nullptr;
@@ -312,6 +312,7 @@ cudaError_t enqueue(ddgi_batch* b, cudaStream_t st, bool timed) {
     tt.split = b->tuning.smem_stack;
     tt.rays_per_warp = b->tuning.rays_per_warp;  // applied per volume through the volume table
     tt.wide = b->tuning.node_width == 4 ? 1u : 0u;
+    tt.wait = b->tuning.straggler_lanes;
     WaveHits wh{b->thit, b->prim, b->front};
     ShadowQueue q{b->q_idx, b->q_pos, b->q_sun, nullptr};
     e = launch_batch_trace(arena_scene(b), bt, b->total, wh, q, b->counters, b->rays, b->stack_cap, b->wstack_cap,
@@ -617,6 +618,8 @@ ddgi_status ddgi_batch_set_tuning(ddgi_batch* b, const ddgi_batch_tuning* t) {
         return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "rays_per_warp = %u: want 0, 1, 2, 4, 8, 16 or 32", r);
     if (t->node_width != 2 && t->node_width != 4)
         return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "node_width = %u: want 2 or 4", t->node_width);
+    if (t->straggler_lanes > 31)
+        return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "straggler_lanes = %u outside [0, 31]", t->straggler_lanes);
     ddgi_status s = wait_previous(b);
     if (s != DDGI_OK) return s;
     b->tuning = *t;
@@ -738,13 +741,23 @@ ddgi_status ddgi_batch_autotune(ddgi_batch* b, const float* orientations, uint32
     const uint32_t split_c[] = {0u, 32u, 24u, 16u};
     const uint32_t refill_c[] = {4u, 8u, 16u, 24u};
     const uint32_t ctas_c[] = {0u, 6u, 4u};
-    for (int p = 0; p < 5 && err == DDGI_OK; ++p) {
-        const uint32_t* cand = p == 0 ? width_c : p == 1 ? rpw_c : p == 2 ? split_c : p == 3 ? refill_c : ctas_c;
-        const int nc = p == 0 ? 2 : p == 1 ? 7 : p == 4 ? 3 : 4;
+    const uint32_t wait_c[] = {4u, 6u, 8u, 10u, 12u};
+    for (int p = 0; p < 6 && err == DDGI_OK; ++p) {
+        const uint32_t* cand = p == 0   ? width_c
+                               : p == 1 ? rpw_c
+                               : p == 2 ? split_c
+                               : p == 3 ? refill_c
+                               : p == 4 ? ctas_c
+                                        : wait_c;
+        const int nc = p == 0 ? 2 : p == 1 ? 7 : p == 4 ? 3 : p == 5 ? 5 : 4;
         for (int i = 0; i < nc && err == DDGI_OK; ++i) {
             ddgi_batch_tuning t = best;
-            uint32_t* field = p == 0 ? &t.node_width : p == 1 ? &t.rays_per_warp : p == 2 ? &t.smem_stack
-                              : p == 3 ? &t.refill_lanes : &t.trace_ctas_per_sm;
+            uint32_t* field = p == 0   ? &t.node_width
+                              : p == 1 ? &t.rays_per_warp
+                              : p == 2 ? &t.smem_stack
+                              : p == 3 ? &t.refill_lanes
+                              : p == 4 ? &t.trace_ctas_per_sm
+                                       : &t.straggler_lanes;
             if (*field == cand[i]) continue;
             const int cap = t.node_width == 4 && b->wstack_cap > 0 ? b->wstack_cap : b->stack_cap;
             if (p == 2 && cand[i] != 0 && (int)cand[i] >= cap) continue;

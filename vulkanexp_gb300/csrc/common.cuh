@@ -47,6 +47,10 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 // ref >= 0: inner node index; ref < 0: leaf, ~ref = (first << 3) | (count - 1)
 // with 1..8 primitives from `first` (triangles in a bottom level, one
 // instance in the top level).
+// Default of the traversals' straggler threshold: a warp leaves its
+// node-search loop once at most this many lanes still look for a first leaf.
+constexpr uint32_t kDefaultWait = 8;
+
 struct __align__(16) BvhNode {
     float4 a, b, c;
     int4 d;

@@ -120,7 +120,7 @@ struct ddgi_ctx {
     // index, selected count}; probe classification scratch
     uint32_t* sched = nullptr;
     // traversal launch tuning; probes in Morton order of the grid (grouped warps)
-    ddgi_trace_tuning tune{0, 8, 0, 0, 2};
+    ddgi_trace_tuning tune{0, 8, 0, 0, 2, ddgi::kDefaultWait};
     int blas_leaf_max = ddgi::kBlasLeafMax;  // triangles per mesh-tree leaf (scene build option)
     ddgi_build_mode build_mode = DDGI_BUILD_FAST_TRACE;  // tree builder (scene build option)
     uint32_t inject = 0;  // one-shot test hooks (DDGI_FAULT_*), cleared by the launch that uses them

@@ -1076,6 +1076,7 @@ TraceTuning trace_tuning(const ddgi_ctx* ctx) {
     t.split = ctx->tune.smem_stack;
     t.rays_per_warp = ctx->tune.rays_per_warp;
     t.wide = ctx->tune.node_width == 4 ? 1u : 0u;
+    t.wait = ctx->tune.straggler_lanes;
     return t;
 }
 
@@ -1306,6 +1307,8 @@ ddgi_status ddgi_set_trace_tuning(ddgi_ctx* ctx, const ddgi_trace_tuning* t) {
         return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "smem_stack or ctas_per_sm out of range");
     if (t->node_width != 2 && t->node_width != 4)
         return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "node_width = %u: want 2 or 4", t->node_width);
+    if (t->straggler_lanes > 31)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "straggler_lanes = %u outside [0, 31]", t->straggler_lanes);
     ctx->tune = *t;
     return DDGI_OK;
 }
@@ -1402,17 +1405,27 @@ ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t re
     const uint32_t refill_c[] = {4u, 8u, 16u, 24u};
     const uint32_t split_c[] = {0u, 32u, 24u, 16u};
     const uint32_t ctas_c[] = {0u, 6u, 4u};
-    for (int p = 0; p < 5 && err == DDGI_OK; ++p) {
-        const uint32_t* cand = p == 0 ? width_c : p == 1 ? rpw_c : p == 2 ? refill_c : p == 3 ? split_c : ctas_c;
-        const int nc = p == 0 ? 2 : p == 1 ? 7 : p == 4 ? 3 : 4;
+    const uint32_t wait_c[] = {4u, 6u, 8u, 10u, 12u};
+    for (int p = 0; p < 6 && err == DDGI_OK; ++p) {
+        const uint32_t* cand = p == 0   ? width_c
+                               : p == 1 ? wait_c
+                               : p == 2 ? rpw_c
+                               : p == 3 ? refill_c
+                               : p == 4 ? split_c
+                                        : ctas_c;
+        const int nc = p == 0 ? 2 : p == 1 ? 5 : p == 2 ? 7 : p == 5 ? 3 : 4;
         for (int i = 0; i < nc && err == DDGI_OK; ++i) {
             ddgi_trace_tuning t = best;
-            uint32_t* field = p == 0 ? &t.node_width : p == 1 ? &t.rays_per_warp : p == 2 ? &t.refill_lanes
-                              : p == 3 ? &t.smem_stack : &t.ctas_per_sm;
+            uint32_t* field = p == 0   ? &t.node_width
+                              : p == 1 ? &t.straggler_lanes
+                              : p == 2 ? &t.rays_per_warp
+                              : p == 3 ? &t.refill_lanes
+                              : p == 4 ? &t.smem_stack
+                                       : &t.ctas_per_sm;
             if (*field == cand[i]) continue;
-            if (p == 1 && grouped_rays_per_warp(cand[i], R) != cand[i]) continue;
+            if (p == 2 && grouped_rays_per_warp(cand[i], R) != cand[i]) continue;
             const int cap = t.node_width == 4 && ctx->scene.wstack_cap > 0 ? ctx->scene.wstack_cap : ctx->scene.stack_cap;
-            if (p == 3 && cand[i] != 0 && (int)cand[i] >= cap) continue;
+            if (p == 4 && cand[i] != 0 && (int)cand[i] >= cap) continue;
             *field = cand[i];
             float tt = 0.0f;
             err = measure(t, &tt);

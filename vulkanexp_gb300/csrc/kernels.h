@@ -37,7 +37,16 @@ struct TraceTuning {
     uint32_t split;          // stack entries in shared memory (0 or >= cap: all)
     uint32_t rays_per_warp;  // 0: a warp per probe in slot order; 1..32: grouped order (see below)
     uint32_t wide;           // 1: four-wide nodes (when the scene has them), 0: binary nodes
+    uint32_t wait = kDefaultWait;  // straggler lanes that end a warp's search loop (0: wait for all)
 };
+// Per-launch constants of the persistent traversal loop.
+struct WalkKnobs {
+    int refill;     // idle lanes that trigger a warp's work request (1..32)
+    uint32_t wait;  // lanes still searching for a first leaf that no longer hold the search loop (0..31)
+};
+inline WalkKnobs walk_knobs(const TraceTuning& t) {
+    return WalkKnobs{(int)(t.refill < 1 ? 1 : (t.refill > 32 ? 32 : t.refill)), t.wait > 31 ? 31u : t.wait};
+}
 // Grouped order: lane groups of rays_per_warp consecutive directions (of the
 // octant-binned ray order) from 32 / rays_per_warp probes taken in `perm`
 // order (Morton order of the grid).  Usable values divide 32 and R (32

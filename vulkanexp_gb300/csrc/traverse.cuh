@@ -209,6 +209,7 @@ struct WarpWalker {
     int sp, cap, ref;
     bool in_blas;
     uint32_t inst_id, steps, mask;
+    uint32_t wait_max;  // lanes still searching that no longer hold the warp in the search loop
     float tmin, tcur;
     HitRec best;
 
@@ -269,12 +270,23 @@ struct WarpWalker {
     // All lanes call this; returns true when an active lane's ray is finished.
     __device__ __forceinline__ bool advance(const DeviceScene& sc, uint32_t* err, bool active) {
         int leaf = kNone;
-        bool searching = active && ref != kNone;
         bool failed = false;
+        // every call counts as a step too: a ray that stopped making progress
+        // (a malformed tree or a scheduling bug) ends with an error, not a hang
+        if (active && ++steps > sc.max_steps) {
+            raise_error(err, DEV_BAD_INDEX);
+            failed = true;
+        }
+        bool searching = active && ref != kNone && !failed;
         const float blo = tmin * kBoxLo, bhi = tcur * kBoxHi;  // tcur is fixed until the leaf phase
-        // step until no lane is still searching for its first leaf (one vote
-        // per step; lanes already holding a leaf walk on speculatively)
-        while (__any_sync(0xffffffffu, searching && leaf == kNone)) {
+        // step while more than `wait_max` lanes are still searching for their
+        // first leaf (one vote per step; lanes already holding a leaf walk on
+        // speculatively), but at least once when any is, so every searching
+        // lane makes progress in every call; the stragglers carry on in the
+        // next call instead of holding the whole warp in this loop
+        for (uint32_t it = 0;; ++it) {
+            const unsigned waiting = __ballot_sync(0xffffffffu, searching && leaf == kNone);
+            if (waiting == 0u || (it > 0u && (uint32_t)__popc(waiting) <= wait_max)) break;
             if (searching) {
                 if (ref >= 0) {
                     if (++steps > sc.max_steps || (uint32_t)ref >= sc.node_count) {
@@ -412,6 +424,7 @@ struct WideWalker {
     int sp, cap, ref;
     bool in_blas;
     uint32_t inst_id, steps, mask;
+    uint32_t wait_max;
     float tmin, tcur;
     HitRec best;
 
@@ -520,9 +533,15 @@ struct WideWalker {
     // All lanes call this; returns true when an active lane's ray is finished.
     __device__ __forceinline__ bool advance(const DeviceScene& sc, uint32_t* err, bool active) {
         int leaf = kNone;
-        bool searching = active && ref != kNone;
         bool failed = false;
-        while (__any_sync(0xffffffffu, searching && leaf == kNone)) {
+        if (active && ++steps > sc.wmax_steps) {  // as in WarpWalker::advance
+            raise_error(err, DEV_BAD_INDEX);
+            failed = true;
+        }
+        bool searching = active && ref != kNone && !failed;
+        for (uint32_t it = 0;; ++it) {  // as in WarpWalker::advance
+            const unsigned waiting = __ballot_sync(0xffffffffu, searching && leaf == kNone);
+            if (waiting == 0u || (it > 0u && (uint32_t)__popc(waiting) <= wait_max)) break;
             if (searching) {
                 if (ref >= 0) {
                     if (++steps > sc.wmax_steps || (uint32_t)ref >= sc.wnode_count) {
