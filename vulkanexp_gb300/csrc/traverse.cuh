@@ -200,10 +200,10 @@ struct SplitStack {
 template <bool ANY, class Stack = SmemStack>
 struct WarpWalker {
     static constexpr bool kWide = false;
-    // resident 128-thread blocks per SM the kernels are built for: 10 (48
-    // registers, a small spill) measured 1.6 % faster than 8 (64 registers)
-    // and 9; 12 (40 registers) slower
-    static constexpr int kMinBlocks = 10;
+    // resident 128-thread blocks per SM the kernels are built for: with the
+    // straggler exit of the search loop, 8 (64 registers, no spill) is 1.7 %
+    // faster than 10 (48 registers, spilling); 9 (56) is level with 8
+    static constexpr int kMinBlocks = 8;
     Ray wr, r;  // world ray, current ray (world or object space)
     Stack stk;
     int sp, cap, ref;
