@@ -473,7 +473,9 @@ typedef struct ddgi_batch_tuning {
     uint32_t refill_lanes;      /* a warp requests new rays once this many lanes are idle (1..32) */
     uint32_t smem_stack;        /* traversal-stack entries per thread in shared memory, deeper ones
                                    in local memory; 0 = the whole stack in shared memory */
-    uint32_t blend_threads;     /* threads per probe of the FP32 blend (32..256, multiple of 32) */
+    uint32_t blend_threads;     /* FP32 blend: 0 = weights computed once per update and shared by tiles of
+                                   probes (default); 32..256 (multiple of 32) = one block of this many
+                                   threads per probe computing its weights per texel */
     uint32_t rays_per_warp;     /* as in ddgi_trace_tuning, per volume (values a volume's ray count
                                    does not allow fall back to 0 for that volume) */
     uint32_t node_width;        /* as in ddgi_trace_tuning */

@@ -95,6 +95,7 @@ def test_batch_equals_single_updates(gpu_lib, volumes, single_results, graph):
     dict(smem_stack=0, refill_lanes=1, trace_ctas_per_sm=2, blend_threads=256),
     dict(node_width=2, rays_per_warp=8, smem_stack=16),
     dict(straggler_lanes=0), dict(straggler_lanes=20, node_width=4),
+    dict(blend_threads=0, refill_lanes=12), dict(blend_threads=32),
 ])
 def test_tunings_do_not_change_results(gpu_lib, volumes, single_results, tuning):
     ctxs = [make_ctx(w) for w in volumes]
@@ -118,7 +119,7 @@ def test_autotune_restores_volumes_and_keeps_results(gpu_lib, volumes, single_re
     b.synchronize()
     before = [atlases(c) for c in ctxs]
     chosen = b.autotune(orientations(volumes, 5), reps=2)
-    assert 1 <= chosen["refill_lanes"] <= 32 and chosen["blend_threads"] in (64, 128, 256)
+    assert 1 <= chosen["refill_lanes"] <= 32 and chosen["blend_threads"] in (0, 64, 128, 256)
     assert b.tuning() == chosen
     for v, c in enumerate(ctxs):
         assert_same(atlases(c), before[v], "volume %d after autotune" % v)

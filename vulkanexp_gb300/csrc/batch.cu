@@ -78,16 +78,16 @@ struct ddgi_batch {
     unsigned long long* d_clock = nullptr;
     uint32_t* d_done = nullptr;
     uint32_t* d_err = nullptr;
-    uint32_t* d_lists = nullptr;  // fp32 list, fp32 tile base, tc list, tc tile base
-    BatchBlendList fp32_bl{}, tc_bl{};
-    uint32_t max_rays_fp32 = 0, max_rows_tc = 0;
+    uint32_t* d_lists = nullptr;  // fp32 list, fp32 tile base, tc list, tc tile base, fp32 shared-weight tile base
+    BatchBlendList fp32_bl{}, tc_bl{}, fp32s_bl{};  // fp32s: tiles of several probes, shared weights
+    uint32_t max_rays_fp32 = 0, max_rows_tc = 0, max_ntex_fp32 = 0;
     size_t tc_smem = 0;
     // per-update staging: [dirs | ray orders | volume table], host pinned + device
     uint8_t* h_stage = nullptr;
     uint8_t* d_stage = nullptr;
     size_t stage_bytes = 0, off_order = 0, off_vols = 0;
     // launch state
-    ddgi_batch_tuning tuning{0, 8, 0, 256, 0, 2, kDefaultWait};
+    ddgi_batch_tuning tuning{0, 8, 0, 0, 0, 2, kDefaultWait};
     bool use_graph = true;
     cudaStream_t cap = nullptr, side = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr, done_ev = nullptr;
@@ -320,8 +320,13 @@ cudaError_t enqueue(ddgi_batch* b, cudaStream_t st, bool timed) {
     if (e != cudaSuccess) return e;
     if (timed) cudaEventRecord(b->ev[3], st);
     const bool both = b->fp32_bl.ntiles > 0 && b->tc_bl.ntiles > 0;
+    auto blend_fp32 = [&](cudaStream_t s) {
+        return b->tuning.blend_threads == 0
+                   ? launch_batch_blend_fp32_shared(bt, b->fp32s_bl, b->max_ntex_fp32, b->max_rays_fp32, b->rays, s)
+                   : launch_batch_blend_fp32(bt, b->fp32_bl, b->max_rays_fp32, b->rays, b->tuning.blend_threads, s);
+    };
     if (timed || !both) {
-        e = launch_batch_blend_fp32(bt, b->fp32_bl, b->max_rays_fp32, b->rays, b->tuning.blend_threads, st);
+        e = blend_fp32(st);
         if (e != cudaSuccess) return e;
         if (timed) cudaEventRecord(b->ev[4], st);
         e = launch_batch_blend_tc(bt, b->tc_bl, b->rays, b->tc_smem, st);
@@ -333,7 +338,7 @@ cudaError_t enqueue(ddgi_batch* b, cudaStream_t st, bool timed) {
     e = cudaEventRecord(b->fork_ev, st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side, b->fork_ev, 0);
     if (e == cudaSuccess)
-        e = launch_batch_blend_fp32(bt, b->fp32_bl, b->max_rays_fp32, b->rays, b->tuning.blend_threads, b->side);
+        e = blend_fp32(b->side);
     if (e == cudaSuccess) e = launch_batch_blend_tc(bt, b->tc_bl, b->rays, b->tc_smem, st);
     if (e == cudaSuccess) e = cudaEventRecord(b->join_ev, b->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(st, b->join_ev, 0);
@@ -423,7 +428,7 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
     }
     // ---- sizes ----
     uint64_t nodes = 0, tris = 0, insts = 0, rays = 0, dirs = 0;
-    std::vector<uint32_t> fp32_list, fp32_base{0}, tc_list, tc_base{0};
+    std::vector<uint32_t> fp32_list, fp32_base{0}, tc_list, tc_base{0}, fp32s_base{0};
     for (uint32_t v = 0; v < count; ++v) {
         const ddgi_ctx* c = b->vols[v];
         const uint32_t P = (uint32_t)c->grid.resolution[0] * c->grid.resolution[1] * c->grid.resolution[2];
@@ -449,7 +454,10 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
         } else {
             fp32_list.push_back(v);
             fp32_base.push_back(fp32_base.back() + P);
+            fp32s_base.push_back(fp32s_base.back() + fp32_shared_tiles(P));
             b->max_rays_fp32 = std::max(b->max_rays_fp32, R);
+            const uint32_t nc = c->grid.color_res - 2, nd = c->grid.depth_res - 2;
+            b->max_ntex_fp32 = std::max(b->max_ntex_fp32, nc * nc + nd * nd);
         }
     }
     b->ray_base.push_back((uint32_t)rays);
@@ -480,7 +488,7 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
         cudaMalloc(&b->d_clock, sizeof(unsigned long long) * (count + 1)) != cudaSuccess ||
         cudaMalloc(&b->d_done, sizeof(uint32_t) * count) != cudaSuccess ||
         cudaMalloc(&b->d_err, sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc(&b->d_lists, sizeof(uint32_t) * (2 * count + 2)) != cudaSuccess) {
+        cudaMalloc(&b->d_lists, sizeof(uint32_t) * (3 * count + 3)) != cudaSuccess) {
         cudaGetLastError();
         return bail(DDGI_ERR_OUT_OF_MEMORY);
     }
@@ -508,6 +516,7 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
     lists.insert(lists.end(), fp32_base.begin(), fp32_base.end());
     lists.insert(lists.end(), tc_list.begin(), tc_list.end());
     lists.insert(lists.end(), tc_base.begin(), tc_base.end());
+    lists.insert(lists.end(), fp32s_base.begin(), fp32s_base.end());
     if (cudaMemcpyAsync(b->d_lists, lists.data(), sizeof(uint32_t) * lists.size(), cudaMemcpyHostToDevice, st) !=
             cudaSuccess ||
         cudaMemcpyAsync(b->d_ray_base, b->ray_base.data(), sizeof(uint32_t) * (count + 1), cudaMemcpyHostToDevice,
@@ -518,6 +527,7 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
     const uint32_t nf = (uint32_t)fp32_list.size(), nt = (uint32_t)tc_list.size();
     b->fp32_bl = BatchBlendList{b->d_lists, b->d_lists + nf, nf, fp32_base.back()};
     b->tc_bl = BatchBlendList{b->d_lists + 2 * nf + 1, b->d_lists + 2 * nf + 1 + nt, nt, tc_base.back()};
+    b->fp32s_bl = BatchBlendList{b->d_lists, b->d_lists + 2 * nf + 2 * nt + 2, nf, fp32s_base.back()};
 
     // ---- arena: copy every volume's trees with rebased references ----
     uint64_t node_off = 0, tri_off = 0, inst_off = 0, wnode_off = 0;
@@ -608,8 +618,8 @@ ddgi_status ddgi_batch_set_tuning(ddgi_batch* b, const ddgi_batch_tuning* t) {
     if (!b || !t) return DDGI_ERR_INVALID_ARGUMENT;
     if (t->refill_lanes < 1 || t->refill_lanes > 32)
         return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "refill_lanes = %u outside [1, 32]", t->refill_lanes);
-    if (t->blend_threads < 32 || t->blend_threads > 256 || t->blend_threads % 32)
-        return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "blend_threads = %u: want a multiple of 32 in [32, 256]",
+    if (t->blend_threads != 0 && (t->blend_threads < 32 || t->blend_threads > 256 || t->blend_threads % 32))
+        return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "blend_threads = %u: want 0 or a multiple of 32 in [32, 256]",
                      t->blend_threads);
     if (t->smem_stack > (uint32_t)kSpillMax || t->trace_ctas_per_sm > 32)
         return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "smem_stack or trace_ctas_per_sm out of range");
@@ -773,8 +783,8 @@ ddgi_status ddgi_batch_autotune(ddgi_batch* b, const float* orientations, uint32
     if (err == DDGI_OK && b->fp32_bl.ntiles > 0) {
         float bt = 0.0f;
         err = measure(best, 1, &bt);
-        const uint32_t thr_c[] = {64u, 128u, 256u};
-        for (int i = 0; i < 3 && err == DDGI_OK; ++i) {
+        const uint32_t thr_c[] = {0u, 64u, 128u, 256u};
+        for (int i = 0; i < 4 && err == DDGI_OK; ++i) {
             if (thr_c[i] == best.blend_threads) continue;
             ddgi_batch_tuning t = best;
             t.blend_threads = thr_c[i];

@@ -275,6 +275,16 @@ ddgi_status ddgi_create(const ddgi_grid_desc* grid, ddgi_ctx** out) {
         }
         cudaMemset(ctx->acc_color, 0, atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, false));
         cudaMemset(ctx->acc_depth, 0, atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, false));
+    } else {
+        // the FP32 wavefront blend's per-update weights (ray x texel) and sums
+        const size_t ntex = (size_t)(grid->color_res - 2) * (grid->color_res - 2) +
+                            (size_t)(grid->depth_res - 2) * (grid->depth_res - 2);
+        if (cudaMalloc(&ctx->tc_weights, fp32_weight_bytes(DDGI_MAX_RAYS_PER_PROBE, grid->color_res,
+                                                           grid->depth_res)) != cudaSuccess ||
+            cudaMalloc(&ctx->tc_rowsum, ntex * sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            return bail(DDGI_ERR_OUT_OF_MEMORY);
+        }
     }
     st = ensure_ray_capacity(ctx, (size_t)P * grid->rays_per_probe);
     if (st != DDGI_OK) return bail(st);
@@ -1080,8 +1090,6 @@ TraceTuning trace_tuning(const ddgi_ctx* ctx) {
     return t;
 }
 
-// Blend + border copy of the ray records in ctx->rays: the FP32 SIMT kernel or
-// the BF16 tensor-core kernel, by the context's precision.
 // One-shot test hook: true once after ddgi_inject_fault(DDGI_FAULT_STALL_TENSOR_WAIT).
 bool take_stall(ddgi_ctx* ctx) {
     const bool s = (ctx->inject & DDGI_FAULT_STALL_TENSOR_WAIT) != 0;
@@ -1089,11 +1097,19 @@ bool take_stall(ddgi_ctx* ctx) {
     return s;
 }
 
+// Blend + border copy of the ray records in ctx->rays, by the context's
+// precision and pipeline: the BF16 tensor-core kernel; the FP32 kernel with
+// the weights computed once per update (wavefront); the per-probe FP32
+// kernel that computes them per texel like the reference's shader (fused).
 cudaError_t launch_blend(ddgi_ctx* ctx, const uint32_t* dlist, uint32_t n, cudaStream_t st) {
     if (ctx->fp16)
         return launch_blend_tc(ctx->dg, dlist, n, ctx->rays, ctx->dirs, ctx->tc_weights, ctx->tc_rowsum, ctx->states,
                                ctx->color, ctx->depth, ctx->acc_color, ctx->acc_depth, ctx->err, st, nullptr,
                                take_stall(ctx));
+    if (ctx->pipeline == DDGI_PIPELINE_WAVEFRONT)
+        return launch_blend_fp32_shared(ctx->dg, dlist, n, ctx->rays, ctx->dirs,
+                                        reinterpret_cast<float*>(ctx->tc_weights), ctx->tc_rowsum, ctx->states,
+                                        static_cast<float4*>(ctx->color), static_cast<float2*>(ctx->depth), st);
     return launch_blend_fp32(ctx->dg, dlist, n, ctx->rays, ctx->dirs, ctx->states, static_cast<float4*>(ctx->color),
                              static_cast<float2*>(ctx->depth), st);
 }
@@ -1214,6 +1230,11 @@ ddgi_status ddgi_update_scheduled(ddgi_ctx* ctx, const float orientation[9], uin
         CK(launch_blend_tc(ctx->dg, ctx->probe_list, P, ctx->rays, ctx->dirs, ctx->tc_weights, ctx->tc_rowsum,
                            ctx->states, ctx->color, ctx->depth, ctx->acc_color, ctx->acc_depth, ctx->err, st, dcount,
                            take_stall(ctx)),
+           "blend launch");
+    else if (ctx->pipeline == DDGI_PIPELINE_WAVEFRONT)
+        CK(launch_blend_fp32_shared(ctx->dg, ctx->probe_list, P, ctx->rays, ctx->dirs,
+                                    reinterpret_cast<float*>(ctx->tc_weights), ctx->tc_rowsum, ctx->states,
+                                    static_cast<float4*>(ctx->color), static_cast<float2*>(ctx->depth), st, dcount),
            "blend launch");
     else
         CK(launch_blend_fp32(ctx->dg, ctx->probe_list, P, ctx->rays, ctx->dirs, ctx->states,

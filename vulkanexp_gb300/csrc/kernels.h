@@ -174,6 +174,15 @@ cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uin
                             void* depth, float4* acc_color, float2* acc_depth, uint32_t* err, cudaStream_t st,
                             const uint32_t* dev_count = nullptr, bool stall = false);
 
+// blend_shared.cu: FP32 blend with the weights computed once per update
+size_t fp32_weight_bytes(uint32_t rays, uint32_t color_res, uint32_t depth_res);
+uint32_t fp32_shared_tiles(uint32_t nprobes);
+cudaError_t launch_blend_fp32_shared(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes,
+                                     const float4* rays, const float4* dirs, float* W, float* wsum, uint32_t* states,
+                                     float4* color, float2* depth, cudaStream_t st, const uint32_t* dev_count = nullptr);
+cudaError_t launch_batch_blend_fp32_shared(const BatchTables& bt, const BatchBlendList& bl, uint32_t max_ntex,
+                                           uint32_t max_rays, const float4* rays, cudaStream_t st);
+
 // blend.cu
 cudaError_t launch_blend_fp32(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
                               const float4* dirs, uint32_t* states, float4* color, float2* depth, cudaStream_t st,
