@@ -439,7 +439,9 @@ __global__ void __launch_bounds__(128) k_batch_classify(BatchTables bt, uint32_t
 
 // Batched shading, pass 2 (k_shade_front with the volume's scene, grid,
 // light, states and atlas; the shadow-queue entry carries the volume).
-__global__ void __launch_bounds__(128, 6) k_batch_shade_front(BatchTables bt, WaveHits hits,
+// Eight resident blocks per SM, like k_shade_front: the 48-volume batch
+// update 30.4 -> 29.9 ms against six.
+__global__ void __launch_bounds__(128, 8) k_batch_shade_front(BatchTables bt, WaveHits hits,
                                                               const uint32_t* front_count, float4* rays_out,
                                                               ShadowQueue q) {
     const uint32_t n = *front_count;
