@@ -428,6 +428,13 @@ typedef enum ddgi_build_mode {
     DDGI_BUILD_FAST_BUILD = 1
 } ddgi_build_mode;
 ddgi_status ddgi_set_build_mode(ddgi_ctx* ctx, ddgi_build_mode mode);
+/* Spatial splits of the fast-trace mesh trees built by the next
+ * ddgi_scene_build: a node whose object split leaves children overlapping by
+ * more than `overlap` of the tree root's surface area also tries splitting
+ * its triangles by a plane (they are then referenced on both sides).  0
+ * turns them off; default 0.003 (smaller: faster traversal, slower build and
+ * more triangle references).  Hits do not depend on it. */
+ddgi_status ddgi_set_spatial_splits(ddgi_ctx* ctx, float overlap);
 
 /* ---- Failure-detection test hooks ---------------------------------------
  * No counterpart in the reference (its fence waits use UINT64_MAX).  Every

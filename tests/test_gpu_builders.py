@@ -8,7 +8,7 @@ from conftest import rel_err
 from oracle.oracle import Oracle, zero_atlas
 from test_gpu_instances import hits_equal, moved
 from vulkanexp_gb300 import abi, scenes
-from vulkanexp_gb300.ddgi import Context
+from vulkanexp_gb300.ddgi import Context, DDGIError
 
 pytestmark = pytest.mark.gpu
 
@@ -82,6 +82,32 @@ def test_sah_top_level_after_instance_updates(gpu_lib, rebuild):
     g, _ = ctx.trace_rays(orig, d, 0.01, 500.0, 0xFF, False)
     r, _ = o.trace(orig, d, 0.01, 500.0, 0xFF, False)
     assert hits_equal(g, r).all()
+    ctx.close()
+
+
+@pytest.mark.parametrize("overlap", [0.0, 1e-2, 1e-5])
+@pytest.mark.parametrize("which", ["room", "terrain"])
+def test_spatial_split_trees_bit_exact(gpu_lib, which, overlap):
+    """Fast-trace mesh trees with spatial splits (triangles referenced from
+    several leaves) give the oracle's closest and any hits bit for bit."""
+    w = workload(which)
+    o = Oracle(w.scene)
+    ctx = Context(w.grid)
+    ctx.set_spatial_splits(overlap)
+    ctx.build_scene(w.scene)
+    ctx.set_light(w.light)
+    orig, d = random_rays(w, which, 20000, 12)
+    for any_hit in (False, True):
+        r, _ = o.trace(orig, d, 0.01, 500.0, 0xFF, any_hit)
+        for width in (2, 4):
+            ctx.set_trace_tuning(node_width=width)
+            g, _ = ctx.trace_rays(orig, d, 0.01, 500.0, 0xFF, any_hit)
+            if any_hit:
+                assert ((g["instance"] == abi.MISS) == (r["instance"] == abi.MISS)).all()
+            else:
+                assert hits_equal(g, r).all(), "%d rays differ from the oracle" % (~hits_equal(g, r)).sum()
+    with pytest.raises(DDGIError):
+        ctx.set_spatial_splits(-1.0)
     ctx.close()
 
 

@@ -1,5 +1,7 @@
 """Host code under AddressSanitizer and UndefinedBehaviorSanitizer, no GPU:
 
+* the spatial-split tree builder (vulkanexp_gb300/csrc/sbvh.cu) through
+  tests/native/sbvh_check.cu;
 * the SAH tree builder (vulkanexp_gb300/csrc/sah.cu) through a structural
   check (tests/native/sah_check.cu) over random, coincident, flat and
   NaN/infinite primitive boxes, every leaf size;
@@ -46,6 +48,33 @@ def test_sah_builder_under_sanitizers(tmp_path):
         subprocess.check_call([nvcc] + flags + ["-c", os.path.join(ROOT, src), "-o", o])
         objs.append(o)
     exe = str(tmp_path / "sah_check")
+    cudart = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "lib64")
+    subprocess.check_call(["g++", "-fsanitize=address", "-fsanitize=undefined"] + objs +
+                          ["-L" + cudart, "-lcudart_static", "-ldl", "-lrt", "-pthread", "-o", exe])
+    r = subprocess.run([exe], capture_output=True, text=True, env=dict(os.environ, **ENV), timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "all ok" in r.stdout
+
+
+def test_spatial_split_builder_under_sanitizers(tmp_path):
+    """tests/native/sbvh_check.cu: references, leaf ranges, depth, and
+    conservativeness at sample points of every triangle, for overlapping box
+    soups (several overlap thresholds, leaf sizes) and a height field."""
+    from vulkanexp_gb300 import build
+
+    nvcc = build.nvcc()
+    if not (os.path.exists(nvcc) or _have(nvcc)) or _runtime("libasan.so") is None:
+        pytest.skip("nvcc or the ASan runtime is missing")
+    flags = ["-std=c++17"] + build.ARCH + ["--expt-relaxed-constexpr"]
+    for f in SAN[:4] + ["-ffp-contract=off"]:
+        flags += ["-Xcompiler", f]
+    flags += ["-g", "-O1"]
+    objs = []
+    for src in ("tests/native/sbvh_check.cu", "vulkanexp_gb300/csrc/sbvh.cu"):
+        o = str(tmp_path / (os.path.basename(src) + ".o"))
+        subprocess.check_call([nvcc] + flags + ["-c", os.path.join(ROOT, src), "-o", o])
+        objs.append(o)
+    exe = str(tmp_path / "sbvh_check")
     cudart = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "lib64")
     subprocess.check_call(["g++", "-fsanitize=address", "-fsanitize=undefined"] + objs +
                           ["-L" + cudart, "-lcudart_static", "-ldl", "-lrt", "-pthread", "-o", exe])

@@ -16,6 +16,11 @@ namespace ddgi {
 
 constexpr int kBlasLeafMax = 2;  // default; measured best of 1, 2, 4, 8 on the 1M-triangle scene
 constexpr int kTlasLeafMax = 1;
+// Overlap (of the root's surface area) above which a fast-trace mesh-tree
+// node tries a spatial split.  On the 1M-triangle terrain + box-cluster
+// scene: 0 -> 13.8 ms per update (0.18 s build), 0.03 -> 11.8 ms (0.6 s),
+// 0.01 -> 10.7 ms (1.1 s), 0.003 -> 10.0 ms (2.2 s), 0.001 -> 9.6 ms (4.1 s).
+constexpr float kDefaultSplitAlpha = 3e-3f;
 // deepest traversal stack of the wavefront kernels (entries per thread in
 // shared memory: 96 x 128 threads x 4 bytes = 48 KB per block)
 constexpr int kMaxStack = 96;
@@ -123,6 +128,7 @@ struct ddgi_ctx {
     ddgi_trace_tuning tune{0, 8, 0, 0, 2, ddgi::kDefaultWait};
     int blas_leaf_max = ddgi::kBlasLeafMax;  // triangles per mesh-tree leaf (scene build option)
     ddgi_build_mode build_mode = DDGI_BUILD_FAST_TRACE;  // tree builder (scene build option)
+    float split_alpha = ddgi::kDefaultSplitAlpha;          // spatial splits of fast-trace mesh trees (0: none)
     uint32_t inject = 0;  // one-shot test hooks (DDGI_FAULT_*), cleared by the launch that uses them
     uint32_t* probe_perm = nullptr;
     float4* init_dirs = nullptr;

@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -620,6 +621,73 @@ bool depth_first_layout(std::vector<BvhNode>& nodes, uint32_t b, uint32_t e) {
     return true;
 }
 
+// A mesh tree built on the host, its references relative to its own first
+// node and first triangle reference.
+struct HostTree {
+    std::vector<BvhNode> nodes;
+    std::vector<uint32_t> order;  // triangle of each leaf position
+    uint32_t depth = 1;
+};
+
+// Fast-trace trees of every mesh (sbvh.cu): meshes of 64K or more triangles
+// one after the other with every host thread, the others in parallel with
+// one thread each.
+void build_host_trees(const ddgi_scene_desc* d, const std::vector<float4>& pos, int leaf_max, float alpha,
+                      std::vector<HostTree>& trees) {
+    trees.assign(d->mesh_count, HostTree{});
+    auto one = [&](uint32_t m, unsigned threads) {
+        const ddgi_mesh& me = d->meshes[m];
+        const uint32_t nt = me.index_count / 3;
+        if (nt == 0) return;
+        std::vector<float> tri((size_t)nt * 9);
+        for (uint32_t t = 0; t < nt; ++t)
+            for (int v = 0; v < 3; ++v) {
+                const float4& p = pos[me.vertex_offset + d->indices[me.index_offset + 3 * t + v]];
+                tri[9 * (size_t)t + 3 * v] = p.x;
+                tri[9 * (size_t)t + 3 * v + 1] = p.y;
+                tri[9 * (size_t)t + 3 * v + 2] = p.z;
+            }
+        sbvh_build(tri.data(), nt, leaf_max, alpha, 0, 0, trees[m].nodes, trees[m].order, &trees[m].depth, threads);
+    };
+    const unsigned hw = host_threads();
+    std::vector<uint32_t> small;
+    for (uint32_t m = 0; m < d->mesh_count; ++m) {
+        if (d->meshes[m].index_count / 3 >= 65536u) one(m, hw);
+        else small.push_back(m);
+    }
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
+        for (size_t i = next.fetch_add(1); i < small.size(); i = next.fetch_add(1)) one(small[i], 1);
+    };
+    std::vector<std::thread> pool;
+    const unsigned nw = std::min<unsigned>(hw, (unsigned)small.size());
+    for (unsigned t = 1; t < nw; ++t) {
+        try {
+            pool.emplace_back(worker);
+        } catch (const std::system_error&) {
+            break;
+        }
+    }
+    worker();
+    for (auto& th : pool) th.join();
+}
+
+// References of a host tree made absolute: inner + node_base, leaf first +
+// prim_base.
+void rebase_tree(std::vector<BvhNode>& nodes, int node_base, int prim_base) {
+    for (BvhNode& n : nodes) {
+        int* r[2] = {&n.d.x, &n.d.y};
+        for (int s = 0; s < 2; ++s) {
+            if (*r[s] >= 0) {
+                *r[s] += node_base;
+            } else {
+                const int code = ~*r[s];
+                *r[s] = ~((((code >> 3) + prim_base) << 3) | (code & 7));
+            }
+        }
+    }
+}
+
 // Depth-first layout of every mesh tree, then four-wide copies of every mesh
 // tree and of the top level.
 ddgi_status build_wide(ddgi_ctx* ctx, const std::vector<int32_t>& mesh_root, cudaStream_t st) {
@@ -747,10 +815,22 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
         nrm[v] = make_float4(vx.normal[0], vx.normal[1], vx.normal[2], 0.0f);
     }
     float4* dpos = nullptr;
+    // fast-trace mesh trees are built on the host first: their node and
+    // triangle-reference counts (spatial splits reference some triangles
+    // more than once) size the device arrays
+    const bool host_trees = ctx->build_mode == DDGI_BUILD_FAST_TRACE;
+    std::vector<HostTree> trees;
+    if (host_trees) build_host_trees(d, pos, ctx->blas_leaf_max, ctx->split_alpha, trees);
     uint64_t total_tris = 0, total_nodes = 0;
     uint32_t max_tris = 0;
     for (uint32_t m = 0; m < d->mesh_count; ++m) {
         uint32_t nt = d->meshes[m].index_count / 3;
+        if (host_trees) {
+            total_tris += trees[m].order.size();
+            total_nodes += trees[m].nodes.size();
+            max_tris = std::max(max_tris, (uint32_t)std::min<size_t>(trees[m].order.size(), 0xFFFFFFFFu));
+            continue;
+        }
         total_tris += nt;
         total_nodes += nt > 1 ? nt - 1 : (nt == 1 ? 1 : 0);
         max_tris = std::max(max_tris, nt);
@@ -835,31 +915,25 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
                 }
             }
         }
-        if (S.build_mode == DDGI_BUILD_FAST_TRACE) {
-            std::vector<float4> tlo(nt), thi(nt);
-            for (uint32_t t = 0; t < nt; ++t) {
-                const float4* v[3];
-                for (int k = 0; k < 3; ++k) v[k] = &pos[me.vertex_offset + d->indices[me.index_offset + 3 * t + k]];
-                tlo[t] = make_float4(fminf(fminf(v[0]->x, v[1]->x), v[2]->x), fminf(fminf(v[0]->y, v[1]->y), v[2]->y),
-                                     fminf(fminf(v[0]->z, v[1]->z), v[2]->z), 0.0f);
-                thi[t] = make_float4(fmaxf(fmaxf(v[0]->x, v[1]->x), v[2]->x), fmaxf(fmaxf(v[0]->y, v[1]->y), v[2]->y),
-                                     fmaxf(fmaxf(v[0]->z, v[1]->z), v[2]->z), 0.0f);
-            }
-            std::vector<BvhNode> tree(nt > 1 ? nt - 1 : 1);
-            std::vector<uint32_t> order(nt);
-            uint32_t dm = 1;
-            sah_build(tlo.data(), thi.data(), nt, ctx->blas_leaf_max, (int)node_base, (int)tri_base, tree.data(),
-                      order.data(), &dm, host_threads());
-            host_blas_depth = std::max(host_blas_depth, dm);
+        if (host_trees) {
+            HostTree& tr = trees[m];
+            rebase_tree(tr.nodes, (int)node_base, (int)tri_base);
+            host_blas_depth = std::max(host_blas_depth, tr.depth);
+            const uint32_t nref = (uint32_t)tr.order.size();
             // pageable sources: both copies have read them when they return
-            CKB(cudaMemcpyAsync(S.nodes + node_base, tree.data(), sizeof(BvhNode) * tree.size(), cudaMemcpyHostToDevice,
-                                st),
+            CKB(cudaMemcpyAsync(S.nodes + node_base, tr.nodes.data(), sizeof(BvhNode) * tr.nodes.size(),
+                                cudaMemcpyHostToDevice, st),
                 "upload mesh tree");
-            CKB(cudaMemcpyAsync(sorted, order.data(), sizeof(uint32_t) * nt, cudaMemcpyHostToDevice, st),
+            CKB(cudaMemcpyAsync(sorted, tr.order.data(), sizeof(uint32_t) * nref, cudaMemcpyHostToDevice, st),
                 "upload leaf order");
-            CKB(gather_mesh_tris(dpos, S.indices, me.vertex_offset, me.vertex_count, me.index_offset, nt, sorted,
+            CKB(gather_mesh_tris(dpos, S.indices, me.vertex_offset, me.vertex_count, me.index_offset, nt, nref, sorted,
                                  S.tris + tri_base, st),
                 "gather triangles");
+            mesh_root[m] = (int32_t)node_base;
+            node_base += tr.nodes.size();
+            tri_base += nref;
+            tr = HostTree{};
+            continue;
         } else {
             CKB(build_mesh_blas(dpos, S.indices, me.vertex_offset, me.vertex_count, me.index_offset, nt,
                                 ctx->blas_leaf_max, S.nodes, (int)node_base, S.tris, (int)tri_base, box_lo, box_hi,
@@ -1347,6 +1421,14 @@ ddgi_status ddgi_inject_fault(ddgi_ctx* ctx, uint32_t faults) {
     if (faults & ~(uint32_t)DDGI_FAULT_STALL_TENSOR_WAIT)
         return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "unknown fault bits 0x%x", faults);
     ctx->inject |= faults;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_set_spatial_splits(ddgi_ctx* ctx, float overlap) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    if (!(overlap >= 0.0f && overlap <= 1.0f))
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "spatial-split overlap %g outside [0, 1]", (double)overlap);
+    ctx->split_alpha = overlap;
     return DDGI_OK;
 }
 

@@ -505,12 +505,14 @@ __global__ void k_tri_boxes(const float4* pos, const uint32_t* indices, uint32_t
                         fmaxf(fmaxf(v[0].z, v[1].z), v[2].z), 0.0f);
 }
 
+// nref leaf positions, each holding one of the mesh's ntri triangles (a
+// permutation of them, or with repeats for a tree with spatial splits).
 __global__ void k_gather_tris(const float4* pos, const uint32_t* indices, uint32_t vbase, uint32_t ibase,
-                              uint32_t ntri, uint32_t nvert, const uint32_t* sorted_ids, BvhTri* out) {
+                              uint32_t nref, uint32_t ntri, uint32_t nvert, const uint32_t* sorted_ids, BvhTri* out) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= ntri) return;
+    if (s >= nref) return;
     uint32_t t = sorted_ids[s];
-    if (t >= ntri) t = 0;  // cannot happen for a permutation
+    if (t >= ntri) t = 0;  // cannot happen: the builders write triangle indices
     float4 v[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -537,16 +539,17 @@ cudaError_t build_mesh_blas(const float4* pos, const uint32_t* indices, uint32_t
     cudaError_t e =
         lbvh_build(box_lo, box_hi, ntri, leaf_max, nodes, node_base, tri_base, sorted_ids, scratch, err, depth, st);
     if (e != cudaSuccess) return e;
-    k_gather_tris<<<div_up(ntri, T), T, 0, st>>>(pos, indices, vbase, ibase, ntri, vcount, sorted_ids,
+    k_gather_tris<<<div_up(ntri, T), T, 0, st>>>(pos, indices, vbase, ibase, ntri, ntri, vcount, sorted_ids,
                                                  tris + tri_base);
     return cudaGetLastError();
 }
 
 cudaError_t gather_mesh_tris(const float4* pos, const uint32_t* indices, uint32_t vbase, uint32_t vcount,
-                             uint32_t ibase, uint32_t ntri, const uint32_t* sorted_ids, BvhTri* tris, cudaStream_t st) {
-    if (ntri == 0) return cudaSuccess;
+                             uint32_t ibase, uint32_t ntri, uint32_t nref, const uint32_t* sorted_ids, BvhTri* tris,
+                             cudaStream_t st) {
+    if (nref == 0) return cudaSuccess;
     const int T = 256;
-    k_gather_tris<<<div_up(ntri, T), T, 0, st>>>(pos, indices, vbase, ibase, ntri, vcount, sorted_ids, tris);
+    k_gather_tris<<<div_up(nref, T), T, 0, st>>>(pos, indices, vbase, ibase, nref, ntri, vcount, sorted_ids, tris);
     return cudaGetLastError();
 }
 

@@ -27,10 +27,12 @@ cudaError_t build_mesh_blas(const float4* pos, const uint32_t* indices, uint32_t
                             int tri_base, float4* box_lo, float4* box_hi, uint32_t* sorted_ids, void* scratch,
                             uint32_t* err, uint32_t* depth, cudaStream_t st);
 
-// Triangles of one mesh gathered in leaf order (sorted_ids[s] = triangle of
-// leaf position s) at tris[0, ntri), for a tree built elsewhere.
+// Triangles of one mesh (ntri of them) gathered in leaf order
+// (sorted_ids[s] = triangle of leaf position s) at tris[0, nref), for a tree
+// built elsewhere; a triangle may fill several positions.
 cudaError_t gather_mesh_tris(const float4* pos, const uint32_t* indices, uint32_t vbase, uint32_t vcount,
-                             uint32_t ibase, uint32_t ntri, const uint32_t* sorted_ids, BvhTri* tris, cudaStream_t st);
+                             uint32_t ibase, uint32_t ntri, uint32_t nref, const uint32_t* sorted_ids, BvhTri* tris,
+                             cudaStream_t st);
 
 // Refit of a top-level tree whose topology is kept: new boxes for its n
 // leaf slots (leaf order); leaf_parent[s] / node_parent[k] = parent node

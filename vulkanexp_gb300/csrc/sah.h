@@ -3,6 +3,8 @@
 
 #include <stdint.h>
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace ddgi {
@@ -17,5 +19,15 @@ namespace ddgi {
 // false when n == 0.
 bool sah_build(const float4* lo, const float4* hi, uint32_t n, int leaf_max, int node_base, int prim_base,
                BvhNode* nodes, uint32_t* order, uint32_t* depth, unsigned threads);
+
+// Mesh tree over n triangles (9 floats each: v0, v1, v2) with object splits
+// and, where the object split's children overlap by more than alpha of the
+// root's surface area, spatial splits (sbvh.cu); alpha <= 0: object splits
+// only.  A triangle may be referenced by several leaves: order (resized to
+// the reference count) holds the triangle of each leaf position, nodes
+// (resized to the inner-node count) the tree depth first, references as in
+// sah_build.  Returns false when n == 0.
+bool sbvh_build(const float* tris, uint32_t n, int leaf_max, float alpha, int node_base, int prim_base,
+                std::vector<BvhNode>& nodes, std::vector<uint32_t>& order, uint32_t* depth, unsigned threads);
 
 }  // namespace ddgi

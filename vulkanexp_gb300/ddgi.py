@@ -73,6 +73,7 @@ _SIGNATURES = [
     ("ddgi_set_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_set_leaf_size", C.c_int, [C.c_void_p, C.c_uint32]),
     ("ddgi_set_build_mode", C.c_int, [C.c_void_p, C.c_int]),
+    ("ddgi_set_spatial_splits", C.c_int, [C.c_void_p, C.c_float]),
     ("ddgi_inject_fault", C.c_int, [C.c_void_p, C.c_uint32]),
     ("ddgi_atlas_save", C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
     ("ddgi_atlas_load", C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
@@ -246,6 +247,11 @@ class Context:
         if mode not in modes:
             raise ValueError("build mode %r: want one of %s" % (mode, sorted(modes)))
         self._check(self.lib.ddgi_set_build_mode(self.h, modes[mode]))
+
+    def set_spatial_splits(self, overlap):
+        """Spatial splits of the next build_scene's fast-trace mesh trees
+        (overlap fraction of the root's surface area; 0 = off)."""
+        self._check(self.lib.ddgi_set_spatial_splits(self.h, float(overlap)))
 
     def trace_tuning(self):
         t = TraceTuning()
