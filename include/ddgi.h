@@ -254,6 +254,12 @@ ddgi_status ddgi_blend_records_noalloc(const ddgi_grid_desc* grid, const float o
  * `bytes` must equal width*height*channels*4.  Synchronous on `stream`. */
 ddgi_status ddgi_get_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, float* dst, size_t bytes,
                            ddgi_stream stream);
+/* Copies an atlas to host memory in its storage format: FP32 texels for an
+ * FP32 context, IEEE half texels (4 x half colour, 2 x half depth) for a
+ * BF16-blend context, the format a renderer samples (the reference's atlases
+ * are 16-bit float images, src/IrradianceProbes.cpp:41, 63).  `bytes` must
+ * equal width*height*channels*(4 or 2).  Synchronous on `stream`. */
+ddgi_status ddgi_get_atlas_raw(ddgi_ctx* ctx, ddgi_atlas_kind kind, void* dst, size_t bytes, ddgi_stream stream);
 /* Replaces an atlas from host FP32 data of the same shape (checkpoint load). */
 ddgi_status ddgi_set_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, const float* src, size_t bytes,
                            ddgi_stream stream);

@@ -125,6 +125,22 @@ def test_checkpoint_refuses_files_that_do_not_fit(gpu_lib, tmp_path):
         ctx.close()
 
 
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP32, abi.PRECISION_BF16])
+def test_raw_atlas_readback(gpu_lib, precision):
+    """ddgi_get_atlas_raw returns the storage format (FP16 texels for the
+    BF16 form), which widened equals ddgi_get_atlas bit for bit."""
+    w = small_room(precision)
+    ctx = context(w)
+    ctx.update(w.orientation(0))
+    for kind in (abi.ATLAS_COLOR, abi.ATLAS_DEPTH):
+        raw = ctx.get_atlas_raw(kind)
+        assert raw.dtype == (np.float16 if precision == abi.PRECISION_BF16 else np.float32)
+        assert np.array_equal(raw.astype(np.float32).view(np.uint32), ctx.get_atlas(kind).view(np.uint32))
+    with pytest.raises(AssertionError):
+        ctx.get_atlas_raw(abi.ATLAS_COLOR, out=np.empty((1, 1, 4), np.float32))
+    ctx.close()
+
+
 def test_nonfinite_vertex_is_refused(gpu_lib):
     w = small_room(abi.PRECISION_FP32)
     sc = copy.deepcopy(w.scene)

@@ -1656,6 +1656,17 @@ ddgi_status ddgi_get_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, float* dst, size
     return check_device_error(ctx);
 }
 
+ddgi_status ddgi_get_atlas_raw(ddgi_ctx* ctx, ddgi_atlas_kind kind, void* dst, size_t bytes, ddgi_stream stream) {
+    if (!ctx || !dst || (kind != DDGI_ATLAS_COLOR && kind != DDGI_ATLAS_DEPTH)) return DDGI_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const size_t need = atlas_bytes(ctx->dg, kind, ctx->fp16);
+    if (bytes != need) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "atlas needs %zu bytes", need);
+    CK(cudaMemcpyAsync(dst, kind == DDGI_ATLAS_COLOR ? ctx->color : ctx->depth, bytes, cudaMemcpyDeviceToHost, st),
+       "atlas download");
+    CK(cudaStreamSynchronize(st), "atlas download");
+    return check_device_error(ctx);
+}
+
 ddgi_status ddgi_set_atlas(ddgi_ctx* ctx, ddgi_atlas_kind kind, const float* src, size_t bytes, ddgi_stream stream) {
     if (!ctx || !src || (kind != DDGI_ATLAS_COLOR && kind != DDGI_ATLAS_DEPTH)) return DDGI_ERR_INVALID_ARGUMENT;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);

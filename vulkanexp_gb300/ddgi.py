@@ -73,6 +73,7 @@ _SIGNATURES = [
     ("ddgi_set_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
     ("ddgi_set_leaf_size", C.c_int, [C.c_void_p, C.c_uint32]),
     ("ddgi_set_build_mode", C.c_int, [C.c_void_p, C.c_int]),
+    ("ddgi_get_atlas_raw", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]),
     ("ddgi_set_spatial_splits", C.c_int, [C.c_void_p, C.c_float]),
     ("ddgi_inject_fault", C.c_int, [C.c_void_p, C.c_uint32]),
     ("ddgi_atlas_save", C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
@@ -353,6 +354,17 @@ class Context:
             out = np.empty(shape, np.float32)
         assert out.shape == shape and out.dtype == np.float32 and out.flags.c_contiguous
         self._check(self.lib.ddgi_get_atlas(self.h, kind, _ptr(out), out.nbytes, _stream_ptr(stream)))
+        return out
+
+    def get_atlas_raw(self, kind, out=None, stream=None):
+        """The atlas in its storage format: float32 (FP32 context) or float16
+        (BF16-blend context) texels, H x W x channels."""
+        shape = self.atlas_shape(kind)
+        dtype = np.float16 if self.grid.precision == abi.PRECISION_BF16 else np.float32
+        if out is None:
+            out = np.empty(shape, dtype)
+        assert out.shape == shape and out.dtype == dtype and out.flags.c_contiguous
+        self._check(self.lib.ddgi_get_atlas_raw(self.h, kind, _ptr(out), out.nbytes, _stream_ptr(stream)))
         return out
 
     def save_atlas(self, path, stream=None):
