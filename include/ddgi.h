@@ -438,7 +438,7 @@ ddgi_status ddgi_set_build_mode(ddgi_ctx* ctx, ddgi_build_mode mode);
  * ddgi_scene_build: a node whose object split leaves children overlapping by
  * more than `overlap` of the tree root's surface area also tries splitting
  * its triangles by a plane (they are then referenced on both sides).  0
- * turns them off; default 0.003 (smaller: faster traversal, slower build and
+ * turns them off; default 0.001 (smaller: faster traversal, slower build and
  * more triangle references).  Hits do not depend on it. */
 ddgi_status ddgi_set_spatial_splits(ddgi_ctx* ctx, float overlap);
 

@@ -18,9 +18,10 @@ constexpr int kBlasLeafMax = 2;  // default; measured best of 1, 2, 4, 8 on the 
 constexpr int kTlasLeafMax = 1;
 // Overlap (of the root's surface area) above which a fast-trace mesh-tree
 // node tries a spatial split.  On the 1M-triangle terrain + box-cluster
-// scene: 0 -> 13.8 ms per update (0.18 s build), 0.03 -> 11.8 ms (0.6 s),
-// 0.01 -> 10.7 ms (1.1 s), 0.003 -> 10.0 ms (2.2 s), 0.001 -> 9.6 ms (4.1 s).
-constexpr float kDefaultSplitAlpha = 3e-3f;
+// scene (update / scene build on 16 Arm cores): 0 -> 13.8 ms / 0.18 s,
+// 0.01 -> 10.7 ms / 1.1 s, 0.003 -> 9.74 ms / 1.3 s, 0.001 -> 9.36 ms /
+// 2.3 s, 0.0003 -> 9.30 ms / 3.8 s.
+constexpr float kDefaultSplitAlpha = 1e-3f;
 // deepest traversal stack of the wavefront kernels (entries per thread in
 // shared memory: 96 x 128 threads x 4 bytes = 48 KB per block)
 constexpr int kMaxStack = 96;

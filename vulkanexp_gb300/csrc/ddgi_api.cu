@@ -630,8 +630,8 @@ struct HostTree {
 };
 
 // Fast-trace trees of every mesh (sbvh.cu): meshes of 64K or more triangles
-// one after the other with every host thread, the others in parallel with
-// one thread each.
+// one after the other with every host thread, the others in parallel, the
+// host threads shared among them.
 void build_host_trees(const ddgi_scene_desc* d, const std::vector<float4>& pos, int leaf_max, float alpha,
                       std::vector<HostTree>& trees) {
     trees.assign(d->mesh_count, HostTree{});
@@ -655,12 +655,16 @@ void build_host_trees(const ddgi_scene_desc* d, const std::vector<float4>& pos, 
         if (d->meshes[m].index_count / 3 >= 65536u) one(m, hw);
         else small.push_back(m);
     }
+    // largest first, so the long builds start early
+    std::sort(small.begin(), small.end(),
+              [&](uint32_t a, uint32_t b) { return d->meshes[a].index_count > d->meshes[b].index_count; });
     std::atomic<size_t> next{0};
+    const unsigned nw = std::min<unsigned>(hw, (unsigned)small.size());
+    const unsigned per = nw > 0 ? std::max(1u, hw / nw) : 1u;  // threads per mesh build
     auto worker = [&]() {
-        for (size_t i = next.fetch_add(1); i < small.size(); i = next.fetch_add(1)) one(small[i], 1);
+        for (size_t i = next.fetch_add(1); i < small.size(); i = next.fetch_add(1)) one(small[i], per);
     };
     std::vector<std::thread> pool;
-    const unsigned nw = std::min<unsigned>(hw, (unsigned)small.size());
     for (unsigned t = 1; t < nw; ++t) {
         try {
             pool.emplace_back(worker);
