@@ -228,8 +228,8 @@ __device__ float3 sample_probes_vjp(float3 position, float3 normal, float3 toCam
             float fx0 = floorf(x), fy0 = floorf(y);
             float ax = x - fx0, ay = y - fy0;
             int iw = (int)g.color_w, ih = (int)g.color_h;
-            int i0 = (((int)fx0 % iw) + iw) % iw, i1 = (((int)fx0 + 1) % iw + iw) % iw;
-            int j0 = (((int)fy0 % ih) + ih) % ih, j1 = (((int)fy0 + 1) % ih + ih) % ih;
+            int i0 = wrap_repeat((int)fx0, iw), i1 = wrap_repeat((int)fx0 + 1, iw);
+            int j0 = wrap_repeat((int)fy0, ih), j1 = wrap_repeat((int)fy0 + 1, ih);
             size_t t00 = (size_t)j0 * g.color_w + i0, t10 = (size_t)j0 * g.color_w + i1;
             size_t t01 = (size_t)j1 * g.color_w + i0, t11 = (size_t)j1 * g.color_w + i1;
             float b00 = (1.0f - ax) * (1.0f - ay), b10 = ax * (1.0f - ay), b01 = (1.0f - ax) * ay, b11 = ax * ay;

@@ -320,6 +320,17 @@ __host__ __device__ __forceinline__ float texel_scale(uint32_t n) {
     return (float)(2.0 / (double)n);
 }
 
+// REPEAT addressing of texel index i on an axis of n texels.  Sample
+// coordinates in [-0.5, 1.5] give indices in [-n, 2n), which one add or
+// subtract brings into range; anything else takes the remainder (the same
+// integer either way, without a division on the common path).
+__device__ __forceinline__ int wrap_repeat(int i, int n) {
+    if (i < 0) i += n;
+    else if (i >= n) i -= n;
+    if ((unsigned)i >= (unsigned)n) i = ((i % n) + n) % n;
+    return i;
+}
+
 // Exact bilinear fetch, LINEAR filter with REPEAT addressing
 // (src/RaytracingDescriptors.hpp:63, 70).
 template <int NC, class Tex>
@@ -331,10 +342,10 @@ __device__ __forceinline__ void bilinear(const Tex& tex, uint32_t w, uint32_t h,
     int i0 = (int)fx0, j0 = (int)fy0;
     int iw = (int)w, ih = (int)h;
     int i1 = i0 + 1, j1 = j0 + 1;
-    i0 = ((i0 % iw) + iw) % iw;
-    i1 = ((i1 % iw) + iw) % iw;
-    j0 = ((j0 % ih) + ih) % ih;
-    j1 = ((j1 % ih) + ih) % ih;
+    i0 = wrap_repeat(i0, iw);
+    i1 = wrap_repeat(i1, iw);
+    j0 = wrap_repeat(j0, ih);
+    j1 = wrap_repeat(j1, ih);
     float t00[NC], t10[NC], t01[NC], t11[NC];
     tex.fetch((size_t)j0 * w + i0, t00);
     tex.fetch((size_t)j0 * w + i1, t10);
