@@ -143,11 +143,16 @@ struct Ray {
     int kx, ky, kz;
 };
 
+// slab reciprocals of a direction (a zero component stands in as 1e-30)
+__device__ __forceinline__ float3 ray_inv(float3 d) {
+    return make_float3(1.0f / (d.x != 0.0f ? d.x : 1e-30f), 1.0f / (d.y != 0.0f ? d.y : 1e-30f),
+                       1.0f / (d.z != 0.0f ? d.z : 1e-30f));
+}
+
 __device__ __forceinline__ void ray_setup(Ray& r, float3 o, float3 d) {
     r.o = o;
     r.d = d;
-    r.inv = make_float3(1.0f / (d.x != 0.0f ? d.x : 1e-30f), 1.0f / (d.y != 0.0f ? d.y : 1e-30f),
-                        1.0f / (d.z != 0.0f ? d.z : 1e-30f));
+    r.inv = ray_inv(d);
     int kz = 0;
     if (fabsf(d.y) > fabsf(d.x)) kz = 1;
     if (fabsf(d.z) > fabsf(sel3(d, kz))) kz = 2;

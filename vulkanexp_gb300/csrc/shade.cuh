@@ -64,28 +64,57 @@ __device__ __forceinline__ float3 grid_probe_pos(const DeviceGrid& g, int x, int
     return f3((float)x * g.cell[0] + g.mn[0], (float)y * g.cell[1] + g.mn[1], (float)z * g.cell[2] + g.mn[2]);
 }
 
-// sampleProbes (src/shaders/irradiance.glsl:145-237)
-template <class AV>
-__device__ float3 sample_probes(float3 position, float3 normal, float3 toCamera, const DeviceGrid& g,
-                                const uint32_t* states, const AV& at) {
+// x / n for a positive integer n, as the atlas coordinates divide: when n is
+// a power of two the quotient is exact and equals the product with 1 / n
+// (no rounding either way), which saves a division sequence.
+struct AtlasDiv {
+    float d, inv;
+    bool pow2;
+    __device__ __forceinline__ explicit AtlasDiv(uint32_t n)
+        : d((float)n), inv(1.0f / (float)n), pow2(n != 0u && (n & (n - 1u)) == 0u) {}
+    __device__ __forceinline__ float operator()(float x) const { return pow2 ? x * inv : x / d; }
+};
+
+// sampleProbes (src/shaders/irradiance.glsl:145-237) for NQ lookups at one
+// position that differ in the direction argument (`normal`): the closest-hit
+// program makes two (reflection and diffuse), which share the eight probes'
+// states, positions, directions and trilinear weights.  Each lookup's
+// arithmetic is the reference's.
+template <int NQ, class AV>
+__device__ void sample_probes_n(float3 position, const float3 (&normal)[NQ], float3 toCamera, const DeviceGrid& g,
+                                const uint32_t* states, const AV& at, float3 (&result)[NQ]) {
     float3 cs = abs3(f3(g.cell[0], g.cell[1], g.cell[2]));
     float3 gridCoords = (position - f3(g.mn[0], g.mn[1], g.mn[2])) / cs;
     // (written so that NaN also returns 0)
-    if (!(gridCoords.x >= 0.0f && gridCoords.y >= 0.0f && gridCoords.z >= 0.0f)) return f3(0, 0, 0);
-    float3 biasedPosition = position + (normal + toCamera) * g.bias;
+    if (!(gridCoords.x >= 0.0f && gridCoords.y >= 0.0f && gridCoords.z >= 0.0f)) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) result[q] = f3(0, 0, 0);
+        return;
+    }
+    float3 biasedPosition[NQ];
+    float2 nuv[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        biasedPosition[q] = position + (normal[q] + toCamera) * g.bias;
+        nuv[q] = sphere_to_oct_uv(normal[q]);
+    }
     // the clamp only matters beyond 2^24 cells, where every corner is off-grid
     int fx = (int)fminf(gridCoords.x, 16777216.0f), fy = (int)fminf(gridCoords.y, 16777216.0f),
         fz = (int)fminf(gridCoords.z, 16777216.0f);
     float3 alpha = (position - grid_probe_pos(g, fx, fy, fz)) / cs;
     alpha = f3(clampf(alpha.x, 0.0f, 1.0f), clampf(alpha.y, 0.0f, 1.0f), clampf(alpha.z, 0.0f, 1.0f));
 
-    float3 finalColor = f3(0, 0, 0), fallbackColor = f3(0, 0, 0);
-    float totalWeight = 0.0f, totalFallbackWeight = 0.0f;
-    const float uvsx = (float)(g.res[0] * g.res[1]), uvsy = (float)g.res[2];
-    const float cr = (float)g.color_res, dr = (float)g.depth_res;
-    const float cscale = (float)(g.color_res - 2) / cr;
-    const float dscale = (float)(g.depth_res - 2) / dr;
-    const float2 nuv = sphere_to_oct_uv(normal);
+    float3 finalColor[NQ], fallbackColor[NQ];
+    float totalWeight[NQ], totalFallbackWeight[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        finalColor[q] = fallbackColor[q] = f3(0, 0, 0);
+        totalWeight[q] = totalFallbackWeight[q] = 0.0f;
+    }
+    const AtlasDiv by_cr(g.color_res), by_dr(g.depth_res);
+    const AtlasDiv by_u((uint32_t)(g.res[0] * g.res[1])), by_v((uint32_t)g.res[2]);
+    const float cscale = by_cr((float)(g.color_res - 2));
+    const float dscale = by_dr((float)(g.depth_res - 2));
 
 #pragma unroll 1
     for (int i = 0; i < 8; ++i) {
@@ -96,46 +125,64 @@ __device__ float3 sample_probes(float3 position, float3 normal, float3 toCamera,
         if (__ldg(states + lin) == 0) continue;
         float3 probePosition = grid_probe_pos(g, px, py, pz);
         float3 directionToProbe = norm3(probePosition - position);
-        float3 biasedDirectionToProbe = probePosition - biasedPosition;
-        float2 duv = sphere_to_oct_uv(-norm3(biasedDirectionToProbe));
         int tile = py * g.res[0] + px;
-        float cu = ((float)((int)g.color_res * tile + 1) / cr + cscale * nuv.x) / uvsx;
-        float cv = ((float)((int)g.color_res * pz + 1) / cr + cscale * nuv.y) / uvsy;
-        float du = ((float)((int)g.depth_res * tile + 1) / dr + dscale * duv.x) / uvsx;
-        float dv = ((float)((int)g.depth_res * pz + 1) / dr + dscale * duv.y) / uvsy;
+        const float ctile = by_cr((float)((int)g.color_res * tile + 1)), cpz = by_cr((float)((int)g.color_res * pz + 1));
+        const float dtile = by_dr((float)((int)g.depth_res * tile + 1)), dpz = by_dr((float)((int)g.depth_res * pz + 1));
         float3 tri = f3(ox ? alpha.x : 1.0f - alpha.x, oy ? alpha.y : 1.0f - alpha.y, oz ? alpha.z : 1.0f - alpha.z);
-        float weight = 1.0f;
-        float bfw = fmaxf(0.0001f, (dot3(directionToProbe, normal) + 1.0f) * 0.5f);
-        weight *= bfw * bfw + 0.2f;
-        float fallbackWeight = weight;
-        float depth[2];
-        bilinear<2>(at.depth, g.depth_w, g.depth_h, du, dv, depth);
-        float mean = depth[0];
-        float variance = fabsf(depth[0] * depth[0] - depth[1]);
-        float dist = len3(probePosition - biasedPosition);
-        float dm = fmaxf(dist - mean, 0.0001f);
-        float cheb = variance / (variance + dm * dm);
-        cheb = fmaxf(cheb * cheb * cheb, 0.0f);
-        weight *= (dist <= mean) ? 1.0f : cheb;
-        weight = fmaxf(0.000001f, weight);
-        const float crush = 0.2f;
-        if (weight < crush) weight *= weight * weight * (1.0f / (crush * crush));
         float triw = tri.x * tri.y * tri.z + 0.001f;
-        weight *= triw;
-        fallbackWeight *= triw;
-        float col[3];
-        bilinear<3>(at.color, g.color_w, g.color_h, cu, cv, col);
-        float3 color = f3(sqrtf(col[0]), sqrtf(col[1]), sqrtf(col[2]));
-        finalColor = finalColor + color * weight;
-        totalWeight += weight;
-        fallbackColor = fallbackColor + color * fallbackWeight;
-        totalFallbackWeight += fallbackWeight;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            float3 biasedDirectionToProbe = probePosition - biasedPosition[q];
+            float2 duv = sphere_to_oct_uv(-norm3(biasedDirectionToProbe));
+            float cu = by_u(ctile + cscale * nuv[q].x);
+            float cv = by_v(cpz + cscale * nuv[q].y);
+            float du = by_u(dtile + dscale * duv.x);
+            float dv = by_v(dpz + dscale * duv.y);
+            float weight = 1.0f;
+            float bfw = fmaxf(0.0001f, (dot3(directionToProbe, normal[q]) + 1.0f) * 0.5f);
+            weight *= bfw * bfw + 0.2f;
+            float fallbackWeight = weight;
+            float depth[2];
+            bilinear<2>(at.depth, g.depth_w, g.depth_h, du, dv, depth);
+            float mean = depth[0];
+            float variance = fabsf(depth[0] * depth[0] - depth[1]);
+            float dist = len3(probePosition - biasedPosition[q]);
+            float dm = fmaxf(dist - mean, 0.0001f);
+            float cheb = variance / (variance + dm * dm);
+            cheb = fmaxf(cheb * cheb * cheb, 0.0f);
+            weight *= (dist <= mean) ? 1.0f : cheb;
+            weight = fmaxf(0.000001f, weight);
+            const float crush = 0.2f;
+            if (weight < crush) weight *= weight * weight * (1.0f / (crush * crush));
+            weight *= triw;
+            fallbackWeight *= triw;
+            float col[3];
+            bilinear<3>(at.color, g.color_w, g.color_h, cu, cv, col);
+            float3 color = f3(sqrtf(col[0]), sqrtf(col[1]), sqrtf(col[2]));
+            finalColor[q] = finalColor[q] + color * weight;
+            totalWeight[q] += weight;
+            fallbackColor[q] = fallbackColor[q] + color * fallbackWeight;
+            totalFallbackWeight[q] += fallbackWeight;
+        }
     }
-    if (totalWeight > 1e-3f) finalColor = finalColor * (1.0f / totalWeight);
-    if (totalFallbackWeight > 1e-3f) fallbackColor = fallbackColor * (1.0f / totalFallbackWeight);
-    finalColor = finalColor * finalColor;
-    fallbackColor = fallbackColor * fallbackColor;
-    return mix3(fallbackColor, finalColor, 8.0f * clampf(totalWeight, 0.0f, 1.0f / 8.0f));
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        float3 fc = finalColor[q], fb = fallbackColor[q];
+        if (totalWeight[q] > 1e-3f) fc = fc * (1.0f / totalWeight[q]);
+        if (totalFallbackWeight[q] > 1e-3f) fb = fb * (1.0f / totalFallbackWeight[q]);
+        fc = fc * fc;
+        fb = fb * fb;
+        result[q] = mix3(fb, fc, 8.0f * clampf(totalWeight[q], 0.0f, 1.0f / 8.0f));
+    }
+}
+
+template <class AV>
+__device__ __forceinline__ float3 sample_probes(float3 position, float3 normal, float3 toCamera, const DeviceGrid& g,
+                                                const uint32_t* states, const AV& at) {
+    const float3 n[1] = {normal};
+    float3 r[1];
+    sample_probes_n<1>(position, n, toCamera, g, states, at, r);
+    return r[0];
 }
 
 // pbrMetallicRoughness (src/shaders/pbrMetallicRoughness.glsl:43-84)
@@ -241,10 +288,11 @@ __device__ __forceinline__ bool shade_surface(const DeviceScene& sc, const Devic
     float3 diffuseColor = albedo * (1.0f - 0.04f) * (1.0f - metal);
     float3 specularColor = mix3(f3(0.04f, 0.04f, 0.04f), albedo, metal);
     float3 reflectDir = dir - normal * (2.0f * dot3(normal, dir));
-    float3 reflection = sample_probes(position, reflectDir, -dir, g, states, at);
-    color = color + specularColor * reflection;
-    float3 indirect = sample_probes(position, normal, -dir, g, states, at);
-    color = color + indirect * diffuseColor;
+    const float3 lookups[2] = {reflectDir, normal};
+    float3 sampled[2];  // reflection, indirect
+    sample_probes_n<2>(position, lookups, -dir, g, states, at, sampled);
+    color = color + specularColor * sampled[0];
+    color = color + sampled[1] * diffuseColor;
     out->base = color;
     out->sun = pbr_metallic_roughness(normal, norm3(-dir), f3(L.color[0], L.color[1], L.color[2]),
                                       f3(L.dir[0], L.dir[1], L.dir[2]), albedo, metal, rough);

@@ -197,6 +197,14 @@ struct SplitStack {
     }
 };
 
+// World-space origin and direction of a walk: the top level needs only the
+// slab reciprocals besides them (its leaves are instances, never triangles),
+// recomputed when the walk leaves a mesh tree, which keeps nine values out of
+// the registers of the persistent kernels.
+struct WorldRay {
+    float3 o, d;
+};
+
 template <bool ANY, class Stack = SmemStack>
 struct WarpWalker {
     static constexpr bool kWide = false;
@@ -204,7 +212,8 @@ struct WarpWalker {
     // straggler exit of the search loop, 8 (64 registers, no spill) is 1.7 %
     // faster than 10 (48 registers, spilling); 9 (56) is level with 8
     static constexpr int kMinBlocks = 8;
-    Ray wr, r;  // world ray, current ray (world or object space)
+    WorldRay wr;  // world ray
+    Ray r;        // current ray (world or object space)
     Stack stk;
     int sp, cap, ref;
     bool in_blas;
@@ -222,8 +231,9 @@ struct WarpWalker {
     // Start at an explicit top-level root (several scenes in one node arena).
     __device__ __forceinline__ bool start_at(const DeviceScene& sc, int32_t root, float3 o, float3 d, float tmin_,
                                              float tmax_, uint32_t mask_) {
-        ray_setup(wr, o, d);
-        r = wr;
+        wr.o = o;
+        wr.d = d;
+        ray_setup(r, o, d);
         tmin = tmin_;
         tcur = tmax_;
         mask = mask_;
@@ -263,7 +273,9 @@ struct WarpWalker {
             ref = stk.get(--sp);
             if (ref != kExit) return true;
             in_blas = false;
-            r = wr;
+            r.o = wr.o;  // back at the top level
+            r.d = wr.d;
+            r.inv = ray_inv(wr.d);
         }
     }
 
