@@ -751,7 +751,7 @@ ddgi_status ddgi_batch_autotune(ddgi_batch* b, const float* orientations, uint32
     const uint32_t split_c[] = {0u, 32u, 24u, 16u};
     const uint32_t refill_c[] = {4u, 8u, 16u, 24u};
     const uint32_t ctas_c[] = {0u, 6u, 4u};
-    const uint32_t wait_c[] = {4u, 6u, 8u, 10u, 12u};
+    const uint32_t wait_c[] = {6u, 8u, 10u, 12u, 14u};
     for (int p = 0; p < 6 && err == DDGI_OK; ++p) {
         const uint32_t* cand = p == 0   ? width_c
                                : p == 1 ? rpw_c

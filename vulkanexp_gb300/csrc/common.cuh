@@ -49,7 +49,7 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 // instance in the top level).
 // Default of the traversals' straggler threshold: a warp leaves its
 // node-search loop once at most this many lanes still look for a first leaf.
-constexpr uint32_t kDefaultWait = 8;
+constexpr uint32_t kDefaultWait = 10;
 
 struct __align__(16) BvhNode {
     float4 a, b, c;

@@ -1512,7 +1512,7 @@ ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t re
     const uint32_t refill_c[] = {4u, 8u, 16u, 24u};
     const uint32_t split_c[] = {0u, 32u, 24u, 16u};
     const uint32_t ctas_c[] = {0u, 6u, 4u};
-    const uint32_t wait_c[] = {4u, 6u, 8u, 10u, 12u};
+    const uint32_t wait_c[] = {6u, 8u, 10u, 12u, 14u};
     for (int p = 0; p < 6 && err == DDGI_OK; ++p) {
         const uint32_t* cand = p == 0   ? width_c
                                : p == 1 ? wait_c

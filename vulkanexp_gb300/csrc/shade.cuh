@@ -64,17 +64,6 @@ __device__ __forceinline__ float3 grid_probe_pos(const DeviceGrid& g, int x, int
     return f3((float)x * g.cell[0] + g.mn[0], (float)y * g.cell[1] + g.mn[1], (float)z * g.cell[2] + g.mn[2]);
 }
 
-// x / n for a positive integer n, as the atlas coordinates divide: when n is
-// a power of two the quotient is exact and equals the product with 1 / n
-// (no rounding either way), which saves a division sequence.
-struct AtlasDiv {
-    float d, inv;
-    bool pow2;
-    __device__ __forceinline__ explicit AtlasDiv(uint32_t n)
-        : d((float)n), inv(1.0f / (float)n), pow2(n != 0u && (n & (n - 1u)) == 0u) {}
-    __device__ __forceinline__ float operator()(float x) const { return pow2 ? x * inv : x / d; }
-};
-
 // sampleProbes (src/shaders/irradiance.glsl:145-237) for NQ lookups at one
 // position that differ in the direction argument (`normal`): the closest-hit
 // program makes two (reflection and diffuse), which share the eight probes'
@@ -111,10 +100,10 @@ __device__ void sample_probes_n(float3 position, const float3 (&normal)[NQ], flo
         finalColor[q] = fallbackColor[q] = f3(0, 0, 0);
         totalWeight[q] = totalFallbackWeight[q] = 0.0f;
     }
-    const AtlasDiv by_cr(g.color_res), by_dr(g.depth_res);
-    const AtlasDiv by_u((uint32_t)(g.res[0] * g.res[1])), by_v((uint32_t)g.res[2]);
-    const float cscale = by_cr((float)(g.color_res - 2));
-    const float dscale = by_dr((float)(g.depth_res - 2));
+    const float uvsx = (float)(g.res[0] * g.res[1]), uvsy = (float)g.res[2];
+    const float cr = (float)g.color_res, dr = (float)g.depth_res;
+    const float cscale = (float)(g.color_res - 2) / cr;
+    const float dscale = (float)(g.depth_res - 2) / dr;
 
 #pragma unroll 1
     for (int i = 0; i < 8; ++i) {
@@ -126,18 +115,18 @@ __device__ void sample_probes_n(float3 position, const float3 (&normal)[NQ], flo
         float3 probePosition = grid_probe_pos(g, px, py, pz);
         float3 directionToProbe = norm3(probePosition - position);
         int tile = py * g.res[0] + px;
-        const float ctile = by_cr((float)((int)g.color_res * tile + 1)), cpz = by_cr((float)((int)g.color_res * pz + 1));
-        const float dtile = by_dr((float)((int)g.depth_res * tile + 1)), dpz = by_dr((float)((int)g.depth_res * pz + 1));
+        const float ctile = (float)((int)g.color_res * tile + 1) / cr, cpz = (float)((int)g.color_res * pz + 1) / cr;
+        const float dtile = (float)((int)g.depth_res * tile + 1) / dr, dpz = (float)((int)g.depth_res * pz + 1) / dr;
         float3 tri = f3(ox ? alpha.x : 1.0f - alpha.x, oy ? alpha.y : 1.0f - alpha.y, oz ? alpha.z : 1.0f - alpha.z);
         float triw = tri.x * tri.y * tri.z + 0.001f;
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
             float3 biasedDirectionToProbe = probePosition - biasedPosition[q];
             float2 duv = sphere_to_oct_uv(-norm3(biasedDirectionToProbe));
-            float cu = by_u(ctile + cscale * nuv[q].x);
-            float cv = by_v(cpz + cscale * nuv[q].y);
-            float du = by_u(dtile + dscale * duv.x);
-            float dv = by_v(dpz + dscale * duv.y);
+            float cu = (ctile + cscale * nuv[q].x) / uvsx;
+            float cv = (cpz + cscale * nuv[q].y) / uvsy;
+            float du = (dtile + dscale * duv.x) / uvsx;
+            float dv = (dpz + dscale * duv.y) / uvsy;
             float weight = 1.0f;
             float bfw = fmaxf(0.0001f, (dot3(directionToProbe, normal[q]) + 1.0f) * 0.5f);
             weight *= bfw * bfw + 0.2f;

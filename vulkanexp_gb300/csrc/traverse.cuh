@@ -209,8 +209,9 @@ template <bool ANY, class Stack = SmemStack>
 struct WarpWalker {
     static constexpr bool kWide = false;
     // resident 128-thread blocks per SM the kernels are built for: with the
-    // straggler exit of the search loop, 8 (64 registers, no spill) is 1.7 %
-    // faster than 10 (48 registers, spilling); 9 (56) is level with 8
+    // straggler exit of the search loop, 8 is 1.7 % faster than 10 (48
+    // registers, spilling); the walker takes 56 registers, and 8 blocks of
+    // its shared-memory stack fill an SM's shared memory
     static constexpr int kMinBlocks = 8;
     WorldRay wr;  // world ray
     Ray r;        // current ray (world or object space)
