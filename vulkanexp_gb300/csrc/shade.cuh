@@ -54,6 +54,26 @@ struct DepthTexF16 {
     }
 };
 
+// Either form, chosen per lookup at run time (the batched kernels, whose
+// volumes may mix the forms): one copy of the shading code instead of one
+// per form.
+struct ColorTexDyn {
+    const void* p;
+    bool half;
+    __device__ __forceinline__ void fetch(size_t i, float* o) const {
+        if (half) ColorTexF16{static_cast<const uint2*>(p)}.fetch(i, o);
+        else ColorTexF32{static_cast<const float4*>(p)}.fetch(i, o);
+    }
+};
+struct DepthTexDyn {
+    const void* p;
+    bool half;
+    __device__ __forceinline__ void fetch(size_t i, float* o) const {
+        if (half) DepthTexF16{static_cast<const uint32_t*>(p)}.fetch(i, o);
+        else DepthTexF32{static_cast<const float2*>(p)}.fetch(i, o);
+    }
+};
+
 template <class CT, class DT>
 struct AtlasView {
     CT color;

@@ -462,17 +462,9 @@ __global__ void __launch_bounds__(128, 8) k_batch_shade_front(BatchTables bt, Wa
         const float4 d4 = __ldg(bt.dirs + vol.dir_base + ray);
         const float3 d = f3(d4.x, d4.y, d4.z);
         const float3 o = probe_origin_exact(vol.g, slot);
-        if (vol.fp16) {
-            AtlasView<ColorTexF16, DepthTexF16> at{{static_cast<const uint2*>(vol.color)},
-                                                   {static_cast<const uint32_t*>(vol.depth)}};
-            enqueue = shade_surface(vol.sc, vol.g, vol.L, vol.states, at, o, d, th.x, th.y, th.z, inst, prim, &s,
-                                    bt.err);
-        } else {
-            AtlasView<ColorTexF32, DepthTexF32> at{{static_cast<const float4*>(vol.color)},
-                                                   {static_cast<const float2*>(vol.depth)}};
-            enqueue = shade_surface(vol.sc, vol.g, vol.L, vol.states, at, o, d, th.x, th.y, th.z, inst, prim, &s,
-                                    bt.err);
-        }
+        const bool half = vol.fp16 != 0;
+        AtlasView<ColorTexDyn, DepthTexDyn> at{{vol.color, half}, {vol.depth, half}};
+        enqueue = shade_surface(vol.sc, vol.g, vol.L, vol.states, at, o, d, th.x, th.y, th.z, inst, prim, &s, bt.err);
         rays_out[i] = make_float4(s.base.x, s.base.y, s.base.z, th.x);
     }
     const uint32_t qk = warp_append(enqueue, q.count);
