@@ -5,6 +5,7 @@
 * the SAH tree builder (vulkanexp_gb300/csrc/sah.cu) through a structural
   check (tests/native/sah_check.cu) over random, coincident, flat and
   NaN/infinite primitive boxes, every leaf size;
+* the REPEAT texel-index wrap of the atlas lookups (tests/native/wrap_check.cu);
 * the CPU checker (oracle/ddgi_oracle.cpp) on a small room: trace, update
   (FP32 and FP64), probe classification and final gather, loaded into a
   Python process with the ASan runtime preloaded.
@@ -79,6 +80,29 @@ def test_spatial_split_builder_under_sanitizers(tmp_path):
     subprocess.check_call(["g++", "-fsanitize=address", "-fsanitize=undefined"] + objs +
                           ["-L" + cudart, "-lcudart_static", "-ldl", "-lrt", "-pthread", "-o", exe])
     r = subprocess.run([exe], capture_output=True, text=True, env=dict(os.environ, **ENV), timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "all ok" in r.stdout
+
+
+def test_texel_wrap_under_sanitizers(tmp_path):
+    """tests/native/wrap_check.cu: the REPEAT texel-index wrap of the atlas
+    lookups equals the remainder form for every index it can get."""
+    from vulkanexp_gb300 import build
+
+    nvcc = build.nvcc()
+    if not (os.path.exists(nvcc) or _have(nvcc)) or _runtime("libasan.so") is None:
+        pytest.skip("nvcc or the ASan runtime is missing")
+    flags = ["-std=c++17"] + build.ARCH + ["--expt-relaxed-constexpr"]
+    for f in SAN[:4]:
+        flags += ["-Xcompiler", f]
+    flags += ["-g", "-O1"]
+    o = str(tmp_path / "wrap_check.o")
+    subprocess.check_call([nvcc] + flags + ["-c", os.path.join(ROOT, "tests/native/wrap_check.cu"), "-o", o])
+    exe = str(tmp_path / "wrap_check")
+    cudart = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "lib64")
+    subprocess.check_call(["g++", "-fsanitize=address", "-fsanitize=undefined", o,
+                           "-L" + cudart, "-lcudart_static", "-ldl", "-lrt", "-pthread", "-o", exe])
+    r = subprocess.run([exe], capture_output=True, text=True, env=dict(os.environ, **ENV), timeout=300)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
     assert "all ok" in r.stdout
 

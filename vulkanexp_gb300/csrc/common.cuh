@@ -329,7 +329,7 @@ __host__ __device__ __forceinline__ float texel_scale(uint32_t n) {
 // coordinates in [-0.5, 1.5] give indices in [-n, 2n), which one add or
 // subtract brings into range; anything else takes the remainder (the same
 // integer either way, without a division on the common path).
-__device__ __forceinline__ int wrap_repeat(int i, int n) {
+__host__ __device__ __forceinline__ int wrap_repeat(int i, int n) {
     if (i < 0) i += n;
     else if (i >= n) i -= n;
     if ((unsigned)i >= (unsigned)n) i = ((i % n) + n) % n;
