@@ -223,7 +223,8 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
         uint32_t oor = 0;
         if (pl < np) {
             const float4* pr = a.rays + (size_t)(p0 + pl) * R;
-            for (uint32_t r = lane; r < R; r += 32) {
+#pragma unroll 8
+            for (uint32_t r = lane; r < R; r += 32) {  // unrolled: eight loads in flight per lane
                 float4 v = pr[r];
                 mx = fmaxf(mx, fmaxf(v.x, fmaxf(v.y, v.z)));
                 if (v.w < 0.0f || v.w > cell) ++oor;
@@ -245,6 +246,13 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
     bool ok = true;
     uint32_t phase = 0;
     for (uint32_t c = 0; c < a.nchunks; ++c) {
+        {   // B: this chunk of both weight matrices, copied while A is built
+            // (the previous chunk's MMAs have completed: its wait ended the
+            // last iteration)
+            const uint4* src = a.wchunks + (size_t)c * chunk16;
+            uint4* dst = reinterpret_cast<uint4*>(sB);
+            for (uint32_t i = tid; i < chunk16; i += kThreads) tc::cp_async16(dst + i, src + i);
+        }
         {   // A: thread = (probe, group of 8 rays); one 16-byte core-matrix row per operand row
             const uint32_t pl = (uint32_t)tid >> 3, j = (uint32_t)tid & 7u;
             const float inv = 1.0f / s_max[pl];  // a power of two: exact
@@ -288,11 +296,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
                 *reinterpret_cast<uint4*>(ad + canon_off(pl * 4 + 3, j)) = z;
             }
         }
-        {   // B: this chunk of both weight matrices
-            const uint4* src = a.wchunks + (size_t)c * chunk16;
-            uint4* dst = reinterpret_cast<uint4*>(sB);
-            for (uint32_t i = tid; i < chunk16; i += kThreads) dst[i] = src[i];
-        }
+        tc::cp_async_wait_all();
         tc::fence_proxy_async();
         __syncthreads();
         if (tid == 0 && !a.stall) {
