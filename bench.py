@@ -43,6 +43,20 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, device):
+    """The largest value of x over the ranks of the default process group
+    (the slowest replica's time); x itself when there is no group or one
+    rank."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -466,10 +480,7 @@ def main():
     clocks = sampler.stop()
     head = forms["wavefront_bf16"]
     ms = head["ms_per_update"]
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, "cuda")
     value = world * P * R / (ms * 1e-3) / 1e9
 
     # e2e through the host-buffer API: the step's ray table up, both atlases
@@ -488,7 +499,8 @@ def main():
         ctx.get_atlas_raw(abi.ATLAS_COLOR, host_c, stream)
         ctx.get_atlas_raw(abi.ATLAS_DEPTH, host_d, stream)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_val = world * P * R / (np.mean(e2e_ms) * 1e-3) / 1e9
+    e2e_mean = max_over_ranks(float(np.mean(e2e_ms)), "cuda")
+    e2e_val = world * P * R / (e2e_mean * 1e-3) / 1e9
 
     # rooflines: the dominant kernel (primary traversal, L1/L2-resident node
     # fetches counted per launch) and the tensor-core blend
@@ -526,7 +538,7 @@ def main():
             # per update: k_primary, k_shade_classify, k_shade_front, k_shadow, k_tc_weights, k_blend_tc
             "gpu_launches": 6 * args.steps, "clocks": clocks, "roofline": roofline,
             "roofline_blend": roofline_blend,
-            "e2e": {"value": e2e_val, "unit": UNIT, "ms_per_step": float(np.mean(e2e_ms)),
+            "e2e": {"value": e2e_val, "unit": UNIT, "ms_per_step": e2e_mean,
                     "h2d_bytes_per_step": R * 20, "d2h_bytes_per_step": int(host_c.nbytes + host_d.nbytes)},
             # sanity of the last e2e step's result as read back
             "atlas_finite": bool(np.isfinite(host_c).all() and np.isfinite(host_d).all())}

@@ -54,3 +54,33 @@ def test_reference_arm_two_ranks_rank0_only():
     lines = _lines(r.stdout)
     assert len(lines) == 1, r.stdout[-2000:]
     _check_line(lines[0], 2)
+
+
+RANKS_SCRIPT = """
+import os, sys
+sys.path.insert(0, {root!r})
+import torch.distributed as dist
+import bench
+dist.init_process_group("gloo")
+r = dist.get_rank()
+with open(os.path.join({out!r}, "rank%d.txt" % r), "w") as f:  # one file per rank: no interleaved output
+    f.write("rank %d max %.3f single %.3f" % (r, bench.max_over_ranks(1.5 + r, "cpu"), 1.5 + r))
+dist.destroy_process_group()
+"""
+
+
+def test_max_over_ranks_two_gloo_ranks(tmp_path):
+    """The replicas' timing reduction (the slowest rank's time) over two
+    gloo ranks on the CPU; without a process group it is the identity."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.max_over_ranks(3.25, "cpu") == 3.25
+    script = tmp_path / "ranks.py"
+    script.write_text(RANKS_SCRIPT.format(root=ROOT, out=str(tmp_path)))
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
+           "127.0.0.1", "--master-port", str(_free_port()), str(script)]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-3000:]
+    got = [(tmp_path / ("rank%d.txt" % k)).read_text() for k in range(2)]
+    assert got == ["rank 0 max 2.500 single 1.500", "rank 1 max 2.500 single 2.500"], r.stdout
