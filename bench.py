@@ -151,6 +151,57 @@ def cpu_baseline(w, sample_probes, threads=None, oracle=None, orientation=0):
             "ms_per_update_extrapolated": dt * 1e3 * P / n}
 
 
+def measure_fp64_error(w, updates, stream, threads=None):
+    """Atlas error of the GPU forms against the FP64 oracle on the full
+    workload: the BF16 headline form and the FP32 wavefront form each run
+    `updates` successive updates from a zero atlas with the same rotations as
+    the FP64 restatement of the reference's update (its shading and blend in
+    double; geometry in FP32, so its hit set is the GPU's).  Per texel
+    relative error |gpu - fp64| / max(|fp64|, 1e-2) over every texel of both
+    atlases (colour RGB, depth mean and mean square), max and RMS; closest-hit
+    IDs of every ray of every update compared with the oracle's.  Rank 0 only,
+    outside every timed region."""
+    from oracle.oracle import Oracle, zero_atlas
+    from vulkanexp_gb300 import abi
+
+    floor = 1e-2
+    P = w.grid.probe_count()
+    t0 = time.perf_counter()
+    o = Oracle(w.scene, threads=threads or os.cpu_count())
+    c64, d64 = zero_atlas(w.grid, fp64=True)
+    st64 = np.ones(P, np.uint32)
+    ctxs = {}
+    for name, prec in (("bf16", abi.PRECISION_BF16), ("fp32", abi.PRECISION_FP32)):
+        ctx, _ = build_context(w, prec, abi.PIPELINE_WAVEFRONT, stream)
+        ctx.record_hits(True)
+        ctxs[name] = ctx
+    mism = {k: 0 for k in ctxs}
+    for k in range(updates):
+        _, hits = o.update(w.grid, w.light, w.orientation(k), c64, d64, st64, fp64=True, want_hits=True)
+        for name, ctx in ctxs.items():
+            ctx.update(w.orientation(k), stream=stream)
+            gh = ctx.get_hits(P, stream)
+            mism[name] += int(((gh["instance"] != hits["instance"]) | (gh["primitive"] != hits["primitive"])).sum())
+    out = {"updates": updates, "probes": P, "rays_compared": updates * P * w.grid.rays_per_probe,
+           "floor": floor, "oracle": "FP64 CPU restatement (double shading and blend, FP32 geometry)"}
+    for name, ctx in ctxs.items():
+        gc, gd = ctx.get_atlas(abi.ATLAS_COLOR, stream=stream), ctx.get_atlas(abi.ATLAS_DEPTH, stream=stream)
+        gs = ctx.get_probe_states(stream)
+        ctx.close()
+        ec = np.abs(gc[..., :3].astype(np.float64) - c64[..., :3]) / np.maximum(np.abs(c64[..., :3]), floor)
+        ed = np.abs(gd.astype(np.float64) - d64) / np.maximum(np.abs(d64), floor)
+        rec = {"color_max": float(ec.max()), "color_rms": float(np.sqrt((ec ** 2).mean())),
+               "depth_max": float(ed.max()), "depth_rms": float(np.sqrt((ed ** 2).mean())),
+               "hit_id_mismatches": mism[name], "probe_state_mismatches": int((gs != st64).sum())}
+        if name == "bf16":
+            out.update(rec)  # the headline form's numbers at the top
+        else:
+            out["fp32_wavefront"] = rec
+    o.close()
+    out["seconds"] = time.perf_counter() - t0
+    return out
+
+
 def run_reference(args, w):
     """The reference arm: the CPU restatement of the reference's probe-update
     shaders on all host cores (the reference itself is Vulkan/GLSL), each
@@ -176,20 +227,22 @@ def run_reference(args, w):
     line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(args.steps, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": config_dict(w, args), "cpu_baseline": cb,
+            "config": config_dict(w, args, "fp32"), "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "reference is Vulkan/GLSL (no graphics stack on this box); timed here is the C++ restatement "
                     "of its probe-update shaders on the host cores"}
     print(json.dumps(line), flush=True)
 
 
-def config_dict(w, args):
+def config_dict(w, args, precision="bf16"):
+    """Workload description; `precision` names the timed form ("bf16": FP32
+    trace, BF16 tensor-core blend, FP16 atlas; "fp32": the CPU restatement's
+    arithmetic)."""
     g = w.grid
     return {"workload": w.name, "probes": g.probe_count(), "grid": list(g.resolution), "rays_per_probe":
             g.rays_per_probe, "triangles": w.scene.triangle_count, "unique_triangles": w.scene.unique_triangle_count,
             "instances": int(len(w.scene.instances)), "color_res": g.color_res, "depth_res": g.depth_res,
-            "precision": "fp32" if g.precision == 0 else "bf16", "l2": "flushed (256 MB write) before each timed update",
-            "seed": w.seed}
+            "precision": precision, "l2": "flushed (256 MB write) before each timed update", "seed": w.seed}
 
 
 def build_context(w, precision, pipeline, stream):
@@ -414,6 +467,8 @@ def main():
     ap.add_argument("--ref-probes", type=int, default=4096,
                     help="probes per step of the reference arm's sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--err-updates", type=int, default=10,
+                    help="updates of the atlas-error check against the FP64 oracle (0: skip)")
     ap.add_argument("--only", default=None, choices=["batching"],
                     help="run one sub-measurement alone and print it")
     ap.add_argument("--headline-only", action="store_true",
@@ -478,9 +533,13 @@ def main():
         if name != "wavefront_bf16":
             ctx.close()
     clocks = sampler.stop()
+    # every per-form time is the slowest replica's
+    for f in forms.values():
+        f["ms_per_update"] = max_over_ranks(f["ms_per_update"], "cuda")
+        f["value"] = world * P * R / (f["ms_per_update"] * 1e-3) / 1e9
+        f["stage_ms"] = {k: max_over_ranks(v, "cuda") for k, v in f["stage_ms"].items()}
     head = forms["wavefront_bf16"]
     ms = head["ms_per_update"]
-    ms = max_over_ranks(ms, "cuda")
     value = world * P * R / (ms * 1e-3) / 1e9
 
     # e2e through the host-buffer API: the step's ray table up, both atlases
@@ -491,6 +550,8 @@ def main():
     host_c = torch.empty((ch, cw, cc), dtype=torch.float16, pin_memory=True).numpy()
     host_d = torch.empty((dh, dw, dc), dtype=torch.float16, pin_memory=True).numpy()
     e2e_ms = []
+    if world > 1:
+        torch.distributed.barrier()
     for k in range(max(args.steps, 1)):
         flush.fill_(k & 255)
         torch.cuda.synchronize()
@@ -534,7 +595,10 @@ def main():
             "config": config_dict(w, args), "impl": "ours",
             "form": "wavefront trace (persistent traversal) + BF16 tcgen05 blend, FP16 atlas",
             "forms": forms,
+            # against the reference-like fused FP32 form, and against the FP32
+            # wavefront form (same trees and traversal: the BF16 blend's own gain)
             "speedup_vs_plain_fp32": forms["plain_fp32"]["ms_per_update"] / head["ms_per_update"],
+            "speedup_vs_wavefront_fp32": forms["wavefront_fp32"]["ms_per_update"] / head["ms_per_update"],
             # per update: k_primary, k_shade_classify, k_shade_front, k_shadow, k_tc_weights, k_blend_tc
             "gpu_launches": 6 * args.steps, "clocks": clocks, "roofline": roofline,
             "roofline_blend": roofline_blend,
@@ -550,6 +614,8 @@ def main():
         line["batching"] = measure_batching(stream, args.steps, args.warmup, flush)
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not args.headline_only:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_probes)
+        if args.err_updates > 0:
+            line["atlas_err_vs_fp64"] = measure_fp64_error(w, args.err_updates, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -7,7 +7,10 @@
  * (src/shaders/traceProbes.rgen, closesthit.glsl with NO_REFLECTION,
  * miss.rmiss, shadow.rmiss, probesUpdate.glsl, probesCopyBorders.comp,
  * probesInit.rgen).  The driver-built Vulkan BLAS/TLAS
- * (src/Renderer.cpp:240-642) is replaced by an LBVH built on the GPU.
+ * (src/Renderer.cpp:240-642) is replaced by this library's own trees:
+ * surface-area-heuristic trees with spatial splits built on the host threads
+ * (the default, like the driver's PREFER_FAST_TRACE structures), or an LBVH
+ * built on the GPU (ddgi_set_build_mode), traversed by CUDA kernels.
  *
  * Conventions
  *  - Every entry point returns a ddgi_status and never throws.
@@ -238,9 +241,10 @@ ddgi_status ddgi_blend_records(ddgi_ctx* ctx, const float orientation[9], const 
  * error word; about 2 MB) is one fixed __device__ array that every GPU using
  * the library holds until the process exits; requests that would need more
  * (rays_per_probe x texel rows beyond 2 MB of weights, or interior tiles
- * above 16 x 16 texels) return DDGI_ERR_UNSUPPORTED.  The first call on a
- * device looks up that array's device address (cudaGetSymbolAddress) and
- * should therefore come before any stream capture.  All calls share the
+ * above 16 x 16 texels) return DDGI_ERR_UNSUPPORTED.  Every call looks up
+ * that array's device address in the caller's current context
+ * (cudaGetSymbolAddress, a host call) and should therefore not be made
+ * during a stream capture.  All calls share the
  * array, so calls that overlap on the GPU (other streams, other host threads)
  * race: serialise them.  Synchronous on `stream`; kernel-detected errors
  * (a probe index outside the grid) return DDGI_ERR_DEVICE. */

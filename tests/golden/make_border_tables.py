@@ -3,8 +3,8 @@ src/shaders/probesCopyBorders.comp:21-220 (irradianceCopiesDst/Src for 8x8
 colour tiles, depthCopiesDst/Src for 16x16 depth tiles) into
 border_tables.json.
 
-Run in a checkout where the reference sources are available:
-    python tests/golden/make_border_tables.py /root/reference
+Run with the root of a checkout of the reference sources as its argument:
+    python tests/golden/make_border_tables.py <reference checkout>
 """
 import json
 import os
@@ -24,7 +24,9 @@ def parse(path):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_border_tables.py <reference checkout>")
+    ref = sys.argv[1]
     t = parse(os.path.join(ref, "src", "shaders", "probesCopyBorders.comp"))
     t["source"] = "src/shaders/probesCopyBorders.comp:21-220"
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "border_tables.json")

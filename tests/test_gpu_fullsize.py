@@ -1,0 +1,113 @@
+"""Parity at the sizes the benchmark times (GPU tests).
+
+* The FP32 wavefront form on the whole 32x16x32-probe, 256-ray terrain grid
+  (~1M unique triangles, 4097 instances) for three successive updates, so the
+  bounce lookup (sampleProbes into the previous, non-zero atlas) is checked
+  on every probe: hit IDs, distance and facing bit-identical; ray records and
+  atlas texels within 1e-4 relative (floor 1e-2); probe states exact.
+* The BF16 precision form (BF16 tensor-core blend with FP32 accumulation,
+  FP32 hysteresis accumulator, FP16 atlas) for ten updates against the FP64
+  oracle, on the room workload (8x8x8 probes, 128 rays) and on the terrain
+  workload: per-texel relative error at most 1e-3 (floor 1e-2), RMS at most
+  5e-4, hit IDs bit-identical on every update.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle.oracle import Oracle, zero_atlas
+from vulkanexp_gb300 import abi, scenes
+from vulkanexp_gb300.ddgi import Context
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+FLOOR = 1e-2
+BF16_MAX = 1e-3
+BF16_RMS = 5e-4
+
+
+def make_ctx(w, precision):
+    g = w.grid.copy()
+    g.precision = precision
+    ctx = Context(g)
+    ctx.set_pipeline(abi.PIPELINE_WAVEFRONT)
+    ctx.build_scene(w.scene)
+    ctx.set_light(w.light)
+    ctx.record_hits(True)
+    return ctx
+
+
+def hit_mismatches(gh, oh):
+    return int(((gh["instance"] != oh["instance"]) | (gh["primitive"] != oh["primitive"])).sum())
+
+
+@pytest.fixture(scope="module")
+def terrain():
+    return scenes.workload(1)
+
+
+@pytest.fixture(scope="module")
+def terrain_oracle(terrain):
+    o = Oracle(terrain.scene)
+    yield o
+    o.close()
+
+
+def test_terrain_full_grid_fp32_three_updates(gpu_lib, terrain, terrain_oracle):
+    w = terrain
+    P = w.grid.probe_count()
+    ctx = make_ctx(w, abi.PRECISION_FP32)
+    c, d = zero_atlas(w.grid)
+    st = np.ones(P, np.uint32)
+    for k in range(3):
+        ctx.update(w.orientation(k))
+        rays, hits = terrain_oracle.update(w.grid, w.light, w.orientation(k), c, d, st, want_rays=True,
+                                           want_hits=True)
+        gh = ctx.get_hits(P)
+        assert hit_mismatches(gh, hits) == 0, "update %d" % k
+        hit = hits["instance"] != abi.MISS
+        assert (gh["t"][hit].view(np.uint32) == hits["t"][hit].view(np.uint32)).all(), "update %d: t" % k
+        assert (gh["backface"][hit] == hits["backface"][hit]).all()
+        er = rel_err(ctx.get_ray_records(P), rays, FLOOR).max()
+        assert er <= TOL, "ray records, update %d: %g" % (k, er)
+        ec = rel_err(ctx.get_atlas(abi.ATLAS_COLOR), c, FLOOR).max()
+        ed = rel_err(ctx.get_atlas(abi.ATLAS_DEPTH), d, FLOOR).max()
+        print("terrain fp32 update %d: records %.2e colour %.2e depth %.2e" % (k, er, ec, ed))
+        assert ec <= TOL and ed <= TOL, "atlas, update %d" % k
+        assert (ctx.get_probe_states() == st).all()
+    ctx.close()
+
+
+def bf16_ten_updates(w, oracle):
+    P = w.grid.probe_count()
+    ctx = make_ctx(w, abi.PRECISION_BF16)
+    c, d = zero_atlas(w.grid, fp64=True)
+    st = np.ones(P, np.uint32)
+    for k in range(10):
+        ctx.update(w.orientation(k))
+        _, hits = oracle.update(w.grid, w.light, w.orientation(k), c, d, st, fp64=True, want_hits=True)
+        assert hit_mismatches(ctx.get_hits(P), hits) == 0, "update %d" % k
+    ec = rel_err(ctx.get_atlas(abi.ATLAS_COLOR)[..., :3], c[..., :3], FLOOR)
+    ed = rel_err(ctx.get_atlas(abi.ATLAS_DEPTH), d, FLOOR)
+    ctx.close()
+    r = {"color_max": ec.max(), "color_rms": np.sqrt((ec ** 2).mean()), "depth_max": ed.max(),
+         "depth_rms": np.sqrt((ed ** 2).mean())}
+    print("%s bf16 after 10 updates vs fp64: %s" % (w.name, {k: "%.2e" % v for k, v in r.items()}))
+    return r
+
+
+def check_bf16(r):
+    assert r["color_max"] <= BF16_MAX and r["depth_max"] <= BF16_MAX, r
+    assert r["color_rms"] <= BF16_RMS and r["depth_rms"] <= BF16_RMS, r
+
+
+def test_bf16_room_ten_updates_vs_fp64(gpu_lib):
+    w = scenes.workload(0)
+    o = Oracle(w.scene)
+    check_bf16(bf16_ten_updates(w, o))
+    o.close()
+
+
+def test_bf16_terrain_ten_updates_vs_fp64(gpu_lib, terrain, terrain_oracle):
+    check_bf16(bf16_ten_updates(terrain, terrain_oracle))

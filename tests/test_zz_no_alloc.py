@@ -45,16 +45,23 @@ def call_noalloc(lib, grid, orientation, d_list, n, d_rec, d_states, d_color, d_
                                           C.c_void_p(d_acc_c), C.c_void_p(d_acc_d), C.c_void_p(stream))
 
 
-def test_noalloc_blend_matches_context_blend(gpu_lib):
+@pytest.mark.parametrize("rays,color_res,depth_res,use_list", [
+    (256, 8, 16, True),
+    # the largest request the fixed scratch takes: 1024 rays x (256 + 256)
+    # texel rows = exactly 2 MB of weights, every probe (no list)
+    (1024, 18, 18, False),
+])
+def test_noalloc_blend_matches_context_blend(gpu_lib, rays, color_res, depth_res, use_list):
     import torch
 
-    g = abi.make_grid((0, 0, 0), (10, 6, 8), (6, 4, 5), 256, hysteresis=0.9, depth_sharpness=50.0,
-                      precision=abi.PRECISION_BF16)
+    g = abi.make_grid((0, 0, 0), (10, 6, 8), (6, 4, 5), rays, color_res=color_res, depth_res=depth_res,
+                      hysteresis=0.9, depth_sharpness=50.0, precision=abi.PRECISION_BF16)
     P, R = g.probe_count(), g.rays_per_probe
     cell = float(np.linalg.norm([(g.extent_max[k] - g.extent_min[k]) / (g.resolution[k] - 1) for k in range(3)]))
-    rng = np.random.default_rng(99)
-    plist = rng.permutation(P)[: P - 7].astype(np.uint32)
-    recs = [records(rng, len(plist), R, cell) for _ in range(2)]
+    rng = np.random.default_rng(99 + rays)
+    plist = rng.permutation(P)[: P - 7].astype(np.uint32) if use_list else None
+    n = P if plist is None else len(plist)
+    recs = [records(rng, n, R, cell) for _ in range(2)]
     orients = [scenes.random_orientation(31, k) for k in range(2)]
 
     # the existing entry point (a context that allocated its buffers)
@@ -75,13 +82,14 @@ def test_noalloc_blend_matches_context_blend(gpu_lib):
     acc_c = torch.zeros((ch, cw, 4), dtype=torch.float32, device=dev)
     acc_d = torch.zeros((dh, dw, 2), dtype=torch.float32, device=dev)
     states = torch.ones(P, dtype=torch.int32, device=dev)
-    d_list = torch.from_numpy(plist.view(np.int32)).to(dev)
+    d_list = torch.from_numpy(plist.view(np.int32)).to(dev) if plist is not None else None
     lib = load_library()
     stream = torch.cuda.current_stream().cuda_stream
     for k in range(2):
         d_rec = torch.from_numpy(recs[k]).to(dev)
         torch.cuda.synchronize()
-        st = call_noalloc(lib, g, orients[k], d_list.data_ptr(), len(plist), d_rec.data_ptr(), states.data_ptr(),
+        st = call_noalloc(lib, g, orients[k], d_list.data_ptr() if d_list is not None else 0, n, d_rec.data_ptr(),
+                          states.data_ptr(),
                           color.data_ptr(), depth.data_ptr(), acc_c.data_ptr(), acc_d.data_ptr(), stream)
         assert st == 0, abi.STATUS_NAMES.get(st, st)
     torch.cuda.synchronize()
@@ -95,10 +103,12 @@ def test_noalloc_blend_matches_context_blend(gpu_lib):
 def test_noalloc_rejects_requests_beyond_its_scratch(gpu_lib):
     lib = load_library()
     eye = np.eye(3, dtype=np.float32)
-    # interior depth tiles above 16 x 16 texels do not fit the fixed scratch
-    g = abi.make_grid((0, 0, 0), (1, 1, 1), (2, 2, 2), 64, color_res=8, depth_res=20,
-                      precision=abi.PRECISION_BF16)
-    st = call_noalloc(lib, g, eye, 0, 8, 1, 1, 1, 1, 1, 1, 0)
-    assert st == 7  # DDGI_ERR_UNSUPPORTED, before touching any pointer
+    # interior tiles above 16 x 16 texels do not fit the fixed scratch, also
+    # at the largest ray count (one step above the largest accepted request)
+    for rays, cres, dres in ((64, 8, 20), (1024, 18, 19), (1024, 19, 18)):
+        g = abi.make_grid((0, 0, 0), (1, 1, 1), (2, 2, 2), rays, color_res=cres, depth_res=dres,
+                          precision=abi.PRECISION_BF16)
+        st = call_noalloc(lib, g, eye, 0, 8, 1, 1, 1, 1, 1, 1, 0)
+        assert st == 7  # DDGI_ERR_UNSUPPORTED, before touching any pointer
     g = abi.make_grid((0, 0, 0), (1, 1, 1), (1, 2, 2), 64, precision=abi.PRECISION_BF16)
     assert call_noalloc(lib, g, eye, 0, 8, 1, 1, 1, 1, 1, 1, 0) == 1  # invalid grid

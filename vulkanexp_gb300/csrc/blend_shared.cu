@@ -274,21 +274,14 @@ size_t fp32_weight_bytes(uint32_t rays, uint32_t color_res, uint32_t depth_res) 
 
 uint32_t fp32_shared_tiles(uint32_t nprobes) { return (nprobes + kProbesPerBlock - 1) / kProbesPerBlock; }
 
-namespace {
-
-// Record staging of kProbesPerBlock probes at up to DDGI_MAX_RAYS_PER_PROBE rays.
+// Record staging of kProbesPerBlock probes at up to DDGI_MAX_RAYS_PER_PROBE
+// rays, on the current device.
 cudaError_t set_shared_smem_limit() {
-    static bool done = false;
-    if (done) return cudaSuccess;
     const int bytes = (int)(sizeof(float4) * kProbesPerBlock * DDGI_MAX_RAYS_PER_PROBE);
-    cudaError_t e = cudaFuncSetAttribute(k_blend_fp32_shared, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch_blend_fp32_shared, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess) done = true;
+    cudaError_t e = ensure_dynamic_smem(k_blend_fp32_shared, bytes);
+    if (e == cudaSuccess) e = ensure_dynamic_smem(k_batch_blend_fp32_shared, bytes);
     return e;
 }
-
-}  // namespace
 
 cudaError_t launch_blend_fp32_shared(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes,
                                      const float4* rays, const float4* dirs, float* W, float* wsum, uint32_t* states,

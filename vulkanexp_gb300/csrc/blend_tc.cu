@@ -74,8 +74,13 @@ struct TcArgs {
 };
 
 // Limit of one tensor-core completion wait (the MMAs of a chunk take
-// microseconds).
+// microseconds).  The limits count global (wall-clock) time, so time the
+// CTA spends preempted or time-sliced with another context's work counts
+// too; the first limit is generous for that reason.  After it runs out the
+// CTA records the error and waits once more, up to kDrainLimitNs, for MMAs
+// that may still be in flight, before it releases its tensor memory.
 constexpr uint64_t kWaitLimitNs = 500ull * 1000 * 1000;
+constexpr uint64_t kDrainLimitNs = 4000ull * 1000 * 1000;
 
 // Byte offset of (row, 8-element K group) in a K-chunk operand.
 __host__ __device__ __forceinline__ uint32_t canon_off(uint32_t row, uint32_t kgroup) {
@@ -332,10 +337,12 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
     }
 
     if (!ok) {
-        // the MMAs did not complete in time: record it, give them one more
-        // bounded wait, then release the tensor memory
+        // the MMAs did not complete in time: record it, give them one more,
+        // longer bounded wait (a stall of the issuing thread means no MMA is
+        // in flight; a preempted CTA's MMAs finish once it runs again), then
+        // release the tensor memory: a CTA must not exit holding it
         if (tid == 0) raise_error(a.err, DEV_WAIT_TIMEOUT);
-        tc::mbar_wait(&s_bar, phase ^ 1u, kWaitLimitNs);
+        if (!a.stall) tc::mbar_wait(&s_bar, phase ^ 1u, kDrainLimitNs);  // the stall hook issued none
     } else {
         // epilogue 1: accumulators -> shared staging (the operand buffers are free now)
         float* S_c = reinterpret_cast<float*>(smem);                        // [32][nc*nc][3]
@@ -550,13 +557,10 @@ __global__ void __launch_bounds__(kThreads) k_batch_blend_tc(BatchTables bt, Bat
     }
 }
 
+// Shared-memory limit of both blend kernels on the current device.
 cudaError_t set_tc_smem_limit() {
-    static bool done = false;
-    if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_blend_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch_blend_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e == cudaSuccess) done = true;
+    cudaError_t e = ensure_dynamic_smem(k_blend_tc, 200 * 1024);
+    if (e == cudaSuccess) e = ensure_dynamic_smem(k_batch_blend_tc, 200 * 1024);
     return e;
 }
 
@@ -617,7 +621,10 @@ cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uin
 
 uint32_t tc_tiles(uint32_t nprobes) { return (nprobes + kTileProbes - 1) / kTileProbes; }
 
-cudaError_t prepare_batch_kernels() { return set_tc_smem_limit(); }
+cudaError_t prepare_batch_kernels() {
+    cudaError_t e = set_tc_smem_limit();
+    return e == cudaSuccess ? set_shared_smem_limit() : e;
+}
 
 size_t batch_tc_smem(uint32_t color_res, uint32_t depth_res) {
     const uint32_t nc = color_res - 2, nd = depth_res - 2;

@@ -8,6 +8,20 @@
 
 namespace ddgi {
 
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` on the
+// current device.  The limit belongs to the device's context, so it is read
+// back on every call (a microsecond, no stream work) rather than remembered
+// per process: a second GPU, or a context made again after a reset, starts
+// from the default limit.
+template <class K>
+inline cudaError_t ensure_dynamic_smem(K* kernel, int bytes) {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    if (fa.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 // trace.cu
 cudaError_t launch_trace_shade(const DeviceScene& sc, const DeviceGrid& g, const DeviceLight& L,
                                const uint32_t* probe_list, uint32_t nprobes, const float4* dirs,
@@ -177,6 +191,7 @@ cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uin
 // blend_shared.cu: FP32 blend with the weights computed once per update
 size_t fp32_weight_bytes(uint32_t rays, uint32_t color_res, uint32_t depth_res);
 uint32_t fp32_shared_tiles(uint32_t nprobes);
+cudaError_t set_shared_smem_limit();  // both shared-weight FP32 blend kernels, current device
 cudaError_t launch_blend_fp32_shared(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes,
                                      const float4* rays, const float4* dirs, float* W, float* wsum, uint32_t* states,
                                      float4* color, float2* depth, cudaStream_t st, const uint32_t* dev_count = nullptr);

@@ -14,7 +14,6 @@
 
 #include <cmath>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/ddgi.h"
 #include "../../include/ddgi_exact.h"
@@ -37,30 +36,21 @@ constexpr size_t kScratchBytes = kWeightsOff + kWeightsMax;
 
 __device__ __align__(256) static unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device, looked up once
-// per device (with that device current) and cached.
+// Device address of the scratch array in the caller's current context.
+// The address belongs to the CUDA context that loaded this library's module
+// on the current device, so it is looked up on every call instead of being
+// remembered: a context made again after cudaDeviceReset, or another device,
+// has its own copy of the array at its own address.  The lookup is a host
+// call with no stream work, cheap next to the synchronisation at the end of
+// the call.
 ddgi_status scratch_address(void** out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
         cudaGetLastError();
         return DDGI_ERR_CUDA;
     }
-    if (dev < 0 || dev >= kMaxDevices) return DDGI_ERR_UNSUPPORTED;
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            return DDGI_ERR_CUDA;
-        }
-        g_scratch_ptr[dev] = p;
-    }
-    *out = g_scratch_ptr[dev];
+    *out = p;
     return DDGI_OK;
 }
 
