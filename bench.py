@@ -153,7 +153,9 @@ def cpu_baseline(w, sample_probes, threads=None, oracle=None, orientation=0):
 
 def measure_fp64_error(w, updates, stream, threads=None):
     """Atlas error of the GPU forms against the FP64 oracle on the full
-    workload: the BF16 headline form and the FP32 wavefront form each run
+    workload: the BF16 headline form, the FP32 wavefront form and the
+    reference-format form (FP32 blend, texels stored rounded to the
+    reference's R11G11B10F / RG16F image formats) each run
     `updates` successive updates from a zero atlas with the same rotations as
     the FP64 restatement of the reference's update (its shading and blend in
     double; geometry in FP32, so its hit set is the GPU's).  Per texel
@@ -171,7 +173,8 @@ def measure_fp64_error(w, updates, stream, threads=None):
     c64, d64 = zero_atlas(w.grid, fp64=True)
     st64 = np.ones(P, np.uint32)
     ctxs = {}
-    for name, prec in (("bf16", abi.PRECISION_BF16), ("fp32", abi.PRECISION_FP32)):
+    for name, prec in (("bf16", abi.PRECISION_BF16), ("fp32", abi.PRECISION_FP32),
+                       ("reference_format", abi.PRECISION_REFERENCE_FORMAT)):
         ctx, _ = build_context(w, prec, abi.PIPELINE_WAVEFRONT, stream)
         ctx.record_hits(True)
         ctxs[name] = ctx
@@ -184,19 +187,27 @@ def measure_fp64_error(w, updates, stream, threads=None):
             mism[name] += int(((gh["instance"] != hits["instance"]) | (gh["primitive"] != hits["primitive"])).sum())
     out = {"updates": updates, "probes": P, "rays_compared": updates * P * w.grid.rays_per_probe,
            "floor": floor, "oracle": "FP64 CPU restatement (double shading and blend, FP32 geometry)"}
+    def err(a, b):
+        ec = np.abs(a[0][..., :3].astype(np.float64) - b[0][..., :3]) / np.maximum(np.abs(b[0][..., :3]), floor)
+        ed = np.abs(a[1].astype(np.float64) - b[1]) / np.maximum(np.abs(b[1]), floor)
+        return {"color_max": float(ec.max()), "color_rms": float(np.sqrt((ec ** 2).mean())),
+                "depth_max": float(ed.max()), "depth_rms": float(np.sqrt((ed ** 2).mean()))}
+
+    atl = {}
     for name, ctx in ctxs.items():
-        gc, gd = ctx.get_atlas(abi.ATLAS_COLOR, stream=stream), ctx.get_atlas(abi.ATLAS_DEPTH, stream=stream)
+        atl[name] = (ctx.get_atlas(abi.ATLAS_COLOR, stream=stream), ctx.get_atlas(abi.ATLAS_DEPTH, stream=stream))
         gs = ctx.get_probe_states(stream)
         ctx.close()
-        ec = np.abs(gc[..., :3].astype(np.float64) - c64[..., :3]) / np.maximum(np.abs(c64[..., :3]), floor)
-        ed = np.abs(gd.astype(np.float64) - d64) / np.maximum(np.abs(d64), floor)
-        rec = {"color_max": float(ec.max()), "color_rms": float(np.sqrt((ec ** 2).mean())),
-               "depth_max": float(ed.max()), "depth_rms": float(np.sqrt((ed ** 2).mean())),
-               "hit_id_mismatches": mism[name], "probe_state_mismatches": int((gs != st64).sum())}
+        rec = err(atl[name], (c64, d64))
+        rec.update(hit_id_mismatches=mism[name], probe_state_mismatches=int((gs != st64).sum()))
         if name == "bf16":
             out.update(rec)  # the headline form's numbers at the top
         else:
-            out["fp32_wavefront"] = rec
+            out[{"fp32": "fp32_wavefront", "reference_format": "reference_format"}[name]] = rec
+    # how far the FP32 and BF16 forms drift from the reference-format form
+    # (the atlas the reference's R11G11B10F / RG16F images would hold)
+    out["drift_from_reference_format"] = {"fp32_wavefront": err(atl["fp32"], atl["reference_format"]),
+                                          "bf16": err(atl["bf16"], atl["reference_format"])}
     o.close()
     out["seconds"] = time.perf_counter() - t0
     return out

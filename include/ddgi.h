@@ -48,7 +48,14 @@ typedef enum ddgi_status {
 /* Blend precision of ddgi_update. */
 typedef enum ddgi_precision {
     DDGI_PRECISION_FP32 = 0, /* plain form: FP32 SIMT blend, FP32 atlas */
-    DDGI_PRECISION_BF16 = 1  /* tcgen05 BF16 contraction, FP32 accumulate, FP16 atlas */
+    DDGI_PRECISION_BF16 = 1, /* tcgen05 BF16 contraction, FP32 accumulate, FP16 atlas */
+    /* FP32 blend whose stored texels are rounded to the reference's atlas image
+     * formats (src/IrradianceProbes.cpp:41, 63): irradiance as
+     * B10G11R11_UFLOAT (11-bit red/green, 10-bit blue unsigned floats; alpha
+     * reads 1), depth as R16G16_SFLOAT; round to nearest even
+     * (ddgi_round_r11/b10/half in ddgi_exact.h).  Texels are kept in the FP32
+     * atlas arrays (each stored value is exactly representable in both). */
+    DDGI_PRECISION_REFERENCE_FORMAT = 2
 } ddgi_precision;
 
 /*
@@ -125,8 +132,9 @@ typedef struct ddgi_instance {
 } ddgi_instance;
 
 /* LightBuffer (src/Light.hpp:6-9): direction points TOWARDS the sun,
- * color.rgb is the sun radiance.  sky.rgb is the constant radiance returned on
- * a miss (replacing the atmospheric sky of src/shaders/sky.glsl). */
+ * color.rgb is the sun radiance, color.a the sun brightness factor the
+ * atmospheric sky multiplies it by (miss.rmiss:22).  sky.rgb is the constant
+ * radiance returned on a miss in the default sky mode (ddgi_set_sky_mode). */
 typedef struct ddgi_light {
     float direction[4];
     float color[4];
@@ -197,6 +205,33 @@ ddgi_status ddgi_destroy(ddgi_ctx* ctx);
  * and precision.  Resolution, colorRes and depthRes must not change. */
 ddgi_status ddgi_set_grid(ddgi_ctx* ctx, const ddgi_grid_desc* grid);
 ddgi_status ddgi_get_grid(const ddgi_ctx* ctx, ddgi_grid_desc* out);
+
+/* IrradianceProbes::TargetHysteresis (src/IrradianceProbes.hpp:46) and the
+ * hysteresis ramp of IrradianceProbes::update (src/IrradianceProbes.cpp:
+ * 462-476).  target in [0, 1] switches the ramp on (or changes its target);
+ * a negative target switches it off, so the grid's hysteresis is blended as
+ * given (the default).  A ramp switched on starts from the grid's hysteresis
+ * (GridParameters.hysteresis) with no probes counted.  Every ddgi_update and
+ * ddgi_update_scheduled then runs the reference's step on the device before
+ * its blend: once a full grid's worth of probes has been refreshed since the
+ * last step, the value is either uploaded and then moved a tenth of the way
+ * to the target (the reference calls updateUniforms() before the increment,
+ * so the blend sees each value one step late) or, within 0.05 of the
+ * target, set to the target and uploaded; then the update's probe count is
+ * added (for ddgi_update_scheduled, the count selected on the device: no
+ * readback).  ddgi_set_grid (updateUniforms) resets both the blended and the
+ * host-side value to the new grid's hysteresis; ddgi_init_probes zeroes the
+ * host-side value.  The reference keeps the probe counter in a function-static
+ * variable shared by every instance; here each context has its own.  Takes
+ * effect from the next update on. */
+ddgi_status ddgi_set_target_hysteresis(ddgi_ctx* ctx, float target);
+/* The ramp's state after the work queued on `stream` (synchronous): the
+ * hysteresis the last update blended with (the reference's uniform buffer
+ * value), the host-side GridParameters.hysteresis and the probes counted
+ * since the last step.  With the ramp off both values are the grid's and the
+ * count is 0.  Any pointer may be NULL. */
+ddgi_status ddgi_get_hysteresis(ddgi_ctx* ctx, float* blended, float* parameter, uint32_t* counted,
+                                ddgi_stream stream);
 uint32_t ddgi_probe_count(const ddgi_ctx* ctx);
 
 /* Builds the bottom-level LBVHs (one per mesh) and the top-level LBVH over
@@ -207,6 +242,19 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* scene, ddgi_s
 /* IrradianceProbes::setLightBuffer / writeLightDescriptor
  * (src/IrradianceProbes.cpp:323-336). */
 ddgi_status ddgi_set_light(ddgi_ctx* ctx, const ddgi_light* light);
+
+/* Radiance of probe rays that miss the scene (src/shaders/miss.rmiss:17-23). */
+typedef enum ddgi_sky_mode {
+    DDGI_SKY_CONSTANT = 0,  /* the light's sky.rgb (default) */
+    /* sky() of src/shaders/sky.glsl:60-127, single-scattering atmosphere seen
+     * from the ray origin along the ray, sun from the light's direction,
+     * color.rgb and color.a (showSun = true); the final gather's sky pixels
+     * use it with brightness 1 and the view direction in position.xyz
+     * (FinalGather.frag:56).  Not with ddgi_forward_record / ddgi_backward
+     * (the sky radiance is a parameter there) nor in a batch. */
+    DDGI_SKY_ATMOSPHERE = 1
+} ddgi_sky_mode;
+ddgi_status ddgi_set_sky_mode(ddgi_ctx* ctx, ddgi_sky_mode mode);
 
 /* IrradianceProbes::update (src/IrradianceProbes.cpp:426-594).
  * `orientation` is the row-major 3x3 rotation applied to the spherical
@@ -366,8 +414,10 @@ ddgi_status ddgi_update_instances(ddgi_ctx* ctx, const uint32_t* ids, const floa
  * back-face hits closer than |cell| becomes OFF (state 0, skipped by the
  * updates and by the bounce lookup), else a probe with such a hit within one
  * cell on every axis gets state 1 (refreshed every update), else 8.
- * Synchronous.  The reference also zeroes the grid hysteresis here for a
- * host-side ramp; this call leaves the grid unchanged. */
+ * Synchronous.  Like the reference (src/IrradianceProbes.cpp:357-358), it
+ * zeroes the hysteresis ramp's host-side value when the ramp is on
+ * (ddgi_set_target_hysteresis); the blended value and the grid stay as they
+ * are. */
 ddgi_status ddgi_init_probes(ddgi_ctx* ctx, const float orientation[9], ddgi_stream stream);
 /* ddgi_update over the probes selectProbesToUpdate
  * (src/IrradianceProbes.cpp:396-424) picks, chosen on the device with no

@@ -88,6 +88,76 @@ static inline int ddgi_affine_inverse(const float o2w[12], float w2o[12]) {
     return 1;
 }
 
+/*
+ * Storage rounding of the reference-format atlas (ddgi_precision
+ * DDGI_PRECISION_REFERENCE_FORMAT).  The reference keeps its irradiance atlas
+ * in VK_FORMAT_B10G11R11_UFLOAT_PACK32 images and its depth atlas in
+ * VK_FORMAT_R16G16_SFLOAT images (src/IrradianceProbes.cpp:41-63), so every
+ * texel it stores is rounded to those formats and the next update's bounce
+ * lookup reads the rounded values.  The functions below give the value a
+ * float becomes in such a format: 5-bit exponent (bias 15, subnormals below
+ * 2^-14), `mbits` stored mantissa bits (6 for the 11-bit red and green
+ * channels, 5 for the 10-bit blue channel, 10 for a half), rounding to
+ * nearest with ties to even, overflow (2^16 and above after rounding) to
+ * infinity; the unsigned 11/10-bit formats store negative values (and -0)
+ * as 0.  NaN stays NaN.  The same code runs on the host and in CUDA kernels.
+ */
+#if defined(__CUDACC__)
+#define DDGI_HD __host__ __device__
+#else
+#define DDGI_HD
+#endif
+
+DDGI_HD static inline uint32_t ddgi_float_bits(float f) {
+    union {
+        float f;
+        uint32_t u;
+    } v;
+    v.f = f;
+    return v.u;
+}
+
+DDGI_HD static inline float ddgi_bits_float(uint32_t u) {
+    union {
+        float f;
+        uint32_t u;
+    } v;
+    v.u = u;
+    return v.f;
+}
+
+DDGI_HD static inline float ddgi_round_small_float(float x, int mbits, int is_unsigned) {
+    const uint32_t u = ddgi_float_bits(x);
+    const uint32_t sign = u & 0x80000000u;
+    uint32_t a = u & 0x7fffffffu;
+    if (a >= 0x7f800000u) { /* infinity or NaN */
+        if (a > 0x7f800000u) return x;
+        return (is_unsigned && sign) ? 0.0f : x;
+    }
+    if (is_unsigned && sign) return 0.0f;
+    if (a < 0x38800000u) {
+        /* below 2^-14: multiples of 2^-(14 + mbits); the scalings are exact */
+        const float up = ddgi_bits_float((uint32_t)(127 + 14 + mbits) << 23);
+        const float down = ddgi_bits_float((uint32_t)(127 - 14 - mbits) << 23);
+        const float r = rintf(ddgi_bits_float(a) * up) * down;
+        a = ddgi_float_bits(r);
+    } else {
+        const int drop = 23 - mbits;
+        a += ((1u << (drop - 1)) - 1u) + ((a >> drop) & 1u);
+        a &= ~((1u << drop) - 1u);
+        if (a >= 0x47800000u) a = 0x7f800000u;
+    }
+    return ddgi_bits_float(a | sign);
+}
+
+/* One colour texel of the reference-format atlas: R and G as unsigned 11-bit
+ * floats, B as an unsigned 10-bit float (the format has no alpha; reads
+ * return 1). */
+DDGI_HD static inline float ddgi_round_r11(float x) { return ddgi_round_small_float(x, 6, 1); }
+DDGI_HD static inline float ddgi_round_b10(float x) { return ddgi_round_small_float(x, 5, 1); }
+/* One depth channel of the reference-format atlas (R16G16_SFLOAT). */
+DDGI_HD static inline float ddgi_round_half(float x) { return ddgi_round_small_float(x, 10, 0); }
+
 #ifdef __cplusplus
 }
 #endif

@@ -41,6 +41,13 @@
  *    all interior texels.
  *  - Texture filtering is exact bilinear (the hardware uses 8-bit weights).
  *  - pow(x, 3) and pow(x, 5) are evaluated as products.
+ *
+ * Atlas storage: the plain form keeps FP32 texels.  The reference-format form
+ * (grid precision DDGI_PRECISION_REFERENCE_FORMAT) rounds every stored texel
+ * to the formats of the reference's atlas images (B10G11R11 unsigned floats
+ * for irradiance, RG16F for depth: src/IrradianceProbes.cpp:41, 63) with
+ * ddgi_round_r11/b10/half of include/ddgi_exact.h, so its bounce lookup reads
+ * the same rounded values the reference's does.
  */
 #include <algorithm>
 #include <atomic>
@@ -419,6 +426,7 @@ struct Grid {
     int res[3];
     uint32_t rays, colorRes, depthRes;
     float sharp, hyst, bias;
+    bool quant;  // reference-format atlas: stores rounded to R11G11B10F / RG16F
     uint32_t count() const { return (uint32_t)res[0] * res[1] * res[2]; }
 };
 
@@ -433,8 +441,19 @@ Grid make_grid(const ddgi_grid_desc* g) {
     o.sharp = g->depth_sharpness;
     o.hyst = g->hysteresis;
     o.bias = g->shadow_bias;
+    o.quant = g->precision == DDGI_PRECISION_REFERENCE_FORMAT;
     return o;
 }
+
+// A stored atlas value of the reference-format form (IrradianceProbes.cpp:41,
+// 63): colour channel c rounded to the B10G11R11 unsigned float it becomes
+// in the reference's irradiance image, a depth channel to a half.  Double
+// values are first rounded to float, as a float32 shader value would be.
+template <class T> T round_color_store(T v, int c) {
+    float f = (float)v;
+    return T(c == 2 ? ddgi_round_b10(f) : ddgi_round_r11(f));
+}
+template <class T> T round_depth_store(T v) { return T(ddgi_round_half((float)v)); }
 
 inline void grid_index(uint32_t index, const Grid& g, int idx[3]) {  // :7-13
     idx[0] = (int)(index % (uint32_t)g.res[0]);
@@ -637,7 +656,107 @@ V3<T> pbr(V3<T> n, V3<T> v, V3<T> lightColor, V3<T> lightDir, V3<T> albedo, T me
 
 struct Light {
     F3 dir, color, sky;
+    float brightness = 1.0f;  // LightBuffer.color.a
 };
+
+// Miss radiance mode (oracle_set_sky_mode): 0 the constant sky radiance,
+// 1 the atmospheric sky of src/shaders/sky.glsl:60-127 (miss.rmiss:22).
+std::atomic<int> g_sky_mode{0};
+
+// sky() of src/shaders/sky.glsl:60-127 with showSun = true, in T; the
+// operation order follows the shader expression by expression.
+template <class T>
+V3<T> atmosphere(V3<T> rayOrigin, V3<T> rayDirection, V3<T> sunPosition, V3<T> sunColor, T brightness) {
+    const T inner = T(100000.0f), outer = T(2500.0f) + inner, avg = T(0.25f);
+    const T scale = T(1) / (outer - inner);
+    const V3<T> invWl(T(1) / T(std::pow(0.650f, 4.0f)), T(1) / T(std::pow(0.570f, 4.0f)),
+                      T(1) / T(std::pow(0.475f, 4.0f)));
+    const T pi = kPi<T>(), Kr = T(0.0025f), Km = T(0.0010f), g = T(-0.990f);
+    const T Kr4PI = Kr * T(4) * pi, Km4PI = Km * T(4) * pi;
+    auto scale_fn = [&](T c) {
+        T x = T(1) - c;
+        return avg * std::exp(T(-0.00287f) + x * (T(0.459f) + x * (T(3.83f) + x * (T(-6.80f) + x * T(5.25f)))));
+    };
+    auto outside = [&](T radius, V3<T> o, V3<T> d) {
+        T a = dot(d, d), b = dot(d, o), c = dot(o, o) - radius * radius;
+        T gg = b * b - a * c;
+        if (gg > T(0)) {
+            T dis = (-std::sqrt(gg) - b) / a;
+            if (dis > T(0)) return dis;
+        }
+        return T(-1);
+    };
+    auto inside = [&](T radius, V3<T> o, V3<T> d) {
+        V3<T> oc = -o;
+        T docdir = dot(oc, d);
+        V3<T> pc = o + d * docdir;
+        T lc = length(pc);
+        T dist = std::sqrt(radius * radius - lc * lc);
+        T lo = length(pc - o);
+        return docdir > T(0) ? dist - lo : dist + lo;
+    };
+    sunColor = sunColor * brightness;
+    V3<T> position = rayOrigin - V3<T>(T(0), -inner - T(100), T(0));
+    T height = length(position);
+    V3<T> lightDir = normalize(sunPosition);
+    if (std::fabs(height - inner) < T(1e-3f)) {
+        position = position + normalize(position) * T(1e-2f);
+        height = length(position);
+    }
+    const V3<T> zero(T(0), T(0), T(0));
+    if (height < outer) {
+        if (height > inner) {
+            T pd = outside(inner, position, rayDirection);
+            if (pd >= T(0)) {
+                T l = std::max(T(0.1f), dot(lightDir, normalize(position + rayDirection * pd)));
+                return V3<T>(l * T(0.05f), l * T(0.05f), l * T(0.05f));
+            }
+        } else {
+            return zero;
+        }
+        T rayDepth = inside(outer, position, rayDirection);
+        if (std::isinf(rayDepth) || std::isnan(rayDepth)) return zero;
+        const T k = scale / avg;
+        T depth = std::exp(k * (inner - height));
+        T startAngle = dot(rayDirection, position) / height;
+        T startOffset = depth * scale_fn(startAngle);
+        T sampleLength = rayDepth / T(64);
+        T scaledLength = sampleLength * scale;
+        V3<T> sampleRay = rayDirection * sampleLength;
+        V3<T> samplePoint = position + sampleRay * T(0.5f);
+        V3<T> color = zero;
+        for (int i = 0; i < 64; ++i) {
+            T h = length(samplePoint);
+            T dep = std::exp(k * (inner - h));
+            T lightAngle = dot(lightDir, samplePoint) / h;
+            T cameraAngle = dot(rayDirection, samplePoint) / h;
+            T scatter = startOffset + dep * (scale_fn(lightAngle) - scale_fn(cameraAngle));
+            V3<T> att(std::exp(-scatter * (invWl.x * Kr4PI + Km4PI)), std::exp(-scatter * (invWl.y * Kr4PI + Km4PI)),
+                      std::exp(-scatter * (invWl.z * Kr4PI + Km4PI)));
+            if (std::isinf(att.x) || std::isinf(att.y) || std::isinf(att.z) || std::isnan(att.x) ||
+                std::isnan(att.y) || std::isnan(att.z))
+                continue;
+            color = color + att * (dep * scaledLength);
+            samplePoint = samplePoint + sampleRay;
+        }
+        V3<T> secondary(color.x * Km * sunColor.x, color.y * Km * sunColor.y, color.z * Km * sunColor.z);
+        color = V3<T>(color.x * (invWl.x * Kr * sunColor.x), color.y * (invWl.y * Kr * sunColor.y),
+                      color.z * (invWl.z * Kr * sunColor.z));
+        T miecos = dot(lightDir, -rayDirection);
+        T g2 = g * g;
+        T phase = T(1.5f) * ((T(1) - g2) / (T(2) + g2)) * (T(1) + miecos * miecos) /
+                  std::pow(std::max(T(1e-3f), T(1) + g2 - T(2) * g * miecos), T(1.5f));
+        color = color + secondary * phase;
+        if (!(std::isinf(color.x) || std::isinf(color.y) || std::isinf(color.z))) return color;
+    } else {
+        T d = outside(outer, position, rayDirection);
+        if (d > T(0)) {
+            T l = dot(lightDir, normalize(position + rayDirection * d)) * T(0.5f);
+            return V3<T>(l * T(0.5294117647f), l * T(0.80784313725f), l * T(0.92156862745f));
+        }
+    }
+    return zero;
+}
 
 // The differentiable parameters of an update: per-material albedo (NULL =
 // the materials' base colour), sun radiance and sky radiance, in T.
@@ -673,10 +792,15 @@ template <class T>
 void shade_hit(const Scene& sc, const Grid& g, const Light& L, const ShadeParams<T>& P, const uint32_t* states,
                const Atlas<T>& prev, F3 origin, F3 dir, const Hit& h, int shadow, bool* shadowed_out, T out[4]) {
     if (shadowed_out) *shadowed_out = false;
-    if (!h.valid()) {  // miss.rmiss:17-23 with a constant sky
-        out[0] = P.sky.x;
-        out[1] = P.sky.y;
-        out[2] = P.sky.z;
+    if (!h.valid()) {  // miss.rmiss:17-23: constant sky, or sky() (sky.glsl:60-127)
+        V3<T> sky = P.sky;
+        if (g_sky_mode.load())
+            sky = atmosphere<T>(V3<T>(T(origin.x), T(origin.y), T(origin.z)), V3<T>(T(dir.x), T(dir.y), T(dir.z)),
+                                V3<T>(T(L.dir.x), T(L.dir.y), T(L.dir.z)),
+                                V3<T>(T(L.color.x), T(L.color.y), T(L.color.z)), T(L.brightness));
+        out[0] = sky.x;
+        out[1] = sky.y;
+        out[2] = sky.z;
         out[3] = T(-1);
         return;
     }
@@ -806,6 +930,8 @@ void blend_probe(const Grid& g, uint32_t linear, const T* rays /* R x 4 */, cons
                 for (int c = 0; c < 3; ++c) maxChange = std::max(maxChange, (T)std::fabs(acc[c] - texel[c]));
                 T h = T(g.hyst);
                 for (int c = 0; c < 3; ++c) texel[c] = acc[c] * (T(1) - h) + texel[c] * h;
+                if (g.quant)  // imageStore into the r11f_g11f_b10f image (probesUpdate.glsl:17, 103)
+                    for (int c = 0; c < 3; ++c) texel[c] = round_color_store(texel[c], c);
                 texel[3] = T(1);
             }
         if (update_state) {  // probesUpdate.glsl:110-119
@@ -849,6 +975,8 @@ void blend_probe(const Grid& g, uint32_t linear, const T* rays /* R x 4 */, cons
                 T* texel = at.depth + (py * at.dw + px) * 2;
                 T h = T(g.hyst);
                 for (int c = 0; c < 2; ++c) texel[c] = acc[c] * (T(1) - h) + texel[c] * h;
+                if (g.quant)  // imageStore into the rg16f image (probesUpdate.glsl:19)
+                    for (int c = 0; c < 2; ++c) texel[c] = round_depth_store(texel[c]);
             }
     }
 }
@@ -883,6 +1011,7 @@ int run_update(const Scene& sc, const ddgi_grid_desc* gd, const ddgi_light* ld, 
     L.dir = F3(ld->direction[0], ld->direction[1], ld->direction[2]);
     L.color = F3(ld->color[0], ld->color[1], ld->color[2]);
     L.sky = F3(ld->sky[0], ld->sky[1], ld->sky[2]);
+    L.brightness = ld->color[3];
     const uint32_t R = g.rays;
     std::vector<float> dirs(4 * (size_t)R);
     ddgi_ray_direction_table(orientation, R, dirs.data());
@@ -962,6 +1091,7 @@ int run_chain(const Scene& sc, const ddgi_grid_desc* gd, const ddgi_light* ld, c
     L.dir = F3(ld->direction[0], ld->direction[1], ld->direction[2]);
     L.color = F3(ld->color[0], ld->color[1], ld->color[2]);
     L.sky = F3(ld->sky[0], ld->sky[1], ld->sky[2]);
+    L.brightness = ld->color[3];
     ShadeParams<T> P = Pover ? *Pover : default_params<T>(L);
     const uint32_t R = g.rays, NP = g.count();
     Atlas<T> at;
@@ -1245,6 +1375,15 @@ void oracle_sphere_to_oct_uv(const float* d3, float* uv) {
     sphere_to_oct_uv(F3(d3[0], d3[1], d3[2]), &uv[0], &uv[1]);
 }
 float oracle_texel_scale(uint32_t n) { return texel_scale(n); }
+// Miss radiance of later calls: 0 constant sky radiance, 1 atmospheric sky.
+void oracle_set_sky_mode(int mode) { g_sky_mode.store(mode); }
+
+// Reference-format storage rounding of n values: kind 0 = 11-bit unsigned
+// float (red, green), 1 = 10-bit unsigned float (blue), 2 = half.
+void oracle_round_store(int kind, const float* in, float* out, uint32_t n) {
+    for (uint32_t i = 0; i < n; ++i)
+        out[i] = kind == 0 ? ddgi_round_r11(in[i]) : (kind == 1 ? ddgi_round_b10(in[i]) : ddgi_round_half(in[i]));
+}
 void oracle_direction_table(const float orientation[9], uint32_t n, float* out4) {
     ddgi_ray_direction_table(orientation, n, out4);
 }
@@ -1357,10 +1496,13 @@ void oracle_final_gather(const ddgi_grid_desc* gd, const ddgi_light* ld, const u
         for (size_t i = b; i < e; ++i) {
             const float* pd = position_depth + 4 * i;
             float* o = out + 4 * i;
-            if (!(pd[3] > 0.0f)) {
-                o[0] = ld->sky[0];
-                o[1] = ld->sky[1];
-                o[2] = ld->sky[2];
+            if (!(pd[3] > 0.0f)) {  // FinalGather.frag:55-57
+                F3 sky(ld->sky[0], ld->sky[1], ld->sky[2]);
+                if (g_sky_mode.load())  // view direction in position.xyz, brightness 1
+                    sky = atmosphere<float>(cam, normalize(F3(pd[0], pd[1], pd[2])), ldir, lc, 1.0f);
+                o[0] = sky.x;
+                o[1] = sky.y;
+                o[2] = sky.z;
                 o[3] = 1.0f;
                 continue;
             }

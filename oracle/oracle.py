@@ -94,6 +94,8 @@ class Oracle:
             lib.oracle_oct_decode.argtypes = [C.c_float, C.c_float, C.c_void_p]
             lib.oracle_sphere_to_oct_uv.argtypes = [C.c_void_p, C.c_void_p]
             lib.oracle_direction_table.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+            lib.oracle_round_store.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_uint32]
+            lib.oracle_set_sky_mode.argtypes = [C.c_int]
             lib.oracle_texel_scale.restype = C.c_float
             lib.oracle_texel_scale.argtypes = [C.c_uint32]
             lib.oracle_pbr.argtypes = [C.c_void_p] * 5 + [C.c_float, C.c_float, C.c_void_p]
@@ -242,6 +244,21 @@ class Oracle:
         o = np.ascontiguousarray(orientation, np.float32).reshape(9)
         out = np.zeros((n, 4), np.float32)
         cls.lib().oracle_direction_table(_ptr(o), n, _ptr(out))
+        return out
+
+    @classmethod
+    def set_sky_mode(cls, mode):
+        """Miss radiance of later calls (process-wide): 0 the light's
+        constant sky radiance, 1 the atmospheric sky of sky.glsl."""
+        cls.lib().oracle_set_sky_mode(int(mode))
+
+    @classmethod
+    def round_store(cls, kind, values):
+        """Reference-format storage rounding (0: 11-bit, 1: 10-bit unsigned
+        float, 2: half) of float32 values."""
+        v = np.ascontiguousarray(values, np.float32)
+        out = np.empty_like(v)
+        cls.lib().oracle_round_store(int(kind), _ptr(v), _ptr(out), v.size)
         return out
 
     @classmethod

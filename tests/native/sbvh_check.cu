@@ -1,6 +1,7 @@
 // Host-only check of the spatial-split tree builder (vulkanexp_gb300/csrc/sbvh.cu),
 // run under AddressSanitizer / UndefinedBehaviorSanitizer by tests/test_native_host.py.
-// For overlapping box soups and a height field: every triangle is referenced,
+// For overlapping box soups (also nearly axis-aligned ones, whose faces the
+// split planes cut at grazing angles) and a height field: every triangle is referenced,
 // references and leaf ranges stay in bounds, the depth is reported correctly,
 // and the tree is conservative: for sample points of every triangle (vertices,
 // edge midpoints, centroid, random interior points) a descent through the
@@ -8,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <array>
 #include <random>
 #include <vector>
@@ -49,7 +51,7 @@ static bool reaches(const std::vector<BvhNode>& nodes, const std::vector<uint32_
     return false;
 }
 
-static void check(const char* name, const std::vector<float>& tris, int leaf_max, float alpha) {
+static void check(const char* name, const std::vector<float>& tris, int leaf_max, float alpha, int samples = 4) {
     const uint32_t n = (uint32_t)(tris.size() / 9);
     std::vector<BvhNode> nodes;
     std::vector<uint32_t> order;
@@ -120,7 +122,7 @@ static void check(const char* name, const std::vector<float>& tris, int leaf_max
             pts.push_back({0.5f * (v[3 * i] + v[3 * j]), 0.5f * (v[3 * i + 1] + v[3 * j + 1]),
                            0.5f * (v[3 * i + 2] + v[3 * j + 2])});
         }
-        for (int s = 0; s < 4; ++s) {
+        for (int s = 0; s < samples; ++s) {
             float a = U(rng), b = U(rng);
             if (a + b > 1.0f) a = 1.0f - a, b = 1.0f - b;
             const float c = 1.0f - a - b;
@@ -138,14 +140,20 @@ static void check(const char* name, const std::vector<float>& tris, int leaf_max
                 100.0 * ((double)order.size() - n) / n, nodes.size(), depth);
 }
 
-static std::vector<float> box_soup(std::mt19937& rng, int boxes, float extent) {
+// Boxes with random centres, sizes and yaw; near_aligned: yaw within
+// +-[1e-6, 1e-3] rad, so faces are nearly parallel to the split planes and
+// clipping them is ill-conditioned.
+static std::vector<float> box_soup(std::mt19937& rng, int boxes, float extent, bool near_aligned = false) {
     std::uniform_real_distribution<float> C(-extent, extent), S(0.05f, 0.6f), Y(0.0f, 6.2831853f);
+    std::uniform_real_distribution<float> L(-6.0f, -3.0f);
     static const int f[12][3] = {{0, 2, 1}, {0, 3, 2}, {4, 5, 6}, {4, 6, 7}, {0, 1, 5}, {0, 5, 4},
                                  {2, 3, 7}, {2, 7, 6}, {1, 2, 6}, {1, 6, 5}, {0, 4, 7}, {0, 7, 3}};
     std::vector<float> out;
     for (int b = 0; b < boxes; ++b) {
         const float cx = C(rng), cy = C(rng) * 0.5f + extent * 0.5f, cz = C(rng);
-        const float sx = S(rng), sy = S(rng), sz = S(rng), yaw = Y(rng), cs = std::cos(yaw), sn = std::sin(yaw);
+        float yaw = Y(rng);
+        if (near_aligned) yaw = (yaw < 3.14159265f ? 1.0f : -1.0f) * std::pow(10.0f, L(rng));
+        const float sx = S(rng), sy = S(rng), sz = S(rng), cs = std::cos(yaw), sn = std::sin(yaw);
         float corner[8][3];
         for (int i = 0; i < 8; ++i) {
             const float x = (i & 1) ? sx : -sx, y = (i & 2) ? sy : -sy, z = (i & 4) ? sz : -sz;
@@ -177,6 +185,69 @@ static std::vector<float> height_field(std::mt19937& rng, int cells, float size)
     return out;
 }
 
+// The clipped reference box against the exact geometry: triangles nearly
+// parallel to a coordinate plane (thickness 1e-6 .. 1e-3 of their size along
+// that axis) cut by a plane through them; every point of the triangle (in
+// double) on either side of the plane lies in that side's clipped box.  (The
+// float clipper this replaced was off by up to 1e-3 of an edge here.)
+static void check_clip(std::mt19937& rng, int cases) {
+    std::uniform_real_distribution<double> U(0.0, 1.0), C(-3.0, 3.0);
+    std::uniform_real_distribution<double> L(-6.0, -3.0);
+    double worst = 0.0;
+    for (int c = 0; c < cases; ++c) {
+        const int k = c % 3;
+        const double thick = std::pow(10.0, L(rng)), base = C(rng);
+        float tri[9];
+        for (int v = 0; v < 3; ++v)
+            for (int j = 0; j < 3; ++j) tri[3 * v + j] = (float)(j == k ? base + thick * U(rng) : C(rng));
+        const double klo = std::min({(double)tri[k], (double)tri[3 + k], (double)tri[6 + k]});
+        const double khi = std::max({(double)tri[k], (double)tri[3 + k], (double)tri[6 + k]});
+        const float plane = (float)(klo + (khi - klo) * U(rng));
+        // the node's slab also cuts the triangle in the other two axes (the
+        // clipper's earlier planes: their rounded crossing points feed the
+        // grazing cut)
+        float nlo[3], nhi[3];
+        for (int j = 0; j < 3; ++j) {
+            const double tlo = std::min({(double)tri[j], (double)tri[3 + j], (double)tri[6 + j]});
+            const double thi = std::max({(double)tri[j], (double)tri[3 + j], (double)tri[6 + j]});
+            nlo[j] = j == k ? -1e30f : (float)(tlo + 0.3 * (thi - tlo) * U(rng));
+            nhi[j] = j == k ? 1e30f : (float)(thi - 0.3 * (thi - tlo) * U(rng));
+        }
+        float lo[2][3], hi[2][3];
+        for (int side = 0; side < 2; ++side) {
+            float slo[3] = {nlo[0], nlo[1], nlo[2]}, shi[3] = {nhi[0], nhi[1], nhi[2]};
+            if (side == 0) shi[k] = plane;
+            else slo[k] = plane;
+            sbvh_clip_box(tri, slo, shi, lo[side], hi[side]);
+        }
+        for (int s = 0; s < 2000; ++s) {
+            double a = U(rng), b = U(rng);
+            if (a + b > 1.0) a = 1.0 - a, b = 1.0 - b;
+            double p[3];
+            for (int j = 0; j < 3; ++j)
+                p[j] = (1.0 - a - b) * tri[j] + a * (double)tri[3 + j] + b * (double)tri[6 + j];
+            bool inside = true;
+            for (int j = 0; j < 3; ++j)
+                if (j != k && !(nlo[j] <= p[j] && p[j] <= nhi[j])) inside = false;
+            if (!inside) continue;
+            for (int side = 0; side < 2; ++side) {
+                if (side == 0 ? !(p[k] <= plane) : !(p[k] >= plane)) continue;
+                for (int j = 0; j < 3; ++j) {
+                    const double out = std::max(lo[side][j] - p[j], p[j] - hi[side][j]);
+                    worst = std::max(worst, out);
+                    if (out > 1e-9) {
+                        std::printf("FAIL clip: case %d axis %d, point outside the side-%d box by %g in axis %d\n",
+                                    c, k, side, out, j);
+                        ++failures;
+                        return;
+                    }
+                }
+            }
+        }
+    }
+    std::printf("ok clip: %d grazing cuts, worst excursion %g\n", cases, worst);
+}
+
 int main(int argc, char** argv) {
     const int scale = argc > 1 ? std::atoi(argv[1]) : 1;
     std::mt19937 rng(7);
@@ -188,7 +259,10 @@ int main(int argc, char** argv) {
     check("box soup leaf 1", box_soup(rng, 200 * scale, 1.0f), 1, 1e-2f);
     check("box soup leaf 4", box_soup(rng, 200 * scale, 1.0f), 4, 1e-2f);
     check("height field", height_field(rng, 40 * scale, 30.0f), 2, 1e-2f);
+    // faces nearly parallel to the split planes, dense interior sampling
+    check("near-aligned box soup", box_soup(rng, 600 * scale, 1.5f, true), 2, 1e-3f, 256);
     check("one triangle", box_soup(rng, 1, 1.0f), 2, 1e-2f);
+    check_clip(rng, 3000 * scale);
     std::printf(failures ? "FAILED %d\n" : "all ok\n", failures);
     return failures ? 1 : 0;
 }

@@ -128,11 +128,11 @@ def test_set_schedule_and_mirror_ramp(gpu_lib, room_workload):
     p.setScene(w.scene)
     p.setLightBuffer(w.light)
     p.initProbes(w.orientation(0))
-    assert p.GridParameters.hysteresis == 0.0
+    assert p.GridParameters.hysteresis == 0.0 and p.hysteresis()[1] == 0.0
     hs = []
     for k in range(40):
         p.update(w.orientation(1 + k))
-        hs.append(p.GridParameters.hysteresis)
+        hs.append(p.hysteresis()[1])
     # ramps up towards the target (one step per probe count of refreshed probes)
     assert hs == sorted(hs) and 0.2 < hs[-1] <= np.float32(0.98)
     p.destroy()

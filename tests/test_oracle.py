@@ -238,3 +238,88 @@ def test_final_gather_known_answers():
                                 float(gb["normal_metalness"][i, 3]), float(gb["albedo_roughness"][i, 3]),
                                 ref.ctypes.data_as(ctypes.c_void_p))
         assert np.allclose(out[i, :3], ref, rtol=1e-5, atol=1e-7)
+
+
+def _small_float_values(mbits):
+    """Every finite non-negative value of an unsigned float with a 5-bit
+    exponent (bias 15) and `mbits` mantissa bits, ascending."""
+    vals = [m / 2.0 ** mbits * 2.0 ** -14 for m in range(2 ** mbits)]
+    for e in range(1, 31):
+        vals += [(1 + m / 2.0 ** mbits) * 2.0 ** (e - 15) for m in range(2 ** mbits)]
+    return np.array(vals, np.float64)
+
+
+@pytest.mark.parametrize("kind,mbits", [(0, 6), (1, 5)])
+def test_reference_format_rounding_r11_b10(kind, mbits):
+    """ddgi_round_r11 / ddgi_round_b10 (the reference's B10G11R11_UFLOAT
+    irradiance image) against a brute-force nearest-value search: round to
+    nearest, ties to the even mantissa, negative values to 0, above the
+    largest finite value (and its half-step) to infinity."""
+    vals = _small_float_values(mbits)
+    rng = np.random.default_rng(kind)
+    x = np.concatenate([
+        rng.uniform(0, 4, 20000), 10.0 ** rng.uniform(-8, 4.8, 20000), vals, (vals[1:] + vals[:-1]) / 2,
+        -rng.uniform(0, 5, 100), [0.0, -0.0, 1e-30, 6.5e4, 7e4, np.inf, -np.inf]]).astype(np.float32)
+    got = Oracle.round_store(kind, x)
+    top = vals[-1] + (vals[-1] - vals[-2]) / 2  # at or above: infinity
+    for xi, gi in zip(x.astype(np.float64), got.astype(np.float64)):
+        if not xi > 0:
+            want = 0.0 if xi <= 0 or xi == -np.inf else xi
+        elif xi >= top:
+            want = np.inf
+        else:
+            j = np.searchsorted(vals, xi)
+            lo, hi = vals[max(j - 1, 0)], vals[min(j, len(vals) - 1)]
+            if xi - lo < hi - xi:
+                want = lo
+            elif hi - xi < xi - lo:
+                want = hi
+            else:  # a tie: the value with the even mantissa (its index in the table)
+                want = lo if (max(j - 1, 0) % 2 == 0) else hi
+        assert gi == want, (xi, gi, want)
+    assert np.isnan(Oracle.round_store(kind, np.array([np.nan], np.float32))).all()
+
+
+def test_reference_format_rounding_half():
+    """ddgi_round_half (the reference's RG16F depth image) equals IEEE
+    float32 -> binary16 round-to-nearest-even conversion."""
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.normal(0, 3, 50000), 10.0 ** rng.uniform(-9, 5, 50000) * rng.choice([-1, 1], 50000),
+                        [0.0, -0.0, 65504.0, 65519.0, 65520.0, 1e6, -1e6, 5.96e-8, 2.98e-8, np.inf]]).astype(np.float32)
+    got = Oracle.round_store(2, x)
+    with np.errstate(over="ignore"):
+        want = x.astype(np.float16).astype(np.float32)
+    assert (got.view(np.uint32) == want.view(np.uint32)).all()
+
+
+def test_atmospheric_sky_known_answers():
+    """The restatement of sky.glsl (oracle sky mode 1) through the final
+    gather's sky pixels (brightness 1, view direction in position.xyz):
+    looking straight down from 10 m hits the planet 110 m below the
+    atmosphere's reference, which returns max(0.1, sun.y) x 0.05 grey;
+    looking up gives a blue sky (Rayleigh scattering: blue > green > red);
+    the constant mode returns the light's sky radiance."""
+    from vulkanexp_gb300 import scenes
+
+    g = abi.make_grid((0, 0, 0), (1, 1, 1), (2, 2, 2), 8)
+    L = scenes.default_light()
+    states = np.ones(8, np.uint32)
+    color = np.zeros((16, 32, 4), np.float32)
+    depth = np.zeros((32, 64, 2), np.float32)
+    dirs = np.array([[0, -1, 0], [0, 1, 0], [0.3, 0.2, 0.9]], np.float32)
+    gb = {"position_depth": np.column_stack([dirs, np.zeros(3)]).astype(np.float32),
+          "normal_metalness": np.zeros((3, 4), np.float32), "albedo_roughness": np.zeros((3, 4), np.float32),
+          "emissive": np.zeros((3, 4), np.float32), "direct_light": np.zeros(3, np.float32)}
+    origin = np.array([0.0, 10.0, 0.0], np.float32)
+    try:
+        Oracle.set_sky_mode(1)
+        out = Oracle.final_gather(g, L, states, color, depth, gb, origin)
+    finally:
+        Oracle.set_sky_mode(0)
+    sun = np.asarray(L.direction[:3], np.float64)
+    sun /= np.linalg.norm(sun)
+    np.testing.assert_allclose(out[0, :3], max(0.1, sun[1]) * 0.05, rtol=1e-5)
+    assert out[1, 2] > out[1, 1] > out[1, 0] > 0.0
+    assert np.isfinite(out).all() and (out[2, :3] > 0).all()
+    const = Oracle.final_gather(g, L, states, color, depth, gb, origin)
+    assert (const[:, :3] == np.asarray(L.sky[:3], np.float32)).all()

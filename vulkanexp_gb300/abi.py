@@ -38,6 +38,9 @@ MISS = 0xFFFFFFFF
 
 PRECISION_FP32 = 0
 PRECISION_BF16 = 1
+PRECISION_REFERENCE_FORMAT = 2  # FP32 blend, texels rounded to R11G11B10F / RG16F on store
+SKY_CONSTANT = 0
+SKY_ATMOSPHERE = 1
 ATLAS_COLOR = 0
 ATLAS_DEPTH = 1
 

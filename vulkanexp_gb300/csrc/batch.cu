@@ -245,6 +245,8 @@ ddgi_status check_volumes(ddgi_batch* b) {
             c->grid.rays_per_probe != g0.rays_per_probe || c->grid.color_res != g0.color_res ||
             c->grid.depth_res != g0.depth_res || c->grid.precision != g0.precision)
             return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "volume %zu: grid sizes changed since the batch was made", v);
+        if (c->dl.sky_mode != DDGI_SKY_CONSTANT)
+            return bfail(b, DDGI_ERR_UNSUPPORTED, "volume %zu: the atmospheric sky is not batched", v);
     }
     return DDGI_OK;
 }

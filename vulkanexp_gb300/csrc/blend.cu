@@ -36,9 +36,10 @@ __device__ __forceinline__ int4 border_entry(int e, int n) {
 }
 
 // Blend of one probe by the whole block: `pr` = its R ray records.
+// `hy` is the hysteresis of this update (the grid's, or the ramp's value).
 __device__ __forceinline__ void blend_probe_fp32(const DeviceGrid& g, uint32_t probe, const float4* __restrict__ pr,
                                                  const float4* __restrict__ dirs, uint32_t* states, float4* color,
-                                                 float2* depth) {
+                                                 float2* depth, const float hy) {
     extern __shared__ float4 smem[];
     const uint32_t R = g.rays;
     float4* s_rays = smem;
@@ -66,7 +67,6 @@ __device__ __forceinline__ void blend_probe_fp32(const DeviceGrid& g, uint32_t p
     const int tile = iy * g.res[0] + ix;
     const int nc = (int)g.color_res - 2, nd = (int)g.depth_res - 2;
     const int ncol = nc * nc, ntex = ncol + nd * nd;
-    const float hy = g.hyst;
 
     for (int t = threadIdx.x; t < ntex; t += blockDim.x) {
         if (t < ncol) {
@@ -93,8 +93,8 @@ __device__ __forceinline__ void blend_probe_fp32(const DeviceGrid& g, uint32_t p
             float4 prev = *texel;
             float mc = fmaxf(fmaxf(fabsf(a0 - prev.x), fabsf(a1 - prev.y)), fabsf(a2 - prev.z));
             atomicMax(&s_max_change, __float_as_uint(mc));
-            *texel = make_float4(a0 * (1.0f - hy) + prev.x * hy, a1 * (1.0f - hy) + prev.y * hy,
-                                 a2 * (1.0f - hy) + prev.z * hy, 1.0f);
+            *texel = store_color(g, a0 * (1.0f - hy) + prev.x * hy, a1 * (1.0f - hy) + prev.y * hy,
+                                 a2 * (1.0f - hy) + prev.z * hy);
         } else {
             int u = t - ncol;
             int tx = u % nd, ty = u / nd;
@@ -118,7 +118,7 @@ __device__ __forceinline__ void blend_probe_fp32(const DeviceGrid& g, uint32_t p
             size_t px = (size_t)((int)g.depth_res * tile + 1 + tx), py = (size_t)((int)g.depth_res * iz + 1 + ty);
             float2* texel = depth + py * g.depth_w + px;
             float2 prev = *texel;
-            *texel = make_float2(a0 * (1.0f - hy) + prev.x * hy, a1 * (1.0f - hy) + prev.y * hy);
+            *texel = store_depth(g, a0 * (1.0f - hy) + prev.x * hy, a1 * (1.0f - hy) + prev.y * hy);
         }
     }
     __syncthreads();
@@ -155,11 +155,12 @@ __device__ __forceinline__ void blend_probe_fp32(const DeviceGrid& g, uint32_t p
 __global__ void __launch_bounds__(256) k_blend_fp32(DeviceGrid g, const uint32_t* __restrict__ probe_list,
                                                     const float4* __restrict__ rays, const float4* __restrict__ dirs,
                                                     uint32_t* states, float4* color, float2* depth,
-                                                    const uint32_t* dev_count) {
+                                                    const uint32_t* dev_count, const float* hyst_dev) {
     const uint32_t slot = blockIdx.x;
     if (dev_count && slot >= *dev_count) return;  // whole block
     const uint32_t probe = probe_list ? probe_list[slot] : slot;
-    blend_probe_fp32(g, probe, rays + (size_t)slot * g.rays, dirs, states, color, depth);
+    blend_probe_fp32(g, probe, rays + (size_t)slot * g.rays, dirs, states, color, depth,
+                     hyst_dev ? *hyst_dev : g.hyst);
 }
 
 // Batched form: block b blends probe (b - tile_base[i]) of volume list[i];
@@ -177,7 +178,7 @@ __global__ void __launch_bounds__(256) k_batch_blend_fp32(BatchTables bt, BatchB
     const BatchVolume& vol = bt.vols[v];
     const uint32_t probe = b - __ldg(bl.tile_base + lo);
     blend_probe_fp32(vol.g, probe, rays + vol.ray_base + (size_t)probe * vol.g.rays, bt.dirs + vol.dir_base,
-                     vol.states, static_cast<float4*>(vol.color), static_cast<float2*>(vol.depth));
+                     vol.states, static_cast<float4*>(vol.color), static_cast<float2*>(vol.depth), vol.g.hyst);
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -190,10 +191,10 @@ __global__ void __launch_bounds__(256) k_batch_blend_fp32(BatchTables bt, BatchB
 
 cudaError_t launch_blend_fp32(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
                               const float4* dirs, uint32_t* states, float4* color, float2* depth, cudaStream_t st,
-                              const uint32_t* dev_count) {
+                              const uint32_t* dev_count, const float* hyst_dev) {
     if (nprobes == 0) return cudaSuccess;
     size_t smem = sizeof(float4) * 2 * g.rays;
-    k_blend_fp32<<<nprobes, 256, smem, st>>>(g, probe_list, rays, dirs, states, color, depth, dev_count);
+    k_blend_fp32<<<nprobes, 256, smem, st>>>(g, probe_list, rays, dirs, states, color, depth, dev_count, hyst_dev);
     return cudaGetLastError();
 }
 

@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(128) k_fp32_weights(DeviceGrid g, const float4
 __device__ __forceinline__ void blend_probes_shared(const DeviceGrid& g, const uint32_t* __restrict__ probe_list,
                                                     uint32_t p0, uint32_t np, const float4* __restrict__ rays,
                                                     const float* __restrict__ W, const float* __restrict__ wsum,
-                                                    uint32_t* states, float4* color, float2* depth) {
+                                                    uint32_t* states, float4* color, float2* depth, const float hy) {
     extern __shared__ float4 s_rec[];  // [kProbesPerBlock][R]: colour xyz, clamped depth w
     __shared__ uint32_t s_max_change[kProbesPerBlock], s_out_of_range[kProbesPerBlock], s_probe[kProbesPerBlock];
     const uint32_t R = g.rays;
@@ -108,7 +108,6 @@ __device__ __forceinline__ void blend_probes_shared(const DeviceGrid& g, const u
     const uint32_t rx = (uint32_t)g.res[0], rxy = (uint32_t)(g.res[0] * g.res[1]);
     const int nc = (int)g.color_res - 2, nd = (int)g.depth_res - 2;
     const uint32_t ncol = (uint32_t)(nc * nc), ntex = ncol + (uint32_t)(nd * nd);
-    const float hy = g.hyst;
     for (uint32_t t = threadIdx.x; t < ntex; t += blockDim.x) {
         const float aw = wsum[t];
         if (t < ncol) {
@@ -145,8 +144,8 @@ __device__ __forceinline__ void blend_probes_shared(const DeviceGrid& g, const u
                 float4 prev = *texel;
                 float mc = fmaxf(fmaxf(fabsf(a0 - prev.x), fabsf(a1 - prev.y)), fabsf(a2 - prev.z));
                 atomicMax(&s_max_change[p], __float_as_uint(mc));
-                *texel = make_float4(a0 * (1.0f - hy) + prev.x * hy, a1 * (1.0f - hy) + prev.y * hy,
-                                     a2 * (1.0f - hy) + prev.z * hy, 1.0f);
+                *texel = store_color(g, a0 * (1.0f - hy) + prev.x * hy, a1 * (1.0f - hy) + prev.y * hy,
+                                     a2 * (1.0f - hy) + prev.z * hy);
             }
         } else {
             float a[kProbesPerBlock][2];
@@ -178,7 +177,7 @@ __device__ __forceinline__ void blend_probes_shared(const DeviceGrid& g, const u
                 size_t px = (size_t)((int)g.depth_res * tile + 1 + tx), py = (size_t)((int)g.depth_res * iz + 1 + ty);
                 float2* texel = depth + py * g.depth_w + px;
                 float2 prev = *texel;
-                *texel = make_float2(a0 * (1.0f - hy) + prev.x * hy, a1 * (1.0f - hy) + prev.y * hy);
+                *texel = store_depth(g, a0 * (1.0f - hy) + prev.x * hy, a1 * (1.0f - hy) + prev.y * hy);
             }
         }
     }
@@ -223,11 +222,13 @@ __global__ void __launch_bounds__(kBlendThreads) k_blend_fp32_shared(DeviceGrid 
                                                                      uint32_t nprobes, const float4* rays,
                                                                      const float* W, const float* wsum,
                                                                      uint32_t* states, float4* color, float2* depth,
-                                                                     const uint32_t* dev_count) {
+                                                                     const uint32_t* dev_count,
+                                                                     const float* hyst_dev) {
     const uint32_t n = dev_count ? min(*dev_count, nprobes) : nprobes;
     const uint32_t p0 = blockIdx.x * kProbesPerBlock;
     if (p0 >= n) return;  // whole block
-    blend_probes_shared(g, probe_list, p0, min(kProbesPerBlock, n - p0), rays, W, wsum, states, color, depth);
+    blend_probes_shared(g, probe_list, p0, min(kProbesPerBlock, n - p0), rays, W, wsum, states, color, depth,
+                        hyst_dev ? *hyst_dev : g.hyst);
 }
 
 // Batched form: weights per FP32 volume (grid y = position in the list),
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(kBlendThreads) k_batch_blend_fp32_shared(Batch
     if (p0 < P)
         blend_probes_shared(vol.g, nullptr, p0, min(kProbesPerBlock, P - p0), rays + vol.ray_base,
                             reinterpret_cast<const float*>(vol.wbuf), vol.rowsum, vol.states,
-                            static_cast<float4*>(vol.color), static_cast<float2*>(vol.depth));
+                            static_cast<float4*>(vol.color), static_cast<float2*>(vol.depth), vol.g.hyst);
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -285,7 +286,8 @@ cudaError_t set_shared_smem_limit() {
 
 cudaError_t launch_blend_fp32_shared(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes,
                                      const float4* rays, const float4* dirs, float* W, float* wsum, uint32_t* states,
-                                     float4* color, float2* depth, cudaStream_t st, const uint32_t* dev_count) {
+                                     float4* color, float2* depth, cudaStream_t st, const uint32_t* dev_count,
+                                     const float* hyst_dev) {
     if (nprobes == 0) return cudaSuccess;
     cudaError_t e = set_shared_smem_limit();
     if (e != cudaSuccess) return e;
@@ -294,7 +296,7 @@ cudaError_t launch_blend_fp32_shared(const DeviceGrid& g, const uint32_t* probe_
     const size_t smem = sizeof(float4) * kProbesPerBlock * g.rays;
     k_blend_fp32_shared<<<fp32_shared_tiles(nprobes), kBlendThreads, smem, st>>>(g, probe_list, nprobes, rays, W,
                                                                                wsum, states, color, depth,
-                                                                               dev_count);
+                                                                               dev_count, hyst_dev);
     return cudaGetLastError();
 }
 

@@ -71,6 +71,7 @@ struct TcArgs {
     uint32_t* err;
     const uint32_t* dev_count;  // listed probes, read on the device (NULL: nprobes)
     uint32_t stall;             // test hook: issue no MMA and no commit, so the completion wait runs out
+    const float* hyst_dev;      // hysteresis of this update in device memory (the ramp's), or NULL: g.hyst
 };
 
 // Limit of one tensor-core completion wait (the MMAs of a chunk take
@@ -393,7 +394,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
         __syncthreads();
 
         // epilogue 2: hysteresis in the FP32 accumulator, FP16 publish
-        const float hy = a.g.hyst;
+        const float hy = a.hyst_dev ? *a.hyst_dev : a.g.hyst;
         const uint32_t rx = (uint32_t)a.g.res[0], rxy = (uint32_t)(a.g.res[0] * a.g.res[1]);
         const uint32_t ntc = a.nc * a.nc, ntd = a.nd * a.nd;
         const uint32_t nprobes_grid = rxy * (uint32_t)a.g.res[2];
@@ -544,6 +545,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_blend_tc(BatchTables bt, Bat
         a.err = bt.err;
         a.dev_count = nullptr;
         a.stall = 0;
+        a.hyst_dev = nullptr;
         s_v = v;
         s_tile = b - __ldg(bl.tile_base + lo);
         s_items = __ldg(bl.tile_base + lo + 1) - __ldg(bl.tile_base + lo);
@@ -581,7 +583,7 @@ bool tc_blend_supported(uint32_t color_res, uint32_t depth_res) {
 cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
                             const float4* dirs, uint8_t* wbuf, float* rowsum, uint32_t* states, void* color,
                             void* depth, float4* acc_color, float2* acc_depth, uint32_t* err, cudaStream_t st,
-                            const uint32_t* dev_count, bool stall) {
+                            const uint32_t* dev_count, bool stall, const float* hyst_dev) {
     if (nprobes == 0) return cudaSuccess;
     const uint32_t nc = g.color_res - 2, nd = g.depth_res - 2;
     const uint32_t Nc = (nc * nc + 15) / 16 * 16, Nd = (nd * nd + 15) / 16 * 16;
@@ -607,6 +609,7 @@ cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uin
     a.err = err;
     a.dev_count = dev_count;
     a.stall = stall ? 1u : 0u;
+    a.hyst_dev = hyst_dev;
     // operand stage (A 64 KB + B up to 128 KB), reused by the epilogue staging
     size_t stage = 65536 + 2 * (size_t)(Nd + Nc) * 128;
     size_t staging = (size_t)kTileProbes * (nc * nc * 3 + nd * nd * 2) * sizeof(float);

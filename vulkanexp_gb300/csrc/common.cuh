@@ -11,6 +11,7 @@
 #include <stdint.h>
 
 #include "../../include/ddgi.h"
+#include "../../include/ddgi_exact.h"
 
 namespace ddgi {
 
@@ -118,10 +119,25 @@ struct DeviceGrid {
     uint32_t rays, color_res, depth_res;
     float sharp, hyst, bias;
     uint32_t color_w, color_h, depth_w, depth_h;  // atlas sizes in texels
+    uint32_t quant;  // reference-format atlas: stored texels rounded to R11G11B10F / RG16F
 };
+
+// Stored texel of the FP32 atlas forms: as computed, or (reference-format
+// form) rounded to the reference's image formats, B10G11R11 unsigned floats
+// for irradiance and RG16F for depth (src/IrradianceProbes.cpp:41, 63).
+__device__ __forceinline__ float4 store_color(const DeviceGrid& g, float r, float gr, float b) {
+    if (g.quant) return make_float4(ddgi_round_r11(r), ddgi_round_r11(gr), ddgi_round_b10(b), 1.0f);
+    return make_float4(r, gr, b, 1.0f);
+}
+__device__ __forceinline__ float2 store_depth(const DeviceGrid& g, float m, float m2) {
+    if (g.quant) return make_float2(ddgi_round_half(m), ddgi_round_half(m2));
+    return make_float2(m, m2);
+}
 
 struct DeviceLight {
     float dir[3], color[3], sky[3];
+    float sun_brightness;  // LightBuffer.color.a: the atmospheric sky's sun factor
+    uint32_t sky_mode;     // ddgi_sky_mode of the miss radiance
 };
 
 // ---------------------------------------------------------------------------

@@ -11,6 +11,7 @@
 
 #include "../../include/ddgi.h"
 #include "common.cuh"
+#include "kernels.h"
 
 namespace ddgi {
 
@@ -123,8 +124,11 @@ struct ddgi_ctx {
     uint32_t* ray_order = nullptr;
     uint32_t* probe_list = nullptr;
     // adaptive schedule (selectProbesToUpdate on the device): {offset, loop
-    // index, selected count}; probe classification scratch
+    // index, selected count, -}, then the hysteresis ramp {blended value,
+    // host-side value, target (float bits), probes counted}
     uint32_t* sched = nullptr;
+    bool ramp_on = false;
+    ddgi::RampCmd ramp_cmd{};  // host changes the next update's ramp step applies first
     // traversal launch tuning; probes in Morton order of the grid (grouped warps)
     ddgi_trace_tuning tune{0, 8, 0, 0, 2, ddgi::kDefaultWait};
     int blas_leaf_max = ddgi::kBlasLeafMax;  // triangles per mesh-tree leaf (scene build option)

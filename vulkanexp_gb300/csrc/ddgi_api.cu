@@ -81,7 +81,8 @@ bool grid_valid(const ddgi_grid_desc* g, char* why, size_t n) {
     if (g->depth_res < 3 || g->depth_res > 64) return snprintf(why, n, "depth_res = %u outside [3, 64]", g->depth_res), false;
     if (!std::isfinite(g->hysteresis) || !std::isfinite(g->depth_sharpness) || !std::isfinite(g->shadow_bias))
         return snprintf(why, n, "non-finite hysteresis/sharpness/bias"), false;
-    if (g->precision != DDGI_PRECISION_FP32 && g->precision != DDGI_PRECISION_BF16)
+    if (g->precision != DDGI_PRECISION_FP32 && g->precision != DDGI_PRECISION_BF16 &&
+        g->precision != DDGI_PRECISION_REFERENCE_FORMAT)
         return snprintf(why, n, "unknown precision %u", g->precision), false;
     uint64_t probes = (uint64_t)g->resolution[0] * g->resolution[1] * g->resolution[2];
     if (probes > (1u << 24)) return snprintf(why, n, "too many probes (%llu)", (unsigned long long)probes), false;
@@ -126,6 +127,7 @@ DeviceGrid make_device_grid(const ddgi_grid_desc& g) {
     d.color_h = g.color_res * g.resolution[2];
     d.depth_w = g.depth_res * g.resolution[0] * g.resolution[1];
     d.depth_h = g.depth_res * g.resolution[2];
+    d.quant = g.precision == DDGI_PRECISION_REFERENCE_FORMAT ? 1u : 0u;
     return d;
 }
 
@@ -242,6 +244,8 @@ ddgi_status ddgi_create(const ddgi_grid_desc* grid, ddgi_ctx** out) {
             ctx->dl.color[k] = 10.0f;
             ctx->dl.sky[k] = 0.0f;
         }
+        ctx->dl.sun_brightness = 10.0f;
+        ctx->dl.sky_mode = DDGI_SKY_CONSTANT;
     }
     cudaError_t e = cudaGetDevice(&ctx->device);
     ddgi_status st = DDGI_OK;
@@ -257,7 +261,7 @@ ddgi_status ddgi_create(const ddgi_grid_desc* grid, ddgi_ctx** out) {
         cudaMalloc(&ctx->dirs, sizeof(float4) * DDGI_MAX_RAYS_PER_PROBE) != cudaSuccess ||
         cudaMalloc(&ctx->ray_order, sizeof(uint32_t) * DDGI_MAX_RAYS_PER_PROBE) != cudaSuccess ||
         cudaMalloc(&ctx->probe_list, sizeof(uint32_t) * P) != cudaSuccess ||
-        cudaMalloc(&ctx->sched, 4 * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&ctx->sched, 8 * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&ctx->probe_perm, sizeof(uint32_t) * P) != cudaSuccess ||
         cudaMalloc(&ctx->err, sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&ctx->counters, 4 * sizeof(uint32_t)) != cudaSuccess) {
@@ -292,7 +296,7 @@ ddgi_status ddgi_create(const ddgi_grid_desc* grid, ddgi_ctx** out) {
     cudaMemset(ctx->color, 0, atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, ctx->fp16));
     cudaMemset(ctx->depth, 0, atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, ctx->fp16));
     cudaMemset(ctx->err, 0, sizeof(uint32_t));
-    cudaMemset(ctx->sched, 0, 4 * sizeof(uint32_t));
+    cudaMemset(ctx->sched, 0, 8 * sizeof(uint32_t));
     {
         std::vector<uint32_t> perm = probe_morton_order(grid->resolution);
         cudaMemcpy(ctx->probe_perm, perm.data(), sizeof(uint32_t) * P, cudaMemcpyHostToDevice);
@@ -377,6 +381,53 @@ ddgi_status ddgi_set_grid(ddgi_ctx* ctx, const ddgi_grid_desc* g) {
     if (st != DDGI_OK) return st;
     ctx->grid = *g;
     ctx->dg = make_device_grid(*g);
+    if (ctx->ramp_on) {  // updateUniforms() uploads GridParameters.hysteresis as given
+        ctx->ramp_cmd.set |= kRampSetBlended | kRampSetParam;
+        ctx->ramp_cmd.blended = ctx->ramp_cmd.param = g->hysteresis;
+    }
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_set_target_hysteresis(ddgi_ctx* ctx, float target) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    if (!std::isfinite(target) || target > 1.0f)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "target hysteresis must be finite and at most 1");
+    if (target < 0.0f) {  // off: the grid's hysteresis is blended as given
+        ctx->ramp_on = false;
+        ctx->ramp_cmd = RampCmd{};
+        return DDGI_OK;
+    }
+    if (!ctx->ramp_on) {  // the ramp starts from the grid's hysteresis with no probes counted
+        ctx->ramp_on = true;
+        ctx->ramp_cmd.set = kRampSetBlended | kRampSetParam | kRampZeroCount;
+        ctx->ramp_cmd.blended = ctx->ramp_cmd.param = ctx->grid.hysteresis;
+    }
+    ctx->ramp_cmd.set |= kRampSetTarget;
+    ctx->ramp_cmd.target = target;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_get_hysteresis(ddgi_ctx* ctx, float* blended, float* parameter, uint32_t* counted,
+                                ddgi_stream stream) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    float b = ctx->grid.hysteresis, p = ctx->grid.hysteresis;
+    uint32_t c = 0;
+    if (ctx->ramp_on) {
+        uint32_t h[4];
+        cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+        CK(cudaMemcpyAsync(h, ctx->sched + 4, sizeof(h), cudaMemcpyDeviceToHost, st), "read ramp");
+        CK(cudaStreamSynchronize(st), "read ramp");
+        std::memcpy(&b, &h[0], 4);
+        std::memcpy(&p, &h[1], 4);
+        c = h[3];
+        const RampCmd& m = ctx->ramp_cmd;  // host changes not applied yet
+        if (m.set & kRampSetBlended) b = m.blended;
+        if (m.set & kRampSetParam) p = m.param;
+        if (m.set & kRampZeroCount) c = 0;
+    }
+    if (blended) *blended = b;
+    if (parameter) *parameter = p;
+    if (counted) *counted = c;
     return DDGI_OK;
 }
 
@@ -389,6 +440,16 @@ ddgi_status ddgi_set_light(ddgi_ctx* ctx, const ddgi_light* l) {
         ctx->dl.color[k] = l->color[k];
         ctx->dl.sky[k] = l->sky[k];
     }
+    if (!std::isfinite(l->color[3])) return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "non-finite light");
+    ctx->dl.sun_brightness = l->color[3];
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_set_sky_mode(ddgi_ctx* ctx, ddgi_sky_mode mode) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    if (mode != DDGI_SKY_CONSTANT && mode != DDGI_SKY_ATMOSPHERE)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "unknown sky mode %d", (int)mode);
+    ctx->dl.sky_mode = (uint32_t)mode;
     return DDGI_OK;
 }
 
@@ -1179,17 +1240,32 @@ bool take_stall(ddgi_ctx* ctx) {
 // precision and pipeline: the BF16 tensor-core kernel; the FP32 kernel with
 // the weights computed once per update (wavefront); the per-probe FP32
 // kernel that computes them per texel like the reference's shader (fused).
-cudaError_t launch_blend(ddgi_ctx* ctx, const uint32_t* dlist, uint32_t n, cudaStream_t st) {
+// hyst: the ramp's hysteresis in device memory (NULL: the grid's); dcount:
+// the selected probe count on the device (NULL: n).
+cudaError_t launch_blend(ddgi_ctx* ctx, const uint32_t* dlist, uint32_t n, cudaStream_t st,
+                         const float* hyst = nullptr, const uint32_t* dcount = nullptr) {
     if (ctx->fp16)
         return launch_blend_tc(ctx->dg, dlist, n, ctx->rays, ctx->dirs, ctx->tc_weights, ctx->tc_rowsum, ctx->states,
-                               ctx->color, ctx->depth, ctx->acc_color, ctx->acc_depth, ctx->err, st, nullptr,
-                               take_stall(ctx));
+                               ctx->color, ctx->depth, ctx->acc_color, ctx->acc_depth, ctx->err, st, dcount,
+                               take_stall(ctx), hyst);
     if (ctx->pipeline == DDGI_PIPELINE_WAVEFRONT)
         return launch_blend_fp32_shared(ctx->dg, dlist, n, ctx->rays, ctx->dirs,
                                         reinterpret_cast<float*>(ctx->tc_weights), ctx->tc_rowsum, ctx->states,
-                                        static_cast<float4*>(ctx->color), static_cast<float2*>(ctx->depth), st);
+                                        static_cast<float4*>(ctx->color), static_cast<float2*>(ctx->depth), st,
+                                        dcount, hyst);
     return launch_blend_fp32(ctx->dg, dlist, n, ctx->rays, ctx->dirs, ctx->states, static_cast<float4*>(ctx->color),
-                             static_cast<float2*>(ctx->depth), st);
+                             static_cast<float2*>(ctx->depth), st, dcount, hyst);
+}
+
+// The hysteresis ramp step of an update when the ramp is on (count: the
+// update's probes, or *dcount on the device); returns the blended value's
+// device address, or NULL when the grid's hysteresis applies.
+const float* ramp_step(ddgi_ctx* ctx, const uint32_t* dcount, uint32_t count, cudaStream_t st, cudaError_t* e) {
+    *e = cudaSuccess;
+    if (!ctx->ramp_on) return nullptr;
+    *e = launch_hysteresis_ramp(ctx->sched, ctx->ramp_cmd, dcount, count, probe_count_of(ctx->grid), st);
+    ctx->ramp_cmd.set = 0;
+    return reinterpret_cast<const float*>(ctx->sched + 4);
 }
 
 }  // namespace
@@ -1243,8 +1319,13 @@ ddgi_status ddgi_update(ddgi_ctx* ctx, const float orientation[9], const uint32_
                             trace_tuning(ctx), ctx->probe_perm),
            "wavefront trace launch");
     }
+    if (ctx->dl.sky_mode == DDGI_SKY_ATMOSPHERE)
+        CK(launch_shade_sky(ctx->dg, ctx->dl, n, nullptr, dlist, ctx->dirs, ctx->rays, st), "sky launch");
     if (ctx->timing) CK(cudaEventRecord(ctx->ev[1], st), "event");
-    CK(launch_blend(ctx, dlist, n, st), "blend launch");
+    cudaError_t re;
+    const float* hyst = ramp_step(ctx, nullptr, n, st, &re);
+    CK(re, "hysteresis ramp launch");
+    CK(launch_blend(ctx, dlist, n, st, hyst), "blend launch");
     if (ctx->timing) {
         CK(cudaEventRecord(ctx->ev[2], st), "event");
         ctx->timing_pending = true;
@@ -1281,6 +1362,10 @@ ddgi_status ddgi_init_probes(ddgi_ctx* ctx, const float orientation[9], ddgi_str
                           ctx->counters, ctx->scene.stack_cap, ctx->err, st),
        "init launch");
     CK(cudaStreamSynchronize(st), "init probes");  // also keeps `d` alive for the copy
+    if (ctx->ramp_on) {  // initProbes restarts the ramp's host value (IrradianceProbes.cpp:357-358)
+        ctx->ramp_cmd.set |= kRampSetParam;
+        ctx->ramp_cmd.param = 0.0f;
+    }
     return check_device_error(ctx);
 }
 
@@ -1303,21 +1388,13 @@ ddgi_status ddgi_update_scheduled(ddgi_ctx* ctx, const float orientation[9], uin
                         ctx->scene.stack_cap, ctx->scene.wstack_cap, ctx->err, st,
                         ctx->timing ? ctx->ev[3] : nullptr, dcount, trace_tuning(ctx), nullptr),
        "wavefront trace launch");
+    if (ctx->dl.sky_mode == DDGI_SKY_ATMOSPHERE)
+        CK(launch_shade_sky(ctx->dg, ctx->dl, P, dcount, ctx->probe_list, ctx->dirs, ctx->rays, st), "sky launch");
     if (ctx->timing) CK(cudaEventRecord(ctx->ev[1], st), "event");
-    if (ctx->fp16)
-        CK(launch_blend_tc(ctx->dg, ctx->probe_list, P, ctx->rays, ctx->dirs, ctx->tc_weights, ctx->tc_rowsum,
-                           ctx->states, ctx->color, ctx->depth, ctx->acc_color, ctx->acc_depth, ctx->err, st, dcount,
-                           take_stall(ctx)),
-           "blend launch");
-    else if (ctx->pipeline == DDGI_PIPELINE_WAVEFRONT)
-        CK(launch_blend_fp32_shared(ctx->dg, ctx->probe_list, P, ctx->rays, ctx->dirs,
-                                    reinterpret_cast<float*>(ctx->tc_weights), ctx->tc_rowsum, ctx->states,
-                                    static_cast<float4*>(ctx->color), static_cast<float2*>(ctx->depth), st, dcount),
-           "blend launch");
-    else
-        CK(launch_blend_fp32(ctx->dg, ctx->probe_list, P, ctx->rays, ctx->dirs, ctx->states,
-                             static_cast<float4*>(ctx->color), static_cast<float2*>(ctx->depth), st, dcount),
-           "blend launch");
+    cudaError_t re;
+    const float* hyst = ramp_step(ctx, dcount, 0, st, &re);
+    CK(re, "hysteresis ramp launch");
+    CK(launch_blend(ctx, ctx->probe_list, P, st, hyst, dcount), "blend launch");
     if (ctx->timing) {
         CK(cudaEventRecord(ctx->ev[2], st), "event");
         ctx->timing_pending = true;
@@ -1948,7 +2025,10 @@ ddgi_status ddgi_forward_record(ddgi_ctx* ctx, uint32_t K, const float* orientat
                                 ddgi_stream stream) {
     ddgi::NvtxRange nvtx_range("ddgi_forward_record");
     if (!ctx || !orientations || K == 0 || checkpoint_every == 0) return DDGI_ERR_INVALID_ARGUMENT;
-    if (ctx->fp16) return fail(ctx, DDGI_ERR_UNSUPPORTED, "gradients need the FP32 form");
+    if (ctx->fp16 || ctx->dg.quant)
+        return fail(ctx, DDGI_ERR_UNSUPPORTED, "gradients need the FP32 form (unrounded atlas)");
+    if (ctx->dl.sky_mode != DDGI_SKY_CONSTANT)
+        return fail(ctx, DDGI_ERR_UNSUPPORTED, "gradients need the constant sky (a parameter)");
     if (!ctx->scene.built) return fail(ctx, DDGI_ERR_NO_SCENE, "no scene");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const uint32_t C = checkpoint_every, ncheck = (K + C - 1) / C;

@@ -16,6 +16,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "sky.cuh"
 #include "shade.cuh"
 
 namespace ddgi {
@@ -28,8 +29,14 @@ __global__ void __launch_bounds__(256) k_final_gather(GatherArgs a, AV at) {
     if (i >= a.pixels) return;
     const float4 pd = __ldg(a.position_depth + i);
     float4 out;
-    if (!(pd.w > 0.0f)) {
+    if (!(pd.w > 0.0f)) {  // FinalGather.frag:55-57
         out = make_float4(a.L.sky[0], a.L.sky[1], a.L.sky[2], 1.0f);
+        if (a.L.sky_mode == DDGI_SKY_ATMOSPHERE) {  // view direction in position.xyz, brightness 1
+            const float3 c = sky::atmosphere(a.origin, sky::nrm3(f3(pd.x, pd.y, pd.z)),
+                                             f3(a.L.dir[0], a.L.dir[1], a.L.dir[2]),
+                                             f3(a.L.color[0], a.L.color[1], a.L.color[2]), 1.0f);
+            out = make_float4(c.x, c.y, c.z, 1.0f);
+        }
     } else {
         const float4 nm = __ldg(a.normal_metalness + i);
         const float4 ar = __ldg(a.albedo_roughness + i);

@@ -88,6 +88,16 @@ cudaError_t launch_init_probes(const DeviceScene& sc, const DeviceGrid& g, const
 // probes go to list[0 .. count).
 cudaError_t launch_select_probes(const uint32_t* states, uint32_t P, uint32_t max_probes, uint32_t* sched,
                                  uint32_t* list, cudaStream_t st);
+// Hysteresis ramp of one update (sched[4..7]: blended value, host-side value,
+// target, probes counted); `cmd` carries the host's changes since the last
+// update; the update's probe count is *dev_count when given, else `count`.
+constexpr uint32_t kRampSetBlended = 1, kRampSetParam = 2, kRampSetTarget = 4, kRampZeroCount = 8;
+struct RampCmd {
+    uint32_t set;
+    float blended, param, target;
+};
+cudaError_t launch_hysteresis_ramp(uint32_t* sched, const RampCmd& cmd, const uint32_t* dev_count, uint32_t count,
+                                   uint32_t P, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Batched update of many probe volumes (batch.cu drives these launchers)
@@ -186,7 +196,8 @@ bool tc_blend_supported(uint32_t color_res, uint32_t depth_res);
 cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
                             const float4* dirs, uint8_t* wbuf, float* rowsum, uint32_t* states, void* color,
                             void* depth, float4* acc_color, float2* acc_depth, uint32_t* err, cudaStream_t st,
-                            const uint32_t* dev_count = nullptr, bool stall = false);
+                            const uint32_t* dev_count = nullptr, bool stall = false,
+                            const float* hyst_dev = nullptr);
 
 // blend_shared.cu: FP32 blend with the weights computed once per update
 size_t fp32_weight_bytes(uint32_t rays, uint32_t color_res, uint32_t depth_res);
@@ -194,13 +205,18 @@ uint32_t fp32_shared_tiles(uint32_t nprobes);
 cudaError_t set_shared_smem_limit();  // both shared-weight FP32 blend kernels, current device
 cudaError_t launch_blend_fp32_shared(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes,
                                      const float4* rays, const float4* dirs, float* W, float* wsum, uint32_t* states,
-                                     float4* color, float2* depth, cudaStream_t st, const uint32_t* dev_count = nullptr);
+                                     float4* color, float2* depth, cudaStream_t st, const uint32_t* dev_count = nullptr,
+                                     const float* hyst_dev = nullptr);
 cudaError_t launch_batch_blend_fp32_shared(const BatchTables& bt, const BatchBlendList& bl, uint32_t max_ntex,
                                            uint32_t max_rays, const float4* rays, cudaStream_t st);
+
+// sky.cu: miss records of an update shaded with the atmospheric sky
+cudaError_t launch_shade_sky(const DeviceGrid& g, const DeviceLight& L, uint32_t nprobes, const uint32_t* dev_count,
+                             const uint32_t* probe_list, const float4* dirs, float4* rays, cudaStream_t st);
 
 // blend.cu
 cudaError_t launch_blend_fp32(const DeviceGrid& g, const uint32_t* probe_list, uint32_t nprobes, const float4* rays,
                               const float4* dirs, uint32_t* states, float4* color, float2* depth, cudaStream_t st,
-                              const uint32_t* dev_count = nullptr);
+                              const uint32_t* dev_count = nullptr, const float* hyst_dev = nullptr);
 
 }  // namespace ddgi

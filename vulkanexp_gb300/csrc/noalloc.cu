@@ -128,6 +128,7 @@ extern "C" ddgi_status ddgi_blend_records_noalloc(const ddgi_grid_desc* grid, co
     dg.color_h = grid->color_res * grid->resolution[2];
     dg.depth_w = grid->depth_res * grid->resolution[0] * grid->resolution[1];
     dg.depth_h = grid->depth_res * grid->resolution[2];
+    dg.quant = 0;
 
     // The scratch keeps the previous call's contents: the error word must
     // start at zero; the table, weights and row sums are rewritten in full.

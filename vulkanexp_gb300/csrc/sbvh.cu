@@ -6,7 +6,7 @@
 // Dietrich 2009): a plane through the node's box, with the triangles that
 // straddle it referenced on both sides, each reference bounded by the part
 // of its triangle on that side (the triangle polygon clipped to the side's
-// slab).  Spatial splits are evaluated only where the object split's two
+// slab, in double precision).  Spatial splits are evaluated only where the object split's two
 // children overlap by more than `alpha` of the root's surface area, and
 // taken when their SAH cost is lower.  Overlapping geometry (the box
 // clusters of the at-scale workload) then needs far fewer node visits per
@@ -15,9 +15,9 @@
 //
 // A ray hit at a point p of a triangle is still found: p lies in the part of
 // the triangle on one side of every split plane, so some reference's box
-// contains it.  Clipped boxes are computed in float and intersected with
-// the exact slab planes; their rounding (a few ulps of the coordinates) is
-// far below the enlargement every node box receives (1e-6 of the
+// contains it.  Clipped boxes are computed in double, rounded outwards to
+// float and intersected with the exact slab planes; their error (ulps of
+// double) is far below the enlargement every node box receives (1e-6 of the
 // coordinates' magnitude and more), so box tests stay conservative and the
 // hit set equals that of any other tree.  The same triangle may be tested
 // twice along a ray; the tie rule (t, instance, primitive) makes that
@@ -35,6 +35,65 @@
 #include "traverse.cuh"
 
 namespace ddgi {
+
+// Bounding box of the part of a triangle inside a slab (lo > hi in some axis
+// when none is), intersected with the slab.  The polygon is clipped in
+// double precision and its box rounded outwards to float: for a triangle
+// nearly parallel to a clipping plane the crossing point's other coordinates
+// follow from a ratio of two nearly equal coordinate differences, and in
+// float their error grew to 1e-3 of the edge length (a face of a box yawed by
+// ~1e-4 rad, 4e-5 m thick in x, clipped by an x plane), far beyond the
+// enlargement of the node boxes: a ray hitting that face between two of its
+// clipped boxes was missed.
+void sbvh_clip_box(const float* tri, const float slab_lo[3], const float slab_hi[3], float out_lo[3],
+                   float out_hi[3]) {
+    double a[10][3], b[10][3];
+    int n = 3;
+    for (int v = 0; v < 3; ++v)
+        for (int k = 0; k < 3; ++k) a[v][k] = (double)tri[3 * v + k];
+    double(*in)[3] = a;
+    double(*out)[3] = b;
+    for (int k = 0; k < 3 && n > 0; ++k) {
+        for (int side = 0; side < 2 && n > 0; ++side) {
+            const double pl = (double)(side ? slab_hi[k] : slab_lo[k]);
+            int m = 0;
+            for (int i = 0; i < n; ++i) {
+                const double* p = in[i];
+                const double* q = in[(i + 1) % n];
+                const bool pin = side ? p[k] <= pl : p[k] >= pl;
+                const bool qin = side ? q[k] <= pl : q[k] >= pl;
+                if (pin && m < 10) {
+                    out[m][0] = p[0], out[m][1] = p[1], out[m][2] = p[2];
+                    ++m;
+                }
+                if (pin != qin && m < 10) {
+                    const double s = (pl - p[k]) / (q[k] - p[k]);
+                    for (int j = 0; j < 3; ++j) out[m][j] = p[j] + (q[j] - p[j]) * s;
+                    out[m][k] = pl;
+                    ++m;
+                }
+            }
+            n = m;
+            std::swap(in, out);
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        out_lo[k] = INFINITY;
+        out_hi[k] = -INFINITY;
+    }
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            float lo = (float)in[i][k], hi = lo;
+            if ((double)lo > in[i][k]) lo = std::nextafter(lo, -INFINITY);
+            if ((double)hi < in[i][k]) hi = std::nextafter(hi, INFINITY);
+            out_lo[k] = fminf(out_lo[k], lo);
+            out_hi[k] = fmaxf(out_hi[k], hi);
+        }
+    for (int k = 0; k < 3; ++k) {
+        out_lo[k] = fmaxf(out_lo[k], slab_lo[k]);
+        out_hi[k] = fminf(out_hi[k], slab_hi[k]);
+    }
+}
 
 namespace {
 
@@ -122,48 +181,10 @@ class Sbvh {
     const float alpha_;
     float root_area_ = 0.0f;
 
-    // Bounding box of the part of triangle `prim` inside `slab` (empty box if
-    // none), intersected with the slab.
     Box clip(uint32_t prim, const Box& slab) const {
-        float a[10][3], b[10][3];
-        int n = 3;
-        const float* t = tris_ + 9 * (size_t)prim;
-        for (int v = 0; v < 3; ++v)
-            for (int k = 0; k < 3; ++k) a[v][k] = t[3 * v + k];
-        float(*in)[3] = a;
-        float(*out)[3] = b;
-        for (int k = 0; k < 3 && n > 0; ++k) {
-            for (int side = 0; side < 2 && n > 0; ++side) {
-                const float pl = side ? slab.hi[k] : slab.lo[k];
-                int m = 0;
-                for (int i = 0; i < n; ++i) {
-                    const float* p = in[i];
-                    const float* q = in[(i + 1) % n];
-                    const bool pin = side ? p[k] <= pl : p[k] >= pl;
-                    const bool qin = side ? q[k] <= pl : q[k] >= pl;
-                    if (pin && m < 10) {
-                        out[m][0] = p[0], out[m][1] = p[1], out[m][2] = p[2];
-                        ++m;
-                    }
-                    if (pin != qin && m < 10) {
-                        const float s = (pl - p[k]) / (q[k] - p[k]);
-                        for (int j = 0; j < 3; ++j) out[m][j] = p[j] + (q[j] - p[j]) * s;
-                        out[m][k] = pl;
-                        ++m;
-                    }
-                }
-                n = m;
-                std::swap(in, out);
-            }
-        }
         Box r;
-        r.reset();
-        for (int i = 0; i < n; ++i)
-            for (int k = 0; k < 3; ++k) {
-                r.lo[k] = fminf(r.lo[k], in[i][k]);
-                r.hi[k] = fmaxf(r.hi[k], in[i][k]);
-            }
-        return intersect(r, slab);
+        sbvh_clip_box(tris_ + 9 * (size_t)prim, slab.lo, slab.hi, r.lo, r.hi);
+        return r;
     }
 
     static int bin_of(float x, float lo, float scale) {

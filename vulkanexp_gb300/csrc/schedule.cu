@@ -80,7 +80,51 @@ __global__ void __launch_bounds__(kThreads) k_select_probes(const uint32_t* __re
     }
 }
 
+// IrradianceProbes::update's hysteresis ramp (src/IrradianceProbes.cpp:462-476)
+// for one update, one thread.  sched[4..7] hold the ramp: the hysteresis the
+// blend uses (the reference's uniform buffer), the host-side
+// GridParameters.hysteresis, TargetHysteresis (float bits) and the probes
+// counted since the last step (the reference's static updatedProbes).  The
+// host's changes since the last update (cmd) apply first.  Once a full probe
+// count has been refreshed, a step either uploads the current value and then
+// moves it a tenth of the way towards the target (updateUniforms() comes
+// before the increment, so the blend sees the value one step late) or, within
+// 0.05 of the target, sets and uploads the target itself; then this update's
+// probe count is added.  Float operations are rounded one by one as the
+// reference's host code computes them; the 0.05 comparison is in double.
+__global__ void k_hysteresis_ramp(uint32_t* sched, RampCmd cmd, const uint32_t* dev_count, uint32_t count,
+                                  uint32_t P) {
+    float* f = reinterpret_cast<float*>(sched + 4);
+    float blended = f[0], h = f[1], target = f[2];
+    uint32_t counted = sched[7];
+    if (cmd.set & kRampSetBlended) blended = cmd.blended;
+    if (cmd.set & kRampSetParam) h = cmd.param;
+    if (cmd.set & kRampSetTarget) target = cmd.target;
+    if (cmd.set & kRampZeroCount) counted = 0;
+    if (counted >= P) {
+        if ((double)fabsf(__fsub_rn(h, target)) > 0.05) {
+            blended = h;
+            h = __fadd_rn(h, __fmul_rn(0.1f, __fsub_rn(target, h)));
+        } else if (h != target) {
+            h = target;
+            blended = h;
+        }
+        counted -= P;
+    }
+    counted += dev_count ? *dev_count : count;
+    f[0] = blended;
+    f[1] = h;
+    f[2] = target;
+    sched[7] = counted;
+}
+
 }  // namespace
+
+cudaError_t launch_hysteresis_ramp(uint32_t* sched, const RampCmd& cmd, const uint32_t* dev_count, uint32_t count,
+                                   uint32_t P, cudaStream_t st) {
+    k_hysteresis_ramp<<<1, 1, 0, st>>>(sched, cmd, dev_count, count, P);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_select_probes(const uint32_t* states, uint32_t P, uint32_t max_probes, uint32_t* sched,
                                  uint32_t* list, cudaStream_t st) {

@@ -71,6 +71,9 @@ _SIGNATURES = [
     ("ddgi_update_instances", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]),
     ("ddgi_final_gather", C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ddgi_set_trace_tuning", C.c_int, [C.c_void_p, C.POINTER(TraceTuning)]),
+    ("ddgi_set_target_hysteresis", C.c_int, [C.c_void_p, C.c_float]),
+    ("ddgi_set_sky_mode", C.c_int, [C.c_void_p, C.c_int]),
+    ("ddgi_get_hysteresis", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ddgi_set_leaf_size", C.c_int, [C.c_void_p, C.c_uint32]),
     ("ddgi_set_build_mode", C.c_int, [C.c_void_p, C.c_int]),
     ("ddgi_get_atlas_raw", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]),
@@ -199,6 +202,20 @@ class Context:
         i = None if ids is None else np.ascontiguousarray(ids, np.uint32)
         self._check(self.lib.ddgi_update_instances(self.h, _ptr(i), _ptr(t), len(t), int(bool(rebuild)),
                                                    _stream_ptr(stream)))
+
+    def set_sky_mode(self, mode):
+        """abi.SKY_CONSTANT (default) or abi.SKY_ATMOSPHERE."""
+        self._check(self.lib.ddgi_set_sky_mode(self.h, int(mode)))
+
+    def set_target_hysteresis(self, target):
+        """Hysteresis ramp towards `target` (None or negative: off)."""
+        self._check(self.lib.ddgi_set_target_hysteresis(self.h, -1.0 if target is None else float(target)))
+
+    def hysteresis(self, stream=None):
+        """(blended, host-side value, probes counted) of the ramp."""
+        b, p, c = C.c_float(), C.c_float(), C.c_uint32()
+        self._check(self.lib.ddgi_get_hysteresis(self.h, C.byref(b), C.byref(p), C.byref(c), _stream_ptr(stream)))
+        return b.value, p.value, c.value
 
     def set_light(self, light):
         self._check(self.lib.ddgi_set_light(self.h, C.byref(light)))
@@ -510,17 +527,32 @@ class Batch:
 
 
 class IrradianceProbes:
-    """Drop-in mirror of VulkanExp's IrradianceProbes over the C ABI."""
+    """Drop-in mirror of VulkanExp's IrradianceProbes over the C ABI.
+
+    The hysteresis ramp of the reference's update (TargetHysteresis,
+    src/IrradianceProbes.cpp:462-476) runs in the library
+    (ddgi_set_target_hysteresis): GridParameters.hysteresis here is the value
+    updateUniforms() uploads; the ramp's current values are `hysteresis()`."""
 
     MaxRaysPerProbe = 1024
 
     def __init__(self):
         # GridInfo defaults (src/IrradianceProbes.hpp:49-60)
         self.GridParameters = abi.make_grid((0, 0, 0), (1, 1, 1), (32, 16, 32), 192, 8, 16, 0.0, 12.0, 0.3)
-        self.TargetHysteresis = 0.98
+        self._target = 0.98
         self.ProbesPerUpdate = 0
         self.ctx = None
-        self._updated = 0
+        self._shadow = 0.0
+
+    @property
+    def TargetHysteresis(self):
+        return self._target
+
+    @TargetHysteresis.setter
+    def TargetHysteresis(self, value):
+        self._target = float(value)
+        if self.ctx:
+            self.ctx.set_target_hysteresis(self._target)
 
     def init(self, extent_min, extent_max):
         self.GridParameters.extent_min[:] = [float(v) for v in extent_min]
@@ -528,6 +560,8 @@ class IrradianceProbes:
         if self.ctx:
             self.ctx.close()
         self.ctx = Context(self.GridParameters)
+        self._shadow = self.GridParameters.hysteresis
+        self.ctx.set_target_hysteresis(self._target)
 
     def setScene(self, scene, stream=None):
         self.ctx.build_scene(scene, stream)
@@ -536,7 +570,17 @@ class IrradianceProbes:
         self.ctx.set_light(light)
 
     def updateUniforms(self):
+        """ddgi_set_grid.  Keeps the ramp's current value unless
+        GridParameters.hysteresis was changed since it was last in step with
+        the library (syncHysteresis reads it back)."""
+        if np.float32(self.GridParameters.hysteresis) == np.float32(self._shadow):
+            self.GridParameters.hysteresis = self.ctx.hysteresis()[1]
         self.ctx.set_grid(self.GridParameters)
+        self._shadow = self.GridParameters.hysteresis
+
+    def syncHysteresis(self, stream=None):
+        """Reads the ramp's current value into GridParameters.hysteresis."""
+        self.GridParameters.hysteresis = self._shadow = self.ctx.hysteresis(stream)[1]
 
     def getProbeCount(self):
         r = self.GridParameters.resolution
@@ -544,37 +588,25 @@ class IrradianceProbes:
 
     def initProbes(self, orientation, stream=None):
         """IrradianceProbes::initProbes (src/IrradianceProbes.cpp:357-394):
-        classify the probes, and restart the hysteresis ramp from 0."""
+        classify the probes; the ramp's host-side value restarts from 0."""
         self.ctx.init_probes(orientation, stream)
-        self.GridParameters.hysteresis = 0.0
-        self.updateUniforms()
-        self._updated = 0
+        self.GridParameters.hysteresis = self._shadow = 0.0
+
+    def hysteresis(self, stream=None):
+        """(value the last update blended with, host-side value, probes
+        counted since the last ramp step)."""
+        return self.ctx.hysteresis(stream)
 
     def update(self, orientation, probe_list=None, stream=None):
         """IrradianceProbes::update (src/IrradianceProbes.cpp:426-594):
         `orientation` is the 3x3 ray-set rotation.  Without a probe list the
         probes are the ones selectProbesToUpdate picks (chosen on the device,
-        at most ProbesPerUpdate, 0 = no cap), and the grid hysteresis ramps
-        towards TargetHysteresis once per probe count of refreshed probes
-        (:462-476; the new value is used by the same update, where the
-        reference uploads it one ramp step later).  The ramp reads the
-        selected count back from the device."""
+        at most ProbesPerUpdate, 0 = no cap); the hysteresis ramp steps on
+        the device, with no readback."""
         if probe_list is not None:
             self.ctx.update(orientation, probe_list, stream)
-            return
-        P = self.getProbeCount()
-        if self._updated >= P:
-            h = np.float32(self.GridParameters.hysteresis)
-            t = np.float32(self.TargetHysteresis)
-            if abs(h - t) > np.float32(0.05):
-                self.GridParameters.hysteresis = float(h + np.float32(0.1) * (t - h))
-                self.updateUniforms()
-            elif h != t:
-                self.GridParameters.hysteresis = float(t)
-                self.updateUniforms()
-            self._updated -= P
-        self.ctx.update_scheduled(orientation, self.ProbesPerUpdate, stream)
-        self._updated += self.ctx.schedule(with_list=False, stream=stream)["count"]
+        else:
+            self.ctx.update_scheduled(orientation, self.ProbesPerUpdate, stream)
 
     def getIrradiance(self):
         return self.ctx.get_atlas(abi.ATLAS_COLOR)
