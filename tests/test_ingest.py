@@ -155,3 +155,45 @@ def test_gltf_cycle_rejected(tmp_path):
     p.write_text(json.dumps(gl))
     with pytest.raises(ingest.IngestError):
         ingest.load(str(p))
+
+
+FIXTURE = __import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "editor_room.scene")
+
+
+def test_editor_saved_scene_fixture():
+    """tests/golden/editor_room.scene is laid out as the editor's
+    Scene::save writes a file (src/Scene.cpp:710-817, made by
+    tests/golden/make_scene_fixture.py, not by this package's writer): the
+    reference's JSON printing (six-decimal reals, "-1" for unset textures,
+    std::map key order), unpadded chunks, 64-byte vertices.  It loads into
+    the renderer's arrays: one offset entry per mesh with triangles (the
+    empty mesh has none), instances ordered by (mesh, material, entity) with
+    global transforms parent x local, materials with unset textures."""
+    data = ingest.read_scene_file(FIXTURE)
+    assert [m["name"] for m in data.meshes] == ["Floor", "Box", "Wall", "Empty"]
+    sc = ingest.to_scene(data)
+    assert len(sc.vertices) == 33 and len(sc.indices) == 48
+    assert sc.offsets.tolist() == [(0, 0, 0), (1, 4, 6), (2, 28, 42)]
+    assert sc.instances["mesh_index"].tolist() == [0, 1, 1, 1, 2]
+    assert sc.instances["custom_index"].tolist() == [0, 1, 1, 1, 2]
+    assert (sc.instances["mask"] == 1).all()
+    # Pillar (mesh 1, material 0) sorts before Box A (material 1), Box B (2)
+    np.testing.assert_array_equal(sc.instances["transform"][1], np.float32([0.5, 0, 0, 5, 0, 4, 0, 2, 0, 0, 0.5, -4]))
+    # Box A: Group (yaw 30 deg, printed as 0.866025 / 0.5) x (scale 1.5, lift 0.75)
+    c, s = 0.866025, 0.5
+    group = np.array([[c, 0, s, 2], [0, 1, 0, 0], [-s, 0, c, 1], [0, 0, 0, 1]])
+    box_a = np.array([[1.5, 0, 0, 0], [0, 1.5, 0, 0.75], [0, 0, 1.5, 0], [0, 0, 0, 1]])
+    np.testing.assert_array_equal(sc.instances["transform"][2], (group @ box_a)[:3].reshape(12).astype(np.float32))
+    assert sc.materials["base_color"][2].tolist() == pytest.approx([0.3, 0.6, 0.9])
+    assert sc.materials["emissive"][2].tolist() == pytest.approx([0.5, 0.4, 0.1])
+    assert (sc.materials["albedo_texture"] == abi.NO_TEXTURE).all()
+    assert (sc.materials["normal_texture"] == abi.NO_TEXTURE).all()
+    # the oracle traces it: rays from above hit the floor or the boxes
+    o = Oracle(sc)
+    rng = np.random.default_rng(4)
+    org = np.column_stack([rng.uniform(-9, 9, 2000), np.full(2000, 8.0), rng.uniform(-9, 9, 2000)]).astype(np.float32)
+    dirs = np.tile(np.float32([0, -1, 0]), (2000, 1))
+    hits, _ = o.trace(org, dirs, 0.01, 100.0)
+    assert (hits["instance"] != abi.MISS).all()
+    assert set(hits["instance"].tolist()) >= {0, 2}
+    o.close()

@@ -11,21 +11,26 @@
 // normalised by the row sums sum_r W[t][r] (the reference's result.w, the
 // same for every probe, so it is computed once per update).
 //
-// Tiling: a CTA takes 32 probes; each probe owns 4 rows of the A operand
-// (r, g, b, 0 for colour; d, d^2, 0, 0 for depth), so A is M = 128 rows x K
-// rays, K-major, and the weights are B (N = texels, padded to 16) x K.
-// K is processed in chunks of 64 rays staged in shared memory as BF16
-// (radiance scaled per probe by 1 / max radiance, depth by 1 / |cell|);
-// one thread issues tcgen05.mma (M = 128, K = 16 per instruction) into two
-// FP32 accumulators in tensor memory (colour at column 0, depth at 256).
-// Both operands are split into a BF16 high part and a BF16 remainder
-// (x = hi + lo) and three products hi*hi + hi*lo + lo*hi are accumulated,
-// which brings the contraction to ~16 mantissa bits; the MMAs are a small
-// part of this memory-bound kernel, and it keeps the atlas error against an
-// FP64 blend below 1e-3 (the FP16 atlas store dominates what is left).
-// The epilogue reads the accumulators with tcgen05.ld, undoes the scaling,
-// normalises, applies hysteresis in FP32 against the FP16 atlas, stores FP16
-// texels, copies the borders and updates the probe states.
+// Tiling: a CTA takes 25 probes; each probe owns 5 rows of the A operand
+// (its ray records' r, g, b, clamped depth d and d^2), so A is M = 128 rows
+// (3 zero) x K rays, K-major, and the weights are B: the depth rows then the
+// colour rows (each texel count padded to 16), N = Nd + Nc <= 256 in one
+// accumulator at tensor-memory column 0 (wider tiles: depth at 0, colour at
+// 256, in two MMAs).  Only the row x column pairs of matching kind are read
+// back; the rest of the product is the price of one MMA per K step, cheap in
+// this memory-bound kernel.  K is processed in chunks of 32 rays staged in
+// shared memory as BF16; both operands are split into a BF16 high part and a
+// BF16 remainder (x = hi + lo) and three products hi*hi + hi*lo + lo*hi are
+// accumulated (~16 mantissa bits, below the FP16 atlas store's rounding;
+// BF16 keeps FP32's exponent range, so no scaling is needed).  One thread
+// issues tcgen05.mma (M = 128, K = 16 per instruction); while a chunk's
+// MMAs run, the next chunk's weights arrive by cp.async into the second B
+// buffer and its records into registers.  With 256 accumulator columns two
+// CTAs share an SM.  The epilogue reads the accumulators with tcgen05.ld,
+// normalises through shared memory into texel order, applies hysteresis in
+// the FP32 accumulators (previous values loaded eight per thread at a time),
+// stores FP16 texels together with the border texels that copy them, and
+// updates the probe states.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -39,17 +44,17 @@ namespace ddgi {
 
 namespace {
 
-constexpr int kTileProbes = 32;  // 128 A rows
-constexpr int kKChunk = 64;      // rays per shared-memory stage
+constexpr int kTileProbes = 25;    // 125 A rows: (r, g, b, d, d^2) per probe
+constexpr int kRowsPerProbe = 5;
+constexpr int kKChunk = 32;        // rays per shared-memory stage
 constexpr int kThreads = 256;
 constexpr uint32_t kSBO = (kKChunk / 8) * 128;  // bytes between 8-row groups
 constexpr uint32_t kLBO = 128;                  // bytes between K-adjacent core matrices
-constexpr uint32_t kDepthCol = 256;             // TMEM column of the depth accumulator
-constexpr uint32_t kTmemCols = 512;
-// Every CTA allocates all 512 tensor-memory columns of its SM, so no two
-// CTAs may share an SM: the shared-memory request is at least this much
-// (two of them exceed the SM's 228 KB).
-constexpr size_t kMinSmem = 120 * 1024;
+constexpr uint32_t kAPart = 128 * kKChunk * 2;  // one BF16 part of the A stage (128 rows)
+// A CTA whose texels need more than 256 accumulator columns allocates all
+// 512 of its SM's: its shared-memory request is then at least this much, so
+// no second CTA shares the SM (two exceed the SM's 228 KB).
+constexpr size_t kOneCtaSmem = 120 * 1024;
 
 struct TcArgs {
     DeviceGrid g;
@@ -135,7 +140,7 @@ __device__ __forceinline__ void tc_weight_row(uint32_t row, uint32_t lane, const
         float sc = texel_scale(n), ce = 0.5f * (float)(n - 1);
         td = oct_decode(sc * ((float)(t % n) - ce), sc * ((float)(t / n) - ce));
     }
-    const size_t part_bytes = (size_t)(Nd + Nc) * 128;  // one chunk of one part
+    const size_t part_bytes = (size_t)(Nd + Nc) * (kKChunk * 2);  // one chunk of one part
     const uint32_t groups = nchunks * (kKChunk / 8);
     float sum = 0.0f;
     for (uint32_t gidx = lane; gidx < groups; gidx += 32) {
@@ -166,7 +171,7 @@ __device__ __forceinline__ void tc_weight_row(uint32_t row, uint32_t lane, const
         }
         sum += part;
         const uint32_t c = gidx / (kKChunk / 8), kg = gidx % (kKChunk / 8);
-        const size_t off = (size_t)c * 2 * part_bytes + (colour ? (size_t)Nd * 128 : 0) + canon_off(t, kg);
+        const size_t off = (size_t)c * 2 * part_bytes + (colour ? (size_t)Nd * (kKChunk * 2) : 0) + canon_off(t, kg);
         *reinterpret_cast<uint4*>(wout + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
         *reinterpret_cast<uint4*>(wout + off + part_bytes) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
     }
@@ -181,161 +186,182 @@ __global__ void k_tc_weights(const float4* dirs, uint32_t R, uint32_t nc, uint32
                   wout, rowsum);
 }
 
-// Blend of the 32-probe tile starting at probe slot p0 (< nprobes) by the
-// whole CTA.
-// Scale of a probe's colour records before the BF16 split: the power of two
-// 2^e >= the largest radiance (so scaled records are <= 1 and the scaling
-// is exact), e clamped to [-100, 100]; a probe whose largest radiance is
-// below 2^-100 (zero, denormal) keeps scale 1, so the reciprocal is always
-// finite and a zero record never meets an infinite one (0 x inf = NaN).
-__device__ __forceinline__ float radiance_scale(float mx) {
-    if (!(mx >= 0x1p-100f)) return 1.0f;  // also NaN
-    int e = 100;
-    if (mx < 0x1p100f) frexpf(mx, &e);
-    return ldexpf(1.0f, e);
+// Calls put(bx, by) for each border texel of a tile of side n that copies
+// interior texel (x, y), 1 <= x, y <= n - 2 (probesCopyBorders.comp:21-245,
+// generalised: the inverse of border_entry); up to 8 for n = 3, 3 otherwise.
+template <class F>
+__device__ __forceinline__ void for_border_targets(int x, int y, int n, F put) {
+    if (x == 1) put(0, n - 1 - y);
+    if (x == n - 2) put(n - 1, n - 1 - y);
+    if (y == 1) put(n - 1 - x, 0);
+    if (y == n - 2) put(n - 1 - x, n - 1);
+    if (x == n - 2 && y == n - 2) put(0, 0);
+    if (x == n - 2 && y == 1) put(0, n - 1);
+    if (x == 1 && y == n - 2) put(n - 1, 0);
+    if (x == 1 && y == 1) put(n - 1, n - 1);
 }
 
+// Shared-memory layout of a tile: the A operand (hi part, lo part), then two
+// B buffers (chunk c in buffer c % 2); the epilogue staging reuses it all.
+__host__ __device__ __forceinline__ size_t tc_b_bytes(uint32_t Nd, uint32_t Nc) { return 2 * (size_t)(Nd + Nc) * (kKChunk * 2); }
+__host__ __device__ __forceinline__ size_t tc_stage_bytes(uint32_t Nd, uint32_t Nc) {
+    return 2 * (size_t)kAPart + 2 * tc_b_bytes(Nd, Nc);
+}
+
+// Dynamic shared memory of a tile: the operand stages or the epilogue
+// staging, whichever is larger; with more than 256 accumulator columns at
+// least kOneCtaSmem (one CTA per SM).
+__host__ __device__ __forceinline__ size_t tc_smem_bytes(uint32_t nc, uint32_t nd, uint32_t Nc, uint32_t Nd) {
+    const size_t stage = tc_stage_bytes(Nd, Nc);
+    const size_t staging = (size_t)kTileProbes * (nc * nc * 3 + nd * nd * 2) * sizeof(float);
+    size_t smem = stage > staging ? stage : staging;
+    if (Nd + Nc > 256 && smem < kOneCtaSmem) smem = kOneCtaSmem;
+    return smem;
+}
+
+// Blend of the tile of kTileProbes probe slots starting at p0 (< nprobes) by
+// the whole CTA.
 __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0, const uint32_t nprobes) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    // A operands (128 x 64 BF16 = 16 KB each): colour hi/lo, depth hi/lo;
-    // then B: high parts of (Nd + Nc) x 64, then the remainders
-    uint8_t* sA_c = smem;
-    uint8_t* sA_cl = smem + 16384;
-    uint8_t* sA_d = smem + 32768;
-    uint8_t* sA_dl = smem + 49152;
-    uint8_t* sB = smem + 65536;
+    uint8_t* sA = smem;                          // hi part, then lo part (kAPart each)
+    uint8_t* sB = smem + 2 * kAPart;             // two buffers of tc_b_bytes
     __shared__ uint64_t s_bar;
     __shared__ uint32_t s_tmem;
-    __shared__ float s_max[kTileProbes];  // per-probe colour scale (radiance_scale)
     __shared__ uint32_t s_oor[kTileProbes], s_maxc[kTileProbes];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t np = min((uint32_t)kTileProbes, nprobes - p0);
     const uint32_t R = a.g.rays;
     const float cell = a.g.cell_len;
+    const bool split = a.Nd + a.Nc > 256;        // two accumulators: depth at column 0, colour at 256
+    const uint32_t cols = split ? 512u : 256u;
+    const uint32_t cbase = split ? 256u : a.Nd;  // first colour column
+    const size_t bbytes = tc_b_bytes(a.Nd, a.Nc);
+    const uint32_t b16 = (uint32_t)(bbytes / 16);
 
-    if (warp == 0) tc::tmem_alloc(&s_tmem, kTmemCols);
+    if (warp == 0) tc::tmem_alloc(&s_tmem, cols);
     if (tid == 0) tc::mbar_init(&s_bar, 1);
-    if (tid < kTileProbes) s_maxc[tid] = 0u;
+    if (tid < kTileProbes) {
+        s_maxc[tid] = 0u;
+        s_oor[tid] = 0u;
+    }
+    // A rows kTileProbes * 5 .. 127 stay zero for the whole tile
+    for (uint32_t r = kTileProbes * kRowsPerProbe + (uint32_t)tid / 4; r < 128; r += kThreads / 4)
+        for (int part = 0; part < 2; ++part)
+            *reinterpret_cast<uint4*>(sA + part * kAPart + canon_off(r, (uint32_t)tid & 3u)) = make_uint4(0, 0, 0, 0);
+    // B of chunk 0
+    {
+        const uint4* src = a.wchunks;
+        uint4* dst = reinterpret_cast<uint4*>(sB);
+        for (uint32_t i = tid; i < b16; i += kThreads) tc::cp_async16(dst + i, src + i);
+        tc::cp_async_commit();
+    }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = s_tmem;
 
-    // pass 1: per-probe radiance maximum and out-of-range count
-    for (int q = 0; q < kTileProbes / 8; ++q) {
-        uint32_t pl = warp * (kTileProbes / 8) + q;
-        float mx = 0.0f;
-        uint32_t oor = 0;
-        if (pl < np) {
-            const float4* pr = a.rays + (size_t)(p0 + pl) * R;
-#pragma unroll 8
-            for (uint32_t r = lane; r < R; r += 32) {  // unrolled: eight loads in flight per lane
-                float4 v = pr[r];
-                mx = fmaxf(mx, fmaxf(v.x, fmaxf(v.y, v.z)));
-                if (v.w < 0.0f || v.w > cell) ++oor;
+    // thread -> (probe, 4 consecutive rays of the chunk); 200 of 256 threads
+    const uint32_t pl = (uint32_t)tid >> 3, j = (uint32_t)tid & 7u;
+    const bool builder = pl < (uint32_t)kTileProbes;
+    const bool live = builder && pl < np;
+    const float4* prec = a.rays + (size_t)(p0 + (live ? pl : 0u)) * R;
+    float4 v[4];
+    auto load = [&](uint32_t c) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const uint32_t r = c * kKChunk + j * 4 + e;
+            v[e] = live && r < R ? __ldg(prec + r) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    };
+    load(0);
+    uint32_t oor = 0;
+    const uint32_t N = a.Nd + a.Nc;
+    const uint32_t id_all = tc::idesc_bf16_f32(128, N), id_d = tc::idesc_bf16_f32(128, a.Nd),
+                   id_c = tc::idesc_bf16_f32(128, a.Nc);
+    bool ok = true;
+    uint32_t failed = 0;  // the chunk whose completion wait ran out
+    for (uint32_t c = 0; c < a.nchunks; ++c) {
+        if (c > 0) {  // the previous chunk's MMAs read A and the other B buffer
+            const bool done = tc::mbar_wait(&s_bar, (c - 1) & 1u, kWaitLimitNs);
+            tc::fence_after_sync();
+            if (!__syncthreads_and(done)) {
+                ok = false;
+                failed = c - 1;
+                break;
             }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            oor += __shfl_xor_sync(0xffffffffu, oor, o);
-        }
-        if (lane == 0) {
-            s_max[pl] = radiance_scale(mx);
-            s_oor[pl] = oor;
-        }
-    }
-    __syncthreads();
-
-    const uint32_t idc = tc::idesc_bf16_f32(128, a.Nc), idd = tc::idesc_bf16_f32(128, a.Nd);
-    const size_t chunk16 = 2 * (size_t)(a.Nd + a.Nc) * 128 / 16;  // both parts
-    bool ok = true;
-    uint32_t phase = 0;
-    for (uint32_t c = 0; c < a.nchunks; ++c) {
-        {   // B: this chunk of both weight matrices, copied while A is built
-            // (the previous chunk's MMAs have completed: its wait ended the
-            // last iteration)
-            const uint4* src = a.wchunks + (size_t)c * chunk16;
-            uint4* dst = reinterpret_cast<uint4*>(sB);
-            for (uint32_t i = tid; i < chunk16; i += kThreads) tc::cp_async16(dst + i, src + i);
-        }
-        {   // A: thread = (probe, group of 8 rays); one 16-byte core-matrix row per operand row
-            const uint32_t pl = (uint32_t)tid >> 3, j = (uint32_t)tid & 7u;
-            const float inv = 1.0f / s_max[pl];  // a power of two: exact
-            const float cinv = 1.0f / cell;
-            // [row][hi/lo][4 words of 2 BF16]: rows r, g, b (colour), d, d^2 (depth)
-            uint32_t w[5][2][4];
+        if (builder) {  // A rows (r, g, b, d, d^2) of this thread's probe, 4 rays: half a core-matrix row
+            uint32_t w[5][2][2];
 #pragma unroll
-            for (int e = 0; e < 8; e += 2) {
-                float4 v[2];
-                float dn[2];
+            for (int e = 0; e < 4; e += 2) {
+                float dep[2];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    uint32_t r = c * kKChunk + j * 8 + e + h;
-                    bool valid = pl < np && r < R;
-                    v[h] = valid ? a.rays[(size_t)(p0 + pl) * R + r] : make_float4(0, 0, 0, 0);
-                    float dep = fminf(cell, v[h].w);
-                    if (dep < 0.0f) dep = cell;
-                    dn[h] = valid ? dep * cinv : 0.0f;
+                    const uint32_t r = c * kKChunk + j * 4 + e + h;
+                    const float wv = v[e + h].w;
+                    if (live && r < R && (wv < 0.0f || wv > cell)) ++oor;
+                    float dd = fminf(cell, wv);
+                    if (dd < 0.0f) dd = cell;
+                    dep[h] = live && r < R ? dd : 0.0f;
                 }
-                w[0][0][e / 2] = pack2(v[0].x * inv, v[1].x * inv, &w[0][1][e / 2]);
-                w[1][0][e / 2] = pack2(v[0].y * inv, v[1].y * inv, &w[1][1][e / 2]);
-                w[2][0][e / 2] = pack2(v[0].z * inv, v[1].z * inv, &w[2][1][e / 2]);
-                w[3][0][e / 2] = pack2(dn[0], dn[1], &w[3][1][e / 2]);
-                w[4][0][e / 2] = pack2(dn[0] * dn[0], dn[1] * dn[1], &w[4][1][e / 2]);
+                w[0][0][e / 2] = pack2(v[e].x, v[e + 1].x, &w[0][1][e / 2]);
+                w[1][0][e / 2] = pack2(v[e].y, v[e + 1].y, &w[1][1][e / 2]);
+                w[2][0][e / 2] = pack2(v[e].z, v[e + 1].z, &w[2][1][e / 2]);
+                w[3][0][e / 2] = pack2(dep[0], dep[1], &w[3][1][e / 2]);
+                w[4][0][e / 2] = pack2(dep[0] * dep[0], dep[1] * dep[1], &w[4][1][e / 2]);
             }
-            const uint4 z = make_uint4(0, 0, 0, 0);
 #pragma unroll
-            for (int part = 0; part < 2; ++part) {
-                uint8_t* ac = part ? sA_cl : sA_c;
-                uint8_t* ad = part ? sA_dl : sA_d;
+            for (int part = 0; part < 2; ++part)
 #pragma unroll
-                for (int ch = 0; ch < 3; ++ch)
-                    *reinterpret_cast<uint4*>(ac + canon_off(pl * 4 + ch, j)) =
-                        make_uint4(w[ch][part][0], w[ch][part][1], w[ch][part][2], w[ch][part][3]);
-                *reinterpret_cast<uint4*>(ac + canon_off(pl * 4 + 3, j)) = z;
-                *reinterpret_cast<uint4*>(ad + canon_off(pl * 4 + 0, j)) =
-                    make_uint4(w[3][part][0], w[3][part][1], w[3][part][2], w[3][part][3]);
-                *reinterpret_cast<uint4*>(ad + canon_off(pl * 4 + 1, j)) =
-                    make_uint4(w[4][part][0], w[4][part][1], w[4][part][2], w[4][part][3]);
-                *reinterpret_cast<uint4*>(ad + canon_off(pl * 4 + 2, j)) = z;
-                *reinterpret_cast<uint4*>(ad + canon_off(pl * 4 + 3, j)) = z;
-            }
+                for (int ch = 0; ch < kRowsPerProbe; ++ch)
+                    *reinterpret_cast<uint2*>(sA + part * kAPart + canon_off(pl * kRowsPerProbe + ch, j >> 1) +
+                                              (j & 1u) * 8u) = make_uint2(w[ch][part][0], w[ch][part][1]);
         }
-        tc::cp_async_wait_all();
+        if (c + 1 < a.nchunks) {  // next chunk: weights by cp.async, records into registers
+            const uint4* src = a.wchunks + (size_t)(c + 1) * b16;
+            uint4* dst = reinterpret_cast<uint4*>(sB + ((c + 1) & 1u) * bbytes);
+            for (uint32_t i = tid; i < b16; i += kThreads) tc::cp_async16(dst + i, src + i);
+            tc::cp_async_commit();
+            load(c + 1);
+            tc::cp_async_wait_group<1>();  // this chunk's weights have landed
+        } else {
+            tc::cp_async_wait_group<0>();
+        }
         tc::fence_proxy_async();
         __syncthreads();
         if (tid == 0 && !a.stall) {
             tc::fence_after_sync();
-            const uint32_t part = (a.Nd + a.Nc) * 128;
-            const uint32_t aC = tc::smem_u32(sA_c), aCl = tc::smem_u32(sA_cl);
-            const uint32_t aD = tc::smem_u32(sA_d), aDl = tc::smem_u32(sA_dl);
-            const uint32_t bD = tc::smem_u32(sB), bC = bD + a.Nd * 128;
+            const uint32_t aH = tc::smem_u32(sA), aL = aH + kAPart;
+            const uint32_t bH = tc::smem_u32(sB + (c & 1u) * bbytes), bL = bH + N * (kKChunk * 2);
             // hi*hi + hi*lo + lo*hi, K = 16 per instruction
-            const uint32_t ac_[3] = {aC, aC, aCl}, ad_[3] = {aD, aD, aDl};
-            const uint32_t bo_[3] = {0u, part, 0u};
+            const uint32_t a_[3] = {aH, aH, aL}, b_[3] = {bH, bL, bH};
 #pragma unroll
             for (uint32_t ks = 0; ks < kKChunk / 16; ++ks) {
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
-                    uint32_t acc = (c > 0 || ks > 0 || q > 0) ? 1u : 0u;
-                    tc::mma_bf16(tmem + 0, tc::smem_desc(ac_[q] + ks * 256, kLBO, kSBO),
-                                 tc::smem_desc(bC + bo_[q] + ks * 256, kLBO, kSBO), idc, acc);
-                    tc::mma_bf16(tmem + kDepthCol, tc::smem_desc(ad_[q] + ks * 256, kLBO, kSBO),
-                                 tc::smem_desc(bD + bo_[q] + ks * 256, kLBO, kSBO), idd, acc);
+                    const uint32_t acc = (c > 0 || ks > 0 || q > 0) ? 1u : 0u;
+                    const uint64_t ad = tc::smem_desc(a_[q] + ks * 256, kLBO, kSBO);
+                    if (!split) {
+                        tc::mma_bf16(tmem, ad, tc::smem_desc(b_[q] + ks * 256, kLBO, kSBO), id_all, acc);
+                    } else {
+                        tc::mma_bf16(tmem, ad, tc::smem_desc(b_[q] + ks * 256, kLBO, kSBO), id_d, acc);
+                        tc::mma_bf16(tmem + 256u, ad,
+                                     tc::smem_desc(b_[q] + a.Nd * (kKChunk * 2) + ks * 256, kLBO, kSBO), id_c, acc);
+                    }
                 }
             }
             tc::commit(&s_bar);
         }
         __syncwarp();
-        bool done = tc::mbar_wait(&s_bar, phase, kWaitLimitNs);
-        phase ^= 1u;
-        tc::fence_after_sync();
-        if (!__syncthreads_and(done)) {
-            ok = false;
-            break;
-        }
     }
+    if (ok) {  // the last chunk's MMAs
+        const bool done = tc::mbar_wait(&s_bar, (a.nchunks - 1) & 1u, kWaitLimitNs);
+        tc::fence_after_sync();
+        ok = __syncthreads_and(done);
+        failed = a.nchunks - 1;
+    }
+    if (live && oor) atomicAdd(&s_oor[pl], oor);
 
     if (!ok) {
         // the MMAs did not complete in time: record it, give them one more,
@@ -343,131 +369,150 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
         // in flight; a preempted CTA's MMAs finish once it runs again), then
         // release the tensor memory: a CTA must not exit holding it
         if (tid == 0) raise_error(a.err, DEV_WAIT_TIMEOUT);
-        if (!a.stall) tc::mbar_wait(&s_bar, phase ^ 1u, kDrainLimitNs);  // the stall hook issued none
+        if (!a.stall) tc::mbar_wait(&s_bar, failed & 1u, kDrainLimitNs);  // the stall hook issued none
     } else {
-        // epilogue 1: accumulators -> shared staging (the operand buffers are free now)
-        float* S_c = reinterpret_cast<float*>(smem);                        // [32][nc*nc][3]
-        float* S_d = S_c + kTileProbes * a.nc * a.nc * 3;                    // [32][nd*nd][2]
+        // epilogue 1: accumulators -> normalised values in shared staging,
+        // texel-major: S_c[probe][texel][r, g, b], S_d[probe][texel][d, d^2]
+        const uint32_t ntc = a.nc * a.nc, ntd = a.nd * a.nd;
+        float* S_c = reinterpret_cast<float*>(smem);
+        float* S_d = S_c + kTileProbes * ntc * 3;
         const uint32_t quarter = (uint32_t)warp & 3u;
         const uint32_t row = quarter * 32u + (uint32_t)lane;
-        const uint32_t pl = row >> 2, ch = row & 3u;
+        const uint32_t rp = row / kRowsPerProbe, ch = row % kRowsPerProbe;
+        const bool rvalid = rp < np;
         const uint32_t lane_base = tmem + ((quarter * 32u) << 16);
-        const float scale_c = s_max[pl];
-        if (warp < 4) {
-            const uint32_t ntex = a.nc * a.nc;
-            for (uint32_t col0 = 0; col0 < a.Nc; col0 += 16) {
-                float v[16];
-                tc::tmem_ld16(lane_base + col0, v);
-                if (ch < 3 && pl < np) {
+        const uint32_t steps_d = a.Nd / 16, steps = steps_d + a.Nc / 16;
+        for (uint32_t s = (uint32_t)warp >> 2; s < steps; s += 2) {  // warps w and w + 4 share the lanes
+            const bool depth = s < steps_d;
+            const uint32_t col0 = depth ? s * 16 : cbase + (s - steps_d) * 16;
+            float vv[16];
+            tc::tmem_ld16(lane_base + col0, vv);
+            if (!rvalid) continue;
+            if (depth && ch >= 3) {
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        uint32_t t = col0 + i;
-                        if (t < ntex) {
-                            float s = a.rowsum[a.Nd + t];
-                            float val = v[i] * scale_c;
-                            if (s > 1e-3f) val /= s;
-                            S_c[(pl * ntex + t) * 3 + ch] = val;
-                        }
+                for (int i = 0; i < 16; ++i) {
+                    const uint32_t u = s * 16 + i;
+                    if (u < ntd) {
+                        const float sum = a.rowsum[u];
+                        S_d[(rp * ntd + u) * 2 + (ch - 3)] = sum > 1e-3f ? vv[i] / sum : vv[i];
                     }
                 }
-            }
-        } else {
-            const uint32_t ntex = a.nd * a.nd;
-            const float unscale = ch == 0 ? cell : cell * cell;
-            for (uint32_t col0 = 0; col0 < a.Nd; col0 += 16) {
-                float v[16];
-                tc::tmem_ld16(lane_base + kDepthCol + col0, v);
-                if (ch < 2 && pl < np) {
+            } else if (!depth && ch < 3) {
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        uint32_t t = col0 + i;
-                        if (t < ntex) {
-                            float s = a.rowsum[t];
-                            float val = v[i] * unscale;
-                            if (s > 1e-3f) val /= s;
-                            S_d[(pl * ntex + t) * 2 + ch] = val;
-                        }
+                for (int i = 0; i < 16; ++i) {
+                    const uint32_t t = (s - steps_d) * 16 + i;
+                    if (t < ntc) {
+                        const float sum = a.rowsum[a.Nd + t];
+                        S_c[(rp * ntc + t) * 3 + ch] = sum > 1e-3f ? vv[i] / sum : vv[i];
                     }
                 }
             }
         }
         __syncthreads();
 
-        // epilogue 2: hysteresis in the FP32 accumulator, FP16 publish
+        // epilogue 2: hysteresis in the FP32 accumulators, FP16 publish of
+        // each interior texel and of the border texels copied from it
+        // (probesCopyBorders.comp); loads of the previous values are issued
+        // eight at a time per thread
         const float hy = a.hyst_dev ? *a.hyst_dev : a.g.hyst;
         const uint32_t rx = (uint32_t)a.g.res[0], rxy = (uint32_t)(a.g.res[0] * a.g.res[1]);
-        const uint32_t ntc = a.nc * a.nc, ntd = a.nd * a.nd;
         const uint32_t nprobes_grid = rxy * (uint32_t)a.g.res[2];
-        for (uint32_t i = tid; i < np * (ntc + ntd); i += kThreads) {
-            uint32_t pl2 = i / (ntc + ntd), t = i % (ntc + ntd);
-            uint32_t probe = a.probe_list ? a.probe_list[p0 + pl2] : p0 + pl2;
-            if (probe >= nprobes_grid) {  // a probe list entry outside the grid
-                raise_error(a.err, DEV_BAD_INDEX);
-                continue;
+        const int ncr = (int)a.g.color_res, ndr = (int)a.g.depth_res;
+        auto texel_of = [&](uint32_t pl2, uint32_t t, uint32_t n, int res, uint32_t width, int* ox, int* oy,
+                            bool* bad) -> size_t {
+            const uint32_t probe = a.probe_list ? a.probe_list[p0 + pl2] : p0 + pl2;
+            *bad = probe >= nprobes_grid;
+            const uint32_t pr = *bad ? 0u : probe;
+            const int ix = (int)(pr % rx), iy = (int)((pr % rxy) / rx), iz = (int)(pr / rxy);
+            *ox = res * (iy * a.g.res[0] + ix);
+            *oy = res * iz;
+            return (size_t)(*oy + 1 + (int)(t / n)) * width + (size_t)(*ox + 1 + (int)(t % n));
+        };
+        constexpr int kBatch = 8;
+        const uint32_t items_c = np * ntc;
+        for (uint32_t base = 0; base < items_c; base += kBatch * kThreads) {
+            float4 prev[kBatch];
+            size_t ti[kBatch];
+            int oxs[kBatch], oys[kBatch];
+            bool bad[kBatch];
+#pragma unroll
+            for (int k = 0; k < kBatch; ++k) {
+                const uint32_t i = base + (uint32_t)k * kThreads + (uint32_t)tid;
+                bad[k] = true;
+                if (i < items_c) {
+                    ti[k] = texel_of(i / ntc, i % ntc, a.nc, ncr, a.g.color_w, &oxs[k], &oys[k], &bad[k]);
+                    if (!bad[k]) prev[k] = a.acc_color[ti[k]];
+                    else raise_error(a.err, DEV_BAD_INDEX);  // a probe list entry outside the grid
+                }
             }
-            int ix = (int)(probe % rx), iy = (int)((probe % rxy) / rx), iz = (int)(probe / rxy);
-            int tile = iy * a.g.res[0] + ix;
-            if (t < ntc) {
-                uint32_t tx = t % a.nc, ty = t / a.nc;
-                size_t px = (size_t)((int)a.g.color_res * tile + 1 + (int)tx);
-                size_t py = (size_t)((int)a.g.color_res * iz + 1 + (int)ty);
-                size_t ti = py * a.g.color_w + px;
-                float4 prev = a.acc_color[ti];
+#pragma unroll
+            for (int k = 0; k < kBatch; ++k) {
+                if (bad[k]) continue;
+                const uint32_t i = base + (uint32_t)k * kThreads + (uint32_t)tid;
+                const uint32_t pl2 = i / ntc, t = i % ntc;
                 const float* res = S_c + (pl2 * ntc + t) * 3;
-                float mc = fmaxf(fmaxf(fabsf(res[0] - prev.x), fabsf(res[1] - prev.y)), fabsf(res[2] - prev.z));
+                const float mc = fmaxf(fmaxf(fabsf(res[0] - prev[k].x), fabsf(res[1] - prev[k].y)),
+                                       fabsf(res[2] - prev[k].z));
                 atomicMax(&s_maxc[pl2], __float_as_uint(mc));
-                float4 nv = make_float4(res[0] * (1.0f - hy) + prev.x * hy, res[1] * (1.0f - hy) + prev.y * hy,
-                                        res[2] * (1.0f - hy) + prev.z * hy, 1.0f);
-                a.acc_color[ti] = nv;
-                a.color[ti] = float4_to_half4(nv.x, nv.y, nv.z, nv.w);
-            } else {
-                uint32_t u = t - ntc, tx = u % a.nd, ty = u / a.nd;
-                size_t px = (size_t)((int)a.g.depth_res * tile + 1 + (int)tx);
-                size_t py = (size_t)((int)a.g.depth_res * iz + 1 + (int)ty);
-                size_t ti = py * a.g.depth_w + px;
-                float2 prev = a.acc_depth[ti];
+                const float4 nv = make_float4(res[0] * (1.0f - hy) + prev[k].x * hy,
+                                              res[1] * (1.0f - hy) + prev[k].y * hy,
+                                              res[2] * (1.0f - hy) + prev[k].z * hy, 1.0f);
+                a.acc_color[ti[k]] = nv;
+                const uint2 hv = float4_to_half4(nv.x, nv.y, nv.z, nv.w);
+                a.color[ti[k]] = hv;
+                const int ox = oxs[k], oy = oys[k];
+                for_border_targets((int)(t % a.nc) + 1, (int)(t / a.nc) + 1, ncr, [&](int bx, int by) {
+                    a.color[(size_t)(oy + by) * a.g.color_w + (size_t)(ox + bx)] = hv;
+                });
+            }
+        }
+        const uint32_t items_d = np * ntd;
+        for (uint32_t base = 0; base < items_d; base += kBatch * kThreads) {
+            float2 prev[kBatch];
+            size_t ti[kBatch];
+            int oxs[kBatch], oys[kBatch];
+            bool bad[kBatch];
+#pragma unroll
+            for (int k = 0; k < kBatch; ++k) {
+                const uint32_t i = base + (uint32_t)k * kThreads + (uint32_t)tid;
+                bad[k] = true;
+                if (i < items_d) {
+                    ti[k] = texel_of(i / ntd, i % ntd, a.nd, ndr, a.g.depth_w, &oxs[k], &oys[k], &bad[k]);
+                    if (!bad[k]) prev[k] = a.acc_depth[ti[k]];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kBatch; ++k) {
+                if (bad[k]) continue;
+                const uint32_t i = base + (uint32_t)k * kThreads + (uint32_t)tid;
+                const uint32_t pl2 = i / ntd, u = i % ntd;
                 const float* res = S_d + (pl2 * ntd + u) * 2;
-                float2 nv = make_float2(res[0] * (1.0f - hy) + prev.x * hy, res[1] * (1.0f - hy) + prev.y * hy);
-                a.acc_depth[ti] = nv;
-                __half2 o = __floats2half2_rn(nv.x, nv.y);
-                a.depth[ti] = *reinterpret_cast<uint32_t*>(&o);
+                const float2 nv = make_float2(res[0] * (1.0f - hy) + prev[k].x * hy, res[1] * (1.0f - hy) + prev[k].y * hy);
+                a.acc_depth[ti[k]] = nv;
+                const __half2 o = __floats2half2_rn(nv.x, nv.y);
+                const uint32_t hv = *reinterpret_cast<const uint32_t*>(&o);
+                a.depth[ti[k]] = hv;
+                const int ox = oxs[k], oy = oys[k];
+                for_border_targets((int)(u % a.nd) + 1, (int)(u / a.nd) + 1, ndr, [&](int bx, int by) {
+                    a.depth[(size_t)(oy + by) * a.g.depth_w + (size_t)(ox + bx)] = hv;
+                });
             }
         }
         __syncthreads();
 
-        // border copy (probesCopyBorders.comp, generalised) and probe state
-        const int ncr = (int)a.g.color_res, ndr = (int)a.g.depth_res;
-        const uint32_t nbc = 4 + 4 * (uint32_t)(ncr - 2), nbd = 4 + 4 * (uint32_t)(ndr - 2);
-        for (uint32_t i = tid; i < np * (nbc + nbd); i += kThreads) {
-            uint32_t pl2 = i / (nbc + nbd), e = i % (nbc + nbd);
-            uint32_t probe = a.probe_list ? a.probe_list[p0 + pl2] : p0 + pl2;
-            if (probe >= nprobes_grid) continue;
-            int ix = (int)(probe % rx), iy = (int)((probe % rxy) / rx), iz = (int)(probe / rxy);
-            int tile = iy * a.g.res[0] + ix;
-            if (e < nbc) {
-                int4 b = border_entry((int)e, ncr);
-                size_t ox = (size_t)ncr * tile, oy = (size_t)ncr * iz;
-                a.color[(oy + b.y) * a.g.color_w + ox + b.x] = a.color[(oy + b.w) * a.g.color_w + ox + b.z];
-            } else {
-                int4 b = border_entry((int)(e - nbc), ndr);
-                size_t ox = (size_t)ndr * tile, oy = (size_t)ndr * iz;
-                a.depth[(oy + b.y) * a.g.depth_w + ox + b.x] = a.depth[(oy + b.w) * a.g.depth_w + ox + b.z];
-            }
-        }
-        uint32_t probe_t = (uint32_t)tid < np ? (a.probe_list ? a.probe_list[p0 + tid] : p0 + tid) : nprobes_grid;
+        const uint32_t probe_t = (uint32_t)tid < np ? (a.probe_list ? a.probe_list[p0 + tid] : p0 + tid) : nprobes_grid;
         if (probe_t < nprobes_grid) {  // probesUpdate.glsl:110-119
-            uint32_t probe = probe_t;
-            uint32_t s = a.states[probe];
+            uint32_t s = a.states[probe_t];
             if (s_oor[tid] >= R) {
                 s = 8;
             } else {
-                float mc = __uint_as_float(s_maxc[tid]);
-                float sf = (float)s;
+                const float mc = __uint_as_float(s_maxc[tid]);
+                const float sf = (float)s;
                 if (mc < 0.02f / sf) s = min(s + 1u, 8u);
                 else if (mc > 0.04f / sf) s = max(s - 1u, 1u);
                 else if (mc > 0.25f) s = 1;
             }
-            a.states[probe] = s;
+            a.states[probe_t] = s;
         }
     }
 
@@ -475,7 +520,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
     __syncthreads();
     if (warp == 0) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(tmem, kTmemCols);
+        tc::tmem_dealloc(tmem, cols);
     }
 }
 
@@ -572,7 +617,7 @@ size_t tc_weight_bytes(uint32_t rays, uint32_t color_res, uint32_t depth_res) {
     uint32_t nc = color_res - 2, nd = depth_res - 2;
     uint32_t Nc = (nc * nc + 15) / 16 * 16, Nd = (nd * nd + 15) / 16 * 16;
     uint32_t nchunks = (rays + kKChunk - 1) / kKChunk;
-    return (size_t)nchunks * 2 * (Nc + Nd) * 128;
+    return (size_t)nchunks * tc_b_bytes(Nd, Nc);
 }
 
 bool tc_blend_supported(uint32_t color_res, uint32_t depth_res) {
@@ -610,11 +655,7 @@ cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uin
     a.dev_count = dev_count;
     a.stall = stall ? 1u : 0u;
     a.hyst_dev = hyst_dev;
-    // operand stage (A 64 KB + B up to 128 KB), reused by the epilogue staging
-    size_t stage = 65536 + 2 * (size_t)(Nd + Nc) * 128;
-    size_t staging = (size_t)kTileProbes * (nc * nc * 3 + nd * nd * 2) * sizeof(float);
-    size_t smem = stage > staging ? stage : staging;
-    if (smem < kMinSmem) smem = kMinSmem;
+    const size_t smem = tc_smem_bytes(nc, nd, Nc, Nd);
     cudaError_t e = set_tc_smem_limit();
     if (e != cudaSuccess) return e;
     uint32_t blocks = (nprobes + kTileProbes - 1) / kTileProbes;
@@ -632,10 +673,7 @@ cudaError_t prepare_batch_kernels() {
 size_t batch_tc_smem(uint32_t color_res, uint32_t depth_res) {
     const uint32_t nc = color_res - 2, nd = depth_res - 2;
     const uint32_t Nc = (nc * nc + 15) / 16 * 16, Nd = (nd * nd + 15) / 16 * 16;
-    size_t stage = 65536 + 2 * (size_t)(Nd + Nc) * 128;
-    size_t staging = (size_t)kTileProbes * (nc * nc * 3 + nd * nd * 2) * sizeof(float);
-    size_t smem = stage > staging ? stage : staging;
-    return smem < kMinSmem ? kMinSmem : smem;
+    return tc_smem_bytes(nc, nd, Nc, Nd);
 }
 
 cudaError_t launch_batch_tc_weights(const BatchTables& bt, const BatchBlendList& bl, uint32_t max_rows,
