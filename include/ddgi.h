@@ -467,7 +467,7 @@ typedef struct ddgi_trace_tuning {
     uint32_t smem_stack;    /* traversal-stack entries per thread in shared memory, deeper ones in local
                                memory; 0 = the whole stack in shared memory (default) */
     uint32_t ctas_per_sm;   /* persistent CTAs per SM; 0 = as many as fit (default) */
-    uint32_t node_width;    /* 2: binary nodes (default), 4: four-wide nodes collapsed from the binary trees */
+    uint32_t node_width;    /* 2: binary nodes (default), 8: eight-wide quantised nodes collapsed from the binary trees */
     uint32_t straggler_lanes; /* a warp leaves its node-search loop to test the leaves its lanes hold once at
                                  most this many lanes still search for one (0..31, default 10; 0: wait for
                                  every lane, the plain while-while traversal) */

@@ -94,7 +94,7 @@ def test_batch_equals_single_updates(gpu_lib, volumes, single_results, graph):
     dict(smem_stack=24, refill_lanes=32, trace_ctas_per_sm=0, blend_threads=128),
     dict(smem_stack=0, refill_lanes=1, trace_ctas_per_sm=2, blend_threads=256),
     dict(node_width=2, rays_per_warp=8, smem_stack=16),
-    dict(straggler_lanes=0), dict(straggler_lanes=20, node_width=4),
+    dict(straggler_lanes=0), dict(straggler_lanes=20, node_width=8),
     dict(blend_threads=0, refill_lanes=12), dict(blend_threads=32),
 ])
 def test_tunings_do_not_change_results(gpu_lib, volumes, single_results, tuning):

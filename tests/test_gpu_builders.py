@@ -48,7 +48,7 @@ def test_sah_trees_bit_exact(gpu_lib, which, leaf):
     orig, d = random_rays(w, which, 20000, 5)
     for any_hit in (False, True):
         r, _ = o.trace(orig, d, 0.01, 500.0, 0xFF, any_hit)
-        for width in (2, 4):
+        for width in (2, 8):
             sah.set_trace_tuning(node_width=width)
             g, _ = sah.trace_rays(orig, d, 0.01, 500.0, 0xFF, any_hit)
             f, _ = lbvh.trace_rays(orig, d, 0.01, 500.0, 0xFF, any_hit)
@@ -99,7 +99,7 @@ def test_spatial_split_trees_bit_exact(gpu_lib, which, overlap):
     orig, d = random_rays(w, which, 20000, 12)
     for any_hit in (False, True):
         r, _ = o.trace(orig, d, 0.01, 500.0, 0xFF, any_hit)
-        for width in (2, 4):
+        for width in (2, 8):
             ctx.set_trace_tuning(node_width=width)
             g, _ = ctx.trace_rays(orig, d, 0.01, 500.0, 0xFF, any_hit)
             if any_hit:

@@ -136,3 +136,24 @@ def test_bf16_room_ten_updates_vs_fp64(gpu_lib):
 
 def test_bf16_terrain_ten_updates_vs_fp64(gpu_lib, terrain, terrain_oracle):
     check_bf16(bf16_ten_updates(terrain, terrain_oracle))
+
+
+def test_terrain_wide_nodes_same_hits_and_atlas(gpu_lib, terrain):
+    """The eight-wide quantised trees (node_width 8) on the whole terrain grid:
+    hits, ray records and atlases bit-identical to the binary trees' over two
+    updates (primary rays, shadow rays and the bounce lookup)."""
+    w = terrain
+    P = w.grid.probe_count()
+    out = []
+    for width in (2, 8):
+        ctx = make_ctx(w, abi.PRECISION_FP32)
+        ctx.set_trace_tuning(node_width=width)
+        for k in range(2):
+            ctx.update(w.orientation(k))
+        out.append((ctx.get_hits(P), ctx.get_ray_records(P), ctx.get_atlas(abi.ATLAS_COLOR),
+                    ctx.get_atlas(abi.ATLAS_DEPTH)))
+        ctx.close()
+    (h2, r2, c2, d2), (h8, r8, c8, d8) = out
+    assert hit_mismatches(h2, h8) == 0
+    assert (r2.view(np.uint32) == r8.view(np.uint32)).all()
+    assert (c2.view(np.uint32) == c8.view(np.uint32)).all() and (d2.view(np.uint32) == d8.view(np.uint32)).all()

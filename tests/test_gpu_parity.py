@@ -188,7 +188,7 @@ def test_errors_are_reported(gpu_lib, room_workload):
     dict(node_width=2), dict(node_width=2, rays_per_warp=8, smem_stack=16),
     dict(rays_per_warp=32), dict(rays_per_warp=8, refill_lanes=16), dict(rays_per_warp=1, smem_stack=16),
     dict(rays_per_warp=4, refill_lanes=1, ctas_per_sm=3, smem_stack=24),
-    dict(straggler_lanes=0), dict(straggler_lanes=31), dict(straggler_lanes=3, node_width=4),
+    dict(straggler_lanes=0), dict(straggler_lanes=31), dict(straggler_lanes=3, node_width=8),
     dict(straggler_lanes=16, rays_per_warp=8, smem_stack=16),
 ])
 def test_trace_tunings_do_not_change_results(gpu_lib, room_workload, tuning):
@@ -223,7 +223,7 @@ def test_autotune_restores_state(gpu_lib, room_workload):
     with pytest.raises(DDGIError):
         ctx.set_trace_tuning(rays_per_warp=3)
     with pytest.raises(DDGIError):
-        ctx.set_trace_tuning(node_width=8)
+        ctx.set_trace_tuning(node_width=4)
     with pytest.raises(DDGIError):
         ctx.set_trace_tuning(straggler_lanes=32)
     ctx.close()

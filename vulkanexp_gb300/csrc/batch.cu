@@ -313,7 +313,7 @@ cudaError_t enqueue(ddgi_batch* b, cudaStream_t st, bool timed) {
     tt.refill = b->tuning.refill_lanes;
     tt.split = b->tuning.smem_stack;
     tt.rays_per_warp = b->tuning.rays_per_warp;  // applied per volume through the volume table
-    tt.wide = b->tuning.node_width == 4 ? 1u : 0u;
+    tt.wide = b->tuning.node_width == 8 ? 1u : 0u;
     tt.wait = b->tuning.straggler_lanes;
     WaveHits wh{b->thit, b->prim, b->front};
     ShadowQueue q{b->q_idx, b->q_pos, b->q_sun, nullptr};
@@ -446,6 +446,7 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
         b->wnode_count += c->scene.wnode_count;
         if (v == 0) b->wstack_cap = c->scene.wstack_cap;
         b->wstack_cap = c->scene.wstack_cap > 0 && b->wstack_cap > 0 ? std::max(b->wstack_cap, c->scene.wstack_cap) : 0;
+        if (b->wnode_count >= kMaxWideNodes) b->wstack_cap = 0;  // beyond the stack entries' node field
         if (c->fp16) {
             tc_list.push_back(v);
             tc_base.push_back(tc_base.back() + tc_tiles(P));
@@ -628,8 +629,8 @@ ddgi_status ddgi_batch_set_tuning(ddgi_batch* b, const ddgi_batch_tuning* t) {
     const uint32_t r = t->rays_per_warp;
     if (!(r == 0 || r == 1 || r == 2 || r == 4 || r == 8 || r == 16 || r == 32))
         return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "rays_per_warp = %u: want 0, 1, 2, 4, 8, 16 or 32", r);
-    if (t->node_width != 2 && t->node_width != 4)
-        return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "node_width = %u: want 2 or 4", t->node_width);
+    if (t->node_width != 2 && t->node_width != 8)
+        return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "node_width = %u: want 2 or 8", t->node_width);
     if (t->straggler_lanes > 31)
         return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "straggler_lanes = %u outside [0, 31]", t->straggler_lanes);
     ddgi_status s = wait_previous(b);
@@ -748,7 +749,7 @@ ddgi_status ddgi_batch_autotune(ddgi_batch* b, const float* orientations, uint32
     ddgi_status err = DDGI_OK;
     float best_t = 0.0f;
     err = measure(best, 0, &best_t);
-    const uint32_t width_c[] = {4u, 2u};
+    const uint32_t width_c[] = {8u, 2u};
     const uint32_t rpw_c[] = {0u, 32u, 16u, 8u, 4u, 2u, 1u};
     const uint32_t split_c[] = {0u, 32u, 24u, 16u};
     const uint32_t refill_c[] = {4u, 8u, 16u, 24u};
@@ -771,7 +772,7 @@ ddgi_status ddgi_batch_autotune(ddgi_batch* b, const float* orientations, uint32
                               : p == 4 ? &t.trace_ctas_per_sm
                                        : &t.straggler_lanes;
             if (*field == cand[i]) continue;
-            const int cap = t.node_width == 4 && b->wstack_cap > 0 ? b->wstack_cap : b->stack_cap;
+            const int cap = t.node_width == 8 && b->wstack_cap > 0 ? b->wstack_cap : b->stack_cap;
             if (p == 2 && cand[i] != 0 && (int)cand[i] >= cap) continue;
             *field = cand[i];
             float tt = 0.0f;

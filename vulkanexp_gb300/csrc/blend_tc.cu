@@ -46,7 +46,8 @@ namespace {
 
 constexpr int kTileProbes = 25;    // 125 A rows: (r, g, b, d, d^2) per probe
 constexpr int kRowsPerProbe = 5;
-constexpr int kKChunk = 32;        // rays per shared-memory stage
+constexpr int kKChunk = 16;        // rays per shared-memory stage (one K step)
+constexpr int kStages = 4;         // operand stages in the ring
 constexpr int kThreads = 256;
 constexpr uint32_t kSBO = (kKChunk / 8) * 128;  // bytes between 8-row groups
 constexpr uint32_t kLBO = 128;                  // bytes between K-adjacent core matrices
@@ -201,31 +202,34 @@ __device__ __forceinline__ void for_border_targets(int x, int y, int n, F put) {
     if (x == 1 && y == 1) put(n - 1, n - 1);
 }
 
-// Shared-memory layout of a tile: the A operand (hi part, lo part), then two
-// B buffers (chunk c in buffer c % 2); the epilogue staging reuses it all.
+// Shared-memory layout of a tile: a ring of kStages operand stages, each the
+// A operand of one chunk (hi part, lo part) then its B operand (hi, lo);
+// chunk c uses stage c % kStages.  The epilogue staging reuses the ring.
 __host__ __device__ __forceinline__ size_t tc_b_bytes(uint32_t Nd, uint32_t Nc) { return 2 * (size_t)(Nd + Nc) * (kKChunk * 2); }
 __host__ __device__ __forceinline__ size_t tc_stage_bytes(uint32_t Nd, uint32_t Nc) {
-    return 2 * (size_t)kAPart + 2 * tc_b_bytes(Nd, Nc);
+    return 2 * (size_t)kAPart + tc_b_bytes(Nd, Nc);
 }
 
-// Dynamic shared memory of a tile: the operand stages or the epilogue
+// Dynamic shared memory of a tile: the operand ring or the epilogue
 // staging, whichever is larger; with more than 256 accumulator columns at
 // least kOneCtaSmem (one CTA per SM).
 __host__ __device__ __forceinline__ size_t tc_smem_bytes(uint32_t nc, uint32_t nd, uint32_t Nc, uint32_t Nd) {
-    const size_t stage = tc_stage_bytes(Nd, Nc);
+    const size_t ring = kStages * tc_stage_bytes(Nd, Nc);
     const size_t staging = (size_t)kTileProbes * (nc * nc * 3 + nd * nd * 2) * sizeof(float);
-    size_t smem = stage > staging ? stage : staging;
+    size_t smem = ring > staging ? ring : staging;
     if (Nd + Nc > 256 && smem < kOneCtaSmem) smem = kOneCtaSmem;
     return smem;
 }
 
 // Blend of the tile of kTileProbes probe slots starting at p0 (< nprobes) by
-// the whole CTA.
+// the whole CTA.  Iteration c fills stage c % kStages with chunk c (weights
+// by cp.async, ray operands from registers loaded two iterations before) and
+// issues the MMAs of chunk c - 1, whose weights were copied one iteration
+// before; a stage is refilled once the MMAs that read it (kStages chunks
+// earlier) have signalled its barrier.
 __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0, const uint32_t nprobes) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t* sA = smem;                          // hi part, then lo part (kAPart each)
-    uint8_t* sB = smem + 2 * kAPart;             // two buffers of tc_b_bytes
-    __shared__ uint64_t s_bar;
+    __shared__ uint64_t s_bar[kStages];
     __shared__ uint32_t s_tmem;
     __shared__ uint32_t s_oor[kTileProbes], s_maxc[kTileProbes];
 
@@ -237,129 +241,138 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
     const uint32_t cols = split ? 512u : 256u;
     const uint32_t cbase = split ? 256u : a.Nd;  // first colour column
     const size_t bbytes = tc_b_bytes(a.Nd, a.Nc);
+    const size_t sbytes = tc_stage_bytes(a.Nd, a.Nc);
     const uint32_t b16 = (uint32_t)(bbytes / 16);
+    auto stage_a = [&](uint32_t c) { return smem + (c % kStages) * sbytes; };
+    auto stage_b = [&](uint32_t c) { return smem + (c % kStages) * sbytes + 2 * kAPart; };
 
     if (warp == 0) tc::tmem_alloc(&s_tmem, cols);
-    if (tid == 0) tc::mbar_init(&s_bar, 1);
+    if (tid < kStages) tc::mbar_init(&s_bar[tid], 1);
     if (tid < kTileProbes) {
         s_maxc[tid] = 0u;
         s_oor[tid] = 0u;
     }
-    // A rows kTileProbes * 5 .. 127 stay zero for the whole tile
-    for (uint32_t r = kTileProbes * kRowsPerProbe + (uint32_t)tid / 4; r < 128; r += kThreads / 4)
-        for (int part = 0; part < 2; ++part)
-            *reinterpret_cast<uint4*>(sA + part * kAPart + canon_off(r, (uint32_t)tid & 3u)) = make_uint4(0, 0, 0, 0);
-    // B of chunk 0
-    {
-        const uint4* src = a.wchunks;
-        uint4* dst = reinterpret_cast<uint4*>(sB);
-        for (uint32_t i = tid; i < b16; i += kThreads) tc::cp_async16(dst + i, src + i);
-        tc::cp_async_commit();
+    // A rows kTileProbes * 5 .. 127 stay zero in every stage
+    for (uint32_t i = tid; i < kStages * 2 * 3 * (kKChunk / 8); i += kThreads) {
+        const uint32_t kg = i % (kKChunk / 8), r = kTileProbes * kRowsPerProbe + (i / (kKChunk / 8)) % 3;
+        const uint32_t part = (i / (3 * (kKChunk / 8))) % 2, st = i / (2 * 3 * (kKChunk / 8));
+        *reinterpret_cast<uint4*>(smem + st * sbytes + part * kAPart + canon_off(r, kg)) = make_uint4(0, 0, 0, 0);
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = s_tmem;
 
-    // thread -> (probe, 4 consecutive rays of the chunk); 200 of 256 threads
+    // thread -> (probe, 2 consecutive rays of the chunk); 200 of 256 threads
     const uint32_t pl = (uint32_t)tid >> 3, j = (uint32_t)tid & 7u;
     const bool builder = pl < (uint32_t)kTileProbes;
     const bool live = builder && pl < np;
     const float4* prec = a.rays + (size_t)(p0 + (live ? pl : 0u)) * R;
-    float4 v[4];
-    auto load = [&](uint32_t c) {
+    float4 va[2], vb[2];  // records of the even / odd chunks in flight
+    auto load = [&](float4* v, uint32_t c) {
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const uint32_t r = c * kKChunk + j * 4 + e;
+        for (int e = 0; e < 2; ++e) {
+            const uint32_t r = c * kKChunk + j * 2 + e;
             v[e] = live && r < R ? __ldg(prec + r) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
     };
-    load(0);
+    load(va, 0);
+    load(vb, 1);
     uint32_t oor = 0;
     const uint32_t N = a.Nd + a.Nc;
     const uint32_t id_all = tc::idesc_bf16_f32(128, N), id_d = tc::idesc_bf16_f32(128, a.Nd),
                    id_c = tc::idesc_bf16_f32(128, a.Nc);
     bool ok = true;
-    uint32_t failed = 0;  // the chunk whose completion wait ran out
-    for (uint32_t c = 0; c < a.nchunks; ++c) {
-        if (c > 0) {  // the previous chunk's MMAs read A and the other B buffer
-            const bool done = tc::mbar_wait(&s_bar, (c - 1) & 1u, kWaitLimitNs);
-            tc::fence_after_sync();
-            if (!__syncthreads_and(done)) {
-                ok = false;
-                failed = c - 1;
-                break;
+    uint32_t waited = 0;  // chunk whose MMAs a completion wait was for (the drain's target on a timeout)
+    int last = -1;        // the last chunk whose MMAs were issued
+    for (uint32_t c = 0; c <= a.nchunks; ++c) {
+        if (c < a.nchunks) {
+            if (c >= (uint32_t)kStages) {  // the MMAs of chunk c - kStages read this stage
+                const uint32_t old = c - kStages;
+                const bool done = tc::mbar_wait(&s_bar[old % kStages], (old / kStages) & 1u, kWaitLimitNs);
+                tc::fence_after_sync();
+                if (!__syncthreads_and(done)) {
+                    ok = false;
+                    waited = old;
+                    break;
+                }
             }
-        }
-        if (builder) {  // A rows (r, g, b, d, d^2) of this thread's probe, 4 rays: half a core-matrix row
-            uint32_t w[5][2][2];
+            {   // weights of chunk c
+                const uint4* src = a.wchunks + (size_t)c * b16;
+                uint4* dst = reinterpret_cast<uint4*>(stage_b(c));
+                for (uint32_t i = tid; i < b16; i += kThreads) tc::cp_async16(dst + i, src + i);
+                tc::cp_async_commit();
+            }
+            if (builder) {  // A rows (r, g, b, d, d^2) of this thread's probe, 2 rays: a quarter core-matrix row
+                float4 v[2];
 #pragma unroll
-            for (int e = 0; e < 4; e += 2) {
+                for (int e = 0; e < 2; ++e) v[e] = (c & 1u) ? vb[e] : va[e];
                 float dep[2];
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const uint32_t r = c * kKChunk + j * 4 + e + h;
-                    const float wv = v[e + h].w;
+                for (int e = 0; e < 2; ++e) {
+                    const uint32_t r = c * kKChunk + j * 2 + e;
+                    const float wv = v[e].w;
                     if (live && r < R && (wv < 0.0f || wv > cell)) ++oor;
                     float dd = fminf(cell, wv);
                     if (dd < 0.0f) dd = cell;
-                    dep[h] = live && r < R ? dd : 0.0f;
+                    dep[e] = live && r < R ? dd : 0.0f;
                 }
-                w[0][0][e / 2] = pack2(v[e].x, v[e + 1].x, &w[0][1][e / 2]);
-                w[1][0][e / 2] = pack2(v[e].y, v[e + 1].y, &w[1][1][e / 2]);
-                w[2][0][e / 2] = pack2(v[e].z, v[e + 1].z, &w[2][1][e / 2]);
-                w[3][0][e / 2] = pack2(dep[0], dep[1], &w[3][1][e / 2]);
-                w[4][0][e / 2] = pack2(dep[0] * dep[0], dep[1] * dep[1], &w[4][1][e / 2]);
+                uint32_t w[5][2];
+                w[0][0] = pack2(v[0].x, v[1].x, &w[0][1]);
+                w[1][0] = pack2(v[0].y, v[1].y, &w[1][1]);
+                w[2][0] = pack2(v[0].z, v[1].z, &w[2][1]);
+                w[3][0] = pack2(dep[0], dep[1], &w[3][1]);
+                w[4][0] = pack2(dep[0] * dep[0], dep[1] * dep[1], &w[4][1]);
+                uint8_t* sa = stage_a(c);
+#pragma unroll
+                for (int part = 0; part < 2; ++part)
+#pragma unroll
+                    for (int ch = 0; ch < kRowsPerProbe; ++ch)
+                        *reinterpret_cast<uint32_t*>(sa + part * kAPart +
+                                                     canon_off(pl * kRowsPerProbe + ch, j >> 2) + (j & 3u) * 4u) =
+                            w[ch][part];
             }
-#pragma unroll
-            for (int part = 0; part < 2; ++part)
-#pragma unroll
-                for (int ch = 0; ch < kRowsPerProbe; ++ch)
-                    *reinterpret_cast<uint2*>(sA + part * kAPart + canon_off(pl * kRowsPerProbe + ch, j >> 1) +
-                                              (j & 1u) * 8u) = make_uint2(w[ch][part][0], w[ch][part][1]);
+            if (c + 2 < a.nchunks) {  // records two chunks ahead
+                if (c & 1u) load(vb, c + 2);
+                else load(va, c + 2);
+            }
         }
-        if (c + 1 < a.nchunks) {  // next chunk: weights by cp.async, records into registers
-            const uint4* src = a.wchunks + (size_t)(c + 1) * b16;
-            uint4* dst = reinterpret_cast<uint4*>(sB + ((c + 1) & 1u) * bbytes);
-            for (uint32_t i = tid; i < b16; i += kThreads) tc::cp_async16(dst + i, src + i);
-            tc::cp_async_commit();
-            load(c + 1);
-            tc::cp_async_wait_group<1>();  // this chunk's weights have landed
-        } else {
-            tc::cp_async_wait_group<0>();
-        }
-        tc::fence_proxy_async();
-        __syncthreads();
-        if (tid == 0 && !a.stall) {
-            tc::fence_after_sync();
-            const uint32_t aH = tc::smem_u32(sA), aL = aH + kAPart;
-            const uint32_t bH = tc::smem_u32(sB + (c & 1u) * bbytes), bL = bH + N * (kKChunk * 2);
-            // hi*hi + hi*lo + lo*hi, K = 16 per instruction
-            const uint32_t a_[3] = {aH, aH, aL}, b_[3] = {bH, bL, bH};
-#pragma unroll
-            for (uint32_t ks = 0; ks < kKChunk / 16; ++ks) {
+        if (c >= 1) {  // the MMAs of chunk c - 1 (its weights were copied an iteration ago)
+            if (c < a.nchunks) tc::cp_async_wait_group<1>();
+            else tc::cp_async_wait_group<0>();
+            tc::fence_proxy_async();
+            __syncthreads();
+            const uint32_t m = c - 1;
+            if (tid == 0 && !a.stall) {
+                tc::fence_after_sync();
+                const uint32_t aH = tc::smem_u32(stage_a(m)), aL = aH + kAPart;
+                const uint32_t bH = tc::smem_u32(stage_b(m)), bL = bH + N * (kKChunk * 2);
+                // hi*hi + hi*lo + lo*hi, K = 16 per instruction
+                const uint32_t a_[3] = {aH, aH, aL}, b_[3] = {bH, bL, bH};
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
-                    const uint32_t acc = (c > 0 || ks > 0 || q > 0) ? 1u : 0u;
-                    const uint64_t ad = tc::smem_desc(a_[q] + ks * 256, kLBO, kSBO);
+                    const uint32_t acc = (m > 0 || q > 0) ? 1u : 0u;
+                    const uint64_t ad = tc::smem_desc(a_[q], kLBO, kSBO);
                     if (!split) {
-                        tc::mma_bf16(tmem, ad, tc::smem_desc(b_[q] + ks * 256, kLBO, kSBO), id_all, acc);
+                        tc::mma_bf16(tmem, ad, tc::smem_desc(b_[q], kLBO, kSBO), id_all, acc);
                     } else {
-                        tc::mma_bf16(tmem, ad, tc::smem_desc(b_[q] + ks * 256, kLBO, kSBO), id_d, acc);
-                        tc::mma_bf16(tmem + 256u, ad,
-                                     tc::smem_desc(b_[q] + a.Nd * (kKChunk * 2) + ks * 256, kLBO, kSBO), id_c, acc);
+                        tc::mma_bf16(tmem, ad, tc::smem_desc(b_[q], kLBO, kSBO), id_d, acc);
+                        tc::mma_bf16(tmem + 256u, ad, tc::smem_desc(b_[q] + a.Nd * (kKChunk * 2), kLBO, kSBO), id_c,
+                                     acc);
                     }
                 }
+                tc::commit(&s_bar[m % kStages]);
             }
-            tc::commit(&s_bar);
+            last = (int)m;
+            __syncwarp();
         }
-        __syncwarp();
     }
-    if (ok) {  // the last chunk's MMAs
-        const bool done = tc::mbar_wait(&s_bar, (a.nchunks - 1) & 1u, kWaitLimitNs);
+    if (ok && last >= 0) {  // the last chunk's MMAs (a commit tracks every earlier MMA too)
+        const uint32_t m = (uint32_t)last;
+        const bool done = tc::mbar_wait(&s_bar[m % kStages], (m / kStages) & 1u, kWaitLimitNs);
         tc::fence_after_sync();
         ok = __syncthreads_and(done);
-        failed = a.nchunks - 1;
+        waited = m;
     }
     if (live && oor) atomicAdd(&s_oor[pl], oor);
 
@@ -369,7 +382,11 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
         // in flight; a preempted CTA's MMAs finish once it runs again), then
         // release the tensor memory: a CTA must not exit holding it
         if (tid == 0) raise_error(a.err, DEV_WAIT_TIMEOUT);
-        if (!a.stall) tc::mbar_wait(&s_bar, failed & 1u, kDrainLimitNs);  // the stall hook issued none
+        if (!a.stall && last >= 0) {  // the stall hook issued none
+            const uint32_t m = (uint32_t)last;
+            tc::mbar_wait(&s_bar[m % kStages], (m / kStages) & 1u, kDrainLimitNs);
+        }
+        (void)waited;
     } else {
         // epilogue 1: accumulators -> normalised values in shared staging,
         // texel-major: S_c[probe][texel][r, g, b], S_d[probe][texel][d, d^2]

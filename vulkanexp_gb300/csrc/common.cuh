@@ -72,15 +72,30 @@ struct __align__(16) GpuInstance {
     uint32_t id;        // index in the caller's instance array
 };
 
-// Four-wide node, 128 bytes, collapsed from the binary trees: the boxes of
-// up to four children as structure-of-arrays (lane k = child k) and their
-// references (>= 0: wide node, < 0: leaf as in BvhNode, kNone: no child).
+// Eight-wide node, 96 bytes, collapsed from the binary trees, with the
+// child boxes quantised to 8 bits per bound on a per-axis power-of-two grid
+// anchored at the node box's lower corner (the compressed wide nodes of
+// Ylitie, Karras & Laine, HPG 2017, with explicit child references):
+//   org.xyz          grid origin o; org.w holds the biased exponents
+//                    e_x | e_y << 8 | e_z << 16 of the grid steps 2^(e - 127)
+//   q[a] (a = x,y,z) bytes 0..7 (.x = slots 0-3, .y = 4-7): lower bounds of
+//                    the slots' boxes, bytes 8..15 (.z, .w): upper bounds, so
+//                    slot k's box is [o + lo_k 2^(e-127), o + hi_k 2^(e-127)]
+//                    per axis, rounded outwards (it contains the binary
+//                    tree's enlarged box); an empty slot has lo 255, hi 0
+//   ref[2]           the eight slots' references (>= 0: wide node, < 0: leaf
+//                    as in BvhNode, kNone: empty)
+// A slot's bit k of its number is set when its box lies on the low side of
+// the node along axis k, so a ray visits slots in decreasing order of
+// (slot ^ octant) for a near-first order without sorting.
 struct __align__(16) WideNode {
-    float4 lox, hix, loy, hiy, loz, hiz;
-    int4 ref;
-    int4 unused;
+    float4 org;
+    uint4 q[3];
+    int4 ref[2];
 };
-static_assert(sizeof(WideNode) == 128, "wide node is 128 bytes");
+static_assert(sizeof(WideNode) == 96, "wide node is 96 bytes");
+// Traversal stack entries of wide trees pack a node index into 23 bits.
+constexpr uint32_t kMaxWideNodes = 0x7FFFFFu;
 
 struct DeviceScene {
     const BvhNode* nodes;

@@ -633,16 +633,20 @@ ddgi_status refresh_wide_top(ddgi_ctx* ctx, cudaStream_t st) {
     collapse_wide(top, 0, w, &lt, &ok);
     if (!ok || S.wide_tlas_start + w.size() > S.wide_cap) return fail(ctx, DDGI_ERR_DEVICE, "wide top level");
     for (auto& n : w) {
-        int* r = &n.ref.x;
-        for (int k = 0; k < 4; ++k)
-            if (r[k] >= 0) r[k] += (int)S.wide_tlas_start;
+        for (int h = 0; h < 2; ++h) {
+            int* r = &n.ref[h].x;
+            for (int k = 0; k < 4; ++k)
+                if (r[k] >= 0) r[k] += (int)S.wide_tlas_start;
+        }
     }
     CK(cudaMemcpyAsync(S.wnodes + S.wide_tlas_start, w.data(), sizeof(WideNode) * w.size(), cudaMemcpyHostToDevice, st),
        "upload wide top level");
     S.wtlas_root = (int32_t)S.wide_tlas_start;
     S.wnode_count = S.wide_tlas_start + (uint32_t)w.size();
-    const int cap = (int)(3 * S.wlevels_blas + 3 * lt + 4);
-    S.wstack_cap = cap <= kMaxStack ? cap : 0;
+    // one node group per level, an exit marker between the levels; node
+    // groups pack the node index into 23 bits
+    const int cap = (int)(S.wlevels_blas + lt + 4);
+    S.wstack_cap = cap <= kMaxStack && S.wnode_count < kMaxWideNodes ? cap : 0;
     return upload_wide_instances(ctx, st);
 }
 
@@ -799,7 +803,7 @@ ddgi_status build_wide(ddgi_ctx* ctx, const std::vector<int32_t>& mesh_root, cud
     S.wnode_count = (uint32_t)w.size();
     S.wtlas_root = -1;
     if (S.tlas_root < 0) {
-        S.wstack_cap = (int)(3 * lb + 4);
+        S.wstack_cap = S.wnode_count < kMaxWideNodes ? (int)(lb + 4) : 0;
         return DDGI_OK;
     }
     return refresh_wide_top(ctx, st);
@@ -1224,7 +1228,7 @@ TraceTuning trace_tuning(const ddgi_ctx* ctx) {
     t.refill = ctx->tune.refill_lanes;
     t.split = ctx->tune.smem_stack;
     t.rays_per_warp = ctx->tune.rays_per_warp;
-    t.wide = ctx->tune.node_width == 4 ? 1u : 0u;
+    t.wide = ctx->tune.node_width == 8 ? 1u : 0u;
     t.wait = ctx->tune.straggler_lanes;
     return t;
 }
@@ -1481,8 +1485,8 @@ ddgi_status ddgi_set_trace_tuning(ddgi_ctx* ctx, const ddgi_trace_tuning* t) {
         return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "refill_lanes = %u outside [1, 32]", t->refill_lanes);
     if (t->smem_stack > (uint32_t)kMaxStack || t->ctas_per_sm > 32)
         return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "smem_stack or ctas_per_sm out of range");
-    if (t->node_width != 2 && t->node_width != 4)
-        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "node_width = %u: want 2 or 4", t->node_width);
+    if (t->node_width != 2 && t->node_width != 8)
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "node_width = %u: want 2 or 8", t->node_width);
     if (t->straggler_lanes > 31)
         return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "straggler_lanes = %u outside [0, 31]", t->straggler_lanes);
     ctx->tune = *t;
@@ -1584,7 +1588,7 @@ ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t re
     float best_t = 0.0f;
     ddgi_status err = measure(best, &best_t);
     const uint32_t R = ctx->grid.rays_per_probe;
-    const uint32_t width_c[] = {4u, 2u};
+    const uint32_t width_c[] = {8u, 2u};
     const uint32_t rpw_c[] = {0u, 32u, 16u, 8u, 4u, 2u, 1u};
     const uint32_t refill_c[] = {4u, 8u, 16u, 24u};
     const uint32_t split_c[] = {0u, 32u, 24u, 16u};
@@ -1608,7 +1612,7 @@ ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t re
                                        : &t.ctas_per_sm;
             if (*field == cand[i]) continue;
             if (p == 2 && grouped_rays_per_warp(cand[i], R) != cand[i]) continue;
-            const int cap = t.node_width == 4 && ctx->scene.wstack_cap > 0 ? ctx->scene.wstack_cap : ctx->scene.stack_cap;
+            const int cap = t.node_width == 8 && ctx->scene.wstack_cap > 0 ? ctx->scene.wstack_cap : ctx->scene.stack_cap;
             if (p == 4 && cand[i] != 0 && (int)cand[i] >= cap) continue;
             *field = cand[i];
             float tt = 0.0f;

@@ -223,7 +223,7 @@ struct WarpWalker {
     float tmin, tcur;
     HitRec best;
 
-
+    __device__ __forceinline__ void clear() { ref = kNone; }  // no ray
 
     __device__ __forceinline__ bool start(const DeviceScene& sc, float3 o, float3 d, float tmin_, float tmax_,
                                           uint32_t mask_) {
@@ -398,48 +398,86 @@ struct WarpWalker {
 };
 
 // ---------------------------------------------------------------------------
-// Four-wide traversal: the walker of WarpWalker (while-while, postponed
-// leaves, shared-memory stack) over WideNode trees.  An inner step tests the
-// four child boxes of a node (the same slab arithmetic and margins as the
-// binary step), continues with the nearest hit child and pushes the others
-// farthest first, so they pop nearest first.  Hit set, tie rule and results
-// equal the binary traversal's.
+// Eight-wide traversal over quantised WideNode trees: the walker of
+// WarpWalker (while-while, postponed leaves, shared-memory stack, straggler
+// exit) with node groups in place of single references (Ylitie, Karras &
+// Laine 2017): the current group is a node and the mask of its children
+// still to visit, in the ray's octant order; visiting a child takes the
+// highest bit; an inner child's own children are box-tested at once (all
+// eight slots, one mask) and the rest of the current group is pushed as one
+// stack entry (node index << 8 | mask).  The slab test of slot k along an
+// axis is fma(q_k, 2^e * inv, (o_node - o_ray) * inv) with q_k the near or
+// far bound byte, the same kind of rounding as the binary step's
+// (lo - o) * inv; with the quantised boxes enclosing the binary tree's
+// enlarged boxes and the same interval margins, pruning stays conservative.
+// Hit set, tie rule and results equal the binary traversal's.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ WideNode load_wide(const WideNode* nodes, int i) {
-    const float4* p = reinterpret_cast<const float4*>(nodes + i);
-    WideNode n;
-    n.lox = __ldg(p + 0);
-    n.hix = __ldg(p + 1);
-    n.loy = __ldg(p + 2);
-    n.hiy = __ldg(p + 3);
-    n.loz = __ldg(p + 4);
-    n.hiz = __ldg(p + 5);
-    float4 r = __ldg(p + 6);
-    n.ref = make_int4(__float_as_int(r.x), __float_as_int(r.y), __float_as_int(r.z), __float_as_int(r.w));
-    return n;
-}
-
-__device__ __forceinline__ float slab_near(float lx, float hx, float ly, float hy, float lz, float hz, const Ray& r,
-                                           float tmin, float tmax, float* tfar) {
-    float a0 = (lx - r.o.x) * r.inv.x, a1 = (hx - r.o.x) * r.inv.x;
-    float a2 = (ly - r.o.y) * r.inv.y, a3 = (hy - r.o.y) * r.inv.y;
-    float a4 = (lz - r.o.z) * r.inv.z, a5 = (hz - r.o.z) * r.inv.z;
-    *tfar = fminf(fminf(fmaxf(a0, a1), fmaxf(a2, a3)), fminf(fmaxf(a4, a5), tmax));
-    return fmaxf(fmaxf(fminf(a0, a1), fminf(a2, a3)), fmaxf(fminf(a4, a5), tmin));
-}
+// Float of an 8-bit integer (exact): its bits under the exponent of 2^23.
+__device__ __forceinline__ float byte_float(uint32_t b) { return __uint_as_float(0x4B000000u | b) - 8388608.0f; }
 
 template <bool ANY, class Stack = SmemStack>
 struct WideWalker {
     static constexpr bool kWide = true;
     static constexpr int kMinBlocks = 7;
-    Ray wr, r;
+    WorldRay wr;  // world ray
+    Ray r;        // current ray (world or object space)
     Stack stk;
-    int sp, cap, ref;
+    int sp, cap;
+    int node;       // node of the current group (kNone: none)
+    uint32_t gmask;  // its children still to visit, bit (slot ^ oct)
+    uint32_t oct;    // octant of r.d: bit k set when the direction's component k is negative
     bool in_blas;
     uint32_t inst_id, steps, mask;
     uint32_t wait_max;
     float tmin, tcur;
     HitRec best;
+
+    __device__ __forceinline__ void clear() {  // no ray
+        node = kNone;
+        gmask = 0;
+    }
+
+    __device__ __forceinline__ static uint32_t octant_of(float3 d) {
+        return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    }
+
+    // Box tests of a node's eight slots; the mask bit of slot k is k ^ oct.
+    __device__ __forceinline__ uint32_t test_children(const DeviceScene& sc, int n) const {
+        const float4* p = reinterpret_cast<const float4*>(sc.wnodes + n);
+        const float4 org = __ldg(p);
+        const uint32_t eb = __float_as_uint(org.w);
+        const float lo = tmin * kBoxLo, hi = tcur * kBoxHi;
+        float tn[8], tf[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            tn[k] = lo;
+            tf[k] = hi;
+        }
+#define DDGI_AXIS(A, O, INV, ORG)                                                                         \
+    {                                                                                                     \
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(p + 1 + A));                                 \
+        const float s = __uint_as_float(((eb >> (8 * A)) & 0xFFu) << 23) * INV;                           \
+        const float b = (ORG - O) * INV;                                                                  \
+        const bool pos = INV >= 0.0f;                                                                     \
+        const uint32_t n0 = pos ? q.x : q.z, n1 = pos ? q.y : q.w, f0 = pos ? q.z : q.x, f1 = pos ? q.w : q.y; \
+        _Pragma("unroll") for (int k = 0; k < 8; ++k) {                                                   \
+            const uint32_t nw = k < 4 ? n0 : n1, fw = k < 4 ? f0 : f1;                                    \
+            const float a = fmaf(byte_float((nw >> (8 * (k & 3))) & 0xFFu), s, b);                        \
+            const float c = fmaf(byte_float((fw >> (8 * (k & 3))) & 0xFFu), s, b);                        \
+            tn[k] = fmaxf(tn[k], a);                                                                      \
+            tf[k] = fminf(tf[k], c);                                                                      \
+        }                                                                                                 \
+    }
+        DDGI_AXIS(0, r.o.x, r.inv.x, org.x)
+        DDGI_AXIS(1, r.o.y, r.inv.y, org.y)
+        DDGI_AXIS(2, r.o.z, r.inv.z, org.z)
+#undef DDGI_AXIS
+        uint32_t m = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (tn[k] <= tf[k]) m |= 1u << ((uint32_t)k ^ oct);
+        return m;
+    }
 
     __device__ __forceinline__ bool start(const DeviceScene& sc, float3 o, float3 d, float tmin_, float tmax_,
                                           uint32_t mask_) {
@@ -447,8 +485,10 @@ struct WideWalker {
     }
     __device__ __forceinline__ bool start_at(const DeviceScene& sc, int32_t root, float3 o, float3 d, float tmin_,
                                              float tmax_, uint32_t mask_) {
-        ray_setup(wr, o, d);
-        r = wr;
+        wr.o = o;
+        wr.d = d;
+        ray_setup(r, o, d);
+        oct = octant_of(d);
         tmin = tmin_;
         tcur = tmax_;
         mask = mask_;
@@ -461,8 +501,12 @@ struct WideWalker {
         in_blas = false;
         inst_id = 0;
         steps = 0;
-        ref = root >= 0 ? root : kNone;
-        return ref != kNone;
+        node = kNone;
+        gmask = 0;
+        if (root < 0 || (uint32_t)root >= sc.wnode_count) return false;
+        node = root;
+        gmask = test_children(sc, root);
+        return gmask != 0;
     }
     __device__ __forceinline__ bool push(int v, uint32_t* err) {
         if (sp >= cap) {
@@ -472,75 +516,36 @@ struct WideWalker {
         stk.set(sp++, v);
         return true;
     }
+    // next group within the current tree level (stops at an EXIT marker)
     __device__ __forceinline__ void pop_level() {
         if (sp == 0 || stk.get(sp - 1) == kExit) {
-            ref = kNone;
+            node = kNone;
+            gmask = 0;
             return;
         }
-        ref = stk.get(--sp);
+        const int e = stk.get(--sp);
+        node = e >> 8;
+        gmask = (uint32_t)e & 0xFFu;
     }
+    // next group across EXIT markers (restoring the world ray); false when empty
     __device__ __forceinline__ bool pop() {
         for (;;) {
             if (sp == 0) return false;
-            ref = stk.get(--sp);
-            if (ref != kExit) return true;
+            const int e = stk.get(--sp);
+            if (e != kExit) {
+                node = e >> 8;
+                gmask = (uint32_t)e & 0xFFu;
+                return true;
+            }
             in_blas = false;
-            r = wr;
+            r.o = wr.o;  // back at the top level
+            r.d = wr.d;
+            r.inv = ray_inv(wr.d);
+            oct = octant_of(wr.d);
         }
     }
-
-    // Inner step at node `ref`: false if the stack overflowed.  The slabs
-    // are taken axis by axis over the four children (the same operations
-    // per box as slab_near), so only one axis' bounds are live at a time.
-    __device__ __forceinline__ bool inner_step(const DeviceScene& sc, uint32_t* err) {
-        const float4* p = reinterpret_cast<const float4*>(sc.wnodes + ref);
-        const float lo = tmin * kBoxLo, hi = tcur * kBoxHi;
-        float t0 = lo, t1 = lo, t2 = lo, t3 = lo, f0 = hi, f1 = hi, f2 = hi, f3 = hi;
-#define DDGI_AXIS(LO4, HI4, O, INV)                                                          \
-    {                                                                                        \
-        const float4 l = LO4, h = HI4;                                                       \
-        float a, b;                                                                          \
-        a = (l.x - O) * INV, b = (h.x - O) * INV;                                            \
-        t0 = fmaxf(t0, fminf(a, b)), f0 = fminf(f0, fmaxf(a, b));                            \
-        a = (l.y - O) * INV, b = (h.y - O) * INV;                                            \
-        t1 = fmaxf(t1, fminf(a, b)), f1 = fminf(f1, fmaxf(a, b));                            \
-        a = (l.z - O) * INV, b = (h.z - O) * INV;                                            \
-        t2 = fmaxf(t2, fminf(a, b)), f2 = fminf(f2, fmaxf(a, b));                            \
-        a = (l.w - O) * INV, b = (h.w - O) * INV;                                            \
-        t3 = fmaxf(t3, fminf(a, b)), f3 = fminf(f3, fmaxf(a, b));                            \
-    }
-        DDGI_AXIS(__ldg(p + 0), __ldg(p + 1), r.o.x, r.inv.x)
-        DDGI_AXIS(__ldg(p + 2), __ldg(p + 3), r.o.y, r.inv.y)
-        DDGI_AXIS(__ldg(p + 4), __ldg(p + 5), r.o.z, r.inv.z)
-#undef DDGI_AXIS
-        const float4 rr = __ldg(p + 6);
-        // misses sort last with key +inf
-        int c0 = __float_as_int(rr.x), c1 = __float_as_int(rr.y), c2 = __float_as_int(rr.z), c3 = __float_as_int(rr.w);
-        if (!(t0 <= f0) || c0 == kNone) t0 = INFINITY, c0 = kNone;
-        if (!(t1 <= f1) || c1 == kNone) t1 = INFINITY, c1 = kNone;
-        if (!(t2 <= f2) || c2 == kNone) t2 = INFINITY, c2 = kNone;
-        if (!(t3 <= f3) || c3 == kNone) t3 = INFINITY, c3 = kNone;
-#define DDGI_CSWAP(ta, ca, tb, cb)             \
-    if (tb < ta) {                             \
-        float tt = ta;                         \
-        ta = tb;                               \
-        tb = tt;                               \
-        int cc = ca;                           \
-        ca = cb;                               \
-        cb = cc;                               \
-    }
-        DDGI_CSWAP(t0, c0, t1, c1)
-        DDGI_CSWAP(t2, c2, t3, c3)
-        DDGI_CSWAP(t0, c0, t2, c2)
-        DDGI_CSWAP(t1, c1, t3, c3)
-        DDGI_CSWAP(t1, c1, t2, c2)
-#undef DDGI_CSWAP
-        if (c3 != kNone && !push(c3, err)) return false;
-        if (c2 != kNone && !push(c2, err)) return false;
-        if (c1 != kNone && !push(c1, err)) return false;
-        if (c0 != kNone) ref = c0;
-        else pop_level();
-        return true;
+    __device__ __forceinline__ int child_ref(const DeviceScene& sc, int n, uint32_t slot) const {
+        return __ldg(reinterpret_cast<const int*>(sc.wnodes + n) + 16 + slot);
     }
 
     // All lanes call this; returns true when an active lane's ray is finished.
@@ -551,27 +556,41 @@ struct WideWalker {
             raise_error(err, DEV_BAD_INDEX);
             failed = true;
         }
-        bool searching = active && ref != kNone && !failed;
+        bool searching = active && node != kNone && !failed;
         for (uint32_t it = 0;; ++it) {  // as in WarpWalker::advance
             const unsigned waiting = __ballot_sync(0xffffffffu, searching && leaf == kNone);
             if (waiting == 0u || (it > 0u && (uint32_t)__popc(waiting) <= wait_max)) break;
             if (searching) {
-                if (ref >= 0) {
-                    if (++steps > sc.wmax_steps || (uint32_t)ref >= sc.wnode_count) {
-                        raise_error(err, DEV_BAD_INDEX);
-                        failed = true;
-                        searching = false;
-                    } else if (!inner_step(sc, err)) {
-                        failed = true;
-                        searching = false;
+                if (gmask != 0u) {
+                    const uint32_t key = 31u - (uint32_t)__clz(gmask);
+                    const int c = child_ref(sc, node, key ^ oct);
+                    if (c >= 0) {
+                        if (++steps > sc.wmax_steps || (uint32_t)c >= sc.wnode_count) {
+                            raise_error(err, DEV_BAD_INDEX);
+                            failed = true;
+                            searching = false;
+                        } else {
+                            gmask &= ~(1u << key);
+                            const uint32_t m = test_children(sc, c);
+                            if (m != 0u) {
+                                if (gmask != 0u && !push((node << 8) | (int)gmask, err)) {
+                                    failed = true;
+                                    searching = false;
+                                }
+                                node = c;
+                                gmask = m;
+                            }
+                        }
+                    } else if (leaf == kNone) {
+                        gmask &= ~(1u << key);
+                        leaf = c;  // postpone it and keep walking
+                    } else {
+                        searching = false;  // holding a leaf and at a second one (it stays in the mask)
                     }
-                } else if (leaf == kNone) {
-                    leaf = ref;  // postpone it and keep walking
-                    pop_level();
                 } else {
-                    searching = false;  // holding a leaf and at a second one
+                    pop_level();
                 }
-                if (ref == kNone) searching = false;
+                if (searching && node == kNone) searching = false;
             }
         }
         if (!active) return false;
@@ -586,16 +605,23 @@ struct WideWalker {
                 const GpuInstance* gi = sc.winstances + slot;
                 int4 meta = __ldg(reinterpret_cast<const int4*>(gi) + 3);  // blas_root (wide), custom, mask, id
                 if (((uint32_t)meta.z & mask) != 0 && meta.x >= 0) {
-                    if (ref != kNone && !push(ref, err)) return true;
+                    if ((uint32_t)meta.x >= sc.wnode_count) {
+                        raise_error(err, DEV_BAD_INDEX);
+                        return true;
+                    }
+                    if (node != kNone && gmask != 0u && !push((node << 8) | (int)gmask, err)) return true;
                     if (!push(kExit, err)) return true;
                     float4 w[3] = {__ldg(&gi->w2o[0]), __ldg(&gi->w2o[1]), __ldg(&gi->w2o[2])};
                     float3 oo, od;
                     xform_exact(w, wr.o, wr.d, &oo, &od);
                     ray_setup(r, oo, od);
+                    oct = octant_of(od);
                     inst_id = (uint32_t)meta.w;
                     in_blas = true;
-                    ref = meta.x;
-                    return false;
+                    node = meta.x;
+                    gmask = test_children(sc, meta.x);
+                    if (gmask != 0u) return false;
+                    node = kNone;  // the mesh tree's root misses: back up
                 }
             } else {
                 int first = (~leaf) >> 3, count = ((~leaf) & 7) + 1;
@@ -627,7 +653,7 @@ struct WideWalker {
                 }
             }
         }
-        if (ref == kNone && !pop()) return true;
+        if ((node == kNone || gmask == 0u) && !pop()) return true;
         return false;
     }
 };

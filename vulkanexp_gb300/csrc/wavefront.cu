@@ -140,7 +140,7 @@ __device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job
     Walker<ANY, Stack> w;
     init_stack(w.stk, s_stack + threadIdx.x, blockDim.x, split, spill.ptr());
     w.cap = stack_cap;
-    w.ref = kNone;
+    w.clear();
     w.wait_max = knobs.wait;
     bool active = false;
     bool drained = false;  // warp-uniform: the work counter has passed `total`
