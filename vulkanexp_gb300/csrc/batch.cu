@@ -15,9 +15,15 @@
 //   * per-update inputs (direction tables, octant-binned ray orders and the
 //     volume table with the current lights) are written into one pinned host
 //     buffer and copied by one memcpy at the head of the update.
-//   * the launch sequence (clear + clock, tensor-core weights, primary
-//     traversal, shading, shadow traversal, FP32 and BF16 blends on two graph
-//     branches) is captured once into a CUDA graph and replayed.
+//   * volumes are kept in increasing order of their ray counts and split
+//     into up to kGroups groups of equal volume count; each group runs its
+//     own pipeline (primary traversal, shading, shadow traversal, FP32 and
+//     BF16 blends) on its own graph branch, so the small volumes' groups,
+//     launched first, finish long before the large ones instead of every
+//     volume waiting for the whole batch's traversal; the branches overlap
+//     where one group's tail leaves SMs idle.  The captured sequence (clear +
+//     clock, tensor-core weights of every volume, the group branches) is
+//     replayed from a CUDA graph.  Results do not depend on the grouping.
 //   * an autotuner times candidate launch parameters on real updates.
 #include <cuda_runtime.h>
 
@@ -80,6 +86,18 @@ struct ddgi_batch {
     uint32_t* d_err = nullptr;
     uint32_t* d_lists = nullptr;  // fp32 list, fp32 tile base, tc list, tc tile base, fp32 shared-weight tile base
     BatchBlendList fp32_bl{}, tc_bl{}, fp32s_bl{};  // fp32s: tiles of several probes, shared weights
+    // internal volume i is the caller's volume order[i] (increasing ray count)
+    std::vector<uint32_t> order;
+    // groups of consecutive internal volumes, each with its own work
+    // counters, queue regions (at its first record) and blend lists
+    struct Group {
+        uint32_t v0, v1, first, total;
+        BatchBlendList fp32_bl, tc_bl, fp32s_bl;
+    };
+    std::vector<Group> groups;
+    uint32_t* d_glists = nullptr;
+    std::vector<cudaStream_t> gstreams;
+    std::vector<cudaEvent_t> gjoin;
     uint32_t max_rays_fp32 = 0, max_rows_tc = 0, max_ntex_fp32 = 0;
     size_t tc_smem = 0;
     // per-update staging: [dirs | ray orders | volume table], host pinned + device
@@ -130,6 +148,8 @@ void bfree(T*& p) {
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+constexpr uint32_t kGroups = 4;  // volume groups of the graph's branches
+
 // Node references of a volume's trees moved into the arena: inner nodes by
 // node_off; leaves of the mesh trees (node index < tlas_start) by tri_off,
 // leaves of the top-level tree by inst_off.
@@ -165,12 +185,13 @@ __global__ void k_rebase_instances(const GpuInstance* __restrict__ src, uint32_t
 
 // Head of every update: clear the work counters and completion counts,
 // stamp the start time.
-__global__ void k_batch_begin(uint32_t* counters, uint32_t* done, unsigned long long* clock, uint32_t nvol) {
+__global__ void k_batch_begin(uint32_t* counters, uint32_t ncounters, uint32_t* done, unsigned long long* clock,
+                              uint32_t nvol) {
     for (uint32_t i = threadIdx.x; i < nvol; i += blockDim.x) {
         done[i] = 0u;
         clock[1 + i] = 0ull;
     }
-    if (threadIdx.x < 4) counters[threadIdx.x] = 0u;
+    for (uint32_t i = threadIdx.x; i < ncounters; i += blockDim.x) counters[i] = 0u;
     if (threadIdx.x == 0) clock[0] = globaltimer_ns();
 }
 
@@ -212,6 +233,7 @@ BatchTables tables(const ddgi_batch* b) {
     t.clock = b->d_clock;
     t.done = b->d_done;
     t.err = b->d_err;
+    t.first = 0;
     return t;
 }
 
@@ -237,16 +259,18 @@ ddgi_status check_volumes(ddgi_batch* b) {
     for (size_t v = 0; v < b->vols.size(); ++v) {
         const ddgi_ctx* c = b->vols[v];
         if (!c->scene.built || c->scene.build_id != b->scene_builds[v])
-            return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "volume %zu: scene rebuilt or released since the batch was made", v);
+            return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "volume %u: scene rebuilt or released since the batch was made",
+                         b->order[v]);
         // extent, hysteresis, sharpness and bias are read per update; the
         // sizes fix the batch's buffers and tables
         const ddgi_grid_desc& g0 = b->grids[v];
         if (memcmp(c->grid.resolution, g0.resolution, sizeof(g0.resolution)) != 0 ||
             c->grid.rays_per_probe != g0.rays_per_probe || c->grid.color_res != g0.color_res ||
             c->grid.depth_res != g0.depth_res || c->grid.precision != g0.precision)
-            return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "volume %zu: grid sizes changed since the batch was made", v);
+            return bfail(b, DDGI_ERR_INVALID_ARGUMENT, "volume %u: grid sizes changed since the batch was made",
+                         b->order[v]);
         if (c->dl.sky_mode != DDGI_SKY_CONSTANT)
-            return bfail(b, DDGI_ERR_UNSUPPORTED, "volume %zu: the atmospheric sky is not batched", v);
+            return bfail(b, DDGI_ERR_UNSUPPORTED, "volume %u: the atmospheric sky is not batched", b->order[v]);
     }
     return DDGI_OK;
 }
@@ -266,7 +290,7 @@ ddgi_status stage_inputs(ddgi_batch* b, const float* orientations) {
         ddgi_ctx* c = b->vols[v];
         const uint32_t R = c->grid.rays_per_probe;
         float* d = dirs + 4 * (size_t)b->dir_base[v];
-        ddgi_ray_direction_table(&orientations[9 * v], R, d);
+        ddgi_ray_direction_table(&orientations[9 * (size_t)b->order[v]], R, d);  // internal v: caller's order[v]
         // the volume's own record of its current direction table
         c->host_dirs.assign(d, d + 4 * (size_t)R);
         const uint32_t rpw = grouped_rays_per_warp(b->tuning.rays_per_warp, R);
@@ -305,7 +329,7 @@ cudaError_t enqueue(ddgi_batch* b, cudaStream_t st, bool timed) {
     if (timed) cudaEventRecord(b->ev[0], st);
     cudaError_t e = cudaMemcpyAsync(b->d_stage, b->h_stage, b->stage_bytes, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
-    k_batch_begin<<<1, 256, 0, st>>>(b->counters, b->d_done, b->d_clock, V);
+    k_batch_begin<<<1, 256, 0, st>>>(b->counters, 4 * (1 + (uint32_t)b->groups.size()), b->d_done, b->d_clock, V);
     e = launch_batch_tc_weights(bt, b->tc_bl, b->max_rows_tc, st);
     if (e != cudaSuccess) return e;
     TraceTuning tt;
@@ -315,6 +339,31 @@ cudaError_t enqueue(ddgi_batch* b, cudaStream_t st, bool timed) {
     tt.rays_per_warp = b->tuning.rays_per_warp;  // applied per volume through the volume table
     tt.wide = b->tuning.node_width == 8 ? 1u : 0u;
     tt.wait = b->tuning.straggler_lanes;
+    if (!timed && b->groups.size() > 1) {  // one branch per volume group, smallest first
+        e = cudaEventRecord(b->fork_ev, st);
+        for (size_t gi = 0; gi < b->groups.size() && e == cudaSuccess; ++gi) {
+            const ddgi_batch::Group& G = b->groups[gi];
+            cudaStream_t gs = b->gstreams[gi];
+            e = cudaStreamWaitEvent(gs, b->fork_ev, 0);
+            BatchTables gbt = bt;
+            gbt.first = G.first;
+            WaveHits gwh{b->thit, b->prim, b->front + G.first};
+            ShadowQueue gq{b->q_idx + G.first, b->q_pos + G.first, b->q_sun + G.first, nullptr};
+            if (e == cudaSuccess)
+                e = launch_batch_trace(arena_scene(b), gbt, G.total, gwh, gq, b->counters + 4 * (1 + gi), b->rays,
+                                       b->stack_cap, b->wstack_cap, tt, gs, nullptr, nullptr);
+            if (e == cudaSuccess && G.fp32_bl.ntiles > 0)
+                e = b->tuning.blend_threads == 0
+                        ? launch_batch_blend_fp32_shared(gbt, G.fp32s_bl, b->max_ntex_fp32, b->max_rays_fp32, b->rays,
+                                                         gs)
+                        : launch_batch_blend_fp32(gbt, G.fp32_bl, b->max_rays_fp32, b->rays, b->tuning.blend_threads,
+                                                  gs);
+            if (e == cudaSuccess && G.tc_bl.ntiles > 0) e = launch_batch_blend_tc(gbt, G.tc_bl, b->rays, b->tc_smem, gs);
+            if (e == cudaSuccess) e = cudaEventRecord(b->gjoin[gi], gs);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(st, b->gjoin[gi], 0);
+        }
+        return e;
+    }
     WaveHits wh{b->thit, b->prim, b->front};
     ShadowQueue q{b->q_idx, b->q_pos, b->q_sun, nullptr};
     e = launch_batch_trace(arena_scene(b), bt, b->total, wh, q, b->counters, b->rays, b->stack_cap, b->wstack_cap,
@@ -418,13 +467,24 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
         return s;
     };
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    b->vols.assign(volumes, volumes + count);
     for (uint32_t v = 0; v < count; ++v) {
-        const ddgi_ctx* c = b->vols[v];
+        const ddgi_ctx* c = volumes[v];
         if (!c) return bail(DDGI_ERR_INVALID_ARGUMENT);
         for (uint32_t u = 0; u < v; ++u)
-            if (b->vols[u] == c) return bail(DDGI_ERR_INVALID_ARGUMENT);  // listed twice
+            if (volumes[u] == c) return bail(DDGI_ERR_INVALID_ARGUMENT);  // listed twice
         if (!c->scene.built) return bail(DDGI_ERR_NO_SCENE);
+    }
+    // internal order: increasing ray count (stable)
+    b->order.resize(count);
+    for (uint32_t v = 0; v < count; ++v) b->order[v] = v;
+    auto rays_of = [&](uint32_t v) {
+        const ddgi_grid_desc& g = volumes[v]->grid;
+        return (uint64_t)g.resolution[0] * g.resolution[1] * g.resolution[2] * g.rays_per_probe;
+    };
+    std::stable_sort(b->order.begin(), b->order.end(), [&](uint32_t x, uint32_t y) { return rays_of(x) < rays_of(y); });
+    for (uint32_t v = 0; v < count; ++v) {
+        ddgi_ctx* c = volumes[b->order[v]];
+        b->vols.push_back(c);
         b->scene_builds.push_back(c->scene.build_id);
         b->grids.push_back(c->grid);
     }
@@ -486,7 +546,7 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
         cudaMalloc(&b->q_idx, sizeof(uint32_t) * N) != cudaSuccess ||
         cudaMalloc(&b->q_pos, sizeof(float4) * N) != cudaSuccess ||
         cudaMalloc(&b->q_sun, sizeof(float4) * N) != cudaSuccess ||
-        cudaMalloc(&b->counters, 4 * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&b->counters, 4 * (1 + kGroups) * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&b->d_ray_base, sizeof(uint32_t) * (count + 1)) != cudaSuccess ||
         cudaMalloc(&b->d_clock, sizeof(unsigned long long) * (count + 1)) != cudaSuccess ||
         cudaMalloc(&b->d_done, sizeof(uint32_t) * count) != cudaSuccess ||
@@ -531,6 +591,69 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
     b->fp32_bl = BatchBlendList{b->d_lists, b->d_lists + nf, nf, fp32_base.back()};
     b->tc_bl = BatchBlendList{b->d_lists + 2 * nf + 1, b->d_lists + 2 * nf + 1 + nt, nt, tc_base.back()};
     b->fp32s_bl = BatchBlendList{b->d_lists, b->d_lists + 2 * nf + 2 * nt + 2, nf, fp32s_base.back()};
+
+    // ---- volume groups: equal volume counts, their own blend lists ----
+    {
+        const uint32_t K = std::min<uint32_t>(kGroups, count);
+        std::vector<uint32_t> gl;
+        struct Off {
+            size_t fl, fb, tl, tb, sb;
+            uint32_t nf, nt, fbt, tbt, sbt;
+        };
+        std::vector<Off> offs;
+        for (uint32_t k = 0; k < K; ++k) {
+            ddgi_batch::Group G{};
+            G.v0 = (uint32_t)((uint64_t)count * k / K);
+            G.v1 = (uint32_t)((uint64_t)count * (k + 1) / K);
+            G.first = b->ray_base[G.v0];
+            G.total = b->ray_base[G.v1] - G.first;
+            std::vector<uint32_t> fl, fb{0}, tl, tb{0}, sb{0};
+            for (uint32_t v = G.v0; v < G.v1; ++v) {
+                const ddgi_ctx* c = b->vols[v];
+                const uint32_t P = (uint32_t)c->grid.resolution[0] * c->grid.resolution[1] * c->grid.resolution[2];
+                if (c->fp16) {
+                    tl.push_back(v);
+                    tb.push_back(tb.back() + tc_tiles(P));
+                } else {
+                    fl.push_back(v);
+                    fb.push_back(fb.back() + P);
+                    sb.push_back(sb.back() + fp32_shared_tiles(P));
+                }
+            }
+            Off o;
+            o.nf = (uint32_t)fl.size();
+            o.nt = (uint32_t)tl.size();
+            o.fbt = fb.back();
+            o.tbt = tb.back();
+            o.sbt = sb.back();
+            o.fl = gl.size(), gl.insert(gl.end(), fl.begin(), fl.end());
+            o.fb = gl.size(), gl.insert(gl.end(), fb.begin(), fb.end());
+            o.tl = gl.size(), gl.insert(gl.end(), tl.begin(), tl.end());
+            o.tb = gl.size(), gl.insert(gl.end(), tb.begin(), tb.end());
+            o.sb = gl.size(), gl.insert(gl.end(), sb.begin(), sb.end());
+            offs.push_back(o);
+            b->groups.push_back(G);
+        }
+        if (cudaMalloc(&b->d_glists, sizeof(uint32_t) * std::max<size_t>(gl.size(), 1)) != cudaSuccess ||
+            cudaMemcpyAsync(b->d_glists, gl.data(), sizeof(uint32_t) * gl.size(), cudaMemcpyHostToDevice, st) !=
+                cudaSuccess) {
+            cudaGetLastError();
+            return bail(DDGI_ERR_OUT_OF_MEMORY);
+        }
+        for (uint32_t k = 0; k < K; ++k) {
+            const Off& o = offs[k];
+            ddgi_batch::Group& G = b->groups[k];
+            G.fp32_bl = BatchBlendList{b->d_glists + o.fl, b->d_glists + o.fb, o.nf, o.fbt};
+            G.tc_bl = BatchBlendList{b->d_glists + o.tl, b->d_glists + o.tb, o.nt, o.tbt};
+            G.fp32s_bl = BatchBlendList{b->d_glists + o.fl, b->d_glists + o.sb, o.nf, o.sbt};
+            cudaStream_t gs = nullptr;
+            cudaEvent_t ge = nullptr;
+            if (cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking) != cudaSuccess) return bail(DDGI_ERR_CUDA);
+            b->gstreams.push_back(gs);
+            if (cudaEventCreateWithFlags(&ge, cudaEventDisableTiming) != cudaSuccess) return bail(DDGI_ERR_CUDA);
+            b->gjoin.push_back(ge);
+        }
+    }
 
     // ---- arena: copy every volume's trees with rebased references ----
     uint64_t node_off = 0, tri_off = 0, inst_off = 0, wnode_off = 0;
@@ -594,6 +717,9 @@ ddgi_status ddgi_batch_destroy(ddgi_batch* b) {
     bfree(b->d_done);
     bfree(b->d_err);
     bfree(b->d_lists);
+    bfree(b->d_glists);
+    for (cudaStream_t gs : b->gstreams) cudaStreamDestroy(gs);
+    for (cudaEvent_t ge : b->gjoin) cudaEventDestroy(ge);
     bfree(b->d_stage);
     if (b->h_stage) cudaFreeHost(b->h_stage);
     if (b->cap) cudaStreamDestroy(b->cap);
@@ -678,8 +804,9 @@ ddgi_status ddgi_batch_completion_ms(ddgi_batch* b, float* ms, uint32_t count) {
     if (s != DDGI_OK) return s;
     std::vector<unsigned long long> clk(V + 1);
     BCK(cudaMemcpy(clk.data(), b->d_clock, sizeof(unsigned long long) * (V + 1), cudaMemcpyDeviceToHost), "read clock");
-    for (uint32_t v = 0; v < V; ++v)
-        ms[v] = clk[1 + v] >= clk[0] && clk[1 + v] != 0 ? (float)((double)(clk[1 + v] - clk[0]) * 1e-6) : -1.0f;
+    for (uint32_t v = 0; v < V; ++v)  // internal volume v is the caller's order[v]
+        ms[b->order[v]] =
+            clk[1 + v] >= clk[0] && clk[1 + v] != 0 ? (float)((double)(clk[1 + v] - clk[0]) * 1e-6) : -1.0f;
     return DDGI_OK;
 }
 

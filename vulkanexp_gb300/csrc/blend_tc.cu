@@ -18,19 +18,20 @@
 // accumulator at tensor-memory column 0 (wider tiles: depth at 0, colour at
 // 256, in two MMAs).  Only the row x column pairs of matching kind are read
 // back; the rest of the product is the price of one MMA per K step, cheap in
-// this memory-bound kernel.  K is processed in chunks of 32 rays staged in
-// shared memory as BF16; both operands are split into a BF16 high part and a
-// BF16 remainder (x = hi + lo) and three products hi*hi + hi*lo + lo*hi are
-// accumulated (~16 mantissa bits, below the FP16 atlas store's rounding;
-// BF16 keeps FP32's exponent range, so no scaling is needed).  One thread
-// issues tcgen05.mma (M = 128, K = 16 per instruction); while a chunk's
-// MMAs run, the next chunk's weights arrive by cp.async into the second B
-// buffer and its records into registers.  With 256 accumulator columns two
-// CTAs share an SM.  The epilogue reads the accumulators with tcgen05.ld,
-// normalises through shared memory into texel order, applies hysteresis in
-// the FP32 accumulators (previous values loaded eight per thread at a time),
-// stores FP16 texels together with the border texels that copy them, and
-// updates the probe states.
+// this memory-bound kernel.  K is processed in chunks of 16 rays (one MMA K
+// step) staged as BF16 in a ring of four shared-memory stages; both operands
+// are split into a BF16 high part and a BF16 remainder (x = hi + lo) and
+// three products hi*hi + hi*lo + lo*hi are accumulated (~16 mantissa bits,
+// below the FP16 atlas store's rounding; BF16 keeps FP32's exponent range,
+// so no scaling is needed).  One thread issues tcgen05.mma (M = 128,
+// K = 16); while a chunk's MMAs run, the next chunks' weights arrive by
+// cp.async and their records into registers.  With 256 accumulator columns
+// two CTAs share an SM.  The epilogue reads the accumulators with
+// tcgen05.ld, normalises (times the reciprocal row sums) through shared
+// memory into texel order, applies hysteresis in the FP32 accumulators
+// (previous values loaded eight per thread at a time), stores FP16 texels
+// together with the border texels that copy them, and updates the probe
+// states.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -232,6 +233,8 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
     __shared__ uint64_t s_bar[kStages];
     __shared__ uint32_t s_tmem;
     __shared__ uint32_t s_oor[kTileProbes], s_maxc[kTileProbes];
+    __shared__ float s_rinv[512];       // 1 / row sum of the weights (1 where the sum is <= 1e-3)
+    __shared__ int2 s_org[kTileProbes];  // atlas tile (x, y) of each probe, in tiles; x < 0: none
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t np = min((uint32_t)kTileProbes, nprobes - p0);
@@ -251,6 +254,22 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
     if (tid < kTileProbes) {
         s_maxc[tid] = 0u;
         s_oor[tid] = 0u;
+        int2 o = make_int2(-1, -1);
+        if ((uint32_t)tid < np) {
+            const uint32_t rx = (uint32_t)a.g.res[0], rxy = (uint32_t)(a.g.res[0] * a.g.res[1]);
+            const uint32_t probe = a.probe_list ? a.probe_list[p0 + tid] : p0 + tid;
+            if (probe < rxy * (uint32_t)a.g.res[2]) {
+                const int ix = (int)(probe % rx), iy = (int)((probe % rxy) / rx), iz = (int)(probe / rxy);
+                o = make_int2(iy * a.g.res[0] + ix, iz);
+            } else {
+                raise_error(a.err, DEV_BAD_INDEX);  // a probe list entry outside the grid
+            }
+        }
+        s_org[tid] = o;
+    }
+    for (uint32_t i = tid; i < a.Nd + a.Nc; i += kThreads) {
+        const float sum = a.rowsum[i];
+        s_rinv[i] = sum > 1e-3f ? 1.0f / sum : 1.0f;
     }
     // A rows kTileProbes * 5 .. 127 stay zero in every stage
     for (uint32_t i = tid; i < kStages * 2 * 3 * (kKChunk / 8); i += kThreads) {
@@ -406,22 +425,18 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
             tc::tmem_ld16(lane_base + col0, vv);
             if (!rvalid) continue;
             if (depth && ch >= 3) {
+                float* dst = S_d + rp * ntd * 2 + (ch - 3);
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
                     const uint32_t u = s * 16 + i;
-                    if (u < ntd) {
-                        const float sum = a.rowsum[u];
-                        S_d[(rp * ntd + u) * 2 + (ch - 3)] = sum > 1e-3f ? vv[i] / sum : vv[i];
-                    }
+                    if (u < ntd) dst[u * 2] = vv[i] * s_rinv[u];
                 }
             } else if (!depth && ch < 3) {
+                float* dst = S_c + rp * ntc * 3 + ch;
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
                     const uint32_t t = (s - steps_d) * 16 + i;
-                    if (t < ntc) {
-                        const float sum = a.rowsum[a.Nd + t];
-                        S_c[(rp * ntc + t) * 3 + ch] = sum > 1e-3f ? vv[i] / sum : vv[i];
-                    }
+                    if (t < ntc) dst[t * 3] = vv[i] * s_rinv[a.Nd + t];
                 }
             }
         }
@@ -432,41 +447,43 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
         // (probesCopyBorders.comp); loads of the previous values are issued
         // eight at a time per thread
         const float hy = a.hyst_dev ? *a.hyst_dev : a.g.hyst;
-        const uint32_t rx = (uint32_t)a.g.res[0], rxy = (uint32_t)(a.g.res[0] * a.g.res[1]);
-        const uint32_t nprobes_grid = rxy * (uint32_t)a.g.res[2];
         const int ncr = (int)a.g.color_res, ndr = (int)a.g.depth_res;
-        auto texel_of = [&](uint32_t pl2, uint32_t t, uint32_t n, int res, uint32_t width, int* ox, int* oy,
-                            bool* bad) -> size_t {
-            const uint32_t probe = a.probe_list ? a.probe_list[p0 + pl2] : p0 + pl2;
-            *bad = probe >= nprobes_grid;
-            const uint32_t pr = *bad ? 0u : probe;
-            const int ix = (int)(pr % rx), iy = (int)((pr % rxy) / rx), iz = (int)(pr / rxy);
-            *ox = res * (iy * a.g.res[0] + ix);
-            *oy = res * iz;
-            return (size_t)(*oy + 1 + (int)(t / n)) * width + (size_t)(*ox + 1 + (int)(t % n));
+        // item i -> (probe, texel) and texel -> (x, y) without integer
+        // division: floor((i + 0.5) / n) in float is exact here (i < 2^13,
+        // n <= 256: the product's error is far below the 0.5 / n margin)
+        const float inv_ntc = 1.0f / (float)ntc, inv_ntd = 1.0f / (float)ntd;
+        const float inv_nc = 1.0f / (float)a.nc, inv_nd = 1.0f / (float)a.nd;
+        auto split_index = [](uint32_t i, uint32_t n, float inv, uint32_t* q) {
+            *q = (uint32_t)(((float)i + 0.5f) * inv);
+            return i - *q * n;
         };
         constexpr int kBatch = 8;
         const uint32_t items_c = np * ntc;
         for (uint32_t base = 0; base < items_c; base += kBatch * kThreads) {
             float4 prev[kBatch];
             size_t ti[kBatch];
-            int oxs[kBatch], oys[kBatch];
-            bool bad[kBatch];
 #pragma unroll
             for (int k = 0; k < kBatch; ++k) {
                 const uint32_t i = base + (uint32_t)k * kThreads + (uint32_t)tid;
-                bad[k] = true;
+                ti[k] = ~(size_t)0;
                 if (i < items_c) {
-                    ti[k] = texel_of(i / ntc, i % ntc, a.nc, ncr, a.g.color_w, &oxs[k], &oys[k], &bad[k]);
-                    if (!bad[k]) prev[k] = a.acc_color[ti[k]];
-                    else raise_error(a.err, DEV_BAD_INDEX);  // a probe list entry outside the grid
+                    uint32_t pl2, ty;
+                    const uint32_t t = split_index(i, ntc, inv_ntc, &pl2);
+                    const uint32_t tx = split_index(t, a.nc, inv_nc, &ty);
+                    const int2 o = s_org[pl2];
+                    if (o.x >= 0) {
+                        ti[k] = (size_t)(ncr * o.y + 1 + (int)ty) * a.g.color_w + (size_t)(ncr * o.x + 1 + (int)tx);
+                        prev[k] = a.acc_color[ti[k]];
+                    }
                 }
             }
 #pragma unroll
             for (int k = 0; k < kBatch; ++k) {
-                if (bad[k]) continue;
+                if (ti[k] == ~(size_t)0) continue;
                 const uint32_t i = base + (uint32_t)k * kThreads + (uint32_t)tid;
-                const uint32_t pl2 = i / ntc, t = i % ntc;
+                uint32_t pl2, ty;
+                const uint32_t t = split_index(i, ntc, inv_ntc, &pl2);
+                const uint32_t tx = split_index(t, a.nc, inv_nc, &ty);
                 const float* res = S_c + (pl2 * ntc + t) * 3;
                 const float mc = fmaxf(fmaxf(fabsf(res[0] - prev[k].x), fabsf(res[1] - prev[k].y)),
                                        fabsf(res[2] - prev[k].z));
@@ -477,8 +494,9 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
                 a.acc_color[ti[k]] = nv;
                 const uint2 hv = float4_to_half4(nv.x, nv.y, nv.z, nv.w);
                 a.color[ti[k]] = hv;
-                const int ox = oxs[k], oy = oys[k];
-                for_border_targets((int)(t % a.nc) + 1, (int)(t / a.nc) + 1, ncr, [&](int bx, int by) {
+                const int2 o = s_org[pl2];
+                const int ox = ncr * o.x, oy = ncr * o.y;
+                for_border_targets((int)tx + 1, (int)ty + 1, ncr, [&](int bx, int by) {
                     a.color[(size_t)(oy + by) * a.g.color_w + (size_t)(ox + bx)] = hv;
                 });
             }
@@ -487,36 +505,45 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
         for (uint32_t base = 0; base < items_d; base += kBatch * kThreads) {
             float2 prev[kBatch];
             size_t ti[kBatch];
-            int oxs[kBatch], oys[kBatch];
-            bool bad[kBatch];
 #pragma unroll
             for (int k = 0; k < kBatch; ++k) {
                 const uint32_t i = base + (uint32_t)k * kThreads + (uint32_t)tid;
-                bad[k] = true;
+                ti[k] = ~(size_t)0;
                 if (i < items_d) {
-                    ti[k] = texel_of(i / ntd, i % ntd, a.nd, ndr, a.g.depth_w, &oxs[k], &oys[k], &bad[k]);
-                    if (!bad[k]) prev[k] = a.acc_depth[ti[k]];
+                    uint32_t pl2, ty;
+                    const uint32_t u = split_index(i, ntd, inv_ntd, &pl2);
+                    const uint32_t tx = split_index(u, a.nd, inv_nd, &ty);
+                    const int2 o = s_org[pl2];
+                    if (o.x >= 0) {
+                        ti[k] = (size_t)(ndr * o.y + 1 + (int)ty) * a.g.depth_w + (size_t)(ndr * o.x + 1 + (int)tx);
+                        prev[k] = a.acc_depth[ti[k]];
+                    }
                 }
             }
 #pragma unroll
             for (int k = 0; k < kBatch; ++k) {
-                if (bad[k]) continue;
+                if (ti[k] == ~(size_t)0) continue;
                 const uint32_t i = base + (uint32_t)k * kThreads + (uint32_t)tid;
-                const uint32_t pl2 = i / ntd, u = i % ntd;
+                uint32_t pl2, ty;
+                const uint32_t u = split_index(i, ntd, inv_ntd, &pl2);
+                const uint32_t tx = split_index(u, a.nd, inv_nd, &ty);
                 const float* res = S_d + (pl2 * ntd + u) * 2;
                 const float2 nv = make_float2(res[0] * (1.0f - hy) + prev[k].x * hy, res[1] * (1.0f - hy) + prev[k].y * hy);
                 a.acc_depth[ti[k]] = nv;
-                const __half2 o = __floats2half2_rn(nv.x, nv.y);
-                const uint32_t hv = *reinterpret_cast<const uint32_t*>(&o);
+                const __half2 h2 = __floats2half2_rn(nv.x, nv.y);
+                const uint32_t hv = *reinterpret_cast<const uint32_t*>(&h2);
                 a.depth[ti[k]] = hv;
-                const int ox = oxs[k], oy = oys[k];
-                for_border_targets((int)(u % a.nd) + 1, (int)(u / a.nd) + 1, ndr, [&](int bx, int by) {
+                const int2 o = s_org[pl2];
+                const int ox = ndr * o.x, oy = ndr * o.y;
+                for_border_targets((int)tx + 1, (int)ty + 1, ndr, [&](int bx, int by) {
                     a.depth[(size_t)(oy + by) * a.g.depth_w + (size_t)(ox + bx)] = hv;
                 });
             }
         }
         __syncthreads();
 
+        const uint32_t rxy = (uint32_t)(a.g.res[0] * a.g.res[1]);
+        const uint32_t nprobes_grid = rxy * (uint32_t)a.g.res[2];
         const uint32_t probe_t = (uint32_t)tid < np ? (a.probe_list ? a.probe_list[p0 + tid] : p0 + tid) : nprobes_grid;
         if (probe_t < nprobes_grid) {  // probesUpdate.glsl:110-119
             uint32_t s = a.states[probe_t];

@@ -136,6 +136,7 @@ struct BatchTables {
     unsigned long long* clock;  // [0] batch start, [1 + v] blend completion of volume v (ns, globaltimer)
     uint32_t* done;             // blend work items finished, per volume
     uint32_t* err;
+    uint32_t first;             // record of a launch's first work item (a group of volumes; 0: all)
 };
 
 // Volumes one blend kernel covers: list[i] is a volume index, its work items

@@ -340,6 +340,7 @@ struct BatchPrimaryJob {
 
     template <class W>
     __device__ __forceinline__ bool start(W& w, const DeviceScene& sc, uint32_t id, uint32_t* out) const {
+        id += bt.first;  // records of the launch's volumes
         const uint32_t v = batch_volume(bt, id);
         const BatchVolume& vol = bt.vols[v];
         const uint32_t R = vol.g.rays;
@@ -417,9 +418,9 @@ __global__ void __launch_bounds__(kPersistThreads, Walker<false, Stack>::kMinBlo
 // Batched shading, pass 1 (k_shade_classify with the record's volume).
 __global__ void __launch_bounds__(128) k_batch_classify(BatchTables bt, uint32_t total, WaveHits hits,
                                                         float4* rays_out, uint32_t* front_count) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = bt.first + blockIdx.x * blockDim.x + threadIdx.x;
     bool is_front = false;
-    if (i < total) {
+    if (i < bt.first + total) {
         const float4 th = hits.thit[i];
         const uint32_t pb = hits.prim[i];
         const uint32_t inst = __float_as_uint(th.w);
