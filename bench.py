@@ -563,8 +563,10 @@ def main():
         if world > 1:
             torch.distributed.barrier()
         ms, stages = time_updates(ctx, w, args.steps, args.warmup, stream, flush)
+        info = ctx.scene_info()
         forms[name] = {"ms_per_update": ms, "value": P * R / (ms * 1e-3) / 1e9, "stage_ms": stages,
-                       "scene_build_s": build_s}
+                       "scene_build_s": build_s, "mesh_tree_build_gpu_ms": info["tree_build_ms"],
+                       "tree_nodes": info["nodes"], "triangle_refs": info["tri_refs"]}
         if name != "wavefront_bf16":
             ctx.close()
     clocks = sampler.stop()

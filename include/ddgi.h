@@ -7,10 +7,10 @@
  * (src/shaders/traceProbes.rgen, closesthit.glsl with NO_REFLECTION,
  * miss.rmiss, shadow.rmiss, probesUpdate.glsl, probesCopyBorders.comp,
  * probesInit.rgen).  The driver-built Vulkan BLAS/TLAS
- * (src/Renderer.cpp:240-642) is replaced by this library's own trees:
- * surface-area-heuristic trees with spatial splits built on the host threads
- * (the default, like the driver's PREFER_FAST_TRACE structures), or an LBVH
- * built on the GPU (ddgi_set_build_mode), traversed by CUDA kernels.
+ * (src/Renderer.cpp:240-642) is replaced by this library's own trees, built
+ * on the GPU: surface-area-heuristic trees with spatial splits (the default,
+ * like the driver's PREFER_FAST_TRACE structures) or an LBVH
+ * (ddgi_set_build_mode), traversed by CUDA kernels.
  *
  * Conventions
  *  - Every entry point returns a ddgi_status and never throws.
@@ -373,6 +373,27 @@ ddgi_status ddgi_trace_rays(ddgi_ctx* ctx, const float* origins, const float* di
 ddgi_status ddgi_count_fetches(ddgi_ctx* ctx, const float orientation[9], const uint32_t* probe_list,
                                uint32_t probe_count, uint64_t out[11], ddgi_stream stream);
 
+/* Sizes of the built scene's trees.  node_count binary nodes (the mesh
+ * trees in mesh order, then the top level), tri_refs triangle references
+ * in leaf order, the deepest mesh tree and the top level's depth (inner
+ * nodes on the longest root-to-leaf path), the builder, and the device time
+ * of the GPU fast-trace mesh-tree build (0 for the other builders). */
+typedef struct ddgi_scene_info {
+    uint64_t node_count;
+    uint64_t tri_refs;
+    uint32_t depth_blas, depth_tlas;
+    uint32_t build_mode;
+    float tree_build_ms;
+} ddgi_scene_info;
+ddgi_status ddgi_get_scene_info(const ddgi_ctx* ctx, ddgi_scene_info* out);
+/* Copies the built trees to host arrays (for tests): up to node_capacity
+ * nodes of 64 bytes (child boxes and references, the library's node
+ * layout) and up to tri_capacity triangles of 48 bytes in leaf order
+ * (v0 xyz + the mesh-local triangle index as bits, v1, v2); NULL skips an
+ * array.  Synchronous on `stream`. */
+ddgi_status ddgi_read_trees(ddgi_ctx* ctx, void* nodes, uint64_t node_capacity, void* tris, uint64_t tri_capacity,
+                            ddgi_stream stream);
+
 /* Replaces the material table of the built scene (same count), e.g. new
  * albedos, without rebuilding the acceleration structures. */
 ddgi_status ddgi_set_materials(ddgi_ctx* ctx, const ddgi_material* materials, uint32_t count);
@@ -478,14 +499,17 @@ ddgi_status ddgi_set_trace_tuning(ddgi_ctx* ctx, const ddgi_trace_tuning* tuning
 ddgi_status ddgi_set_leaf_size(ddgi_ctx* ctx, uint32_t max_triangles);
 /* Tree builder of the next ddgi_scene_build (mesh trees and top level) and
  * of ddgi_update_instances' top-level rebuilds.  Hits do not depend on it.
- *   DDGI_BUILD_FAST_TRACE (default): surface-area-heuristic trees built on
- *     the host (the reference's PREFER_FAST_TRACE structures,
- *     src/Renderer.cpp:334);
+ *   DDGI_BUILD_FAST_TRACE (default): surface-area-heuristic trees with
+ *     spatial splits built on the GPU (the reference's PREFER_FAST_TRACE
+ *     structures, src/Renderer.cpp:334);
  *   DDGI_BUILD_FAST_BUILD: linear BVHs built on the GPU (PREFER_FAST_BUILD,
- *     src/Renderer.cpp:364). */
+ *     src/Renderer.cpp:364);
+ *   DDGI_BUILD_FAST_TRACE_HOST: the same trees as DDGI_BUILD_FAST_TRACE,
+ *     built on the host threads. */
 typedef enum ddgi_build_mode {
     DDGI_BUILD_FAST_TRACE = 0,
-    DDGI_BUILD_FAST_BUILD = 1
+    DDGI_BUILD_FAST_BUILD = 1,
+    DDGI_BUILD_FAST_TRACE_HOST = 2
 } ddgi_build_mode;
 ddgi_status ddgi_set_build_mode(ddgi_ctx* ctx, ddgi_build_mode mode);
 /* Spatial splits of the fast-trace mesh trees built by the next

@@ -188,8 +188,8 @@ static std::vector<float> height_field(std::mt19937& rng, int cells, float size)
 // The clipped reference box against the exact geometry: triangles nearly
 // parallel to a coordinate plane (thickness 1e-6 .. 1e-3 of their size along
 // that axis) cut by a plane through them; every point of the triangle (in
-// double) on either side of the plane lies in that side's clipped box.  (The
-// float clipper this replaced was off by up to 1e-3 of an edge here.)
+// double) on either side of the plane lies in that side's clipped box.  (A
+// sequential float polygon clipper was off by up to 1e-3 of an edge here.)
 static void check_clip(std::mt19937& rng, int cases) {
     std::uniform_real_distribution<double> U(0.0, 1.0), C(-3.0, 3.0);
     std::uniform_real_distribution<double> L(-6.0, -3.0);
@@ -218,7 +218,7 @@ static void check_clip(std::mt19937& rng, int cases) {
             float slo[3] = {nlo[0], nlo[1], nlo[2]}, shi[3] = {nhi[0], nhi[1], nhi[2]};
             if (side == 0) shi[k] = plane;
             else slo[k] = plane;
-            sbvh_clip_box(tri, slo, shi, lo[side], hi[side]);
+            sbvh_clip_box(tri, k, slo, shi, lo[side], hi[side]);
         }
         for (int s = 0; s < 2000; ++s) {
             double a = U(rng), b = U(rng);

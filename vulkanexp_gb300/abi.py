@@ -119,6 +119,12 @@ class Timings(C.Structure):
                 ("copy_ms", C.c_float), ("primary_ms", C.c_float)]
 
 
+class SceneInfo(C.Structure):
+    """ddgi_scene_info: sizes of the built trees."""
+    _fields_ = [("node_count", C.c_uint64), ("tri_refs", C.c_uint64), ("depth_blas", C.c_uint32),
+                ("depth_tlas", C.c_uint32), ("build_mode", C.c_uint32), ("tree_build_ms", C.c_float)]
+
+
 class BatchTuning(C.Structure):
     """ddgi_batch_tuning: launch parameters of a batch."""
     _fields_ = [("trace_ctas_per_sm", C.c_uint32), ("refill_lanes", C.c_uint32), ("smem_stack", C.c_uint32),

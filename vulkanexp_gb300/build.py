@@ -22,7 +22,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-Xptxas", "-warn-spills"]
 SOURCES = ["lbvh.cu", "trace.cu", "wavefront.cu", "blend.cu", "blend_tc.cu", "adjoint.cu", "ddgi_api.cu",
-           "noalloc.cu", "batch.cu", "schedule.cu", "gather.cu", "wide.cu", "sah.cu", "blend_shared.cu", "sbvh.cu", "sky.cu"]
+           "noalloc.cu", "batch.cu", "schedule.cu", "gather.cu", "wide.cu", "sah.cu", "blend_shared.cu", "sbvh.cu", "sky.cu",
+           "gbuild.cu"]
 
 
 def nvcc():

@@ -43,6 +43,7 @@ struct SceneBuffers {
     uint64_t node_count = 0, tri_count = 0;
     uint64_t build_id = 0;  // distinct for every successful build or instance update in the process
     ddgi_build_mode build_mode = DDGI_BUILD_FAST_BUILD;  // builder of these trees
+    float gpu_build_ms = 0.0f;  // device time of the GPU fast-trace mesh-tree build
     bool built = false;
     // top level, kept for instance updates (refit / rebuild)
     std::vector<GpuInstance> host_inst;      // caller order

@@ -30,6 +30,7 @@
 #include "kernels.h"
 #include "lbvh.h"
 #include "nvtx.h"
+#include "gbuild.h"
 #include "sah.h"
 #include "wide.h"
 
@@ -540,6 +541,20 @@ ddgi_status build_top_level(ddgi_ctx* ctx, uint64_t node_base, void* scratch, fl
     std::vector<uint32_t> order(ni);
     std::vector<BvhNode> top(inner);
     if (S.build_mode == DDGI_BUILD_FAST_TRACE) {
+        CK(cudaMemcpyAsync(box_lo, S.inst_lo.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
+        CK(cudaMemcpyAsync(box_hi, S.inst_hi.data(), sizeof(float4) * ni, cudaMemcpyHostToDevice, st), "upload boxes");
+        GpuTreeBuilder gtb;
+        CK(gtb.build_boxes(box_lo, box_hi, ni, kTlasLeafMax, ctx->err, st), "top-level build");
+        CK(gtb.write(S.nodes, std::vector<int>{(int)node_base}, std::vector<int>{0}, sorted, std::vector<uint32_t>{0},
+                     st),
+           "top-level build");
+        const uint32_t d = gtb.depths()[0];
+        CK(cudaMemcpyAsync(depth_dev, &d, sizeof(d), cudaMemcpyHostToDevice, st), "upload depth");
+        CK(cudaMemcpyAsync(order.data(), sorted, sizeof(uint32_t) * ni, cudaMemcpyDeviceToHost, st), "read order");
+        CK(cudaMemcpyAsync(top.data(), S.nodes + node_base, sizeof(BvhNode) * inner, cudaMemcpyDeviceToHost, st),
+           "read top level");
+        CK(cudaStreamSynchronize(st), "top-level build");
+    } else if (S.build_mode == DDGI_BUILD_FAST_TRACE_HOST) {
         uint32_t d = 1;
         sah_build(S.inst_lo.data(), S.inst_hi.data(), ni, kTlasLeafMax, (int)node_base, 0, top.data(), order.data(), &d,
                   host_threads());
@@ -884,31 +899,8 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
         nrm[v] = make_float4(vx.normal[0], vx.normal[1], vx.normal[2], 0.0f);
     }
     float4* dpos = nullptr;
-    // fast-trace mesh trees are built on the host first: their node and
-    // triangle-reference counts (spatial splits reference some triangles
-    // more than once) size the device arrays
-    const bool host_trees = ctx->build_mode == DDGI_BUILD_FAST_TRACE;
-    std::vector<HostTree> trees;
-    if (host_trees) build_host_trees(d, pos, ctx->blas_leaf_max, ctx->split_alpha, trees);
-    uint64_t total_tris = 0, total_nodes = 0;
-    uint32_t max_tris = 0;
-    for (uint32_t m = 0; m < d->mesh_count; ++m) {
-        uint32_t nt = d->meshes[m].index_count / 3;
-        if (host_trees) {
-            total_tris += trees[m].order.size();
-            total_nodes += trees[m].nodes.size();
-            max_tris = std::max(max_tris, (uint32_t)std::min<size_t>(trees[m].order.size(), 0xFFFFFFFFu));
-            continue;
-        }
-        total_tris += nt;
-        total_nodes += nt > 1 ? nt - 1 : (nt == 1 ? 1 : 0);
-        max_tris = std::max(max_tris, nt);
-    }
-    uint32_t ni = d->instance_count;
-    uint64_t tlas_nodes = ni > 1 ? ni - 1 : (ni == 1 ? 1 : 0);
-    uint32_t max_prims = std::max(max_tris, ni);
-    if (total_tris >= (1ull << 28) - 8 || total_nodes + tlas_nodes >= (1ull << 31))
-        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "scene too large (%llu triangles)", (unsigned long long)total_tris);
+    float* dsoup = nullptr;      // triangles as 9 floats (GPU fast-trace builder input)
+    uint32_t* gorder = nullptr;  // leaf order of the GPU-built mesh trees
     void* scratch = nullptr;
     float4* box_lo = nullptr;
     float4* box_hi = nullptr;
@@ -916,6 +908,8 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
     uint32_t* depth = nullptr;  // [0] deepest mesh tree, [1] top-level tree
     auto cleanup = [&]() {
         if (dpos) cudaFree(dpos);
+        if (dsoup) cudaFree(dsoup);
+        if (gorder) cudaFree(gorder);
         if (scratch) cudaFree(scratch);
         if (box_lo) cudaFree(box_lo);
         if (box_hi) cudaFree(box_hi);
@@ -937,19 +931,6 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
     CKB(cudaMalloc(&S.indices, sizeof(uint32_t) * std::max<uint32_t>(d->index_count, 1)), "alloc indices");
     CKB(cudaMalloc(&S.offsets, sizeof(ddgi_offset_entry) * std::max<uint32_t>(d->offset_count, 1)), "alloc offsets");
     CKB(cudaMalloc(&S.materials, sizeof(ddgi_material) * std::max<uint32_t>(d->material_count, 1)), "alloc materials");
-    CKB(cudaMalloc(&S.nodes, sizeof(BvhNode) * std::max<uint64_t>(total_nodes + tlas_nodes, 1)), "alloc nodes");
-    CKB(cudaMalloc(&S.tris, sizeof(BvhTri) * std::max<uint64_t>(total_tris, 1)), "alloc triangles");
-    CKB(cudaMalloc(&S.inst_leaf, sizeof(GpuInstance) * std::max<uint32_t>(ni, 1)), "alloc instances");
-    CKB(cudaMalloc(&S.inst_id, sizeof(GpuInstance) * std::max<uint32_t>(ni, 1)), "alloc instances");
-    CKB(cudaMalloc(&scratch, lbvh_scratch_bytes(std::max<uint32_t>(max_prims, 1))), "alloc build scratch");
-    CKB(cudaMalloc(&box_lo, sizeof(float4) * std::max<uint32_t>(max_prims, 1)), "alloc build boxes");
-    CKB(cudaMalloc(&box_hi, sizeof(float4) * std::max<uint32_t>(max_prims, 1)), "alloc build boxes");
-    CKB(cudaMalloc(&sorted, sizeof(uint32_t) * std::max<uint32_t>(max_prims, 1)), "alloc build order");
-    CKB(cudaMalloc(&depth, 2 * sizeof(uint32_t)), "alloc depth");
-    {
-        const uint32_t one[2] = {1u, 1u};
-        CKB(cudaMemcpyAsync(depth, one, sizeof(one), cudaMemcpyHostToDevice, st), "init depth");
-    }
     if (d->vertex_count) {
         CKB(cudaMemcpyAsync(dpos, pos.data(), sizeof(float4) * d->vertex_count, cudaMemcpyHostToDevice, st), "upload");
         CKB(cudaMemcpyAsync(S.normals, nrm.data(), sizeof(float4) * d->vertex_count, cudaMemcpyHostToDevice, st), "upload");
@@ -964,11 +945,79 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
                             st),
             "upload");
 
+    // fast-trace mesh trees are built first: their node and triangle-reference
+    // counts (spatial splits reference some triangles more than once) size
+    // the device arrays
+    const bool host_trees = ctx->build_mode == DDGI_BUILD_FAST_TRACE_HOST;
+    const bool gpu_trees = ctx->build_mode == DDGI_BUILD_FAST_TRACE;
+    std::vector<HostTree> trees;
+    if (host_trees) build_host_trees(d, pos, ctx->blas_leaf_max, ctx->split_alpha, trees);
+    GpuTreeBuilder gtb;
+    if (gpu_trees) {
+        std::vector<uint32_t> counts(d->mesh_count);
+        uint64_t soup = 0;
+        for (uint32_t m = 0; m < d->mesh_count; ++m) soup += counts[m] = d->meshes[m].index_count / 3;
+        CKB(cudaMalloc(&dsoup, sizeof(float) * 9 * std::max<uint64_t>(soup, 1)), "alloc build triangles");
+        uint64_t o = 0;
+        for (uint32_t m = 0; m < d->mesh_count; ++m) {
+            const ddgi_mesh& me = d->meshes[m];
+            CKB(gather_triangle_soup(dpos, S.indices, me.vertex_offset, me.index_offset, counts[m], dsoup + 9 * o, st),
+                "gather build triangles");
+            o += counts[m];
+        }
+        CKB(gtb.build_triangles(dsoup, counts, ctx->blas_leaf_max, ctx->split_alpha, ctx->err, st), "mesh tree build");
+        S.gpu_build_ms = gtb.build_ms();
+    }
+    uint64_t total_tris = 0, total_nodes = 0;
+    uint32_t max_tris = 0;
+    for (uint32_t m = 0; m < d->mesh_count; ++m) {
+        uint32_t nt = d->meshes[m].index_count / 3;
+        if (host_trees) {
+            total_tris += trees[m].order.size();
+            total_nodes += trees[m].nodes.size();
+            max_tris = std::max(max_tris, (uint32_t)std::min<size_t>(trees[m].order.size(), 0xFFFFFFFFu));
+            continue;
+        }
+        if (gpu_trees) {
+            total_tris += gtb.ref_counts()[m];
+            total_nodes += gtb.node_counts()[m];
+            max_tris = std::max(max_tris, gtb.ref_counts()[m]);
+            continue;
+        }
+        total_tris += nt;
+        total_nodes += nt > 1 ? nt - 1 : (nt == 1 ? 1 : 0);
+        max_tris = std::max(max_tris, nt);
+    }
+    uint32_t ni = d->instance_count;
+    uint64_t tlas_nodes = ni > 1 ? ni - 1 : (ni == 1 ? 1 : 0);
+    uint32_t max_prims = std::max(max_tris, ni);
+    if (total_tris >= (1ull << 28) - 8 || total_nodes + tlas_nodes >= (1ull << 31)) {
+        cleanup();
+        free_scene(ctx->scene);
+        return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "scene too large (%llu triangles)", (unsigned long long)total_tris);
+    }
+    CKB(cudaMalloc(&S.nodes, sizeof(BvhNode) * std::max<uint64_t>(total_nodes + tlas_nodes, 1)), "alloc nodes");
+    CKB(cudaMalloc(&S.tris, sizeof(BvhTri) * std::max<uint64_t>(total_tris, 1)), "alloc triangles");
+    CKB(cudaMalloc(&S.inst_leaf, sizeof(GpuInstance) * std::max<uint32_t>(ni, 1)), "alloc instances");
+    CKB(cudaMalloc(&S.inst_id, sizeof(GpuInstance) * std::max<uint32_t>(ni, 1)), "alloc instances");
+    CKB(cudaMalloc(&scratch, lbvh_scratch_bytes(std::max<uint32_t>(max_prims, 1))), "alloc build scratch");
+    CKB(cudaMalloc(&box_lo, sizeof(float4) * std::max<uint32_t>(max_prims, 1)), "alloc build boxes");
+    CKB(cudaMalloc(&box_hi, sizeof(float4) * std::max<uint32_t>(max_prims, 1)), "alloc build boxes");
+    CKB(cudaMalloc(&sorted, sizeof(uint32_t) * std::max<uint32_t>(max_prims, 1)), "alloc build order");
+    CKB(cudaMalloc(&depth, 2 * sizeof(uint32_t)), "alloc depth");
+    if (gpu_trees) CKB(cudaMalloc(&gorder, sizeof(uint32_t) * std::max<uint64_t>(total_tris, 1)), "alloc leaf order");
+    {
+        const uint32_t one[2] = {1u, 1u};
+        CKB(cudaMemcpyAsync(depth, one, sizeof(one), cudaMemcpyHostToDevice, st), "init depth");
+    }
+
     // ---- bottom level: one tree per mesh ----
     S.build_mode = ctx->build_mode;
     uint32_t host_blas_depth = 1;
     std::vector<int32_t> mesh_root(d->mesh_count, -1);
     std::vector<float> mesh_lo((size_t)d->mesh_count * 3, INFINITY), mesh_hi((size_t)d->mesh_count * 3, -INFINITY);
+    std::vector<int> gnode_base(d->mesh_count, 0), gprim_base(d->mesh_count, 0);
+    std::vector<uint32_t> gorder_base(d->mesh_count, 0);
     uint64_t node_base = 0, tri_base = 0;
     for (uint32_t m = 0; m < d->mesh_count; ++m) {
         const ddgi_mesh& me = d->meshes[m];
@@ -983,6 +1032,16 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
                     mesh_hi[m * 3 + k] = std::max(mesh_hi[m * 3 + k], pp[k]);
                 }
             }
+        }
+        if (gpu_trees) {
+            gnode_base[m] = (int)node_base;
+            gprim_base[m] = (int)tri_base;
+            gorder_base[m] = (uint32_t)tri_base;
+            host_blas_depth = std::max(host_blas_depth, gtb.depths()[m]);
+            mesh_root[m] = (int32_t)node_base;
+            node_base += gtb.node_counts()[m];
+            tri_base += gtb.ref_counts()[m];
+            continue;
         }
         if (host_trees) {
             HostTree& tr = trees[m];
@@ -1012,6 +1071,17 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
         mesh_root[m] = (int32_t)node_base;
         node_base += nt > 1 ? nt - 1 : 1;
         tri_base += nt;
+    }
+    if (gpu_trees) {
+        CKB(gtb.write(S.nodes, gnode_base, gprim_base, gorder, gorder_base, st), "write mesh trees");
+        for (uint32_t m = 0; m < d->mesh_count; ++m) {
+            const ddgi_mesh& me = d->meshes[m];
+            const uint32_t nt = me.index_count / 3;
+            if (nt == 0) continue;
+            CKB(gather_mesh_tris(dpos, S.indices, me.vertex_offset, me.vertex_count, me.index_offset, nt,
+                                 gtb.ref_counts()[m], gorder + gorder_base[m], S.tris + gprim_base[m], st),
+                "gather triangles");
+        }
     }
 
     // ---- top level over instance world boxes ----
@@ -1519,9 +1589,35 @@ ddgi_status ddgi_set_spatial_splits(ddgi_ctx* ctx, float overlap) {
 
 ddgi_status ddgi_set_build_mode(ddgi_ctx* ctx, ddgi_build_mode mode) {
     if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
-    if (mode != DDGI_BUILD_FAST_TRACE && mode != DDGI_BUILD_FAST_BUILD)
+    if (mode != DDGI_BUILD_FAST_TRACE && mode != DDGI_BUILD_FAST_BUILD && mode != DDGI_BUILD_FAST_TRACE_HOST)
         return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "unknown build mode %d", (int)mode);
     ctx->build_mode = mode;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_get_scene_info(const ddgi_ctx* ctx, ddgi_scene_info* out) {
+    if (!ctx || !out) return DDGI_ERR_INVALID_ARGUMENT;
+    const SceneBuffers& S = ctx->scene;
+    if (!S.built) return DDGI_ERR_NO_SCENE;
+    out->node_count = S.node_count;
+    out->tri_refs = S.tri_count;
+    out->depth_blas = S.depth_blas;
+    out->depth_tlas = S.depth_tlas;
+    out->build_mode = (uint32_t)S.build_mode;
+    out->tree_build_ms = S.build_mode == DDGI_BUILD_FAST_TRACE ? S.gpu_build_ms : 0.0f;
+    return DDGI_OK;
+}
+
+ddgi_status ddgi_read_trees(ddgi_ctx* ctx, void* nodes, uint64_t node_capacity, void* tris, uint64_t tri_capacity,
+                            ddgi_stream stream) {
+    if (!ctx) return DDGI_ERR_INVALID_ARGUMENT;
+    const SceneBuffers& S = ctx->scene;
+    if (!S.built) return fail(ctx, DDGI_ERR_NO_SCENE, "ddgi_read_trees before ddgi_scene_build");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const uint64_t nn = std::min<uint64_t>(node_capacity, S.node_count), nt = std::min<uint64_t>(tri_capacity, S.tri_count);
+    if (nodes && nn) CK(cudaMemcpyAsync(nodes, S.nodes, sizeof(BvhNode) * nn, cudaMemcpyDeviceToHost, st), "read nodes");
+    if (tris && nt) CK(cudaMemcpyAsync(tris, S.tris, sizeof(BvhTri) * nt, cudaMemcpyDeviceToHost, st), "read triangles");
+    CK(cudaStreamSynchronize(st), "read trees");
     return DDGI_OK;
 }
 

@@ -30,11 +30,11 @@ bool sah_build(const float4* lo, const float4* hi, uint32_t n, int leaf_max, int
 bool sbvh_build(const float* tris, uint32_t n, int leaf_max, float alpha, int node_base, int prim_base,
                 std::vector<BvhNode>& nodes, std::vector<uint32_t>& order, uint32_t* depth, unsigned threads);
 
-// The spatial-split builder's clipped reference box: the bounds of the part
-// of triangle `tri` (9 floats) inside the slab [slab_lo, slab_hi], rounded
-// outwards to float and intersected with the slab (lo > hi in some axis when
-// the triangle misses the slab).
-void sbvh_clip_box(const float* tri, const float slab_lo[3], const float slab_hi[3], float out_lo[3],
+// The spatial-split builder's reference split (tri_split.h): the bounds of
+// the part of triangle `tri` (9 floats) between slab_lo[axis] and
+// slab_hi[axis], widened outwards, intersected with the slab in every axis
+// (lo > hi in some axis when the triangle misses it).
+void sbvh_clip_box(const float* tri, int axis, const float slab_lo[3], const float slab_hi[3], float out_lo[3],
                    float out_hi[3]);
 
 }  // namespace ddgi

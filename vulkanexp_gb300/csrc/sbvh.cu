@@ -5,23 +5,24 @@
 // sah.cu: primitives by centroid) or by a spatial split (Stich, Friedrich &
 // Dietrich 2009): a plane through the node's box, with the triangles that
 // straddle it referenced on both sides, each reference bounded by the part
-// of its triangle on that side (the triangle polygon clipped to the side's
-// slab, in double precision).  Spatial splits are evaluated only where the object split's two
-// children overlap by more than `alpha` of the root's surface area, and
-// taken when their SAH cost is lower.  Overlapping geometry (the box
-// clusters of the at-scale workload) then needs far fewer node visits per
-// ray, at the price of triangle references in several leaves; meshes whose
-// triangles do not overlap (a height field) are built as by sah.cu.
+// of its triangle on that side (tri_split.h: the triangle between the
+// plane and the reference's own bounds along the split axis, in float
+// interval arithmetic, intersected with the reference's box).  Spatial
+// splits are evaluated only where the object split's two children overlap
+// by more than `alpha` of the root's surface area, and taken when their SAH
+// cost is lower.  Overlapping geometry (the box clusters of the at-scale
+// workload) then needs far fewer node visits per ray, at the price of
+// triangle references in several leaves; meshes whose triangles do not
+// overlap (a height field) are built as by sah.cu.
 //
 // A ray hit at a point p of a triangle is still found: p lies in the part of
 // the triangle on one side of every split plane, so some reference's box
-// contains it.  Clipped boxes are computed in double, rounded outwards to
-// float and intersected with the exact slab planes; their error (ulps of
-// double) is far below the enlargement every node box receives (1e-6 of the
-// coordinates' magnitude and more), so box tests stay conservative and the
-// hit set equals that of any other tree.  The same triangle may be tested
-// twice along a ray; the tie rule (t, instance, primitive) makes that
-// harmless.
+// contains it.  Reference boxes contain the exact parts (every operation of
+// the split widened outwards), so box tests stay conservative and the hit
+// set equals that of any other tree.  The same triangle may be tested twice
+// along a ray; the tie rule (t, instance, primitive) makes that harmless.
+// The GPU builder (gbuild.cu) runs this algorithm with the same operations
+// and builds the same trees.
 #include <stdint.h>
 
 #include <algorithm>
@@ -33,66 +34,13 @@
 
 #include "sah.h"
 #include "traverse.cuh"
+#include "tri_split.h"
 
 namespace ddgi {
 
-// Bounding box of the part of a triangle inside a slab (lo > hi in some axis
-// when none is), intersected with the slab.  The polygon is clipped in
-// double precision and its box rounded outwards to float: for a triangle
-// nearly parallel to a clipping plane the crossing point's other coordinates
-// follow from a ratio of two nearly equal coordinate differences, and in
-// float their error grew to 1e-3 of the edge length (a face of a box yawed by
-// ~1e-4 rad, 4e-5 m thick in x, clipped by an x plane), far beyond the
-// enlargement of the node boxes: a ray hitting that face between two of its
-// clipped boxes was missed.
-void sbvh_clip_box(const float* tri, const float slab_lo[3], const float slab_hi[3], float out_lo[3],
+void sbvh_clip_box(const float* tri, int axis, const float slab_lo[3], const float slab_hi[3], float out_lo[3],
                    float out_hi[3]) {
-    double a[10][3], b[10][3];
-    int n = 3;
-    for (int v = 0; v < 3; ++v)
-        for (int k = 0; k < 3; ++k) a[v][k] = (double)tri[3 * v + k];
-    double(*in)[3] = a;
-    double(*out)[3] = b;
-    for (int k = 0; k < 3 && n > 0; ++k) {
-        for (int side = 0; side < 2 && n > 0; ++side) {
-            const double pl = (double)(side ? slab_hi[k] : slab_lo[k]);
-            int m = 0;
-            for (int i = 0; i < n; ++i) {
-                const double* p = in[i];
-                const double* q = in[(i + 1) % n];
-                const bool pin = side ? p[k] <= pl : p[k] >= pl;
-                const bool qin = side ? q[k] <= pl : q[k] >= pl;
-                if (pin && m < 10) {
-                    out[m][0] = p[0], out[m][1] = p[1], out[m][2] = p[2];
-                    ++m;
-                }
-                if (pin != qin && m < 10) {
-                    const double s = (pl - p[k]) / (q[k] - p[k]);
-                    for (int j = 0; j < 3; ++j) out[m][j] = p[j] + (q[j] - p[j]) * s;
-                    out[m][k] = pl;
-                    ++m;
-                }
-            }
-            n = m;
-            std::swap(in, out);
-        }
-    }
-    for (int k = 0; k < 3; ++k) {
-        out_lo[k] = INFINITY;
-        out_hi[k] = -INFINITY;
-    }
-    for (int i = 0; i < n; ++i)
-        for (int k = 0; k < 3; ++k) {
-            float lo = (float)in[i][k], hi = lo;
-            if ((double)lo > in[i][k]) lo = std::nextafter(lo, -INFINITY);
-            if ((double)hi < in[i][k]) hi = std::nextafter(hi, INFINITY);
-            out_lo[k] = fminf(out_lo[k], lo);
-            out_hi[k] = fmaxf(out_hi[k], hi);
-        }
-    for (int k = 0; k < 3; ++k) {
-        out_lo[k] = fmaxf(out_lo[k], slab_lo[k]);
-        out_hi[k] = fminf(out_hi[k], slab_hi[k]);
-    }
+    tri_split_box(tri, axis, slab_lo, slab_hi, out_lo, out_hi);
 }
 
 namespace {
@@ -181,9 +129,9 @@ class Sbvh {
     const float alpha_;
     float root_area_ = 0.0f;
 
-    Box clip(uint32_t prim, const Box& slab) const {
+    Box clip(uint32_t prim, const Box& slab, int axis) const {
         Box r;
-        sbvh_clip_box(tris_ + 9 * (size_t)prim, slab.lo, slab.hi, r.lo, r.hi);
+        tri_split_box(tris_ + 9 * (size_t)prim, axis, slab.lo, slab.hi, r.lo, r.hi);
         return r;
     }
 
@@ -278,7 +226,7 @@ class Sbvh {
                         Box slab = r.box;
                         slab.lo[k] = fmaxf(slab.lo[k], plane[j]);
                         slab.hi[k] = fminf(slab.hi[k], plane[j + 1]);
-                        const Box c = clip(r.prim, slab);
+                        const Box c = clip(r.prim, slab, k);
                         if (!c.empty()) bins[j].grow(c);
                     }
                 }
@@ -318,7 +266,7 @@ class Sbvh {
                     Box lb = r.box, rb = r.box;
                     lb.hi[sax] = splane;
                     rb.lo[sax] = splane;
-                    const Box a = clip(r.prim, lb), b = clip(r.prim, rb);
+                    const Box a = clip(r.prim, lb, sax), b = clip(r.prim, rb, sax);
                     if (!a.empty()) L.push_back(Ref{a, r.prim});
                     if (!b.empty()) R.push_back(Ref{b, r.prim});
                     if (a.empty() && b.empty()) L.push_back(r);  // cannot happen for a real triangle

@@ -16,7 +16,7 @@ import os
 import numpy as np
 
 from . import abi
-from .abi import HIT_DTYPE, BatchTuning, GBuffer, GridDesc, Light, SceneDesc, Timings, TraceTuning
+from .abi import HIT_DTYPE, BatchTuning, GBuffer, GridDesc, Light, SceneDesc, SceneInfo, Timings, TraceTuning
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libddgi_gb300.so")
@@ -76,6 +76,8 @@ _SIGNATURES = [
     ("ddgi_get_hysteresis", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ddgi_set_leaf_size", C.c_int, [C.c_void_p, C.c_uint32]),
     ("ddgi_set_build_mode", C.c_int, [C.c_void_p, C.c_int]),
+    ("ddgi_get_scene_info", C.c_int, [C.c_void_p, C.POINTER(SceneInfo)]),
+    ("ddgi_read_trees", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_void_p]),
     ("ddgi_get_atlas_raw", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]),
     ("ddgi_set_spatial_splits", C.c_int, [C.c_void_p, C.c_float]),
     ("ddgi_inject_fault", C.c_int, [C.c_void_p, C.c_uint32]),
@@ -259,9 +261,10 @@ class Context:
         self._check(self.lib.ddgi_set_leaf_size(self.h, int(max_triangles)))
 
     def set_build_mode(self, mode):
-        """Tree builder for the next build_scene: "fast_trace" (host SAH
-        trees) or "fast_build" (GPU linear BVHs)."""
-        modes = {"fast_trace": 0, "fast_build": 1}
+        """Tree builder for the next build_scene: "fast_trace" (SAH trees
+        with spatial splits built on the GPU), "fast_build" (GPU linear BVHs)
+        or "fast_trace_host" (the fast-trace trees built on the host)."""
+        modes = {"fast_trace": 0, "fast_build": 1, "fast_trace_host": 2}
         if mode not in modes:
             raise ValueError("build mode %r: want one of %s" % (mode, sorted(modes)))
         self._check(self.lib.ddgi_set_build_mode(self.h, modes[mode]))
@@ -314,6 +317,24 @@ class Context:
 
     def set_schedule(self, offset, loop, stream=None):
         self._check(self.lib.ddgi_set_schedule(self.h, int(offset), int(loop), _stream_ptr(stream)))
+
+    def scene_info(self):
+        """Tree sizes, depths, builder and GPU build time of the built scene."""
+        info = SceneInfo()
+        self._check(self.lib.ddgi_get_scene_info(self.h, C.byref(info)))
+        return {"nodes": int(info.node_count), "tri_refs": int(info.tri_refs), "depth_blas": int(info.depth_blas),
+                "depth_tlas": int(info.depth_tlas), "build_mode": int(info.build_mode),
+                "tree_build_ms": float(info.tree_build_ms)}
+
+    def read_trees(self, stream=None):
+        """The built trees: nodes (N x 16 words of 32 bits) and triangles in
+        leaf order (M x 12 words), as uint32 arrays."""
+        info = self.scene_info()
+        nodes = np.zeros((info["nodes"], 16), np.uint32)
+        tris = np.zeros((info["tri_refs"], 12), np.uint32)
+        self._check(self.lib.ddgi_read_trees(self.h, _ptr(nodes), nodes.shape[0], _ptr(tris), tris.shape[0],
+                                             _stream_ptr(stream)))
+        return nodes, tris
 
     def count_fetches(self, orientation, probe_list=None, stream=None):
         """Fetch counters of one trace + shade pass (see ddgi_count_fetches)."""
