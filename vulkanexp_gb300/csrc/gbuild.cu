@@ -18,9 +18,9 @@
 //                  and whether its children overlap enough for spatial
 //                  splits (Stich, Friedrich & Dietrich 2009);
 //   k_bin_spatial  for those nodes: references binned by their extent,
-//                  chopped at the bin planes (the reference split of
-//                  tri_split.h per bin); the last block keeps a spatial
-//                  plane only if its cost is lower;
+//                  chopped at the bin planes (the reference splits of
+//                  tri_split.h, one plane per thread); the last block
+//                  keeps a spatial plane only if its cost is lower;
 //   k_count        each chunk counts the references going left and right
 //                  (both the spatial and the object partition); the node's
 //                  last block scans the chunks, falls back from a spatial
@@ -175,13 +175,14 @@ __device__ __forceinline__ DBox key_box(const uint32_t* k) {
     return b;
 }
 
-// The reference split of tri_split.h (the host builder's operations).
-__device__ __forceinline__ DBox clip_tri(const float* __restrict__ tri, const DBox& slab, int axis) {
-    float t[9];
+__device__ __forceinline__ void load_tri(const float* __restrict__ tri, float t[9]) {
     for (int i = 0; i < 9; ++i) t[i] = __ldg(tri + i);
-    DBox r;
-    tri_split_box(t, axis, slab.lo, slab.hi, r.lo, r.hi);
-    return r;
+}
+__device__ __forceinline__ void box_clip(DBox& b, const DBox& o) {
+    for (int k = 0; k < 3; ++k) {
+        b.lo[k] = fmaxf(b.lo[k], o.lo[k]);
+        b.hi[k] = fminf(b.hi[k], o.hi[k]);
+    }
 }
 
 // The host writers' box enlargement, each operation rounded separately.
@@ -489,9 +490,20 @@ __device__ __forceinline__ float plane_at(float lo, float hi, float w, int j) {
     return j == kBins ? hi : __fadd_rn(lo, __fmul_rn((float)j, w));
 }
 
+__device__ __forceinline__ void grow_bin(uint32_t* q, const DBox& b) {
+    for (int a = 0; a < 3; ++a) {
+        atomicMin(q + a, fkey(b.lo[a]));
+        atomicMax(q + 3 + a, fkey(b.hi[a]));
+    }
+}
+
 __global__ void __launch_bounds__(kThreads) k_bin_spatial(Pass P) {
     __shared__ uint32_t s_bin[3 * kBins * kSpWords];
     __shared__ float s_lo[3], s_hi[3], s_w[3], s_scale[3];
+    __shared__ uint32_t s_cnt[3 * kThreads], s_off[3 * kThreads], s_total;
+    __shared__ uint8_t s_b0[3 * kThreads];
+    __shared__ float s_above[kThreads][6];
+    __shared__ float s_carry[6];
     __shared__ int s_last;
     const uint32_t c = blockIdx.x;
     BNode& N = P.nodes[P.chunk_node[c]];
@@ -510,29 +522,111 @@ __global__ void __launch_bounds__(kThreads) k_bin_spatial(Pass P) {
     __syncthreads();
     uint32_t p0, p1;
     chunk_range(N, c, p0, p1);
-    for (uint32_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-        const Ref r = P.in[p];
-        const DBox rb = ref_box(r);
-        const float* tri = P.tris + 9 * (size_t)ref_prim(r);
-        for (int k = 0; k < 3; ++k) {
-            if (s_scale[k] == 0.0f) continue;
-            const int b0 = bin_of(rb.lo[k], s_lo[k], s_scale[k]);
-            const int b1 = max(b0, bin_of(rb.hi[k], s_lo[k], s_scale[k]));
-            atomicAdd(s_bin + kSpWords * (k * kBins + b0), 1u);
-            atomicAdd(s_bin + kSpWords * (k * kBins + b1) + 1, 1u);
-            for (int j = b0; j <= b1; ++j) {
-                DBox part = rb;
-                if (b0 != b1) {
-                    DBox slab = rb;
-                    slab.lo[k] = fmaxf(slab.lo[k], plane_at(s_lo[k], s_hi[k], s_w[k], j));
-                    slab.hi[k] = fminf(slab.hi[k], plane_at(s_lo[k], s_hi[k], s_w[k], j + 1));
-                    part = clip_tri(tri, slab, k);
-                    if (box_empty(part)) continue;
+    // Rounds of kThreads references.  A reference spanning bins b0 < b1
+    // along axis k has the m = b1 - b0 inner bin planes p_(b0+1) .. p_(b1);
+    // the (reference, axis, plane) triples of a round are numbered
+    // axis-major and dealt out one per thread, each thread computing the
+    // triangle's bounds below and above its plane (tri_split.h).  Bin
+    // b0 + i then gets the reference's box cut to "below plane i" and
+    // "above plane i - 1" (the previous triple, the neighbouring thread or
+    // the previous sub-round's last one), bin b1 the box cut to "above plane
+    // m - 1": sbvh.cu's binning, dealt out evenly.
+    for (uint32_t r0 = p0; r0 < p1; r0 += kThreads) {
+        const uint32_t nr = min((uint32_t)kThreads, p1 - r0);
+        __syncthreads();  // the previous round's tables are read
+        {
+            const uint32_t t = threadIdx.x;
+            for (int k = 0; k < 3; ++k) {
+                uint32_t m = 0;
+                int b0 = 0;
+                if (t < nr && s_scale[k] != 0.0f) {
+                    const DBox rb = ref_box(P.in[r0 + t]);
+                    b0 = bin_of(rb.lo[k], s_lo[k], s_scale[k]);
+                    const int b1 = max(b0, bin_of(rb.hi[k], s_lo[k], s_scale[k]));
+                    uint32_t* sb = s_bin + kSpWords * kBins * k;
+                    atomicAdd(sb + kSpWords * b0, 1u);
+                    atomicAdd(sb + kSpWords * b1 + 1, 1u);
+                    if (b0 == b1) grow_bin(sb + kSpWords * b0 + 2, rb);
+                    m = (uint32_t)(b1 - b0);
                 }
-                uint32_t* q = s_bin + kSpWords * (k * kBins + j) + 2;
+                s_cnt[k * kThreads + t] = m;
+                s_b0[k * kThreads + t] = (uint8_t)b0;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {  // exclusive scan of the 3 x kThreads plane counts
+            uint32_t run = 0;
+            for (int base = 0; base < 3 * kThreads; base += 32) {
+                const uint32_t v = s_cnt[base + threadIdx.x];
+                uint32_t x = v;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                    if ((int)threadIdx.x >= o) x += y;
+                }
+                s_off[base + threadIdx.x] = run + x - v;
+                run += __shfl_sync(0xFFFFFFFFu, x, 31);
+            }
+            if (threadIdx.x == 0) s_total = run;
+        }
+        __syncthreads();
+        const uint32_t total = s_total;
+        for (uint32_t g0 = 0; g0 < total; g0 += kThreads) {
+            const uint32_t g = g0 + threadIdx.x;
+            DBox below, above, rb;
+            int bin = -1, k = 0;
+            bool last = false;
+            uint32_t i = 0;
+            if (g < total) {
+                // the triple holding plane g: the last entry with s_off <= g
+                int lo = 0, hi = 3 * kThreads - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (s_off[mid] <= g) lo = mid;
+                    else hi = mid - 1;
+                }
+                // (an entry without planes shares its offset with the next
+                // one, so the last entry at or below g has planes)
+                k = lo / kThreads;
+                const uint32_t t = (uint32_t)(lo % kThreads);
+                i = g - s_off[lo];
+                last = i + 1 == s_cnt[lo];
+                const int b0 = s_b0[lo];
+                bin = b0 + (int)i;
+                const Ref r = P.in[r0 + t];
+                rb = ref_box(r);
+                float tri[9];
+                load_tri(P.tris + 9 * (size_t)ref_prim(r), tri);
+                const float pl = plane_at(s_lo[k], s_hi[k], s_w[k], bin + 1);
+                if (k == 0) tri_plane_bounds_k<0>(tri, pl, below.lo, below.hi, above.lo, above.hi);
+                else if (k == 1) tri_plane_bounds_k<1>(tri, pl, below.lo, below.hi, above.lo, above.hi);
+                else tri_plane_bounds_k<2>(tri, pl, below.lo, below.hi, above.lo, above.hi);
                 for (int a = 0; a < 3; ++a) {
-                    atomicMin(q + a, fkey(part.lo[a]));
-                    atomicMax(q + 3 + a, fkey(part.hi[a]));
+                    s_above[threadIdx.x][a] = above.lo[a];
+                    s_above[threadIdx.x][3 + a] = above.hi[a];
+                }
+            }
+            __syncthreads();
+            DBox prev;
+            if (g < total && i > 0) {
+                const float* q = threadIdx.x > 0 ? s_above[threadIdx.x - 1] : s_carry;
+                for (int a = 0; a < 3; ++a) {
+                    prev.lo[a] = q[a];
+                    prev.hi[a] = q[3 + a];
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == kThreads - 1)
+                for (int a = 0; a < 6; ++a) s_carry[a] = s_above[kThreads - 1][a];
+            if (g < total) {
+                uint32_t* sb = s_bin + kSpWords * kBins * k;
+                DBox part = rb;
+                if (i > 0) box_clip(part, prev);
+                box_clip(part, below);
+                if (!box_empty(part)) grow_bin(sb + kSpWords * bin + 2, part);
+                if (last) {
+                    DBox tail = rb;
+                    box_clip(tail, above);
+                    if (!box_empty(tail)) grow_bin(sb + kSpWords * (bin + 1) + 2, tail);
                 }
             }
         }
@@ -600,12 +694,12 @@ __device__ __forceinline__ void spatial_side(const Ref& r, const float* tris, in
     } else if (b.lo[ax] >= pl) {
         to_l = false, to_r = true;
     } else {
-        const float* tri = tris + 9 * (size_t)ref_prim(r);
-        DBox sl = b, sr = b;
-        sl.hi[ax] = pl;
-        sr.lo[ax] = pl;
-        bl = clip_tri(tri, sl, ax);
-        br = clip_tri(tri, sr, ax);
+        float t[9];
+        load_tri(tris + 9 * (size_t)ref_prim(r), t);
+        DBox below, above;
+        tri_plane_bounds(t, ax, pl, below.lo, below.hi, above.lo, above.hi);
+        box_clip(bl, below);
+        box_clip(br, above);
         to_l = !box_empty(bl);
         to_r = !box_empty(br);
         if (!to_l && !to_r) {
@@ -1374,7 +1468,8 @@ cudaError_t GpuTreeBuilder::run(bool triangles, const float* tris, const float4*
     size_t total = 0;
     for (uint32_t n : counts) total += n;
     // spatial splits reference some triangles more than once
-    size_t cap = triangles && alpha > 0.0f ? 2 * total + 4096 : total + 4096;
+    // (the 1M-triangle terrain ends with 3.2 references per triangle)
+    size_t cap = triangles && alpha > 0.0f ? 4 * total + 4096 : total + 4096;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

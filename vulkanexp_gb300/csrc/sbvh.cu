@@ -129,10 +129,10 @@ class Sbvh {
     const float alpha_;
     float root_area_ = 0.0f;
 
-    Box clip(uint32_t prim, const Box& slab, int axis) const {
-        Box r;
-        tri_split_box(tris_ + 9 * (size_t)prim, axis, slab.lo, slab.hi, r.lo, r.hi);
-        return r;
+    // Bounds of the triangle's parts below and above the plane x_axis = pl
+    // (tri_split.h).
+    void plane_split(uint32_t prim, int axis, float pl, Box& below, Box& above) const {
+        tri_plane_bounds(tris_ + 9 * (size_t)prim, axis, pl, below.lo, below.hi, above.lo, above.hi);
     }
 
     static int bin_of(float x, float lo, float scale) {
@@ -222,12 +222,18 @@ class Sbvh {
                         bins[b0].grow(r.box);
                         continue;
                     }
+                    // bin j: the reference's box, cut to the triangle's part
+                    // above bin j's lower plane and below its upper plane
+                    Box above;
                     for (int j = b0; j <= b1; ++j) {
-                        Box slab = r.box;
-                        slab.lo[k] = fmaxf(slab.lo[k], plane[j]);
-                        slab.hi[k] = fminf(slab.hi[k], plane[j + 1]);
-                        const Box c = clip(r.prim, slab, k);
-                        if (!c.empty()) bins[j].grow(c);
+                        Box part = r.box;
+                        if (j > b0) part = intersect(part, above);
+                        if (j < b1) {
+                            Box below;
+                            plane_split(r.prim, k, plane[j + 1], below, above);
+                            part = intersect(part, below);
+                        }
+                        if (!part.empty()) bins[j].grow(part);
                     }
                 }
                 float rcost[kBins];
@@ -263,10 +269,9 @@ class Sbvh {
                 } else if (r.box.lo[sax] >= splane) {
                     R.push_back(r);
                 } else {
-                    Box lb = r.box, rb = r.box;
-                    lb.hi[sax] = splane;
-                    rb.lo[sax] = splane;
-                    const Box a = clip(r.prim, lb, sax), b = clip(r.prim, rb, sax);
+                    Box below, above;
+                    plane_split(r.prim, sax, splane, below, above);
+                    const Box a = intersect(r.box, below), b = intersect(r.box, above);
                     if (!a.empty()) L.push_back(Ref{a, r.prim});
                     if (!b.empty()) R.push_back(Ref{b, r.prim});
                     if (a.empty() && b.empty()) L.push_back(r);  // cannot happen for a real triangle
