@@ -473,6 +473,9 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
         for (uint32_t u = 0; u < v; ++u)
             if (volumes[u] == c) return bail(DDGI_ERR_INVALID_ARGUMENT);  // listed twice
         if (!c->scene.built) return bail(DDGI_ERR_NO_SCENE);
+        // the arena carries the wide trees for node_width 8 tunings
+        const ddgi_status ws = ensure_wide(volumes[v]);
+        if (ws != DDGI_OK) return bail(ws);
     }
     // internal order: increasing ray count (stable)
     b->order.resize(count);

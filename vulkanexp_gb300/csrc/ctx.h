@@ -66,6 +66,8 @@ struct SceneBuffers {
     int32_t wtlas_root = -1;
     int wstack_cap = 0;  // 0: no wide trees (too deep for the stack)
     std::vector<int32_t> wide_root_of_mesh;
+    std::vector<int32_t> mesh_root;  // root node of each mesh tree (-1: empty mesh)
+    bool wide_ready = false;         // the wide copies exist (made on first use)
 };
 
 }  // namespace ddgi
@@ -224,5 +226,9 @@ inline DeviceScene device_scene(const ddgi_ctx* c) {
     set_step_limits(s);
     return s;
 }
+
+// The eight-wide copies of the built scene's trees (ddgi_api.cu), made on
+// first use: by a node_width 8 tuning, an autotune or a batch.
+ddgi_status ensure_wide(ddgi_ctx* ctx);
 
 }  // namespace ddgi

@@ -772,30 +772,39 @@ void rebase_tree(std::vector<BvhNode>& nodes, int node_base, int prim_base) {
     }
 }
 
-// Depth-first layout of every mesh tree, then four-wide copies of every mesh
-// tree and of the top level.
-ddgi_status build_wide(ddgi_ctx* ctx, const std::vector<int32_t>& mesh_root, cudaStream_t st) {
+// Depth-first layout of every mesh tree of a linear BVH build (the
+// fast-trace builders write theirs depth first already).
+ddgi_status layout_depth_first(ddgi_ctx* ctx, const std::vector<int32_t>& mesh_root, cudaStream_t st) {
     SceneBuffers& S = ctx->scene;
+    const uint32_t blas_end = S.tlas_root >= 0 ? (uint32_t)S.tlas_root : (uint32_t)S.node_count;
+    if (blas_end == 0) return DDGI_OK;
+    std::vector<BvhNode> bin(blas_end);
+    CK(cudaMemcpyAsync(bin.data(), S.nodes, sizeof(BvhNode) * blas_end, cudaMemcpyDeviceToHost, st), "read trees");
+    CK(cudaStreamSynchronize(st), "read trees");
+    // mesh trees occupy consecutive ranges in mesh order, the top level follows
+    std::vector<uint32_t> roots;
+    for (int32_t r : mesh_root)
+        if (r >= 0) roots.push_back((uint32_t)r);
+    for (size_t i = 0; i < roots.size(); ++i) {
+        const uint32_t e = i + 1 < roots.size() ? roots[i + 1] : blas_end;
+        if (roots[i] < e && e <= blas_end) depth_first_layout(bin, roots[i], e);
+    }
+    CK(cudaMemcpyAsync(S.nodes, bin.data(), sizeof(BvhNode) * blas_end, cudaMemcpyHostToDevice, st),
+       "upload mesh trees");
+    CK(cudaStreamSynchronize(st), "upload mesh trees");  // `bin` is pageable and local
+    return DDGI_OK;
+}
+
+// Eight-wide copies of every mesh tree and of the top level (node_width 8).
+ddgi_status build_wide(ddgi_ctx* ctx, cudaStream_t st) {
+    SceneBuffers& S = ctx->scene;
+    const std::vector<int32_t>& mesh_root = S.mesh_root;
     S.wstack_cap = 0;
     if (S.node_count == 0) return DDGI_OK;
     std::vector<BvhNode> bin(S.node_count);
     CK(cudaMemcpyAsync(bin.data(), S.nodes, sizeof(BvhNode) * S.node_count, cudaMemcpyDeviceToHost, st),
        "read trees");
     CK(cudaStreamSynchronize(st), "read trees");
-    {
-        // mesh trees occupy consecutive ranges in mesh order, the top level follows
-        std::vector<uint32_t> roots;
-        for (int32_t r : mesh_root)
-            if (r >= 0) roots.push_back((uint32_t)r);
-        const uint32_t blas_end = S.tlas_root >= 0 ? (uint32_t)S.tlas_root : (uint32_t)S.node_count;
-        for (size_t i = 0; i < roots.size(); ++i) {
-            const uint32_t e = i + 1 < roots.size() ? roots[i + 1] : blas_end;
-            if (roots[i] < e && e <= S.node_count) depth_first_layout(bin, roots[i], e);
-        }
-        if (blas_end > 0)
-            CK(cudaMemcpyAsync(S.nodes, bin.data(), sizeof(BvhNode) * blas_end, cudaMemcpyHostToDevice, st),
-               "upload mesh trees");
-    }
     std::vector<WideNode> w;
     bool ok = true;
     uint32_t lb = 0;
@@ -825,6 +834,28 @@ ddgi_status build_wide(ddgi_ctx* ctx, const std::vector<int32_t>& mesh_root, cud
 }
 
 }  // namespace
+
+}  // extern "C"
+
+namespace ddgi {
+// The eight-wide trees of the built scene, made on first use (they are
+// collapsed from the binary trees on the host).
+ddgi_status ensure_wide(ddgi_ctx* ctx) {
+    SceneBuffers& S = ctx->scene;
+    if (!S.built || S.wide_ready) return DDGI_OK;
+    // every stream's work on the trees (an instance refit) is done
+    CK(cudaDeviceSynchronize(), "synchronise before the wide trees");
+    ddgi_status s = build_wide(ctx, nullptr);
+    if (s == DDGI_OK) {
+        cudaError_t e = cudaStreamSynchronize(nullptr);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "wide trees");
+        S.wide_ready = true;
+    }
+    return s;
+}
+}  // namespace ddgi
+
+extern "C" {
 
 ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_stream stream) {
     ddgi::NvtxRange nvtx_range("ddgi_scene_build");
@@ -1135,17 +1166,27 @@ ddgi_status ddgi_scene_build(ddgi_ctx* ctx, const ddgi_scene_desc* d, ddgi_strea
     S.instance_count = ni;
     S.node_count = total_nodes + tlas_nodes;
     S.tri_count = total_tris;
-    {
-        ddgi_status ws = build_wide(ctx, mesh_root, st);
+    S.mesh_root = mesh_root;
+    if (S.build_mode == DDGI_BUILD_FAST_BUILD) {
+        ddgi_status ls = layout_depth_first(ctx, mesh_root, st);
+        if (ls != DDGI_OK) {
+            free_scene(ctx->scene);
+            return ls;
+        }
+    }
+    S.build_id = next_build_id();
+    S.built = true;
+    if (ctx->tune.node_width == 8) {  // the wide copies are made when first asked for
+        ddgi_status ws = ensure_wide(ctx);
         if (ws != DDGI_OK) {
             free_scene(ctx->scene);
             return ws;
         }
     }
-    S.build_id = next_build_id();
-    S.built = true;
     return check_device_error(ctx);
 }
+
+
 
 // ---------------------------------------------------------------------------
 // Moving instances (Renderer::updateAccelerationStructureInstances +
@@ -1560,7 +1601,7 @@ ddgi_status ddgi_set_trace_tuning(ddgi_ctx* ctx, const ddgi_trace_tuning* t) {
     if (t->straggler_lanes > 31)
         return fail(ctx, DDGI_ERR_INVALID_ARGUMENT, "straggler_lanes = %u outside [0, 31]", t->straggler_lanes);
     ctx->tune = *t;
-    return DDGI_OK;
+    return t->node_width == 8 ? ensure_wide(ctx) : DDGI_OK;
 }
 
 ddgi_status ddgi_set_leaf_size(ddgi_ctx* ctx, uint32_t max_triangles) {
@@ -1631,6 +1672,10 @@ ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t re
                           ddgi_trace_tuning* chosen) {
     if (!ctx || !orientation) return DDGI_ERR_INVALID_ARGUMENT;
     if (!ctx->scene.built) return fail(ctx, DDGI_ERR_NO_SCENE, "ddgi_autotune before ddgi_scene_build");
+    {
+        ddgi_status ws = ensure_wide(ctx);  // node_width 8 is one of the candidates
+        if (ws != DDGI_OK) return ws;
+    }
     if (reps == 0) reps = 3;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     // save what the trial updates overwrite
