@@ -16,14 +16,16 @@
 //     volume table with the current lights) are written into one pinned host
 //     buffer and copied by one memcpy at the head of the update.
 //   * volumes are kept in increasing order of their ray counts and split
-//     into up to kGroups groups of equal volume count; each group runs its
-//     own pipeline (primary traversal, shading, shadow traversal, FP32 and
-//     BF16 blends) on its own graph branch, so the small volumes' groups,
-//     launched first, finish long before the large ones instead of every
-//     volume waiting for the whole batch's traversal; the branches overlap
-//     where one group's tail leaves SMs idle.  The captured sequence (clear +
-//     clock, tensor-core weights of every volume, the group branches) is
-//     replayed from a CUDA graph.  Results do not depend on the grouping.
+//     into up to kGroups groups of equal volume count; the groups' pipelines
+//     (primary traversal, shading, shadow traversal, FP32 and BF16 blends)
+//     run one after another, smallest first, so a group's volumes are done
+//     when its own pipeline ends instead of every volume waiting for the
+//     whole batch's traversal.  (Groups on concurrent graph branches do not
+//     give that: each group's persistent traversal holds the SMs it gets,
+//     and the first group's shading and blends queue behind the others'
+//     traversals.)  The captured sequence (clear + clock, tensor-core
+//     weights of every volume, the groups) is replayed from a CUDA graph.
+//     Results do not depend on the grouping.
 //   * an autotuner times candidate launch parameters on real updates.
 #include <cuda_runtime.h>
 
@@ -96,8 +98,6 @@ struct ddgi_batch {
     };
     std::vector<Group> groups;
     uint32_t* d_glists = nullptr;
-    std::vector<cudaStream_t> gstreams;
-    std::vector<cudaEvent_t> gjoin;
     uint32_t max_rays_fp32 = 0, max_rows_tc = 0, max_ntex_fp32 = 0;
     size_t tc_smem = 0;
     // per-update staging: [dirs | ray orders | volume table], host pinned + device
@@ -339,12 +339,10 @@ cudaError_t enqueue(ddgi_batch* b, cudaStream_t st, bool timed) {
     tt.rays_per_warp = b->tuning.rays_per_warp;  // applied per volume through the volume table
     tt.wide = b->tuning.node_width == 8 ? 1u : 0u;
     tt.wait = b->tuning.straggler_lanes;
-    if (!timed && b->groups.size() > 1) {  // one branch per volume group, smallest first
-        e = cudaEventRecord(b->fork_ev, st);
+    if (!timed && b->groups.size() > 1) {  // the volume groups one after another, smallest first
         for (size_t gi = 0; gi < b->groups.size() && e == cudaSuccess; ++gi) {
             const ddgi_batch::Group& G = b->groups[gi];
-            cudaStream_t gs = b->gstreams[gi];
-            e = cudaStreamWaitEvent(gs, b->fork_ev, 0);
+            cudaStream_t gs = st;
             BatchTables gbt = bt;
             gbt.first = G.first;
             WaveHits gwh{b->thit, b->prim, b->front + G.first};
@@ -359,8 +357,6 @@ cudaError_t enqueue(ddgi_batch* b, cudaStream_t st, bool timed) {
                         : launch_batch_blend_fp32(gbt, G.fp32_bl, b->max_rays_fp32, b->rays, b->tuning.blend_threads,
                                                   gs);
             if (e == cudaSuccess && G.tc_bl.ntiles > 0) e = launch_batch_blend_tc(gbt, G.tc_bl, b->rays, b->tc_smem, gs);
-            if (e == cudaSuccess) e = cudaEventRecord(b->gjoin[gi], gs);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(st, b->gjoin[gi], 0);
         }
         return e;
     }
@@ -649,12 +645,6 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
             G.fp32_bl = BatchBlendList{b->d_glists + o.fl, b->d_glists + o.fb, o.nf, o.fbt};
             G.tc_bl = BatchBlendList{b->d_glists + o.tl, b->d_glists + o.tb, o.nt, o.tbt};
             G.fp32s_bl = BatchBlendList{b->d_glists + o.fl, b->d_glists + o.sb, o.nf, o.sbt};
-            cudaStream_t gs = nullptr;
-            cudaEvent_t ge = nullptr;
-            if (cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking) != cudaSuccess) return bail(DDGI_ERR_CUDA);
-            b->gstreams.push_back(gs);
-            if (cudaEventCreateWithFlags(&ge, cudaEventDisableTiming) != cudaSuccess) return bail(DDGI_ERR_CUDA);
-            b->gjoin.push_back(ge);
         }
     }
 
@@ -721,8 +711,6 @@ ddgi_status ddgi_batch_destroy(ddgi_batch* b) {
     bfree(b->d_err);
     bfree(b->d_lists);
     bfree(b->d_glists);
-    for (cudaStream_t gs : b->gstreams) cudaStreamDestroy(gs);
-    for (cudaEvent_t ge : b->gjoin) cudaEventDestroy(ge);
     bfree(b->d_stage);
     if (b->h_stage) cudaFreeHost(b->h_stage);
     if (b->cap) cudaStreamDestroy(b->cap);
