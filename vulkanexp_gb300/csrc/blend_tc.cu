@@ -11,9 +11,10 @@
 // normalised by the row sums sum_r W[t][r] (the reference's result.w, the
 // same for every probe, so it is computed once per update).
 //
-// Tiling: a CTA takes 25 probes; each probe owns 5 rows of the A operand
+// Tiling: a CTA takes up to 25 probes (the launch picks the tile size that
+// fills the SMs' CTA slots best); each probe owns 5 rows of the A operand
 // (its ray records' r, g, b, clamped depth d and d^2), so A is M = 128 rows
-// (3 zero) x K rays, K-major, and the weights are B: the depth rows then the
+// (the rest zero) x K rays, K-major, and the weights are B: the depth rows then the
 // colour rows (each texel count padded to 16), N = Nd + Nc <= 256 in one
 // accumulator at tensor-memory column 0 (wider tiles: depth at 0, colour at
 // 256, in two MMAs).  Only the row x column pairs of matching kind are read
@@ -45,7 +46,7 @@ namespace ddgi {
 
 namespace {
 
-constexpr int kTileProbes = 25;    // 125 A rows: (r, g, b, d, d^2) per probe
+constexpr int kTileProbes = 25;    // 5 A rows per probe: (r, g, b, d, d^2); at most 25 (128 rows)
 constexpr int kRowsPerProbe = 5;
 constexpr int kKChunk = 16;        // rays per shared-memory stage (one K step)
 constexpr int kStages = 4;         // operand stages in the ring
@@ -78,6 +79,7 @@ struct TcArgs {
     uint32_t* err;
     const uint32_t* dev_count;  // listed probes, read on the device (NULL: nprobes)
     uint32_t stall;             // test hook: issue no MMA and no commit, so the completion wait runs out
+    uint32_t tile;              // probes per CTA (1 .. kTileProbes)
     const float* hyst_dev;      // hysteresis of this update in device memory (the ramp's), or NULL: g.hyst
 };
 
@@ -222,8 +224,8 @@ __host__ __device__ __forceinline__ size_t tc_smem_bytes(uint32_t nc, uint32_t n
     return smem;
 }
 
-// Blend of the tile of kTileProbes probe slots starting at p0 (< nprobes) by
-// the whole CTA.  Iteration c fills stage c % kStages with chunk c (weights
+// Blend of the tile of a.tile probe slots starting at p0 (< nprobes) by the
+// whole CTA.  Iteration c fills stage c % kStages with chunk c (weights
 // by cp.async, ray operands from registers loaded two iterations before) and
 // issues the MMAs of chunk c - 1, whose weights were copied one iteration
 // before; a stage is refilled once the MMAs that read it (kStages chunks
@@ -237,7 +239,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
     __shared__ int2 s_org[kTileProbes];  // atlas tile (x, y) of each probe, in tiles; x < 0: none
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t np = min((uint32_t)kTileProbes, nprobes - p0);
+    const uint32_t np = min(a.tile, nprobes - p0);
     const uint32_t R = a.g.rays;
     const float cell = a.g.cell_len;
     const bool split = a.Nd + a.Nc > 256;        // two accumulators: depth at column 0, colour at 256
@@ -271,10 +273,11 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
         const float sum = a.rowsum[i];
         s_rinv[i] = sum > 1e-3f ? 1.0f / sum : 1.0f;
     }
-    // A rows kTileProbes * 5 .. 127 stay zero in every stage
-    for (uint32_t i = tid; i < kStages * 2 * 3 * (kKChunk / 8); i += kThreads) {
-        const uint32_t kg = i % (kKChunk / 8), r = kTileProbes * kRowsPerProbe + (i / (kKChunk / 8)) % 3;
-        const uint32_t part = (i / (3 * (kKChunk / 8))) % 2, st = i / (2 * 3 * (kKChunk / 8));
+    // A rows tile * 5 .. 127 stay zero in every stage
+    const uint32_t zrows = 128u - a.tile * kRowsPerProbe;
+    for (uint32_t i = tid; i < kStages * 2 * zrows * (kKChunk / 8); i += kThreads) {
+        const uint32_t kg = i % (kKChunk / 8), r = a.tile * kRowsPerProbe + (i / (kKChunk / 8)) % zrows;
+        const uint32_t part = (i / (zrows * (kKChunk / 8))) % 2, st = i / (2 * zrows * (kKChunk / 8));
         *reinterpret_cast<uint4*>(smem + st * sbytes + part * kAPart + canon_off(r, kg)) = make_uint4(0, 0, 0, 0);
     }
     tc::fence_before_sync();
@@ -284,7 +287,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
 
     // thread -> (probe, 2 consecutive rays of the chunk); 200 of 256 threads
     const uint32_t pl = (uint32_t)tid >> 3, j = (uint32_t)tid & 7u;
-    const bool builder = pl < (uint32_t)kTileProbes;
+    const bool builder = pl < a.tile;
     const bool live = builder && pl < np;
     const float4* prec = a.rays + (size_t)(p0 + (live ? pl : 0u)) * R;
     float4 va[2], vb[2];  // records of the even / odd chunks in flight
@@ -570,7 +573,7 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
 
 __global__ void __launch_bounds__(kThreads) k_blend_tc(TcArgs a) {
     const uint32_t n = a.dev_count ? *a.dev_count : a.nprobes;
-    const uint32_t p0 = blockIdx.x * kTileProbes;
+    const uint32_t p0 = blockIdx.x * a.tile;
     if (p0 >= n) return;  // whole CTA, before any tensor-memory allocation
     blend_tc_tile(a, p0, n);
 }
@@ -635,6 +638,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_blend_tc(BatchTables bt, Bat
         a.dev_count = nullptr;
         a.stall = 0;
         a.hyst_dev = nullptr;
+        a.tile = kTileProbes;
         s_v = v;
         s_tile = b - __ldg(bl.tile_base + lo);
         s_items = __ldg(bl.tile_base + lo + 1) - __ldg(bl.tile_base + lo);
@@ -646,6 +650,34 @@ __global__ void __launch_bounds__(kThreads) k_batch_blend_tc(BatchTables bt, Bat
         __threadfence();
         if (atomicAdd(bt.done + s_v, 1u) == s_items - 1u) bt.clock[1 + s_v] = globaltimer_ns();
     }
+}
+
+// Probes per CTA for a launch over n probes with `per_sm` CTAs resident per
+// SM: the grid runs in rounds of (SMs x per_sm) CTAs, and a CTA's time is
+// a fixed part (the chunk pipeline, the accumulator read-back) plus a part
+// per probe, measured on GB300 as about 70 probes' worth of fixed cost
+// (tiles of 25 / 20 / 18 / 16 probes over 16,384 probes: 0.115 / 0.109 /
+// 0.107 / 0.133 ms); the size with the fewest rounds x (70 + size) wins,
+// the larger on ties.
+uint32_t tc_tile_size(uint32_t n, uint32_t per_sm) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        return kTileProbes;
+    }
+    const uint64_t slots = (uint64_t)sms * per_sm;
+    uint32_t best = kTileProbes;
+    uint64_t best_cost = ~0ull;
+    for (uint32_t t = kTileProbes; t >= 16; --t) {
+        const uint64_t tiles = (n + t - 1) / t, rounds = (tiles + slots - 1) / slots;
+        const uint64_t cost = rounds * (70 + t);
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = t;
+        }
+    }
+    return best;
 }
 
 // Shared-memory limit of both blend kernels on the current device.
@@ -702,7 +734,8 @@ cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uin
     const size_t smem = tc_smem_bytes(nc, nd, Nc, Nd);
     cudaError_t e = set_tc_smem_limit();
     if (e != cudaSuccess) return e;
-    uint32_t blocks = (nprobes + kTileProbes - 1) / kTileProbes;
+    a.tile = tc_tile_size(nprobes, Nd + Nc > 256 ? 1u : 2u);
+    uint32_t blocks = (nprobes + a.tile - 1) / a.tile;
     k_blend_tc<<<blocks, kThreads, smem, st>>>(a);
     return cudaGetLastError();
 }
