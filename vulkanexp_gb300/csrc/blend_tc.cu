@@ -80,6 +80,7 @@ struct TcArgs {
     const uint32_t* dev_count;  // listed probes, read on the device (NULL: nprobes)
     uint32_t stall;             // test hook: issue no MMA and no commit, so the completion wait runs out
     uint32_t tile;              // probes per CTA (1 .. kTileProbes)
+    uint32_t smem_bytes;        // dynamic shared memory of the launch
     const float* hyst_dev;      // hysteresis of this update in device memory (the ramp's), or NULL: g.hyst
 };
 
@@ -216,11 +217,30 @@ __host__ __device__ __forceinline__ size_t tc_stage_bytes(uint32_t Nd, uint32_t 
 // Dynamic shared memory of a tile: the operand ring or the epilogue
 // staging, whichever is larger; with more than 256 accumulator columns at
 // least kOneCtaSmem (one CTA per SM).
+__host__ __device__ __forceinline__ size_t tc_staging_bytes(uint32_t nc, uint32_t nd) {
+    return ((size_t)kTileProbes * (nc * nc * 3 + nd * nd * 2) * sizeof(float) + 15) / 16 * 16;
+}
+// The published FP16 tiles of the CTA's probes, border texels included,
+// assembled after the staging so that they leave in whole rows.
+__host__ __device__ __forceinline__ size_t tc_color_tiles_bytes(uint32_t nc) {
+    return ((size_t)kTileProbes * (nc + 2) * (nc + 2) * 8 + 15) / 16 * 16;
+}
+__host__ __device__ __forceinline__ size_t tc_tiles_bytes(uint32_t nc, uint32_t nd) {
+    return tc_color_tiles_bytes(nc) + (size_t)kTileProbes * (nd + 2) * (nd + 2) * 4;
+}
+// Largest request that still lets two CTAs share an SM (228 KB, of which
+// each CTA also holds ~3 KB of static shared memory and 1 KB reserved).
+constexpr size_t kTwoCtaSmem = 108 * 1024;
+
 __host__ __device__ __forceinline__ size_t tc_smem_bytes(uint32_t nc, uint32_t nd, uint32_t Nc, uint32_t Nd) {
     const size_t ring = kStages * tc_stage_bytes(Nd, Nc);
-    const size_t staging = (size_t)kTileProbes * (nc * nc * 3 + nd * nd * 2) * sizeof(float);
+    const size_t staging = tc_staging_bytes(nc, nd), with_tiles = staging + tc_tiles_bytes(nc, nd);
+    const bool wide = Nd + Nc > 256;
     size_t smem = ring > staging ? ring : staging;
-    if (Nd + Nc > 256 && smem < kOneCtaSmem) smem = kOneCtaSmem;
+    // the tile images where they fit without losing the second CTA per SM
+    // (or beside a wide tile's single CTA)
+    if (with_tiles > smem && with_tiles <= (wide ? (size_t)200 * 1024 : kTwoCtaSmem)) smem = with_tiles;
+    if (wide && smem < kOneCtaSmem) smem = kOneCtaSmem;
     return smem;
 }
 
@@ -448,7 +468,13 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
         // epilogue 2: hysteresis in the FP32 accumulators, FP16 publish of
         // each interior texel and of the border texels copied from it
         // (probesCopyBorders.comp); loads of the previous values are issued
-        // eight at a time per thread
+        // eight at a time per thread.  Where they fit, the FP16 tiles are
+        // assembled in shared memory first and leave in whole rows
+        // (sector-aligned 16-byte stores instead of scattered texels).
+        const size_t stg_bytes = tc_staging_bytes(a.nc, a.nd);
+        const bool assemble = stg_bytes + tc_tiles_bytes(a.nc, a.nd) <= a.smem_bytes;
+        uint2* Tc = reinterpret_cast<uint2*>(smem + stg_bytes);  // [probe][ncr x ncr]
+        uint32_t* Td = reinterpret_cast<uint32_t*>(smem + stg_bytes + tc_color_tiles_bytes(a.nc));
         const float hy = a.hyst_dev ? *a.hyst_dev : a.g.hyst;
         const int ncr = (int)a.g.color_res, ndr = (int)a.g.depth_res;
         // item i -> (probe, texel) and texel -> (x, y) without integer
@@ -496,12 +522,18 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
                                               res[2] * (1.0f - hy) + prev[k].z * hy, 1.0f);
                 a.acc_color[ti[k]] = nv;
                 const uint2 hv = float4_to_half4(nv.x, nv.y, nv.z, nv.w);
-                a.color[ti[k]] = hv;
-                const int2 o = s_org[pl2];
-                const int ox = ncr * o.x, oy = ncr * o.y;
-                for_border_targets((int)tx + 1, (int)ty + 1, ncr, [&](int bx, int by) {
-                    a.color[(size_t)(oy + by) * a.g.color_w + (size_t)(ox + bx)] = hv;
-                });
+                if (assemble) {
+                    uint2* T = Tc + (size_t)pl2 * ncr * ncr;
+                    T[((int)ty + 1) * ncr + (int)tx + 1] = hv;
+                    for_border_targets((int)tx + 1, (int)ty + 1, ncr, [&](int bx, int by) { T[by * ncr + bx] = hv; });
+                } else {
+                    a.color[ti[k]] = hv;
+                    const int2 o = s_org[pl2];
+                    const int ox = ncr * o.x, oy = ncr * o.y;
+                    for_border_targets((int)tx + 1, (int)ty + 1, ncr, [&](int bx, int by) {
+                        a.color[(size_t)(oy + by) * a.g.color_w + (size_t)(ox + bx)] = hv;
+                    });
+                }
             }
         }
         const uint32_t items_d = np * ntd;
@@ -535,15 +567,48 @@ __device__ __forceinline__ void blend_tc_tile(const TcArgs& a, const uint32_t p0
                 a.acc_depth[ti[k]] = nv;
                 const __half2 h2 = __floats2half2_rn(nv.x, nv.y);
                 const uint32_t hv = *reinterpret_cast<const uint32_t*>(&h2);
-                a.depth[ti[k]] = hv;
-                const int2 o = s_org[pl2];
-                const int ox = ndr * o.x, oy = ndr * o.y;
-                for_border_targets((int)tx + 1, (int)ty + 1, ndr, [&](int bx, int by) {
-                    a.depth[(size_t)(oy + by) * a.g.depth_w + (size_t)(ox + bx)] = hv;
-                });
+                if (assemble) {
+                    uint32_t* T = Td + (size_t)pl2 * ndr * ndr;
+                    T[((int)ty + 1) * ndr + (int)tx + 1] = hv;
+                    for_border_targets((int)tx + 1, (int)ty + 1, ndr, [&](int bx, int by) { T[by * ndr + bx] = hv; });
+                } else {
+                    a.depth[ti[k]] = hv;
+                    const int2 o = s_org[pl2];
+                    const int ox = ndr * o.x, oy = ndr * o.y;
+                    for_border_targets((int)tx + 1, (int)ty + 1, ndr, [&](int bx, int by) {
+                        a.depth[(size_t)(oy + by) * a.g.depth_w + (size_t)(ox + bx)] = hv;
+                    });
+                }
             }
         }
         __syncthreads();
+        if (assemble) {  // the tiles out, row by row, 16 bytes per store where the rows allow
+            // texels per store: uint4 where rows and the atlas allow it, else one texel
+            const uint32_t cq = (ncr * 8) % 16 == 0 && (reinterpret_cast<uintptr_t>(a.color) & 15u) == 0 ? 2u : 1u;
+            const uint32_t c_per_row = ncr / cq, c_items = np * ncr * c_per_row;
+            for (uint32_t i = tid; i < c_items; i += kThreads) {
+                const uint32_t p = i / (ncr * c_per_row), r = i % (ncr * c_per_row), y = r / c_per_row,
+                               x = (r % c_per_row) * cq;
+                const int2 o = s_org[p];
+                if (o.x < 0) continue;
+                const uint2* src = Tc + (size_t)p * ncr * ncr + y * ncr + x;
+                uint2* dst = a.color + (size_t)(ncr * o.y + (int)y) * a.g.color_w + (size_t)(ncr * o.x + (int)x);
+                if (cq == 2) *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(src);
+                else *dst = *src;
+            }
+            const uint32_t dq = (ndr * 4) % 16 == 0 && (reinterpret_cast<uintptr_t>(a.depth) & 15u) == 0 ? 4u : 1u;
+            const uint32_t d_per_row = ndr / dq, d_items = np * ndr * d_per_row;
+            for (uint32_t i = tid; i < d_items; i += kThreads) {
+                const uint32_t p = i / (ndr * d_per_row), r = i % (ndr * d_per_row), y = r / d_per_row,
+                               x = (r % d_per_row) * dq;
+                const int2 o = s_org[p];
+                if (o.x < 0) continue;
+                const uint32_t* src = Td + (size_t)p * ndr * ndr + y * ndr + x;
+                uint32_t* dst = a.depth + (size_t)(ndr * o.y + (int)y) * a.g.depth_w + (size_t)(ndr * o.x + (int)x);
+                if (dq == 4) *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(src);
+                else *dst = *src;
+            }
+        }
 
         const uint32_t rxy = (uint32_t)(a.g.res[0] * a.g.res[1]);
         const uint32_t nprobes_grid = rxy * (uint32_t)a.g.res[2];
@@ -603,7 +668,7 @@ __global__ void k_batch_tc_weights(BatchTables bt, BatchBlendList bl) {
 // Batched blend: CTA b takes tile (b - tile_base[i]) of volume list[i]; the
 // CTA that finishes a volume's last tile stamps its completion time.
 __global__ void __launch_bounds__(kThreads) k_batch_blend_tc(BatchTables bt, BatchBlendList bl,
-                                                             const float4* __restrict__ rays) {
+                                                             const float4* __restrict__ rays, uint32_t smem_bytes) {
     __shared__ TcArgs s_args;
     __shared__ uint32_t s_v, s_tile, s_items;
     if (threadIdx.x == 0) {
@@ -639,6 +704,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_blend_tc(BatchTables bt, Bat
         a.stall = 0;
         a.hyst_dev = nullptr;
         a.tile = kTileProbes;
+        a.smem_bytes = smem_bytes;
         s_v = v;
         s_tile = b - __ldg(bl.tile_base + lo);
         s_items = __ldg(bl.tile_base + lo + 1) - __ldg(bl.tile_base + lo);
@@ -735,6 +801,7 @@ cudaError_t launch_blend_tc(const DeviceGrid& g, const uint32_t* probe_list, uin
     cudaError_t e = set_tc_smem_limit();
     if (e != cudaSuccess) return e;
     a.tile = tc_tile_size(nprobes, Nd + Nc > 256 ? 1u : 2u);
+    a.smem_bytes = (uint32_t)smem;
     uint32_t blocks = (nprobes + a.tile - 1) / a.tile;
     k_blend_tc<<<blocks, kThreads, smem, st>>>(a);
     return cudaGetLastError();
@@ -765,7 +832,7 @@ cudaError_t launch_batch_blend_tc(const BatchTables& bt, const BatchBlendList& b
     if (bl.ntiles == 0) return cudaSuccess;
     cudaError_t e = set_tc_smem_limit();
     if (e != cudaSuccess) return e;
-    k_batch_blend_tc<<<bl.ntiles, kThreads, smem, st>>>(bt, bl, rays);
+    k_batch_blend_tc<<<bl.ntiles, kThreads, smem, st>>>(bt, bl, rays, (uint32_t)smem);
     return cudaGetLastError();
 }
 
