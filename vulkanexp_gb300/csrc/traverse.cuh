@@ -172,11 +172,13 @@ __device__ __forceinline__ bool traverse(const DeviceScene& sc, float3 wo, float
 // the held leaves: an instance leaf moves the ray into the mesh tree, a
 // triangle leaf runs the watertight tests.  The stack lives in shared memory
 // (one column per thread).  Hit set, tie rule and results equal `traverse`.
+// Threads of the blocks that run the walkers: a thread's stack entry i is
+// at column i * kWalkerThreads of the block's shared array.
+constexpr int kWalkerThreads = 128;
 struct SmemStack {
     int* base;
-    int stride;
-    __device__ __forceinline__ int get(int i) const { return base[i * stride]; }
-    __device__ __forceinline__ void set(int i, int v) { base[i * stride] = v; }
+    __device__ __forceinline__ int get(int i) const { return base[i * kWalkerThreads]; }
+    __device__ __forceinline__ void set(int i, int v) { base[i * kWalkerThreads] = v; }
 };
 
 // The first `split` entries in shared memory, deeper ones in a per-thread
@@ -187,12 +189,11 @@ struct SmemStack {
 constexpr int kSpillMax = 96;
 struct SplitStack {
     int* base;
-    int stride;
     int split;
     int* spill;
-    __device__ __forceinline__ int get(int i) const { return i < split ? base[i * stride] : spill[i - split]; }
+    __device__ __forceinline__ int get(int i) const { return i < split ? base[i * kWalkerThreads] : spill[i - split]; }
     __device__ __forceinline__ void set(int i, int v) {
-        if (i < split) base[i * stride] = v;
+        if (i < split) base[i * kWalkerThreads] = v;
         else spill[i - split] = v;
     }
 };

@@ -23,7 +23,7 @@ namespace ddgi {
 
 namespace {
 
-constexpr int kPersistThreads = 128;
+constexpr int kPersistThreads = kWalkerThreads;  // the walkers' shared-memory stacks assume it
 constexpr unsigned kFull = 0xffffffffu;
 
 // Work item `id` of a grouped order: groups of G = 32 / rpw probes (in perm
@@ -105,13 +105,9 @@ struct ShadowJob {
     }
 };
 
-__device__ __forceinline__ void init_stack(SmemStack& s, int* base, int stride, int, int*) {
+__device__ __forceinline__ void init_stack(SmemStack& s, int* base, int, int*) { s.base = base; }
+__device__ __forceinline__ void init_stack(SplitStack& s, int* base, int split, int* spill) {
     s.base = base;
-    s.stride = stride;
-}
-__device__ __forceinline__ void init_stack(SplitStack& s, int* base, int stride, int split, int* spill) {
-    s.base = base;
-    s.stride = stride;
     s.split = split;
     s.spill = spill;
 }
@@ -138,7 +134,7 @@ __device__ __forceinline__ void persistent_walk(const DeviceScene& sc, const Job
     const unsigned lt = (1u << lane) - 1u;
     SpillArea<Stack> spill;
     Walker<ANY, Stack> w;
-    init_stack(w.stk, s_stack + threadIdx.x, blockDim.x, split, spill.ptr());
+    init_stack(w.stk, s_stack + threadIdx.x, split, spill.ptr());
     w.cap = stack_cap;
     w.clear();
     w.wait_max = knobs.wait;
