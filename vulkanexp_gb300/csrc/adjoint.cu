@@ -35,20 +35,6 @@ constexpr uint32_t kShadowBit = 1u << 30;
 constexpr uint32_t kBackBit = 1u << 31;
 constexpr uint32_t kPrimMask = (1u << 28) - 1u;
 
-__device__ __forceinline__ int4 border_entry(int e, int n) {
-    int m = n - 2;
-    if (e == 0) return make_int4(0, 0, n - 2, n - 2);
-    if (e == 1) return make_int4(0, n - 1, n - 2, 1);
-    if (e == 2) return make_int4(n - 1, 0, 1, n - 2);
-    if (e == 3) return make_int4(n - 1, n - 1, 1, 1);
-    e -= 4;
-    int side = e / m, j = e % m + 1;
-    if (side == 0) return make_int4(0, j, 1, n - 1 - j);
-    if (side == 1) return make_int4(n - 1, j, n - 2, n - 1 - j);
-    if (side == 2) return make_int4(j, 0, n - 1 - j, 1);
-    return make_int4(j, n - 1, n - 1 - j, n - 2);
-}
-
 __device__ __forceinline__ float night_fade(const DeviceLight& L) {
     return L.dir[1] < 0.0f ? 1.0f - clampf(-L.dir[1], 0.0f, 0.1f) / 0.1f : 1.0f;
 }

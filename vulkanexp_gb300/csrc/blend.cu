@@ -20,21 +20,6 @@ namespace ddgi {
 
 namespace {
 
-// Border entry e of a tile of side n: (dst x, dst y, src x, src y).
-__device__ __forceinline__ int4 border_entry(int e, int n) {
-    int m = n - 2;
-    if (e == 0) return make_int4(0, 0, n - 2, n - 2);
-    if (e == 1) return make_int4(0, n - 1, n - 2, 1);
-    if (e == 2) return make_int4(n - 1, 0, 1, n - 2);
-    if (e == 3) return make_int4(n - 1, n - 1, 1, 1);
-    e -= 4;
-    int side = e / m, j = e % m + 1;
-    if (side == 0) return make_int4(0, j, 1, n - 1 - j);
-    if (side == 1) return make_int4(n - 1, j, n - 2, n - 1 - j);
-    if (side == 2) return make_int4(j, 0, n - 1 - j, 1);
-    return make_int4(j, n - 1, n - 1 - j, n - 2);
-}
-
 // Blend of one probe by the whole block: `pr` = its R ray records.
 // `hy` is the hysteresis of this update (the grid's, or the ramp's value).
 __device__ __forceinline__ void blend_probe_fp32(const DeviceGrid& g, uint32_t probe, const float4* __restrict__ pr,

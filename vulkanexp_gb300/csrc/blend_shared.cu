@@ -26,22 +26,6 @@ namespace {
 constexpr uint32_t kProbesPerBlock = 8;
 constexpr uint32_t kBlendThreads = 256;
 
-// Border entry e of a tile of side n: (dst x, dst y, src x, src y); the
-// generalised probesCopyBorders.comp table of blend.cu.
-__device__ __forceinline__ int4 border_entry_s(int e, int n) {
-    int m = n - 2;
-    if (e == 0) return make_int4(0, 0, n - 2, n - 2);
-    if (e == 1) return make_int4(0, n - 1, n - 2, 1);
-    if (e == 2) return make_int4(n - 1, 0, 1, n - 2);
-    if (e == 3) return make_int4(n - 1, n - 1, 1, 1);
-    e -= 4;
-    int side = e / m, j = e % m + 1;
-    if (side == 0) return make_int4(0, j, 1, n - 1 - j);
-    if (side == 1) return make_int4(n - 1, j, n - 2, n - 1 - j);
-    if (side == 2) return make_int4(j, 0, n - 1 - j, 1);
-    return make_int4(j, n - 1, n - 1 - j, n - 2);
-}
-
 // Weights of one texel over all rays (thread t of the grid = texel t).
 __device__ __forceinline__ void texel_weights(const DeviceGrid& g, const float4* __restrict__ dirs, uint32_t t,
                                               float* __restrict__ W, float* __restrict__ wsum) {
@@ -192,11 +176,11 @@ __device__ __forceinline__ void blend_probes_shared(const DeviceGrid& g, const u
         const int ix = (int)(probe % rx), iy = (int)((probe % rxy) / rx), iz = (int)(probe / rxy);
         const int tile = iy * g.res[0] + ix;
         if (e < nbc) {
-            int4 b = border_entry_s(e, (int)g.color_res);
+            int4 b = border_entry(e, (int)g.color_res);
             size_t ox = (size_t)g.color_res * tile, oy = (size_t)g.color_res * iz;
             color[(oy + b.y) * g.color_w + ox + b.x] = color[(oy + b.w) * g.color_w + ox + b.z];
         } else {
-            int4 b = border_entry_s(e - nbc, (int)g.depth_res);
+            int4 b = border_entry(e - nbc, (int)g.depth_res);
             size_t ox = (size_t)g.depth_res * tile, oy = (size_t)g.depth_res * iz;
             depth[(oy + b.y) * g.depth_w + ox + b.x] = depth[(oy + b.w) * g.depth_w + ox + b.z];
         }

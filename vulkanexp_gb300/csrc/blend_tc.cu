@@ -108,20 +108,6 @@ __device__ __forceinline__ uint32_t pack2(float a, float b, uint32_t* lo) {
     return *reinterpret_cast<uint32_t*>(&h);
 }
 
-__device__ __forceinline__ int4 border_entry(int e, int n) {
-    int m = n - 2;
-    if (e == 0) return make_int4(0, 0, n - 2, n - 2);
-    if (e == 1) return make_int4(0, n - 1, n - 2, 1);
-    if (e == 2) return make_int4(n - 1, 0, 1, n - 2);
-    if (e == 3) return make_int4(n - 1, n - 1, 1, 1);
-    e -= 4;
-    int side = e / m, j = e % m + 1;
-    if (side == 0) return make_int4(0, j, 1, n - 1 - j);
-    if (side == 1) return make_int4(n - 1, j, n - 2, n - 1 - j);
-    if (side == 2) return make_int4(j, 0, n - 1 - j, 1);
-    return make_int4(j, n - 1, n - 1 - j, n - 2);
-}
-
 __device__ __forceinline__ uint2 float4_to_half4(float a, float b, float c, float d) {
     __half2 x = __floats2half2_rn(a, b), y = __floats2half2_rn(c, d);
     return make_uint2(*reinterpret_cast<uint32_t*>(&x), *reinterpret_cast<uint32_t*>(&y));
@@ -193,7 +179,8 @@ __global__ void k_tc_weights(const float4* dirs, uint32_t R, uint32_t nc, uint32
 
 // Calls put(bx, by) for each border texel of a tile of side n that copies
 // interior texel (x, y), 1 <= x, y <= n - 2 (probesCopyBorders.comp:21-245,
-// generalised: the inverse of border_entry); up to 8 for n = 3, 3 otherwise.
+// generalised: the inverse of border_entry in common.cuh); up to 8 for n = 3,
+// 3 otherwise.
 template <class F>
 __device__ __forceinline__ void for_border_targets(int x, int y, int n, F put) {
     if (x == 1) put(0, n - 1 - y);

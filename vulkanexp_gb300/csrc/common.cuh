@@ -158,6 +158,24 @@ struct DeviceLight {
 // ---------------------------------------------------------------------------
 // Exact helpers
 // ---------------------------------------------------------------------------
+// Border entry e of an octahedral tile of side n: (dst x, dst y, src x,
+// src y), the table of src/shaders/probesCopyBorders.comp:21-245 generalised
+// to any side: entries 0-3 the corners, then the four edges of n - 2 texels,
+// each a copy of the mirrored interior texel next to the opposite edge.
+__device__ __forceinline__ int4 border_entry(int e, int n) {
+    int m = n - 2;
+    if (e == 0) return make_int4(0, 0, n - 2, n - 2);
+    if (e == 1) return make_int4(0, n - 1, n - 2, 1);
+    if (e == 2) return make_int4(n - 1, 0, 1, n - 2);
+    if (e == 3) return make_int4(n - 1, n - 1, 1, 1);
+    e -= 4;
+    int side = e / m, j = e % m + 1;
+    if (side == 0) return make_int4(0, j, 1, n - 1 - j);
+    if (side == 1) return make_int4(n - 1, j, n - 2, n - 1 - j);
+    if (side == 2) return make_int4(j, 0, n - 1 - j, 1);
+    return make_int4(j, n - 1, n - 1 - j, n - 2);
+}
+
 __device__ __forceinline__ float sel3(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
 
 __device__ __forceinline__ float3 probe_origin_exact(const DeviceGrid& g, uint32_t linear) {
