@@ -5,15 +5,15 @@
  * Closest-hit instance and triangle IDs are required to be bit-identical
  * between the CUDA path and any CPU implementation of the same update.  That
  * only holds if both trace bit-identical rays, so the inputs of the ray
- * generation are fixed here, computed once on the host in double precision
- * and rounded to float:
+ * generation are fixed here, computed once on the host:
  *
  *  - the per-update ray-direction table: the rotated spherical Fibonacci set
- *    of src/shaders/irradiance.glsl:52-64 and src/shaders/traceProbes.rgen:36
- *    (the reference stores the same table in its `rayDirection` image,
+ *    of src/shaders/irradiance.glsl:52-64 and src/shaders/traceProbes.rgen:36,
+ *    evaluated in float operation by operation as the shaders write it (the
+ *    reference stores the same table in its `rayDirection` image,
  *    src/shaders/traceProbes.rgen:46-47);
  *  - the world-to-object transform of an instance (the reference gets it from
- *    the ray-tracing driver as gl_WorldToObjectEXT).
+ *    the ray-tracing driver as gl_WorldToObjectEXT), in double, rounded.
  *
  * Compile users of this header with -ffp-contract=off: the functions below
  * assume every operation is rounded separately.
@@ -28,28 +28,30 @@
 extern "C" {
 #endif
 
-/* Golden-ratio constant of sphericalFibonacci (irradiance.glsl:53). */
-#define DDGI_PHI_MINUS_ONE 0.61803398874989484820
-
-/* Ray direction `i` of `n`: M * sphericalFibonacci(i, n), M row-major 3x3.
- * Written as (x, y, z, 1) into out[0..3]. */
+/* Ray direction `i` of `n`: M * sphericalFibonacci(i, n), M row-major 3x3,
+ * written as (x, y, z, 1) into out[0..3].  The float operations of
+ * irradiance.glsl:52-64 (pi = 3.1415926538f, common.glsl:4) in their order,
+ * each rounded separately:
+ *   PHI = sqrt(5) * 0.5 + 0.5;  a = i * (PHI - 1);  phi = (2 pi) (a - floor(a))
+ *   cosTheta = 1 - (2 i + 1) * (1 / n);  sinTheta = sqrt(clamp(1 - cosTheta^2, 0, 1))
+ *   v = (cos(phi) sinTheta, sin(phi) sinTheta, cosTheta)
+ * with cos and sin of the float phi correctly rounded (evaluated in double,
+ * then rounded: the most accurate result GLSL permits, and the same on every
+ * host); then the rotation as mat3 * vec3 (traceProbes.rgen:36), column 0 * x
+ * + column 1 * y + column 2 * z. */
 static inline void ddgi_ray_direction(const float m[9], uint32_t i, uint32_t n, float out[4]) {
-    const double two_pi = 6.283185307179586476925;
-    double a = (double)i * DDGI_PHI_MINUS_ONE;
-    double frac = a - floor(a);
-    double phi = two_pi * frac;
-    double cos_theta = 1.0 - (2.0 * (double)i + 1.0) / (double)n;
-    double s2 = 1.0 - cos_theta * cos_theta;
-    if (s2 < 0.0) s2 = 0.0;
-    if (s2 > 1.0) s2 = 1.0;
-    double sin_theta = sqrt(s2);
-    double v[3] = {cos(phi) * sin_theta, sin(phi) * sin_theta, cos_theta};
-    for (int r = 0; r < 3; ++r) {
-        double acc = (double)m[3 * r + 0] * v[0];
-        acc = acc + (double)m[3 * r + 1] * v[1];
-        acc = acc + (double)m[3 * r + 2] * v[2];
-        out[r] = (float)acc;
-    }
+    const float phi_golden = sqrtf(5.0f) * 0.5f + 0.5f;
+    const float fi = (float)i;
+    const float a = fi * (phi_golden - 1.0f);
+    const float frac = a - floorf(a);
+    const float phi = (2.0f * 3.1415926538f) * frac;
+    const float cos_theta = 1.0f - (2.0f * fi + 1.0f) * (1.0f / (float)n);
+    float s2 = 1.0f - cos_theta * cos_theta;
+    if (s2 < 0.0f) s2 = 0.0f;
+    if (s2 > 1.0f) s2 = 1.0f;
+    const float sin_theta = sqrtf(s2);
+    const float v[3] = {(float)cos((double)phi) * sin_theta, (float)sin((double)phi) * sin_theta, cos_theta};
+    for (int r = 0; r < 3; ++r) out[r] = (m[3 * r + 0] * v[0] + m[3 * r + 1] * v[1]) + m[3 * r + 2] * v[2];
     out[3] = 1.0f;
 }
 

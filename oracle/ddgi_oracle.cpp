@@ -42,6 +42,13 @@
  *  - Texture filtering is exact bilinear (the hardware uses 8-bit weights).
  *  - pow(x, 3) and pow(x, 5) are evaluated as products.
  *
+ * Pinned to the reference's own shader code: the files above, compiled as
+ * C++ by oracle/build_ref_glsl.py and run on the host (every invocation a
+ * thread, traceRayEXT through this file's traversal), give the same
+ * reference-format atlases and probe states as this restatement's float
+ * form, bit for bit, on the update passes and on a whole room update
+ * (tests/test_reference_shaders.py, fixtures in tests/golden/).
+ *
  * Atlas storage: the plain form keeps FP32 texels.  The reference-format form
  * (grid precision DDGI_PRECISION_REFERENCE_FORMAT) rounds every stored texel
  * to the formats of the reference's atlas images (B10G11R11 unsigned floats
@@ -1272,6 +1279,36 @@ int oracle_update(const oracle_scene* s, const ddgi_grid_desc* g, const ddgi_lig
                              hit_out, nthreads);
 }
 
+// Trace + shade (float) of n given probe rays against a previous atlas:
+// rays[8 k ...] = origin, direction, tmin, tmax; out[4 k ...] = radiance and
+// hit distance as the probe update records them.  For checking the shading
+// against the reference's own stages on the same rays.
+void oracle_shade_rays(const oracle_scene* s, const ddgi_grid_desc* gd, const ddgi_light* ld, const uint32_t* states,
+                       const float* color, const float* depth, const float* rays, uint32_t n, float* out, int nthreads) {
+    Grid g = make_grid(gd);
+    Light L;
+    L.dir = F3(ld->direction[0], ld->direction[1], ld->direction[2]);
+    L.color = F3(ld->color[0], ld->color[1], ld->color[2]);
+    L.sky = F3(ld->sky[0], ld->sky[1], ld->sky[2]);
+    L.brightness = ld->color[3];
+    Atlas<float> at;
+    at.color = const_cast<float*>(color);
+    at.depth = const_cast<float*>(depth);
+    at.cw = g.colorRes * g.res[0] * g.res[1];
+    at.ch = g.colorRes * g.res[2];
+    at.dw = g.depthRes * g.res[0] * g.res[1];
+    at.dh = g.depthRes * g.res[2];
+    parallel_for(n, nthreads, [&](size_t b, size_t e) {
+        for (size_t k = b; k < e; ++k) {
+            const float* r = rays + 8 * k;
+            const F3 o(r[0], r[1], r[2]), d(r[3], r[4], r[5]);
+            Hit h;
+            trace(s->s, o, d, r[6], r[7], 0x3u, false, &h);
+            shade_hit<float>(s->s, g, L, default_params<float>(L), states, at, o, d, h, -1, nullptr, out + 4 * k);
+        }
+    }, 64);
+}
+
 // Blend + border only, from given ray records (R x 4 per listed probe) — for
 // checking the blend kernel in isolation.
 int oracle_blend(const ddgi_grid_desc* gd, const float orientation[9], const uint32_t* list, uint32_t nlist,
@@ -1375,8 +1412,23 @@ void oracle_sphere_to_oct_uv(const float* d3, float* uv) {
     sphere_to_oct_uv(F3(d3[0], d3[1], d3[2]), &uv[0], &uv[1]);
 }
 float oracle_texel_scale(uint32_t n) { return texel_scale(n); }
+void oracle_probe_world_position(const ddgi_grid_desc* gd, uint32_t index, float* out3) {
+    const Grid g = make_grid(gd);
+    int idx[3];
+    grid_index(index, g, idx);
+    const F3 p = probe_pos<float>(idx, g);
+    out3[0] = p.x; out3[1] = p.y; out3[2] = p.z;
+}
 // Miss radiance of later calls: 0 constant sky radiance, 1 atmospheric sky.
 void oracle_set_sky_mode(int mode) { g_sky_mode.store(mode); }
+// The atmospheric sky in float (sky.glsl's sky() with showSun = true).
+void oracle_sky(const float* origin, const float* dir, const float* sun_pos, const float* sun_color, float brightness,
+                float* out3) {
+    const F3 c = atmosphere<float>(F3(origin[0], origin[1], origin[2]), F3(dir[0], dir[1], dir[2]),
+                                   F3(sun_pos[0], sun_pos[1], sun_pos[2]), F3(sun_color[0], sun_color[1], sun_color[2]),
+                                   brightness);
+    out3[0] = c.x; out3[1] = c.y; out3[2] = c.z;
+}
 
 // Reference-format storage rounding of n values: kind 0 = 11-bit unsigned
 // float (red, green), 1 = 10-bit unsigned float (blue), 2 = half.

@@ -93,6 +93,10 @@ class Oracle:
             lib.oracle_border_table.argtypes = [C.c_int, C.c_void_p]
             lib.oracle_oct_decode.argtypes = [C.c_float, C.c_float, C.c_void_p]
             lib.oracle_sphere_to_oct_uv.argtypes = [C.c_void_p, C.c_void_p]
+            lib.oracle_shade_rays.argtypes = [C.c_void_p, C.POINTER(GridDesc), C.POINTER(Light)] + [C.c_void_p] * 4 + [
+                C.c_uint32, C.c_void_p, C.c_int]
+            lib.oracle_probe_world_position.argtypes = [C.POINTER(GridDesc), C.c_uint32, C.c_void_p]
+            lib.oracle_sky.argtypes = [C.c_void_p] * 4 + [C.c_float, C.c_void_p]
             lib.oracle_direction_table.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
             lib.oracle_round_store.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_uint32]
             lib.oracle_set_sky_mode.argtypes = [C.c_int]
@@ -161,6 +165,16 @@ class Oracle:
         return rays, hits
 
     # -- differentiation support (FP64, all probes, hit set recorded once) -----
+    def shade_rays(self, grid, light, states, color, depth, rays):
+        """Trace + shade (float) of given rays (n x 8: origin, direction,
+        tmin, tmax) against the previous atlas: n x 4 records (radiance,
+        hit distance) as the probe update writes them."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        out = np.zeros((len(rays), 4), np.float32)
+        self.lib().oracle_shade_rays(self._h, C.byref(grid), C.byref(light), _ptr(states), _ptr(color), _ptr(depth),
+                                     _ptr(rays), len(rays), _ptr(out), self.threads)
+        return out
+
     def record(self, grid, light, orientations, states, color, depth):
         """K FP64 updates (orientations K x 9) in place on color/depth
         (float64) and states; returns the recording: hits (K, P, R) and the
@@ -237,6 +251,20 @@ class Oracle:
         d = np.ascontiguousarray(d, np.float32)
         out = np.zeros(2, np.float32)
         cls.lib().oracle_sphere_to_oct_uv(_ptr(d), _ptr(out))
+        return out
+
+    @classmethod
+    def probe_world_position(cls, grid, index):
+        out = np.zeros(3, np.float32)
+        cls.lib().oracle_probe_world_position(C.byref(grid), index, _ptr(out))
+        return out
+
+    @classmethod
+    def sky(cls, origin, direction, sun_pos, sun_color, brightness):
+        """The atmospheric sky radiance (float) seen along `direction`."""
+        a = [np.ascontiguousarray(x, np.float32) for x in (origin, direction, sun_pos, sun_color)]
+        out = np.zeros(3, np.float32)
+        cls.lib().oracle_sky(*[_ptr(x) for x in a], brightness, _ptr(out))
         return out
 
     @classmethod

@@ -48,22 +48,44 @@ def test_oct_decode_unit_and_roundtrip():
                 assert abs((2 * u - 1) - x) < 2e-5 and abs((2 * v - 1) - y) < 2e-5
 
 
+def fibonacci_float32(n):
+    """irradiance.glsl:52-64 in float32, operation by operation (cos and sin
+    of the float angle in float64, then rounded)."""
+    f = np.float32
+    i = np.arange(n, dtype=np.float32)
+    phi_golden = f(np.sqrt(f(5.0))) * f(0.5) + f(0.5)
+    a = i * (phi_golden - f(1.0))
+    phi = (f(2.0) * f(3.1415926538)) * (a - np.floor(a))
+    cos_t = f(1.0) - (f(2.0) * i + f(1.0)) * (f(1.0) / f(n))
+    sin_t = np.sqrt(np.clip(f(1.0) - cos_t * cos_t, f(0.0), f(1.0)))
+    x = np.cos(phi.astype(np.float64)).astype(np.float32) * sin_t
+    y = np.sin(phi.astype(np.float64)).astype(np.float32) * sin_t
+    return np.stack([x, y, cos_t], 1)
+
+
 def test_spherical_fibonacci_table():
-    """Unrotated table: z_i = 1 - (2i+1)/N, unit length, the golden-angle
-    spiral (irradiance.glsl:52-64); a rotation keeps lengths and dots."""
-    n = 128
+    """The unrotated table is the shader's float formula bit for bit
+    (irradiance.glsl:52-64), and within the float rounding of i (PHI - 1)
+    (2 pi i 2^-23 radians) of the real-number golden-angle spiral with
+    z_i = 1 - (2i+1)/N; a rotation is mat3 * vec3 (traceProbes.rgen:36),
+    column by column in float."""
+    n = 256
     t = Oracle.direction_table(np.eye(3, dtype=np.float32).reshape(9), n)
+    v32 = fibonacci_float32(n)
+    assert (t[:, :3] == v32).all()
+    assert (t[:, 3] == 1.0).all()
     i = np.arange(n)
     z = 1.0 - (2 * i + 1) / n
     phi = 2 * np.pi * np.mod(i * 0.6180339887498949, 1.0)
     s = np.sqrt(np.clip(1 - z * z, 0, 1))
     v = np.stack([np.cos(phi) * s, np.sin(phi) * s, z], 1)
-    np.testing.assert_allclose(t[:, :3], v, atol=1e-6)
-    assert (t[:, 3] == 1.0).all()
-    M = scenes.random_orientation(4, 2).reshape(3, 3)
+    bound = 2 * np.pi * np.maximum(i, 1) * 2.0 ** -23 + 1e-6
+    assert (np.abs(t[:, :3] - v).max(axis=1) <= bound).all()
+    M = scenes.random_orientation(4, 2).reshape(3, 3).astype(np.float32)
     np.testing.assert_allclose(M @ M.T, np.eye(3), atol=1e-6)
     tr = Oracle.direction_table(M.reshape(9), n)
-    np.testing.assert_allclose(tr[:, :3], v @ M.T.astype(np.float64), atol=2e-6)
+    rot = (M[:, 0][None, :] * v32[:, 0:1] + M[:, 1][None, :] * v32[:, 1:2]) + M[:, 2][None, :] * v32[:, 2:3]
+    assert (tr[:, :3] == rot).all()
 
 
 def _empty_scene():
