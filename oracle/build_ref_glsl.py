@@ -29,16 +29,19 @@ LIB = os.path.join(OUT, "libref_glsl.so")
 SHADERS = ["common.glsl", "ProbeGrid.glsl", "irradiance.glsl", "pbrMetallicRoughness.glsl", "sky.glsl",
            "probesUpdate.glsl", "probesCopyBorders.comp", "traceProbes.rgen", "closesthit.glsl",
            "closesthit_noreflection.rchit", "miss.rmiss", "shadow.rmiss", "rayPayload.glsl", "InstanceMasks.glsl",
-           "Lights.glsl", "Vertex.glsl", "Material.glsl", "unpackMaterial.glsl"]
+           "Lights.glsl", "Vertex.glsl", "Material.glsl", "unpackMaterial.glsl", "probesInit.rgen",
+           "probeInitMiss.rmiss", "backfaceTest.rchit", "FinalGather.frag"]
 SOURCES = ["ref_glsl_irradiance.cpp", "ref_glsl_pbr.cpp", "ref_glsl_sky.cpp", "ref_glsl_update_irradiance.cpp",
            "ref_glsl_update_depth.cpp", "ref_glsl_copy_borders.cpp", "ref_glsl_trace.cpp", "ref_glsl_closesthit.cpp",
-           "ref_glsl_miss.cpp"]
+           "ref_glsl_miss.cpp", "ref_glsl_probe_init.cpp", "ref_glsl_final_gather.cpp"]
 FORMATS = ("rgba32f", "r11f_g11f_b10f", "rg16f")
 
 
 def translate(text):
     """GLSL resource declarations as C++ declarations:
     * `#version` / `#extension` lines: removed;
+    * a stage input or output `layout(...) in|out T name;`: thread_local
+      (one thread per invocation or fragment);
     * `layout(local_size_x = X, local_size_y = Y, local_size_z = Z) in;`:
       the gl_WorkGroupSize constant it defines;
     * a uniform or buffer block without an instance name: its members as
@@ -51,6 +54,7 @@ def translate(text):
     * a private global `T name;` at file scope: thread_local (one thread per
       invocation)."""
     text = re.sub(r"(?m)^[ \t]*#[ \t]*(version|extension)\b.*$", "", text)
+    text = re.sub(r"layout\s*\([^)]*\)\s*(?:in|out)\s+(\w+)\s+(\w+)\s*;", r"thread_local \1 \2;", text)
     text = re.sub(r"layout\s*\(\s*local_size_x\s*=\s*(\d+)\s*,\s*local_size_y\s*=\s*(\d+)\s*,"
                   r"\s*local_size_z\s*=\s*(\d+)\s*\)\s*in\s*;",
                   r"const uvec3 gl_WorkGroupSize = uvec3(\1u, \2u, \3u);", text)

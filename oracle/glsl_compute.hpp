@@ -40,6 +40,11 @@ struct uswz2 {
     uint e[3];
     operator uvec2() const { return uvec2{e[A], e[B]}; }
 };
+struct uvec3;
+struct uswz3 {
+    uint e[3];
+    operator uvec3() const;
+};
 struct uvec3 {
     union {
         struct {
@@ -47,6 +52,7 @@ struct uvec3 {
         };
         uswz2<0, 1> xy;
         uswz2<1, 2> yz;
+        uswz3 xyz;
     };
     uvec3() { x = y = z = 0u; }
     uvec3(uint a, uint b, uint c) {
@@ -66,6 +72,9 @@ struct uvec3 {
         return *this;
     }
 };
+inline uswz3::operator uvec3() const { return uvec3(e[0], e[1], e[2]); }
+inline ivec3::ivec3(const uvec3& v) : x((int)v.x), y((int)v.y), z((int)v.z) {}
+
 // Matrices are arrays of columns, as in GLSL.
 struct mat4 {
     vec4 c[4];
@@ -88,6 +97,54 @@ struct mat3 {
     }
 };
 inline vec3 operator*(const mat3& m, const vec3& v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z; }
+inline vec4 operator*(const mat4& m, const vec4& v) {
+    return ((m.c[0] * v.x + m.c[1] * v.y) + m.c[2] * v.z) + m.c[3] * v.w;
+}
+// inverse(mat4): the adjugate over the determinant, by 2x2 minors, in float.
+inline mat4 inverse(const mat4& M) {
+    float a[4][4];  // a[row][col]
+    for (int c = 0; c < 4; ++c) {
+        a[0][c] = M.c[c].x, a[1][c] = M.c[c].y, a[2][c] = M.c[c].z, a[3][c] = M.c[c].w;
+    }
+    const float s0 = a[0][0] * a[1][1] - a[1][0] * a[0][1], s1 = a[0][0] * a[1][2] - a[1][0] * a[0][2];
+    const float s2 = a[0][0] * a[1][3] - a[1][0] * a[0][3], s3 = a[0][1] * a[1][2] - a[1][1] * a[0][2];
+    const float s4 = a[0][1] * a[1][3] - a[1][1] * a[0][3], s5 = a[0][2] * a[1][3] - a[1][2] * a[0][3];
+    const float c5 = a[2][2] * a[3][3] - a[3][2] * a[2][3], c4 = a[2][1] * a[3][3] - a[3][1] * a[2][3];
+    const float c3 = a[2][1] * a[3][2] - a[3][1] * a[2][2], c2 = a[2][0] * a[3][3] - a[3][0] * a[2][3];
+    const float c1 = a[2][0] * a[3][2] - a[3][0] * a[2][2], c0 = a[2][0] * a[3][1] - a[3][0] * a[2][1];
+    const float det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+    const float r = 1.0f / det;
+    float b[4][4];
+    b[0][0] = (a[1][1] * c5 - a[1][2] * c4 + a[1][3] * c3) * r;
+    b[0][1] = (-a[0][1] * c5 + a[0][2] * c4 - a[0][3] * c3) * r;
+    b[0][2] = (a[3][1] * s5 - a[3][2] * s4 + a[3][3] * s3) * r;
+    b[0][3] = (-a[2][1] * s5 + a[2][2] * s4 - a[2][3] * s3) * r;
+    b[1][0] = (-a[1][0] * c5 + a[1][2] * c2 - a[1][3] * c1) * r;
+    b[1][1] = (a[0][0] * c5 - a[0][2] * c2 + a[0][3] * c1) * r;
+    b[1][2] = (-a[3][0] * s5 + a[3][2] * s2 - a[3][3] * s1) * r;
+    b[1][3] = (a[2][0] * s5 - a[2][2] * s2 + a[2][3] * s1) * r;
+    b[2][0] = (a[1][0] * c4 - a[1][1] * c2 + a[1][3] * c0) * r;
+    b[2][1] = (-a[0][0] * c4 + a[0][1] * c2 - a[0][3] * c0) * r;
+    b[2][2] = (a[3][0] * s4 - a[3][1] * s2 + a[3][3] * s0) * r;
+    b[2][3] = (-a[2][0] * s4 + a[2][1] * s2 - a[2][3] * s0) * r;
+    b[3][0] = (-a[1][0] * c3 + a[1][1] * c1 - a[1][2] * c0) * r;
+    b[3][1] = (a[0][0] * c3 - a[0][1] * c1 + a[0][2] * c0) * r;
+    b[3][2] = (-a[3][0] * s3 + a[3][1] * s1 - a[3][2] * s0) * r;
+    b[3][3] = (a[2][0] * s3 - a[2][1] * s1 + a[2][2] * s0) * r;
+    mat4 out;
+    for (int c = 0; c < 4; ++c) out.c[c] = vec4(b[0][c], b[1][c], b[2][c], b[3][c]);
+    return out;
+}
+
+// Fragment-stage inputs: one value per pixel of the current fragment.
+struct subpassInput {
+    const float* texels = nullptr;  // 4 floats per pixel
+};
+inline thread_local size_t gl_current_pixel = 0;
+inline vec4 subpassLoad(const subpassInput& s) {
+    const float* t = s.texels + 4 * gl_current_pixel;
+    return vec4(t[0], t[1], t[2], t[3]);
+}
 // row vector times matrix: one dot product per column
 inline vec4 operator*(const vec3& v, const mat4x3& m) {
     return vec4(dot(v, m.c[0]), dot(v, m.c[1]), dot(v, m.c[2]), dot(v, m.c[3]));

@@ -159,6 +159,12 @@ struct vec4 {
         z = c_;
         w = d_;
     }
+    vec4(const vec2& v, float c_, float d_) {
+        x = v.x;
+        y = v.y;
+        z = c_;
+        w = d_;
+    }
     vec4(const vec3& v, float d_) {
         x = v.x;
         y = v.y;
@@ -237,6 +243,7 @@ struct ivec3 {
     ivec3(int s) : x(s), y(s), z(s) {}
     ivec3(int a, int b, int c) : x(a), y(b), z(c) {}
     explicit ivec3(const vec3& v) : x((int)v.x), y((int)v.y), z((int)v.z) {}
+    explicit ivec3(const struct uvec3& v);
 };
 struct bvec3 {
     bool x, y, z;

@@ -39,6 +39,10 @@ def lib():
         L.ref_pbr.argtypes = [C.c_void_p] * 5 + [C.c_float, C.c_float, C.c_void_p]
         L.ref_sky.argtypes = [C.c_void_p] * 4 + [C.c_float, C.c_int, C.c_void_p]
         L.ref_probes_update.argtypes = [C.POINTER(GridDesc), C.c_void_p, C.c_uint32] + [C.c_void_p] * 5
+        L.ref_init_probes.argtypes = [C.POINTER(GridDesc), C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_int]
+        L.ref_final_gather.argtypes = ([C.POINTER(GridDesc)] + [C.c_void_p] * 5 + [C.c_int, C.c_int] +
+                                       [C.c_void_p] * 9 + [C.c_int])
         L.ref_trace_probes.argtypes = ([C.POINTER(GridDesc)] + [C.c_void_p] * 7 + [C.c_uint32] + [C.c_void_p] * 4 +
                                        [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p] + [C.c_void_p] * 3 + [C.c_int])
         _lib = L
@@ -136,3 +140,34 @@ def trace_probes(oracle, scene, grid, light, orientation, probe_list, states, co
                            _ptr(f32(np.asarray(orientation).reshape(9))), _ptr(lst), n, trace_fn,
                            C.c_void_p(oracle._h), _ptr(rays), _ptr(rec), _ptr(dimg), int(threads))
     return rays, rec, dimg
+
+
+def init_probes(oracle, scene, grid, orientation, threads=16):
+    """The reference's probe classification (probesInit.rgen with its miss
+    and back-face closest-hit stages), hits found by the oracle's traversal:
+    one state per probe (0 off, 1 near geometry, 8)."""
+    from oracle.oracle import Oracle
+
+    states = np.zeros(grid.probe_count(), np.uint32)
+    trace_fn = C.cast(Oracle.lib().oracle_trace, C.c_void_p)
+    lib().ref_init_probes(C.byref(grid), _ptr(np.ascontiguousarray(scene.instances)), len(scene.instances),
+                          _ptr(f32(np.asarray(orientation).reshape(9))), trace_fn, C.c_void_p(oracle._h),
+                          _ptr(states), int(threads))
+    return states
+
+
+def final_gather(grid, light, states, color, depth, gbuffer, view, proj, threads=16):
+    """The reference's FinalGather.frag over an H x W G-buffer (dict of
+    float32 arrays position_depth, normal_metalness, albedo_roughness,
+    emissive, direct_light (.r used), reflection: H x W x 4); view, proj:
+    4x4 row-major matrices (world to view, view to clip).  Returns
+    H x W x 4."""
+    h, w = gbuffer["position_depth"].shape[:2]
+    ins = [f32(gbuffer[k]) for k in ("position_depth", "normal_metalness", "albedo_roughness", "emissive",
+                                      "direct_light", "reflection")]
+    out = np.zeros((h, w, 4), np.float32)
+    lib().ref_final_gather(C.byref(grid), _ptr(f32(light.direction[:])), _ptr(f32(light.color[:])),
+                           _ptr(np.ascontiguousarray(states, np.uint32)), _ptr(f32(color)), _ptr(f32(depth)), w, h,
+                           *[_ptr(a) for a in ins], _ptr(f32(np.asarray(view).T)), _ptr(f32(np.asarray(proj).T)),
+                           _ptr(out), int(threads))
+    return out

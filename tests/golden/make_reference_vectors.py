@@ -26,6 +26,15 @@ Cases (inputs seeded, numpy's legacy RandomState, whose streams are fixed):
   listed (the trace writes direction row i from the launch of list
   position i).
 
+* the probe classification (probesInit.rgen with probeInitMiss.rmiss and
+  backfaceTest.rchit): the room at 4x3x4 probes and 64 rays, the editor
+  scene at 6x3x6 and 96 rays (512 rays per probe, directions past
+  raysPerProbe degenerate, as the shader has them);
+* the final gather (FinalGather.frag) of a 16 x 16 G-buffer against the
+  room's updated atlas: random surface points, a quarter of the pixels sky,
+  a camera at an exact position (so inverse(view) is exact) and a
+  perspective projection.
+
 Atlases are reference-format (R11G11B10F colour, RG16F depth) and stored as
 float16, which holds every value of both formats exactly.
 
@@ -210,6 +219,73 @@ def trace(rng, out):
     Oracle.set_sky_mode(abi.SKY_CONSTANT)
 
 
+def probe_init(rng, out):
+    from oracle import ref_glsl as ref
+    from oracle.oracle import Oracle
+    from vulkanexp_gb300 import ingest, scenes
+    room = scenes.Scene(*[out["trace_room_" + f] for f in ("vertices", "indices", "meshes", "instances", "offsets",
+                                                           "materials")])
+    room.bounds = (np.zeros(3), np.array([10.0, 6.0, 10.0]))
+    editor = ingest.load(os.path.join(HERE, "editor_room.scene"))
+    for name, sc, res, R in (("room", room, (4, 3, 4), 64), ("editor", editor, (6, 3, 6), 96)):
+        g = scenes.fit_grid(sc, res, R)
+        orient = scenes.random_orientation(int(rng.randint(0, 1 << 30)), 0).astype(np.float32)
+        o = Oracle(sc)
+        out["init_%s_grid" % name] = grid_words(g)
+        out["init_%s_orientation" % name] = orient.reshape(9)
+        out["init_%s_states" % name] = ref.init_probes(o, sc, g, orient)
+        o.close()
+
+
+def gather_camera():
+    """World-to-view (a translation to an exact camera position) and a
+    perspective projection, row-major."""
+    cam = np.array([4.25, 3.5, 2.0], np.float32)
+    view = np.eye(4, dtype=np.float32)
+    view[:3, 3] = -cam
+    proj = np.zeros((4, 4), np.float32)
+    proj[0, 0], proj[1, 1] = 1.0 / np.tan(0.5), 1.0 / np.tan(0.5)
+    proj[2, 2], proj[2, 3], proj[3, 2] = 100.0 / (0.1 - 100.0), 10.0 / (0.1 - 100.0), -1.0
+    return cam, view, proj
+
+
+def final_gather(rng, out):
+    from oracle import ref_glsl as ref
+    W = H = 16
+    N = W * H
+    g = grid_from_words(out["trace_room_grid"])
+    L = light_from_words(out["trace_room_light"])
+    color = np.zeros(out["trace_room_color_out"].shape[:2] + (4,), np.float32)
+    color[..., :3] = out["trace_room_color_out"].astype(np.float32)
+    color[..., 3] = 1.0
+    depth = out["trace_room_depth_out"].astype(np.float32)
+    states = out["trace_room_states_out"]
+    pos = rng.uniform([0.2, 0.2, 0.2], [9.8, 5.8, 9.8], (N, 3))
+    dist = rng.uniform(0.5, 10, N)
+    dist[rng.uniform(size=N) < 0.25] = 0.0  # sky
+    gb = {"position_depth": np.concatenate([pos, dist[:, None]], 1),
+          "normal_metalness": np.concatenate([rng.normal(size=(N, 3)), rng.uniform(0, 1, (N, 1))], 1),
+          "albedo_roughness": np.concatenate([rng.uniform(0, 1, (N, 3)), rng.uniform(0.05, 1, (N, 1))], 1),
+          "emissive": np.concatenate([rng.uniform(0, 0.2, (N, 3)), np.zeros((N, 1))], 1),
+          "direct_light": np.concatenate([(rng.uniform(size=(N, 1)) > 0.3), np.zeros((N, 3))], 1),
+          "reflection": np.concatenate([rng.uniform(0, 1, (N, 3)), np.ones((N, 1))], 1)}
+    gb = {k: v.astype(np.float32).reshape(H, W, 4) for k, v in gb.items()}
+    cam, view, proj = gather_camera()
+    for k, v in gb.items():
+        out["gather_" + k] = v
+    out["gather_out"] = ref.final_gather(g, L, states, color, depth, gb, view, proj)
+
+
+def grid_from_words(words):
+    from vulkanexp_gb300 import abi
+    return abi.GridDesc.from_buffer_copy(np.ascontiguousarray(words, np.uint32).tobytes())
+
+
+def light_from_words(words):
+    from vulkanexp_gb300 import abi
+    return abi.Light.from_buffer_copy(np.ascontiguousarray(words, np.float32).tobytes())
+
+
 def main(reference_root):
     from oracle import build_ref_glsl
     from oracle.oracle import build_oracle
@@ -221,6 +297,8 @@ def main(reference_root):
     helpers(rng, out)
     update_passes(rng, out)
     trace(rng, out)
+    probe_init(rng, out)
+    final_gather(rng, out)
     np.savez_compressed(OUT, **out)
     print(OUT, "%d arrays, %d bytes" % (len(out), os.path.getsize(OUT)))
 

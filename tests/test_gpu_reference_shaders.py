@@ -19,13 +19,18 @@ atlas, probe states, orientation and probe list.  Bars:
   at most 1 % of texels not bit-identical; probe states equal;
 * the passes alone (ddgi_blend_records on the fixture's records): the same
   atlas bars, states equal; at 192 rays depth only (the reference's
-  irradiance pass loads 36 directions, probesUpdate.glsl:63-68)."""
+  irradiance pass loads 36 directions, probesUpdate.glsl:63-68);
+* probe classification (ddgi_init_probes against probesInit.rgen): every
+  state equal;
+* final gather (ddgi_final_gather against FinalGather.frag, on the room's
+  updated atlas): surface pixels within 1e-5 relative, sky pixels within
+  1e-4 (the view direction is the camera ray computed in double)."""
 import os
 
 import numpy as np
 import pytest
 
-from test_reference_shaders import atlas_from, format_steps, grid_from, light_from, rel, room_scene
+from test_reference_shaders import atlas_from, format_steps, gather_inputs, grid_from, light_from, rel, room_scene
 from vulkanexp_gb300 import abi, ingest
 from vulkanexp_gb300.ddgi import Context
 
@@ -111,4 +116,41 @@ def test_passes_against_reference_shaders(gpu_lib, vec, R):
         for ch in range(2):
             assert format_steps(dd[..., ch], rd[..., ch], 10).max() <= 2.0 + 1e-9
         assert (dd != rd).any(axis=-1).mean() <= 0.01
+    ctx.close()
+
+
+@pytest.mark.parametrize("name", ["room", "editor"])
+def test_probe_classification_against_reference_shaders(gpu_lib, vec, name):
+    sc = room_scene(vec) if name == "room" else ingest.load(os.path.join(GOLDEN, "editor_room.scene"))
+    g = grid_from(vec["init_%s_grid" % name])
+    ctx = Context(g)
+    ctx.build_scene(sc)
+    ctx.init_probes(vec["init_%s_orientation" % name])
+    st = ctx.get_probe_states()
+    ref = vec["init_%s_states" % name]
+    assert (st == ref).all(), "%d of %d probe states differ" % ((st != ref).sum(), len(st))
+    ctx.close()
+
+
+def test_final_gather_against_reference_shaders(gpu_lib, vec):
+    import torch
+
+    g, L, c, d, st, gb, cam, sky = gather_inputs(vec)
+    H, W = vec["gather_out"].shape[:2]
+    ctx = Context(g)
+    ctx.set_sky_mode(abi.SKY_ATMOSPHERE)
+    ctx.set_light(L)
+    ctx.set_atlas(abi.ATLAS_COLOR, c)
+    ctx.set_atlas(abi.ATLAS_DEPTH, d)
+    ctx.set_probe_states(st)
+    dev = {k: torch.from_numpy(v.reshape(H, W) if v.ndim == 1 else v.reshape(H, W, 4)).cuda().contiguous()
+           for k, v in gb.items()}
+    out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    ctx.final_gather(dev, cam, out)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().reshape(-1, 4)
+    ref = vec["gather_out"].reshape(-1, 4)
+    r = rel(got[:, :3], ref[:, :3], 1e-3)
+    print("final gather: surface max rel %.2e, sky max rel %.2e" % (r[~sky].max(), r[sky].max()))
+    assert r[~sky].max() <= 1e-5 and r[sky].max() <= 1e-4
     ctx.close()

@@ -15,6 +15,11 @@ The oracle is checked against them here, on CPU:
   the same ray records: reference-format atlases and probe states bit for
   bit (at 192 rays the depth pass only: the reference's irradiance pass
   loads 36 directions, probesUpdate.glsl:63-68);
+* the probe classification (probesInit.rgen + its miss and back-face
+  stages): every state equal;
+* the final gather (FinalGather.frag): surface pixels within 2e-6
+  relative, sky pixels within 2e-5 (the view direction is the fixture's
+  camera ray computed in double, the shader's in float);
 * the probe trace (traceProbes.rgen + closest-hit + miss stages) on the
   same rays: hit distance bit for bit, radiance within 2e-6 relative; then
   the whole update (the oracle's own rays) against the reference's trace +
@@ -191,6 +196,57 @@ def test_whole_update(vec, name):
     assert (st == vec[k + "states_out"]).all()
 
 
+@pytest.mark.parametrize("name", ["room", "editor"])
+def test_probe_classification(vec, name):
+    sc = room_scene(vec) if name == "room" else ingest.load(os.path.join(GOLDEN, "editor_room.scene"))
+    g = grid_from(vec["init_%s_grid" % name])
+    o = Oracle(sc)
+    st = o.init_probes(g, vec["init_%s_orientation" % name])
+    o.close()
+    ref = vec["init_%s_states" % name]
+    assert (st == ref).all(), "%d of %d probe states differ" % ((st != ref).sum(), len(st))
+    assert len(np.unique(ref)) >= 2
+
+
+def gather_inputs(v):
+    """The final-gather case: grid, light, the room's updated atlas and
+    states, the G-buffer as N x 4 arrays (direct light N), and for sky pixels
+    the view direction in position.xyz (the C ABI's convention), computed in
+    double from the fixture's camera."""
+    from golden.make_reference_vectors import gather_camera
+    g, L = grid_from(v["trace_room_grid"]), light_from(v["trace_room_light"])
+    c, d = zero_atlas(g)
+    c[..., :3] = v["trace_room_color_out"].astype(np.float32)
+    c[..., 3] = 1.0
+    d[...] = v["trace_room_depth_out"].astype(np.float32)
+    H, W = v["gather_out"].shape[:2]
+    gb = {k: v["gather_" + k].reshape(-1, 4).copy() for k in ("position_depth", "normal_metalness",
+                                                              "albedo_roughness", "emissive", "reflection")}
+    gb["direct_light"] = v["gather_direct_light"].reshape(-1, 4)[:, 0].copy()
+    cam, view, proj = gather_camera()
+    p = np.arange(H * W)
+    u, w = ((p % W) + 0.5) / W, ((p // W) + 0.5) / H
+    q = (np.linalg.inv(proj.astype(np.float64)) @ np.stack([2 * u - 1, 2 * w - 1, np.zeros_like(u),
+                                                            np.ones_like(u)])).T[:, :3]
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    sky = gb["position_depth"][:, 3] <= 0
+    gb["position_depth"][sky, :3] = (np.linalg.inv(view.astype(np.float64))[:3, :3] @ q.T).T[sky]
+    return g, L, c, d, v["trace_room_states_out"], gb, cam, sky
+
+
+def test_final_gather(vec):
+    g, L, c, d, st, gb, cam, sky = gather_inputs(vec)
+    Oracle.set_sky_mode(abi.SKY_ATMOSPHERE)
+    try:
+        out = Oracle.final_gather(g, L, st, c, d, gb, cam)
+    finally:
+        Oracle.set_sky_mode(abi.SKY_CONSTANT)
+    ref = vec["gather_out"].reshape(-1, 4)
+    r = rel(out[:, :3], ref[:, :3], 1e-3)
+    assert r[~sky].max() <= 2e-6 and r[sky].max() <= 2e-5
+    assert 0.1 < sky.mean() < 0.5
+
+
 def test_fixture_scene_is_current(vec):
     """The stored room is what the trace saw (its arrays are in the
     fixture), and the editor scene file still loads to the same arrays."""
@@ -276,3 +332,13 @@ def test_live_trace_and_update():
     finally:
         Oracle.set_sky_mode(abi.SKY_CONSTANT)
         o.close()
+
+
+def test_live_probe_classification():
+    ref = _ref()
+    w = scenes.terrain_workload(3, resolution=(8, 4, 8), rays=128, n_instances=60, boxes_per_cluster=200, cells=64)
+    o = Oracle(w.scene)
+    for k in range(2):
+        a = ref.init_probes(o, w.scene, w.grid, w.orientation(k))
+        assert (a == o.init_probes(w.grid, w.orientation(k))).all()
+    o.close()
