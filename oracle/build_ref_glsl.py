@@ -5,7 +5,11 @@ pbrMetallicRoughness.glsl, sky.glsl) compile over oracle/glsl_shim.hpp; the
 probe-update compute passes (probesUpdate.glsl as probesUpdateIrradiance.comp
 and probesUpdateDepth.comp include it, and probesCopyBorders.comp) compile
 over oracle/glsl_compute.hpp, which runs a dispatch's workgroups with one
-thread per invocation.
+thread per invocation; the ray-tracing stages (probe trace, probe
+classification) over oracle/glsl_rt.hpp; FinalGather.frag once per pixel.
+The host-side probe selection (IrradianceProbes::selectProbesToUpdate) is
+copied out of src/IrradianceProbes.cpp as written and compiled inside a
+stand-in class (oracle/ref_host_select.cpp).
 
 Recipe: the files are copied from the reference tree into oracle/_ref/glsl/
 with their `#version` and `#extension` lines removed and their resource
@@ -82,6 +86,21 @@ def translate(text):
     return text
 
 
+def extract_function(text, signature):
+    """The definition that starts with `signature` in a C++ source text, up to
+    its matching closing brace."""
+    start = text.index(signature)
+    depth, i = 0, text.index("{", start)
+    while True:
+        if text[i] == "{":
+            depth += 1
+        elif text[i] == "}":
+            depth -= 1
+            if depth == 0:
+                return text[start:i + 1] + "\n"
+        i += 1
+
+
 def build(reference_root):
     """Builds the library from the shader files under `reference_root`;
     returns its path, or None when the reference tree is absent."""
@@ -96,8 +115,22 @@ def build(reference_root):
         text = translate(text)
         with open(os.path.join(glsl_dir, f), "w") as fh:
             fh.write(text)
+    # the reference's host-side probe selection, its definition as written
+    src_out = os.path.join(OUT, "src")
+    os.makedirs(src_out, exist_ok=True)
+    with open(os.path.join(reference_root, "src", "IrradianceProbes.cpp")) as fh:
+        fn = extract_function(fh.read(), "uint32_t IrradianceProbes::selectProbesToUpdate()")
+    with open(os.path.join(src_out, "selectProbesToUpdate.inc"), "w") as fh:
+        fh.write(fn)
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fsingle-precision-constant", "-ffp-contract=off",
-           "-w", "-I", HERE, "-I", glsl_dir, "-o", LIB + ".tmp"] + [os.path.join(HERE, s) for s in SOURCES]
+           "-w", "-I", HERE, "-I", glsl_dir, "-I", src_out, "-o", LIB + ".tmp"] + [os.path.join(HERE, s) for s in SOURCES]
+    # the host selection is plain C++: no single-precision literals there
+    host = os.path.join(OUT, "ref_host_select.o")
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-c", "-w", "-I", src_out, "-o", host,
+                        os.path.join(HERE, "ref_host_select.cpp")], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference selection build failed:\n" + r.stdout + r.stderr)
+    cmd.append(host)
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("reference shader build failed:\n" + r.stdout + r.stderr)

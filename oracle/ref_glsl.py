@@ -43,6 +43,7 @@ def lib():
                                       C.c_void_p, C.c_void_p, C.c_int]
         L.ref_final_gather.argtypes = ([C.POINTER(GridDesc)] + [C.c_void_p] * 5 + [C.c_int, C.c_int] +
                                        [C.c_void_p] * 9 + [C.c_int])
+        L.ref_select_sequence.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32] + [C.c_void_p] * 4
         L.ref_trace_probes.argtypes = ([C.POINTER(GridDesc)] + [C.c_void_p] * 7 + [C.c_uint32] + [C.c_void_p] * 4 +
                                        [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p] + [C.c_void_p] * 3 + [C.c_int])
         _lib = L
@@ -171,3 +172,18 @@ def final_gather(grid, light, states, color, depth, gbuffer, view, proj, threads
                            *[_ptr(a) for a in ins], _ptr(f32(np.asarray(view).T)), _ptr(f32(np.asarray(proj).T)),
                            _ptr(out), int(threads))
     return out
+
+
+def select_sequence(states, caps):
+    """K successive calls of the reference's selectProbesToUpdate (its own
+    source) on one object: states K x n, caps K (0 = no cap).  Returns the K
+    lists and the offsets each call leaves.  Its loop index is a
+    function-local static: a process's calls form one sequence."""
+    states = np.ascontiguousarray(states, np.uint32)
+    K, n = states.shape
+    caps = np.ascontiguousarray(caps, np.uint32)
+    lists = np.zeros((K, n), np.uint32)
+    counts = np.zeros(K, np.uint32)
+    offsets = np.zeros(K, np.uint32)
+    lib().ref_select_sequence(_ptr(states), n, K, _ptr(caps), _ptr(lists), _ptr(counts), _ptr(offsets))
+    return [lists[k, :counts[k]].copy() for k in range(K)], offsets

@@ -35,6 +35,10 @@ Cases (inputs seeded, numpy's legacy RandomState, whose streams are fixed):
   a camera at an exact position (so inverse(view) is exact) and a
   perspective projection.
 
+* the probe selection (IrradianceProbes::selectProbesToUpdate, the
+  reference's own C++ compiled from its source): 16 successive selections
+  over 108 probes with random states (0 to 8) and caps 0 (none) to 100.
+
 Atlases are reference-format (R11G11B10F colour, RG16F depth) and stored as
 float16, which holds every value of both formats exactly.
 
@@ -286,6 +290,22 @@ def light_from_words(words):
     return abi.Light.from_buffer_copy(np.ascontiguousarray(words, np.float32).tobytes())
 
 
+def selection(rng, out):
+    from oracle import ref_glsl as ref
+    K, n = 16, 108
+    states = rng.randint(0, 9, (K, n)).astype(np.uint32)
+    caps = np.array([0, 40, 17, 0, 5, 60, 0, 1, 30, 0, 100, 7, 0, 25, 0, 50], np.uint32)
+    lists, offsets = ref.select_sequence(states, caps)
+    padded = np.full((K, n), 0xFFFFFFFF, np.uint32)
+    for k, l in enumerate(lists):
+        padded[k, :len(l)] = l
+    out["sel_states"] = states
+    out["sel_caps"] = caps
+    out["sel_lists"] = padded
+    out["sel_counts"] = np.array([len(l) for l in lists], np.uint32)
+    out["sel_offsets"] = offsets
+
+
 def main(reference_root):
     from oracle import build_ref_glsl
     from oracle.oracle import build_oracle
@@ -299,6 +319,7 @@ def main(reference_root):
     trace(rng, out)
     probe_init(rng, out)
     final_gather(rng, out)
+    selection(rng, out)
     np.savez_compressed(OUT, **out)
     print(OUT, "%d arrays, %d bytes" % (len(out), os.path.getsize(OUT)))
 

@@ -22,6 +22,9 @@ atlas, probe states, orientation and probe list.  Bars:
   irradiance pass loads 36 directions, probesUpdate.glsl:63-68);
 * probe classification (ddgi_init_probes against probesInit.rgen): every
   state equal;
+* probe selection (ddgi_update_scheduled against the reference's
+  selectProbesToUpdate): the 16-call sequence's lists, each call's states
+  set before it;
 * final gather (ddgi_final_gather against FinalGather.frag, on the room's
   updated atlas): surface pixels within 1e-5 relative, sky pixels within
   1e-4 (the view direction is the camera ray computed in double)."""
@@ -153,4 +156,21 @@ def test_final_gather_against_reference_shaders(gpu_lib, vec):
     r = rel(got[:, :3], ref[:, :3], 1e-3)
     print("final gather: surface max rel %.2e, sky max rel %.2e" % (r[~sky].max(), r[sky].max()))
     assert r[~sky].max() <= 1e-5 and r[sky].max() <= 1e-4
+    ctx.close()
+
+
+def test_probe_selection_against_reference(gpu_lib, vec):
+    from vulkanexp_gb300 import scenes
+    sc = ingest.load(os.path.join(GOLDEN, "editor_room.scene"))
+    g = scenes.fit_grid(sc, (6, 3, 6), 32)
+    assert g.probe_count() == vec["sel_states"].shape[1]
+    ctx = Context(g)
+    ctx.build_scene(sc)
+    ctx.set_light(scenes.default_light())
+    for k in range(len(vec["sel_caps"])):
+        ctx.set_probe_states(vec["sel_states"][k])
+        ctx.update_scheduled(scenes.random_orientation(9, k), int(vec["sel_caps"][k]))
+        s = ctx.schedule()
+        assert np.array_equal(s["list"], vec["sel_lists"][k, :vec["sel_counts"][k]]), k
+        assert s["offset"] == vec["sel_offsets"][k], k
     ctx.close()

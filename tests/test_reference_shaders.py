@@ -17,6 +17,9 @@ The oracle is checked against them here, on CPU:
   loads 36 directions, probesUpdate.glsl:63-68);
 * the probe classification (probesInit.rgen + its miss and back-face
   stages): every state equal;
+* the probe selection (IrradianceProbes::selectProbesToUpdate, the
+  reference's C++ compiled from its source): every list and offset of a
+  16-call sequence;
 * the final gather (FinalGather.frag): surface pixels within 2e-6
   relative, sky pixels within 2e-5 (the view direction is the fixture's
   camera ray computed in double, the shader's in float);
@@ -245,6 +248,18 @@ def test_final_gather(vec):
     r = rel(out[:, :3], ref[:, :3], 1e-3)
     assert r[~sky].max() <= 2e-6 and r[sky].max() <= 2e-5
     assert 0.1 < sky.mean() < 0.5
+
+
+def test_probe_selection(vec):
+    """IrradianceProbes::selectProbesToUpdate, the reference's C++ compiled
+    from its source: 16 successive selections with changing states and caps
+    equal the restatement's, list and offset."""
+    from oracle.oracle import select_probes
+    off, loop = 0, 0
+    for k in range(len(vec["sel_caps"])):
+        picked, off, loop = select_probes(vec["sel_states"][k], off, loop, int(vec["sel_caps"][k]))
+        assert np.array_equal(picked, vec["sel_lists"][k, :vec["sel_counts"][k]]), k
+        assert off == vec["sel_offsets"][k], k
 
 
 def test_fixture_scene_is_current(vec):
