@@ -162,21 +162,32 @@ public:
 
     ddgi_ctx* context() const { return _ctx; }
 
+    // genBasis (src/IrradianceProbes.cpp:347-355) in float with GLM's
+    // operation order: b1 = (n.x > 0.9 ? y : x) - n dot(b1, n), normalised
+    // as b1 * (1 / sqrt(dot(b1, b1))), b2 = cross(n, b1); dot sums left to
+    // right.
+    static void genBasis(const float n[3], float b1[3], float b2[3]) {
+        b1[0] = n[0] > 0.9f ? 0.0f : 1.0f;
+        b1[1] = n[0] > 0.9f ? 1.0f : 0.0f;
+        b1[2] = 0.0f;
+        const float d = b1[0] * n[0] + b1[1] * n[1] + b1[2] * n[2];
+        for (int k = 0; k < 3; ++k) b1[k] -= n[k] * d;
+        const float il = 1.0f / std::sqrt(b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2]);
+        for (int k = 0; k < 3; ++k) b1[k] *= il;
+        b2[0] = n[1] * b1[2] - b1[1] * n[2];
+        b2[1] = n[2] * b1[0] - b1[2] * n[0];
+        b2[2] = n[0] * b1[1] - b1[0] * n[1];
+    }
+
     // A rotation as the reference draws one: Z uniform on the unit sphere,
-    // genBasis (src/IrradianceProbes.cpp:347-355), rows X, Y, Z of
-    // transpose(mat3(X, Y, Z)).
+    // genBasis, rows X, Y, Z of transpose(mat3(X, Y, Z)).
     void randomOrientation(float m[9]) {
         std::uniform_real_distribution<double> u(-1.0, 1.0), a(0.0, 6.283185307179586);
         const double z = u(_rng), phi = a(_rng);
         const double r = std::sqrt(z * z < 1.0 ? 1.0 - z * z : 0.0);
         const float Z[3] = {(float)(r * std::cos(phi)), (float)(r * std::sin(phi)), (float)z};
-        float X[3] = {0.0f, 0.0f, 0.0f};
-        X[Z[0] > 0.9f ? 1 : 0] = 1.0f;
-        const float d = X[0] * Z[0] + X[1] * Z[1] + X[2] * Z[2];
-        for (int k = 0; k < 3; ++k) X[k] -= Z[k] * d;
-        const float l = std::sqrt(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]);
-        for (int k = 0; k < 3; ++k) X[k] /= l;
-        const float Y[3] = {Z[1] * X[2] - Z[2] * X[1], Z[2] * X[0] - Z[0] * X[2], Z[0] * X[1] - Z[1] * X[0]};
+        float X[3], Y[3];
+        genBasis(Z, X, Y);
         for (int k = 0; k < 3; ++k) {
             m[k] = X[k];
             m[3 + k] = Y[k];

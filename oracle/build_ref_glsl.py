@@ -9,7 +9,8 @@ thread per invocation; the ray-tracing stages (probe trace, probe
 classification) over oracle/glsl_rt.hpp; FinalGather.frag once per pixel.
 The host-side probe selection (IrradianceProbes::selectProbesToUpdate) is
 copied out of src/IrradianceProbes.cpp as written and compiled inside a
-stand-in class (oracle/ref_host_select.cpp).
+stand-in class (oracle/ref_host_select.cpp), and genBasis with the
+reference's vendored GLM (oracle/ref_host_basis.cpp).
 
 Recipe: the files are copied from the reference tree into oracle/_ref/glsl/
 with their `#version` and `#extension` lines removed and their resource
@@ -119,18 +120,23 @@ def build(reference_root):
     src_out = os.path.join(OUT, "src")
     os.makedirs(src_out, exist_ok=True)
     with open(os.path.join(reference_root, "src", "IrradianceProbes.cpp")) as fh:
-        fn = extract_function(fh.read(), "uint32_t IrradianceProbes::selectProbesToUpdate()")
+        text = fh.read()
+    fn = extract_function(text, "uint32_t IrradianceProbes::selectProbesToUpdate()")
     with open(os.path.join(src_out, "selectProbesToUpdate.inc"), "w") as fh:
         fh.write(fn)
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fsingle-precision-constant", "-ffp-contract=off",
            "-w", "-I", HERE, "-I", glsl_dir, "-I", src_out, "-o", LIB + ".tmp"] + [os.path.join(HERE, s) for s in SOURCES]
-    # the host selection is plain C++: no single-precision literals there
-    host = os.path.join(OUT, "ref_host_select.o")
-    r = subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-c", "-w", "-I", src_out, "-o", host,
-                        os.path.join(HERE, "ref_host_select.cpp")], capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("reference selection build failed:\n" + r.stdout + r.stderr)
-    cmd.append(host)
+    # and its genBasis, over the reference's vendored GLM
+    with open(os.path.join(src_out, "genBasis.inc"), "w") as fh:
+        fh.write(extract_function(text, "void genBasis(const glm::vec3& n, glm::vec3& b1, glm::vec3& b2)"))
+    # the host functions are plain C++: no single-precision literals there
+    for name, extra in (("ref_host_select", []), ("ref_host_basis", ["-I", os.path.join(reference_root, "ext", "glm")])):
+        obj = os.path.join(OUT, name + ".o")
+        r = subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-c", "-w", "-ffp-contract=off", "-I", src_out] + extra +
+                           ["-o", obj, os.path.join(HERE, name + ".cpp")], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("reference host build failed:\n" + r.stdout + r.stderr)
+        cmd.append(obj)
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("reference shader build failed:\n" + r.stdout + r.stderr)

@@ -44,6 +44,7 @@ def lib():
         L.ref_final_gather.argtypes = ([C.POINTER(GridDesc)] + [C.c_void_p] * 5 + [C.c_int, C.c_int] +
                                        [C.c_void_p] * 9 + [C.c_int])
         L.ref_select_sequence.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32] + [C.c_void_p] * 4
+        L.ref_gen_basis.argtypes = [C.c_void_p] * 3
         L.ref_trace_probes.argtypes = ([C.POINTER(GridDesc)] + [C.c_void_p] * 7 + [C.c_uint32] + [C.c_void_p] * 4 +
                                        [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p] + [C.c_void_p] * 3 + [C.c_int])
         _lib = L
@@ -187,3 +188,10 @@ def select_sequence(states, caps):
     offsets = np.zeros(K, np.uint32)
     lib().ref_select_sequence(_ptr(states), n, K, _ptr(caps), _ptr(lists), _ptr(counts), _ptr(offsets))
     return [lists[k, :counts[k]].copy() for k in range(K)], offsets
+
+
+def gen_basis(n):
+    """The reference's genBasis (its source over its vendored GLM): b1, b2."""
+    b1, b2 = np.zeros(3, np.float32), np.zeros(3, np.float32)
+    lib().ref_gen_basis(_ptr(f32(n)), _ptr(b1), _ptr(b2))
+    return b1, b2

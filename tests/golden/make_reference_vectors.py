@@ -39,6 +39,10 @@ Cases (inputs seeded, numpy's legacy RandomState, whose streams are fixed):
   reference's own C++ compiled from its source): 16 successive selections
   over 108 probes with random states (0 to 8) and caps 0 (none) to 100.
 
+* genBasis (src/IrradianceProbes.cpp:347-355, compiled from its source
+  over the reference's vendored GLM): 300 random unit vectors and the
+  branch's edge (n.x at and around 0.9, the axes).
+
 Atlases are reference-format (R11G11B10F colour, RG16F depth) and stored as
 float16, which holds every value of both formats exactly.
 
@@ -306,6 +310,20 @@ def selection(rng, out):
     out["sel_offsets"] = offsets
 
 
+def basis(rng, out):
+    from oracle import ref_glsl as ref
+    n = unit(rng, 300)
+    edge = []
+    for x in (0.9, np.nextafter(np.float32(0.9), np.float32(1)), np.nextafter(np.float32(0.9), np.float32(0)), 0.95,
+              -0.9):
+        r = np.sqrt(1 - np.float64(x) ** 2)
+        edge.append([x, r * 0.6, r * 0.8])
+    edge += [[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]]
+    n = np.concatenate([n, np.asarray(edge, np.float32)]).astype(np.float32)
+    out["basis_in"] = n
+    out["basis_out"] = np.stack([np.concatenate(ref.gen_basis(v)) for v in n])
+
+
 def main(reference_root):
     from oracle import build_ref_glsl
     from oracle.oracle import build_oracle
@@ -320,6 +338,7 @@ def main(reference_root):
     probe_init(rng, out)
     final_gather(rng, out)
     selection(rng, out)
+    basis(rng, out)
     np.savez_compressed(OUT, **out)
     print(OUT, "%d arrays, %d bytes" % (len(out), os.path.getsize(OUT)))
 

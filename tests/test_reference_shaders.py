@@ -19,7 +19,8 @@ The oracle is checked against them here, on CPU:
   stages): every state equal;
 * the probe selection (IrradianceProbes::selectProbesToUpdate, the
   reference's C++ compiled from its source): every list and offset of a
-  16-call sequence;
+  16-call sequence; genBasis (the reference's over its vendored GLM) against
+  the C++ facade's, bit for bit;
 * the final gather (FinalGather.frag): surface pixels within 2e-6
   relative, sky pixels within 2e-5 (the view direction is the fixture's
   camera ray computed in double, the shader's in float);
@@ -260,6 +261,20 @@ def test_probe_selection(vec):
         picked, off, loop = select_probes(vec["sel_states"][k], off, loop, int(vec["sel_caps"][k]))
         assert np.array_equal(picked, vec["sel_lists"][k, :vec["sel_counts"][k]]), k
         assert off == vec["sel_offsets"][k], k
+
+
+def test_gen_basis(vec, tmp_path):
+    """The facade's genBasis (include/irradiance_probes.hpp) compiled here
+    equals the reference's genBasis over its vendored GLM, bit for bit."""
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "gen_basis")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(root, "include"),
+                    os.path.join(root, "tests", "native", "gen_basis.cpp"), "-o", exe], check=True)
+    r = subprocess.run([exe], input=np.ascontiguousarray(vec["basis_in"], np.float32).tobytes(), capture_output=True,
+                       check=True)
+    got = np.frombuffer(r.stdout, np.float32).reshape(-1, 6)
+    assert (got.view(np.uint32) == vec["basis_out"].view(np.uint32)).all()
 
 
 def test_fixture_scene_is_current(vec):
