@@ -9,8 +9,9 @@ thread per invocation; the ray-tracing stages (probe trace, probe
 classification) over oracle/glsl_rt.hpp; FinalGather.frag once per pixel.
 The host-side probe selection (IrradianceProbes::selectProbesToUpdate) is
 copied out of src/IrradianceProbes.cpp as written and compiled inside a
-stand-in class (oracle/ref_host_select.cpp), and genBasis with the
-reference's vendored GLM (oracle/ref_host_basis.cpp).
+stand-in class (oracle/ref_host_select.cpp), the hysteresis ramp block of
+update() in a stand-in member function (oracle/ref_host_ramp.cpp), and
+genBasis with the reference's vendored GLM (oracle/ref_host_basis.cpp).
 
 Recipe: the files are copied from the reference tree into oracle/_ref/glsl/
 with their `#version` and `#extension` lines removed and their resource
@@ -126,11 +127,17 @@ def build(reference_root):
         fh.write(fn)
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fsingle-precision-constant", "-ffp-contract=off",
            "-w", "-I", HERE, "-I", glsl_dir, "-I", src_out, "-o", LIB + ".tmp"] + [os.path.join(HERE, s) for s in SOURCES]
+    # the hysteresis ramp of update(), the block as written
+    a = text.index("	static uint32_t updatedProbes = 0;")
+    b = text.index("updatedProbes += probeCount;", a) + len("updatedProbes += probeCount;")
+    with open(os.path.join(src_out, "hysteresisRamp.inc"), "w") as fh:
+        fh.write(text[a:b] + "\n")
     # and its genBasis, over the reference's vendored GLM
     with open(os.path.join(src_out, "genBasis.inc"), "w") as fh:
         fh.write(extract_function(text, "void genBasis(const glm::vec3& n, glm::vec3& b1, glm::vec3& b2)"))
     # the host functions are plain C++: no single-precision literals there
-    for name, extra in (("ref_host_select", []), ("ref_host_basis", ["-I", os.path.join(reference_root, "ext", "glm")])):
+    for name, extra in (("ref_host_select", []), ("ref_host_ramp", []),
+                        ("ref_host_basis", ["-I", os.path.join(reference_root, "ext", "glm")])):
         obj = os.path.join(OUT, name + ".o")
         r = subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-c", "-w", "-ffp-contract=off", "-I", src_out] + extra +
                            ["-o", obj, os.path.join(HERE, name + ".cpp")], capture_output=True, text=True)

@@ -45,6 +45,8 @@ def lib():
                                        [C.c_void_p] * 9 + [C.c_int])
         L.ref_select_sequence.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32] + [C.c_void_p] * 4
         L.ref_gen_basis.argtypes = [C.c_void_p] * 3
+        L.ref_ramp_sequence.argtypes = [C.c_float, C.c_float, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
+                                        C.c_void_p]
         L.ref_trace_probes.argtypes = ([C.POINTER(GridDesc)] + [C.c_void_p] * 7 + [C.c_uint32] + [C.c_void_p] * 4 +
                                        [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p] + [C.c_void_p] * 3 + [C.c_int])
         _lib = L
@@ -195,3 +197,15 @@ def gen_basis(n):
     b1, b2 = np.zeros(3, np.float32), np.zeros(3, np.float32)
     lib().ref_gen_basis(_ptr(f32(n)), _ptr(b1), _ptr(b2))
     return b1, b2
+
+
+def ramp_sequence(h0, target, P, counts):
+    """The reference's hysteresis ramp (its own block of update()) over
+    updates of counts[k] probes: (uploaded value per update,
+    GridParameters.hysteresis after it).  Its counter is a function-local
+    static: a process's calls form one sequence."""
+    counts = np.ascontiguousarray(counts, np.uint32)
+    u = np.zeros(len(counts), np.float32)
+    p = np.zeros(len(counts), np.float32)
+    lib().ref_ramp_sequence(float(h0), float(target), int(P), _ptr(counts), len(counts), _ptr(u), _ptr(p))
+    return u, p

@@ -43,6 +43,10 @@ Cases (inputs seeded, numpy's legacy RandomState, whose streams are fixed):
   over the reference's vendored GLM): 300 random unit vectors and the
   branch's edge (n.x at and around 0.9, the axes).
 
+* the hysteresis ramp (the block of IrradianceProbes::update at
+  src/IrradianceProbes.cpp:462-476, compiled from its source): 80 updates
+  of 0 to 48 probes on a 48-probe grid from hysteresis 0 towards 0.98.
+
 Atlases are reference-format (R11G11B10F colour, RG16F depth) and stored as
 float16, which holds every value of both formats exactly.
 
@@ -324,6 +328,16 @@ def basis(rng, out):
     out["basis_out"] = np.stack([np.concatenate(ref.gen_basis(v)) for v in n])
 
 
+def ramp(rng, out):
+    from oracle import ref_glsl as ref
+    counts = rng.randint(0, 49, 80).astype(np.uint32)
+    counts[:10] = 48
+    u, p = ref.ramp_sequence(0.0, 0.98, 48, counts)
+    out["ramp_counts"] = counts
+    out["ramp_uniform"] = u
+    out["ramp_param"] = p
+
+
 def main(reference_root):
     from oracle import build_ref_glsl
     from oracle.oracle import build_oracle
@@ -339,6 +353,7 @@ def main(reference_root):
     final_gather(rng, out)
     selection(rng, out)
     basis(rng, out)
+    ramp(rng, out)
     np.savez_compressed(OUT, **out)
     print(OUT, "%d arrays, %d bytes" % (len(out), os.path.getsize(OUT)))
 

@@ -20,7 +20,8 @@ The oracle is checked against them here, on CPU:
 * the probe selection (IrradianceProbes::selectProbesToUpdate, the
   reference's C++ compiled from its source): every list and offset of a
   16-call sequence; genBasis (the reference's over its vendored GLM) against
-  the C++ facade's, bit for bit;
+  the C++ facade's, bit for bit; the hysteresis ramp of update() against
+  the restatement that the GPU ramp tests use, bit for bit;
 * the final gather (FinalGather.frag): surface pixels within 2e-6
   relative, sky pixels within 2e-5 (the view direction is the fixture's
   camera ray computed in double, the shader's in float);
@@ -275,6 +276,19 @@ def test_gen_basis(vec, tmp_path):
                        check=True)
     got = np.frombuffer(r.stdout, np.float32).reshape(-1, 6)
     assert (got.view(np.uint32) == vec["basis_out"].view(np.uint32)).all()
+
+
+def test_hysteresis_ramp(vec):
+    """The hysteresis ramp restatement that holds the C ABI's device ramp
+    (ReferenceRamp of test_gpu_hysteresis.py) equals the reference's own
+    block of update(), uploaded value and GridParameters.hysteresis after
+    each of 80 updates, bit for bit."""
+    from test_gpu_hysteresis import ReferenceRamp
+    r = ReferenceRamp(0.0, 0.98)
+    for k, n in enumerate(vec["ramp_counts"]):
+        u = r.update(int(n), 48)
+        assert u == vec["ramp_uniform"][k] and r.param == vec["ramp_param"][k], k
+    assert len(set(vec["ramp_uniform"].tolist())) > 10
 
 
 def test_fixture_scene_is_current(vec):
