@@ -446,32 +446,101 @@ def profiled_traffic(summary):
     return int(m.group(1)) if m else None
 
 
-def measure_final_gather(ctx, w, stream, flush, reps=10, width=1920, height=1080):
-    """The atlas consumer: FinalGather.frag over a seeded 1920x1080 G-buffer
-    (positions inside the probe grid, random normals and materials, 10% sky
-    pixels) on the context's current atlas.  CUDA events over `reps`
-    launches, L2 flushed before each; algorithmic bytes per pixel: the
-    G-buffer read (4 x float4 + float + float4 reflection) and the float4
-    written = 100 B (probe-atlas texels are L2-resident)."""
+def rendered_gbuffer(ctx, w, width, height):
+    """A G-buffer as the reference's GBuffer pass would leave it for a camera
+    view of the scene: one camera ray per pixel (60-degree vertical field of
+    view, from above one side of the probe grid towards the ground at its
+    centre) traced
+    by ddgi_trace_rays; position and depth from the hit, the interpolated
+    vertex normal in world space, the hit material's albedo, roughness,
+    metalness and emissive, direct light 1 where a shadow ray towards the
+    sun (tmin 0.1, any hit) escapes, reflection 0; sky pixels (misses) carry
+    depth 0 and the view direction in position.xyz.  Host arrays."""
+    from vulkanexp_gb300 import abi
+
+    g, sc = w.grid, w.scene
+    lo, hi = np.array(g.extent_min, np.float64), np.array(g.extent_max, np.float64)
+    c, ext = 0.5 * (lo + hi), hi - lo
+    eye = np.array([c[0], lo[1] + 0.8 * ext[1], lo[2] + 0.05 * ext[2]])
+    fwd = np.array([c[0], lo[1], c[2]]) - eye  # towards the ground at the grid's centre
+    fwd /= np.linalg.norm(fwd)
+    right = np.cross(fwd, [0.0, 1.0, 0.0])
+    right /= np.linalg.norm(right)
+    up = np.cross(right, fwd)
+    th = np.tan(np.radians(30.0))
+    px = (np.arange(width) + 0.5) / width * 2 - 1
+    py = 1 - (np.arange(height) + 0.5) / height * 2
+    X, Y = np.meshgrid(px * th * width / height, py * th)
+    d = fwd[None, None] + X[..., None] * right[None, None] + Y[..., None] * up[None, None]
+    d = (d / np.linalg.norm(d, axis=-1, keepdims=True)).reshape(-1, 3).astype(np.float32)
+    n = len(d)
+    o = np.repeat(eye[None].astype(np.float32), n, 0)
+    tmax = float(np.linalg.norm(ext)) * 4
+    hits, bary = ctx.trace_rays(o, d, 0.01, tmax, 0xFF, False)
+    hit = hits["instance"] != abi.MISS
+    t = np.where(hit, hits["t"], 0.0).astype(np.float32)
+    pos = np.where(hit[:, None], o + d * t[:, None], d)
+    inst = sc.instances[np.where(hit, hits["instance"], 0)]
+    off = sc.offsets[inst["custom_index"]]
+    tri = off["index_offset"][:, None] + 3 * hits["primitive"][:, None].astype(np.int64) + np.arange(3)[None]
+    vi = off["vertex_offset"][:, None] + sc.indices[np.where(hit[:, None], tri, 0)]
+    nv = sc.vertices["normal"][vi].astype(np.float64)
+    b1, b2 = bary[:, 0:1].astype(np.float64), bary[:, 1:2].astype(np.float64)
+    nrm = nv[:, 0] * (1 - b1 - b2) + nv[:, 1] * b1 + nv[:, 2] * b2
+    A = inst["transform"].reshape(-1, 3, 4)[:, :, :3].astype(np.float64)
+    nrm = np.einsum("kij,kj->ki", np.linalg.inv(A).transpose(0, 2, 1), nrm)  # normal matrix
+    nrm /= np.maximum(np.linalg.norm(nrm, axis=1, keepdims=True), 1e-30)
+    mat = sc.materials[off["material_index"]]
+    sun = np.repeat(np.array(w.light.direction[:3], np.float32)[None], n, 0)
+    sh, _ = ctx.trace_rays(pos.astype(np.float32), sun, 0.1, 1e4, 0xFF, True)
+    lit = (sh["instance"] == abi.MISS) & hit
+    f4 = lambda a: np.ascontiguousarray(a.reshape(height, width, 4), np.float32)
+    z = np.zeros((n, 1))
+    return {"position_depth": f4(np.concatenate([pos, t[:, None]], 1)),
+            "normal_metalness": f4(np.concatenate([nrm, mat["metallic"][:, None]], 1)),
+            "albedo_roughness": f4(np.concatenate([mat["base_color"], mat["roughness"][:, None]], 1)),
+            "emissive": f4(np.concatenate([mat["emissive"], z], 1)),
+            "direct_light": np.ascontiguousarray(lit.reshape(height, width), np.float32),
+            "reflection": f4(np.zeros((n, 4)))}, eye, float(hit.mean())
+
+
+def measure_final_gather(ctx, w, stream, flush, reps=10, width=1920, height=1080, view="scattered"):
+    """The atlas consumer: FinalGather.frag over a 1920x1080 G-buffer on the
+    context's current atlas.  view "rendered": the G-buffer of a camera view
+    of the scene (rendered_gbuffer), whose neighbouring pixels look up
+    neighbouring probes, as a renderer's do; "scattered": a seeded
+    worst case (positions uniform inside the probe grid, random normals and
+    materials, 10% sky pixels), where no two pixels of a warp share probes.
+    CUDA events over `reps` launches, L2 flushed before each; algorithmic
+    bytes per pixel: the G-buffer read (4 x float4 + float + float4
+    reflection) and the float4 written = 100 B (probe-atlas texels are
+    L2-resident)."""
     import torch
 
     g = w.grid
     n = width * height
-    gen = torch.Generator(device="cuda").manual_seed(1239)
-    lo = torch.tensor(list(g.extent_min), device="cuda")
-    hi = torch.tensor(list(g.extent_max), device="cuda")
-    pos = lo + (hi - lo) * torch.rand((n, 3), device="cuda", generator=gen)
-    depth = torch.where(torch.rand(n, device="cuda", generator=gen) < 0.1, 0.0, 1.0)
-    u = lambda *sh: torch.rand(sh, device="cuda", generator=gen)
-    gb = {"position_depth": torch.cat([pos, depth[:, None]], 1).reshape(height, width, 4).contiguous(),
-          "normal_metalness": torch.cat([torch.randn((n, 3), device="cuda", generator=gen), u(n, 1)], 1)
-          .reshape(height, width, 4).contiguous(),
-          "albedo_roughness": u(n, 4).reshape(height, width, 4).contiguous(),
-          "emissive": (0.1 * u(n, 4)).reshape(height, width, 4).contiguous(),
-          "direct_light": u(n).reshape(height, width).contiguous(),
-          "reflection": u(n, 4).reshape(height, width, 4).contiguous()}
+    extra = {}
+    if view == "rendered":
+        host, eye, hit_frac = rendered_gbuffer(ctx, w, width, height)
+        gb = {k: torch.from_numpy(v).cuda() for k, v in host.items()}
+        origin = [float(x) for x in eye]
+        extra = {"surface_pixels": hit_frac}
+    else:
+        gen = torch.Generator(device="cuda").manual_seed(1239)
+        lo = torch.tensor(list(g.extent_min), device="cuda")
+        hi = torch.tensor(list(g.extent_max), device="cuda")
+        pos = lo + (hi - lo) * torch.rand((n, 3), device="cuda", generator=gen)
+        depth = torch.where(torch.rand(n, device="cuda", generator=gen) < 0.1, 0.0, 1.0)
+        u = lambda *sh: torch.rand(sh, device="cuda", generator=gen)
+        gb = {"position_depth": torch.cat([pos, depth[:, None]], 1).reshape(height, width, 4).contiguous(),
+              "normal_metalness": torch.cat([torch.randn((n, 3), device="cuda", generator=gen), u(n, 1)], 1)
+              .reshape(height, width, 4).contiguous(),
+              "albedo_roughness": u(n, 4).reshape(height, width, 4).contiguous(),
+              "emissive": (0.1 * u(n, 4)).reshape(height, width, 4).contiguous(),
+              "direct_light": u(n).reshape(height, width).contiguous(),
+              "reflection": u(n, 4).reshape(height, width, 4).contiguous()}
+        origin = [0.5 * (a + b) for a, b in zip(g.extent_min, g.extent_max)]
     out = torch.empty((height, width, 4), dtype=torch.float32, device="cuda")
-    origin = [0.5 * (a + b) for a, b in zip(g.extent_min, g.extent_max)]
     for _ in range(3):
         ctx.final_gather(gb, origin, out, stream)
     ms = []
@@ -486,8 +555,9 @@ def measure_final_gather(ctx, w, stream, flush, reps=10, width=1920, height=1080
     t = float(np.median(ms))
     hbm, _, _ = load_peaks()
     gbs = n * 100 / (t * 1e-3) / 1e9
-    return {"kernel": "k_final_gather", "pixels": n, "ms": t, "gpixels_per_s": n / (t * 1e-3) / 1e9,
-            "achieved_gbs": gbs, "frac_hbm": gbs / hbm, "bytes_per_pixel": 100}
+    return dict({"kernel": "k_final_gather", "view": view, "pixels": n, "ms": t,
+                 "gpixels_per_s": n / (t * 1e-3) / 1e9, "achieved_gbs": gbs, "frac_hbm": gbs / hbm,
+                 "bytes_per_pixel": 100}, **extra)
 
 
 def main():
@@ -542,7 +612,7 @@ def main():
                 ctx.update(w.orientation(k), stream=stream)
             ctx.synchronize(stream)
             if prec == abi.PRECISION_BF16:  # one final gather over the BF16 atlas
-                measure_final_gather(ctx, w, stream, flush, reps=1)
+                measure_final_gather(ctx, w, stream, flush, reps=1, view="rendered")
             ctx.close()
         print(json.dumps({"profile_target": w.name, "updates": 4, "final_gathers": 4}), flush=True)
         return
@@ -647,7 +717,8 @@ def main():
             # sanity of the last e2e step's result as read back
             "atlas_finite": bool(np.isfinite(host_c).all() and np.isfinite(host_d).all())}
     if not args.headline_only:
-        line["final_gather"] = measure_final_gather(ctx, w, stream, flush)
+        line["final_gather"] = measure_final_gather(ctx, w, stream, flush, view="rendered")
+        line["final_gather_scattered"] = measure_final_gather(ctx, w, stream, flush, view="scattered")
     ctx.close()
     if not args.headline_only:
         line["differentiation"] = measure_differentiation(stream)
