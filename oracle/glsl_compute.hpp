@@ -1,12 +1,13 @@
 // glsl_compute.hpp — what the reference's compute shaders
 // (src/shaders/probesUpdate.glsl through probesUpdateIrradiance.comp and
 // probesUpdateDepth.comp, and probesCopyBorders.comp) need beyond
-// glsl_shim.hpp to run on the host: unsigned vectors, the built-in
+// glsl_shim.hpp to run on the host: unsigned vectors, matrices, the built-in
 // invocation IDs, storage images with their formats' rounding on store,
 // workgroup barriers and shared-memory atomics, and a dispatch that runs
-// every invocation of a workgroup as its own thread.  Test infrastructure:
-// built by oracle/build_ref_glsl.py into oracle/_ref/, loaded only by tests
-// and the fixture generator.
+// every invocation of a workgroup as its own thread; and what
+// FinalGather.frag adds: subpass inputs read at the current fragment and
+// inverse(mat4).  Test infrastructure: built by oracle/build_ref_glsl.py
+// into oracle/_ref/, loaded only by tests and the fixture generator.
 //
 // Execution model: workgroups run one after the other (the shaders'
 // workgroups touch disjoint texels and probe states); inside a workgroup all

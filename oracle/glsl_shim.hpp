@@ -2,9 +2,10 @@
 // compile the reference's own shader helper files (src/shaders/common.glsl,
 // ProbeGrid.glsl, irradiance.glsl, pbrMetallicRoughness.glsl, sky.glsl)
 // unchanged on the host, so that the oracle's restatements of them can be
-// checked against the reference's code.  Test infrastructure: built by
-// oracle/build_ref_glsl.py into oracle/_ref/, loaded only by tests and the
-// fixture generator.
+// checked against the reference's code; glsl_compute.hpp and glsl_rt.hpp
+// build the compute, fragment and ray-tracing stages on it.  Test
+// infrastructure: built by oracle/build_ref_glsl.py into oracle/_ref/,
+// loaded only by tests and the fixture generator.
 //
 // The shader files are included inside namespace glsl, so unqualified calls
 // (cos, sqrt, max, ...) find the overloads below and never the C library's.
