@@ -20,8 +20,9 @@ namespace ddgi {
 // Box sets (build_boxes): the object splits of sah.cu, binned above
 // kSweepMax primitives and by an exact sweep below.  Every decision uses the
 // host builders' arithmetic (same bins, same separately rounded operations,
-// clipping in double), and partitions keep the references' order, so a set's
-// tree is the host builder's tree.
+// the reference splits of tri_split.h in float interval arithmetic), and
+// partitions keep the references' order, so a set's tree is the host
+// builder's tree.
 class GpuTreeBuilder {
   public:
     GpuTreeBuilder() = default;
