@@ -415,6 +415,10 @@ struct WarpWalker {
 // ---------------------------------------------------------------------------
 // Float of an 8-bit integer (exact): its bits under the exponent of 2^23.
 __device__ __forceinline__ float byte_float(uint32_t b) { return __uint_as_float(0x4B000000u | b) - 8388608.0f; }
+// The same for byte i of w, the float's bits assembled by one byte permute.
+__device__ __forceinline__ float byte_float_at(uint32_t w, int i) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)i)) - 8388608.0f;
+}
 
 template <bool ANY, class Stack = SmemStack>
 struct WideWalker {
@@ -463,8 +467,8 @@ struct WideWalker {
         const uint32_t n0 = pos ? q.x : q.z, n1 = pos ? q.y : q.w, f0 = pos ? q.z : q.x, f1 = pos ? q.w : q.y; \
         _Pragma("unroll") for (int k = 0; k < 8; ++k) {                                                   \
             const uint32_t nw = k < 4 ? n0 : n1, fw = k < 4 ? f0 : f1;                                    \
-            const float a = fmaf(byte_float((nw >> (8 * (k & 3))) & 0xFFu), s, b);                        \
-            const float c = fmaf(byte_float((fw >> (8 * (k & 3))) & 0xFFu), s, b);                        \
+            const float a = fmaf(byte_float_at(nw, k & 3), s, b);                                         \
+            const float c = fmaf(byte_float_at(fw, k & 3), s, b);                                         \
             tn[k] = fmaxf(tn[k], a);                                                                      \
             tf[k] = fminf(tf[k], c);                                                                      \
         }                                                                                                 \
