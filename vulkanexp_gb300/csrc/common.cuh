@@ -413,4 +413,34 @@ __device__ __forceinline__ void bilinear(const Tex& tex, uint32_t w, uint32_t h,
     }
 }
 
+// bilinear() for a sample inside one probe tile of an atlas, as every
+// lookup of sampleProbes makes: the texture coordinate keeps the sample at
+// least half a texel inside the tile (the tile's border texels, filled by
+// probesCopyBorders, surround the interior it addresses), so REPEAT
+// addressing is the identity and the four texels are found without it; the
+// indices are clamped into the atlas all the same, so a fetch never leaves
+// it.  32-bit texel indices (atlases below 2^31 texels).
+template <int NC, class Tex>
+__device__ __forceinline__ void bilinear_tile(const Tex& tex, uint32_t w, uint32_t h, float u, float v, float* out) {
+    float x = u * (float)w - 0.5f;
+    float y = v * (float)h - 0.5f;
+    float fx0 = floorf(x), fy0 = floorf(y);
+    float ax = x - fx0, ay = y - fy0;
+    const int iw = (int)w, ih = (int)h;
+    const int i0 = max((int)fx0, 0), j0 = max((int)fy0, 0);
+    const int i1 = min(i0 + 1, iw - 1), j1 = min(j0 + 1, ih - 1);
+    const uint32_t r0 = (uint32_t)j0 * w, r1 = (uint32_t)j1 * w;
+    float t00[NC], t10[NC], t01[NC], t11[NC];
+    tex.fetch(r0 + (uint32_t)i0, t00);
+    tex.fetch(r0 + (uint32_t)i1, t10);
+    tex.fetch(r1 + (uint32_t)i0, t01);
+    tex.fetch(r1 + (uint32_t)i1, t11);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        float top = t00[c] * (1.0f - ax) + t10[c] * ax;
+        float bot = t01[c] * (1.0f - ax) + t11[c] * ax;
+        out[c] = top * (1.0f - ay) + bot * ay;
+    }
+}
+
 }  // namespace ddgi

@@ -152,7 +152,7 @@ __device__ void sample_probes_n(float3 position, const float3 (&normal)[NQ], flo
             weight *= bfw * bfw + 0.2f;
             float fallbackWeight = weight;
             float depth[2];
-            bilinear<2>(at.depth, g.depth_w, g.depth_h, du, dv, depth);
+            bilinear_tile<2>(at.depth, g.depth_w, g.depth_h, du, dv, depth);
             float mean = depth[0];
             float variance = fabsf(depth[0] * depth[0] - depth[1]);
             float dist = len3(probePosition - biasedPosition[q]);
@@ -166,7 +166,7 @@ __device__ void sample_probes_n(float3 position, const float3 (&normal)[NQ], flo
             weight *= triw;
             fallbackWeight *= triw;
             float col[3];
-            bilinear<3>(at.color, g.color_w, g.color_h, cu, cv, col);
+            bilinear_tile<3>(at.color, g.color_w, g.color_h, cu, cv, col);
             float3 color = f3(sqrtf(col[0]), sqrtf(col[1]), sqrtf(col[2]));
             finalColor[q] = finalColor[q] + color * weight;
             totalWeight[q] += weight;
