@@ -62,7 +62,7 @@ struct ddgi_batch {
     uint64_t node_count = 0, tri_count = 0, inst_count = 0;
     std::vector<int32_t> roots;
     int stack_cap = 1;
-    // the four-wide trees of every volume (wstack_cap 0: some volume has none)
+    // the eight-wide trees of every volume (wstack_cap 0: some volume has none)
     WideNode* wnodes = nullptr;
     GpuInstance* winsts = nullptr;
     uint64_t wnode_count = 0;

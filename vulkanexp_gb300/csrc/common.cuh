@@ -109,7 +109,7 @@ struct DeviceScene {
     int32_t tlas_root;      // -1: empty scene
     uint32_t vertex_count, index_count, offset_count, material_count;
     uint32_t node_count, tri_count, instance_count;  // bounds of the references above
-    // the same trees as four-wide nodes; instances (leaf order) whose
+    // the same trees as eight-wide nodes; instances (leaf order) whose
     // blas_root is a wide-node index
     const WideNode* wnodes;
     const GpuInstance* winstances;

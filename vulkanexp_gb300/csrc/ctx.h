@@ -58,7 +58,7 @@ struct SceneBuffers {
     uint32_t* refit_flags = nullptr;
     float4* sub_lo = nullptr;
     float4* sub_hi = nullptr;
-    // four-wide copy of the trees: [mesh trees | top level, with room for
+    // eight-wide copy of the trees: [mesh trees | top level, with room for
     // a rebuilt top level]; instances in leaf order with wide mesh roots
     WideNode* wnodes = nullptr;
     GpuInstance* winst_leaf = nullptr;

@@ -50,7 +50,7 @@ struct TraceTuning {
     uint32_t refill;         // idle lanes that trigger a warp's work request
     uint32_t split;          // stack entries in shared memory (0 or >= cap: all)
     uint32_t rays_per_warp;  // 0: a warp per probe in slot order; 1..32: grouped order (see below)
-    uint32_t wide;           // 1: four-wide nodes (when the scene has them), 0: binary nodes
+    uint32_t wide;           // 1: eight-wide quantised nodes (made on first use), 0: binary nodes
     uint32_t wait = kDefaultWait;  // straggler lanes that end a warp's search loop (0: wait for all)
 };
 // Per-launch constants of the persistent traversal loop.

@@ -1,4 +1,4 @@
-// wide.h — four-wide trees collapsed from the binary LBVH trees (wide.cu).
+// wide.h — eight-wide quantised trees collapsed from the binary trees (wide.cu).
 #pragma once
 
 #include <cuda_runtime.h>
