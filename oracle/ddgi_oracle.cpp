@@ -5,8 +5,9 @@
  *
  * A scalar restatement of VulkanExp's probe-update shaders, templated on the
  * arithmetic type (float for the parity form, double for the error
- * reference), multithreaded over probes with an explicit worker count (the
- * role of the reference's ThreadPool/TaskQueue, src/ThreadPool.hpp:10-75).
+ * reference), multithreaded over probes on a worker pool with the interface
+ * of the reference's ThreadPool/TaskQueue (src/ThreadPool.hpp:10-75) and an
+ * explicit worker count.
  *
  * Followed line by line:
  *   src/shaders/traceProbes.rgen:29-49        ray generation, tmin/tmax
@@ -56,12 +57,18 @@
  * ddgi_round_r11/b10/half of include/ddgi_exact.h, so its bounce lookup reads
  * the same rounded values the reference's does.
  */
+#include <unistd.h>
+
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstdint>
 #include <cstring>
+#include <deque>
 #include <functional>
+#include <future>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -110,26 +117,122 @@ using F3 = V3<float>;
 template <class T> constexpr T kPi() { return T(3.1415926538); }
 
 // ---------------------------------------------------------------------------
-// Worker pool: explicit thread count, chunked parallel loop.
+// Worker pool with the interface of the reference's ThreadPool
+// (src/ThreadPool.hpp:10-75, ThreadPool.cpp:5-28): `threadCount` workers fed
+// from one task queue, queue() returning the task's future, and a TaskQueue
+// that collects the futures of a batch and waits for them.  The reference
+// keeps one global pool of hardware_concurrency() - 1 workers
+// (ThreadPool.hpp:31, 37-40); the checker's pools take an explicit worker
+// count instead (the caller's, normally every host core), one pool per
+// count, made on first use in each process.
 // ---------------------------------------------------------------------------
+thread_local bool t_pool_worker = false;  // the current thread is a pool worker
+
+class ThreadPool {
+  public:
+    class TaskQueue {
+      public:
+        explicit TaskQueue(ThreadPool& pool) : pool_(pool) {}
+        TaskQueue(const TaskQueue&) = delete;
+        TaskQueue& operator=(const TaskQueue&) = delete;
+        ~TaskQueue() { wait(); }
+        void start(std::function<void()>&& fn) { futures_.push_back(pool_.queue(std::move(fn))); }
+        void wait() {
+            for (auto& f : futures_) f.wait();
+            futures_.clear();
+        }
+
+      private:
+        ThreadPool& pool_;
+        std::vector<std::future<void>> futures_;
+    };
+
+    explicit ThreadPool(uint32_t threadCount) { startThreads(threadCount); }
+    ThreadPool(const ThreadPool&) = delete;
+    ThreadPool& operator=(const ThreadPool&) = delete;
+    ~ThreadPool() {
+        {
+            std::lock_guard<std::mutex> lock(mutex_);
+            closing_ = true;
+        }
+        ready_.notify_all();
+        for (auto& t : workers_) t.join();
+    }
+
+    void startThreads(uint32_t threadCount) {
+        for (uint32_t i = 0; i < threadCount; ++i) workers_.emplace_back([this] { work(); });
+    }
+    uint32_t threadCount() const { return (uint32_t)workers_.size(); }
+
+    std::future<void> queue(std::function<void()>&& fn) {
+        std::packaged_task<void()> task(std::move(fn));
+        std::future<void> done = task.get_future();
+        {
+            std::lock_guard<std::mutex> lock(mutex_);
+            pending_.push_back(std::move(task));
+        }
+        ready_.notify_one();
+        return done;
+    }
+
+    // The pool of `threadCount` workers of this process.  Pools are kept
+    // until the process ends; a process forked after a pool was made has no
+    // workers behind the inherited object, so it makes its own.
+    static ThreadPool& withThreads(uint32_t threadCount) {
+        static std::mutex registry_mutex;
+        static std::vector<ThreadPool*> registry;
+        std::lock_guard<std::mutex> lock(registry_mutex);
+        const pid_t self = getpid();
+        for (ThreadPool* p : registry)
+            if (p->owner_ == self && p->threadCount() == threadCount) return *p;
+        registry.push_back(new ThreadPool(threadCount));  // never freed: workers live as long as the process
+        return *registry.back();
+    }
+
+  private:
+    void work() {
+        t_pool_worker = true;
+        for (;;) {
+            std::packaged_task<void()> task;
+            {
+                std::unique_lock<std::mutex> lock(mutex_);
+                ready_.wait(lock, [this] { return closing_ || !pending_.empty(); });
+                if (pending_.empty()) return;  // closing, nothing left to run
+                task = std::move(pending_.front());
+                pending_.pop_front();
+            }
+            task();
+        }
+    }
+
+    const pid_t owner_ = getpid();
+    std::vector<std::thread> workers_;
+    std::deque<std::packaged_task<void()>> pending_;
+    std::mutex mutex_;
+    std::condition_variable ready_;
+    bool closing_ = false;
+};
+
+// fn(begin, end) over [0, n) in chunks of `grain`, on a pool of `nthreads`
+// workers (each takes chunks from a shared counter until none is left); the
+// calling thread waits.  Serial for one thread, a small n, or a call made from
+// inside a pool task (a worker waiting on its own pool could starve it).
 void parallel_for(size_t n, int nthreads, const std::function<void(size_t, size_t)>& fn, size_t grain = 1) {
-    if (nthreads <= 1 || n <= grain) {
+    if (nthreads <= 1 || n <= grain || t_pool_worker) {
         fn(0, n);
         return;
     }
     std::atomic<size_t> next{0};
-    auto worker = [&]() {
-        for (;;) {
-            size_t b = next.fetch_add(grain);
-            if (b >= n) break;
-            fn(b, std::min(n, b + grain));
-        }
-    };
-    std::vector<std::thread> threads;
-    threads.reserve(nthreads - 1);
-    for (int i = 0; i < nthreads - 1; ++i) threads.emplace_back(worker);
-    worker();
-    for (auto& t : threads) t.join();
+    ThreadPool::TaskQueue batch(ThreadPool::withThreads((uint32_t)nthreads));
+    for (int i = 0; i < nthreads; ++i)
+        batch.start([&]() {
+            for (;;) {
+                const size_t b = next.fetch_add(grain);
+                if (b >= n) break;
+                fn(b, std::min(n, b + grain));
+            }
+        });
+    batch.wait();
 }
 
 // ---------------------------------------------------------------------------
