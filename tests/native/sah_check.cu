@@ -1,5 +1,6 @@
 // Host-only structural check of the SAH tree builder (vulkanexp_gb300/csrc/sah.cu),
-// run under AddressSanitizer / UndefinedBehaviorSanitizer by tests/test_native_host.py.
+// run under AddressSanitizer / UndefinedBehaviorSanitizer and under ThreadSanitizer
+// (its 40,000-box case builds subtrees on other threads) by tests/test_native_host.py.
 // For each case: every leaf position appears in exactly one leaf, `order` is a
 // permutation, every child box contains the boxes of all primitives below it,
 // references stay inside the node range, the reported depth is the longest

@@ -1,5 +1,7 @@
 // Host-only check of the spatial-split tree builder (vulkanexp_gb300/csrc/sbvh.cu),
-// run under AddressSanitizer / UndefinedBehaviorSanitizer by tests/test_native_host.py.
+// run under AddressSanitizer / UndefinedBehaviorSanitizer by tests/test_native_host.py
+// (and with the argument `threads`, inputs that build subtrees on other
+// threads, under ThreadSanitizer).
 // For overlapping box soups (also nearly axis-aligned ones, whose faces the
 // split planes cut at grazing angles) and a height field: every triangle is referenced,
 // references and leaf ranges stay in bounds, the depth is reported correctly,
@@ -9,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <algorithm>
 #include <array>
 #include <random>
@@ -249,8 +252,16 @@ static void check_clip(std::mt19937& rng, int cases) {
 }
 
 int main(int argc, char** argv) {
-    const int scale = argc > 1 ? std::atoi(argv[1]) : 1;
     std::mt19937 rng(7);
+    if (argc > 1 && std::strcmp(argv[1], "threads") == 0) {
+        // inputs above the 8,192 references that send a subtree to another
+        // thread, one sample point per triangle (for the race detector run)
+        check("threaded box soup", box_soup(rng, 1200, 2.0f), 2, 1e-2f, 1);
+        check("threaded height field", height_field(rng, 100, 30.0f), 2, 1e-2f, 1);
+        std::printf(failures ? "FAILED %d\n" : "all ok\n", failures);
+        return failures ? 1 : 0;
+    }
+    const int scale = argc > 1 ? std::atoi(argv[1]) : 1;
     for (float alpha : {1e-2f, 1e-5f, 0.0f}) {
         char name[64];
         std::snprintf(name, sizeof name, "box soup alpha=%g", alpha);

@@ -1,4 +1,4 @@
-"""Host code under AddressSanitizer and UndefinedBehaviorSanitizer, no GPU:
+"""Host code under AddressSanitizer, UndefinedBehaviorSanitizer and ThreadSanitizer, no GPU:
 
 * the spatial-split tree builder (vulkanexp_gb300/csrc/sbvh.cu) through
   tests/native/sbvh_check.cu;
@@ -8,7 +8,10 @@
 * the REPEAT texel-index wrap of the atlas lookups (tests/native/wrap_check.cu);
 * the CPU checker (oracle/ddgi_oracle.cpp) on a small room: trace, update
   (FP32 and FP64), probe classification and final gather, loaded into a
-  Python process with the ASan runtime preloaded.
+  Python process with the ASan runtime preloaded;
+* under ThreadSanitizer: the checker's worker pool and parallel loops (the
+  TSan runtime preloaded the same way), and the host tree builders' subtree
+  threads (sah_check, sbvh_check with inputs large enough to spawn them).
 
 Any sanitizer report aborts the child process, which fails the test."""
 import os
@@ -151,3 +154,73 @@ def test_oracle_under_sanitizers(tmp_path):
                        timeout=600)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
     assert "oracle ok" in r.stdout
+
+
+TSAN_SCRIPT = textwrap.dedent("""
+    import numpy as np
+    from oracle.oracle import Oracle, zero_atlas
+    from vulkanexp_gb300 import scenes
+    w = scenes.room_workload(62, n_boxes=30, resolution=(4, 3, 4), rays=32)
+    for threads in (4, 3):  # two pools of the same process
+        o = Oracle(w.scene, threads=threads)
+        st = np.ones(w.grid.probe_count(), np.uint32)
+        c, dd = zero_atlas(w.grid)
+        for k in range(2):
+            o.update(w.grid, w.light, w.orientation(k), c, dd, st)
+        o.init_probes(w.grid, w.orientation(0))
+        Oracle.blend(w.grid, w.orientation(0), np.zeros((w.grid.probe_count(), 32, 4), np.float32), c, dd, st,
+                     threads=threads)
+        o.close()
+    print("oracle ok")
+""")
+
+
+def test_oracle_worker_pool_under_thread_sanitizer(tmp_path):
+    # the checker's worker pool (task queue, futures, one pool per worker
+    # count) and the parallel loops over it, with ThreadSanitizer preloaded
+    tsan = _runtime("libtsan.so")
+    if tsan is None:
+        pytest.skip("the ThreadSanitizer runtime is missing")
+    lib = str(tmp_path / "libddgi_oracle_tsan.so")
+    subprocess.check_call(["g++", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread",
+                           "-fsanitize=thread", "-g", "-O1", "-o", lib, os.path.join(ROOT, "oracle", "ddgi_oracle.cpp")])
+    env = dict(os.environ)
+    env.update({"LD_PRELOAD": tsan, "DDGI_ORACLE_LIB": lib, "PYTHONPATH": ROOT, "TSAN_OPTIONS": "halt_on_error=1",
+                "OPENBLAS_NUM_THREADS": "1", "OMP_NUM_THREADS": "1"})
+    r = subprocess.run([sys.executable, "-c", TSAN_SCRIPT], capture_output=True, text=True, env=env, cwd=ROOT,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "oracle ok" in r.stdout
+
+
+@pytest.mark.parametrize("check,sources,args", [
+    # 40,000 boxes: subtrees above 16,384 primitives go to other threads
+    ("sah_check", ("tests/native/sah_check.cu", "vulkanexp_gb300/csrc/sah.cu"), []),
+    # a 14,400-triangle box soup and a 20,000-triangle height field, above
+    # the 8,192 references that send a subtree to another thread
+    ("sbvh_check", ("tests/native/sbvh_check.cu", "vulkanexp_gb300/csrc/sbvh.cu"), ["threads"]),
+])
+def test_host_tree_builders_under_thread_sanitizer(tmp_path, check, sources, args):
+    """The host tree builders build subtrees on their own threads (four in
+    these checks); ThreadSanitizer watches the shared node and reference
+    arrays they fill."""
+    from vulkanexp_gb300 import build
+
+    nvcc = build.nvcc()
+    if not (os.path.exists(nvcc) or _have(nvcc)) or _runtime("libtsan.so") is None:
+        pytest.skip("nvcc or the ThreadSanitizer runtime is missing")
+    flags = ["-std=c++17"] + build.ARCH + ["--expt-relaxed-constexpr", "-Xcompiler", "-fsanitize=thread",
+                                           "-Xcompiler", "-ffp-contract=off", "-g", "-O1"]
+    objs = []
+    for src in sources:
+        o = str(tmp_path / (os.path.basename(src) + ".o"))
+        subprocess.check_call([nvcc] + flags + ["-c", os.path.join(ROOT, src), "-o", o])
+        objs.append(o)
+    exe = str(tmp_path / check)
+    cudart = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "lib64")
+    subprocess.check_call(["g++", "-fsanitize=thread"] + objs +
+                          ["-L" + cudart, "-lcudart_static", "-ldl", "-lrt", "-pthread", "-o", exe])
+    r = subprocess.run([exe] + args, capture_output=True, text=True,
+                       env=dict(os.environ, TSAN_OPTIONS="halt_on_error=1"), timeout=900)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "all ok" in r.stdout
