@@ -79,6 +79,10 @@ typedef struct ddgi_grid_desc {
 } ddgi_grid_desc;
 
 #define DDGI_MAX_RAYS_PER_PROBE 1024u
+/* Limit of probes x rays_per_probe, the rays of one update: ray indices are
+ * 32-bit, with headroom for the work counters of the persistent kernels
+ * (an update that large needs more than 300 GB of ray and hit buffers). */
+#define DDGI_MAX_RAYS_PER_UPDATE 0xFFF00000u
 
 /* Vertex record, 64 bytes.  Same layout as src/vulkan/Vertex.hpp:8-15. */
 typedef struct ddgi_vertex {

@@ -66,6 +66,17 @@ def test_create_rejects_bad_grid_without_gpu(lib, field, value):
     assert not h.value
 
 
+def test_create_rejects_more_rays_than_32_bit_indices(lib):
+    # 2^24 probes (the probe limit) x 1024 rays: 2^34 rays in one update,
+    # beyond DDGI_MAX_RAYS_PER_UPDATE; 2^24 x 64 rays is accepted by the check
+    g = abi.make_grid((0, 0, 0), (1, 1, 1), (256, 256, 256), 1024)
+    h = C.c_void_p()
+    lib.ddgi_create.argtypes = [C.POINTER(abi.GridDesc), C.POINTER(C.c_void_p)]
+    assert lib.ddgi_create(C.byref(g), C.byref(h)) == 1
+    assert not h.value
+    assert 256 ** 3 * 1024 > 0xFFF00000 >= 256 ** 3 * 64
+
+
 def test_create_rejects_empty_extent(lib):
     g = abi.make_grid((0, 0, 0), (1, 0, 1), (4, 4, 4), 64)
     h = C.c_void_p()

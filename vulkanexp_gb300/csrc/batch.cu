@@ -523,7 +523,7 @@ ddgi_status ddgi_batch_create(ddgi_ctx* const* volumes, uint32_t count, ddgi_str
         }
     }
     b->ray_base.push_back((uint32_t)rays);
-    if (rays >= (1ull << 32) || tris >= (1ull << 28) - 8 || insts >= (1ull << 28) - 8 || nodes >= (1ull << 31))
+    if (rays > DDGI_MAX_RAYS_PER_UPDATE || tris >= (1ull << 28) - 8 || insts >= (1ull << 28) - 8 || nodes >= (1ull << 31))
         return bail(DDGI_ERR_UNSUPPORTED);
     b->total = (uint32_t)rays;
     b->dir_total = (uint32_t)dirs;

@@ -87,6 +87,10 @@ bool grid_valid(const ddgi_grid_desc* g, char* why, size_t n) {
         return snprintf(why, n, "unknown precision %u", g->precision), false;
     uint64_t probes = (uint64_t)g->resolution[0] * g->resolution[1] * g->resolution[2];
     if (probes > (1u << 24)) return snprintf(why, n, "too many probes (%llu)", (unsigned long long)probes), false;
+    if (probes * g->rays_per_probe > DDGI_MAX_RAYS_PER_UPDATE)
+        return snprintf(why, n, "probes x rays_per_probe = %llu above %u", (unsigned long long)(probes * g->rays_per_probe),
+                        DDGI_MAX_RAYS_PER_UPDATE),
+               false;
     uint64_t w = (uint64_t)g->depth_res * g->resolution[0] * g->resolution[1];
     if (w > (1u << 30)) return snprintf(why, n, "atlas too wide"), false;
     return true;
