@@ -77,6 +77,17 @@ def test_create_rejects_more_rays_than_32_bit_indices(lib):
     assert 256 ** 3 * 1024 > 0xFFF00000 >= 256 ** 3 * 64
 
 
+@pytest.mark.parametrize("color_res,depth_res", [(16, 8), (8, 17)])
+def test_create_rejects_atlases_beyond_32_bit_texel_indices(lib, color_res, depth_res):
+    # 2^24 probes with 16 x 16 colour tiles: 2^32 texels, one more than the
+    # lookups' 32-bit texel indices reach (15 x 15 tiles would be accepted)
+    g = abi.make_grid((0, 0, 0), (1, 1, 1), (256, 256, 256), 1, color_res=color_res, depth_res=depth_res)
+    h = C.c_void_p()
+    lib.ddgi_create.argtypes = [C.POINTER(abi.GridDesc), C.POINTER(C.c_void_p)]
+    assert lib.ddgi_create(C.byref(g), C.byref(h)) == 1
+    assert not h.value
+
+
 def test_create_rejects_empty_extent(lib):
     g = abi.make_grid((0, 0, 0), (1, 0, 1), (4, 4, 4), 64)
     h = C.c_void_p()

@@ -93,6 +93,13 @@ bool grid_valid(const ddgi_grid_desc* g, char* why, size_t n) {
                false;
     uint64_t w = (uint64_t)g->depth_res * g->resolution[0] * g->resolution[1];
     if (w > (1u << 30)) return snprintf(why, n, "atlas too wide"), false;
+    // texel indices of the atlas lookups are 32-bit
+    for (const uint32_t side : {g->color_res, g->depth_res}) {
+        const uint64_t texels = (uint64_t)side * side * probes;
+        if (texels > 0xFFFFFFFFull)
+            return snprintf(why, n, "atlas of %llu texels (tile side %u) above 2^32 - 1", (unsigned long long)texels, side),
+                   false;
+    }
     return true;
 }
 
