@@ -432,15 +432,16 @@ def measure_batching(stream, steps, warmup, flush):
     return out
 
 
-def profiled_traffic(summary):
-    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum of
-    one ncu capture of the same workload) from the committed summary under
-    profiles/, or None."""
+def profiled_traffic(summary, key="traffic_bytes_per_launch"):
+    """Bytes per launch recorded in a committed ncu summary under profiles/
+    (one capture of the same workload), or None: by default the DRAM bytes
+    (dram__bytes_read.sum + dram__bytes_write.sum); key
+    "l2_traffic_bytes_per_launch" gives the L2 bytes (lts__t_bytes.sum)."""
     import re
 
     try:
         with open(os.path.join(ROOT, "profiles", summary)) as f:
-            m = re.search(r"traffic_bytes_per_launch:\s*(\d+)", f.read())
+            m = re.search(r"^" + key + r":\s*(\d+)", f.read(), re.M)
     except OSError:
         return None
     return int(m.group(1)) if m else None
@@ -678,12 +679,16 @@ def main():
     alg_bytes = fetches["nodes"] * 64 + fetches["tris"] * 48 + fetches["instances"] * 64
     achieved = alg_bytes / (prim_ms * 1e-3) / 1e9
     l2 = measure_l2_copy_gbs()
+    l2_bytes = profiled_traffic("k_primary_terrain_32x16x32_r256.md", "l2_traffic_bytes_per_launch")
     roofline = {"bound": "hbm", "kernel": "k_primary", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_source": peak_kind,
                 "l2_copy_gbs": l2, "frac_l2": achieved / l2,
                 "l2_source": "measured in this run: L2-resident 24 MB device copy (read + write bytes / time)",
                 "traffic": profiled_traffic("k_primary_terrain_32x16x32_r256.md"),
                 "traffic_source": "ncu capture, profiles/k_primary_terrain_32x16x32_r256.md",
+                "l2_traffic": l2_bytes,
+                "l2_achieved_gbs": l2_bytes / (prim_ms * 1e-3) / 1e9 if l2_bytes else None,
+                "l2_traffic_source": "lts__t_bytes.sum of one ncu capture, profiles/k_primary_terrain_32x16x32_r256.md",
                 "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": prim_ms,
                 "note": "fetch-counted node/triangle/instance bytes of the primary rays; they are served mostly by "
                         "L1/L2, so frac > 1 is cache reuse, not DRAM traffic",
