@@ -547,12 +547,17 @@ ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t re
  * No single counterpart in the reference, which updates one IrradianceProbes
  * volume per call (src/IrradianceProbes.cpp:426-594); a batch runs that
  * update for several contexts ("volumes") at once.  Each volume keeps its own
- * grid, scene, light, precision and atlases.  One update of the batch is:
- * one persistent work-queue traversal launch over the primary rays of every
- * volume, one shading launch, one persistent shadow-ray launch, and one blend
- * launch per precision (FP32 SIMT, BF16 tensor core), captured once into a
- * CUDA graph and replayed per update.  The result of every volume equals
- * ddgi_update of that volume alone over all its probes.
+ * grid, scene, light, precision and atlases.  The volumes are ordered by
+ * ray count and split into up to four groups, run one after another
+ * (smallest first, so small volumes finish early); a group's update is one
+ * persistent work-queue traversal launch over the primary rays of all its
+ * volumes, one shading launch, one persistent shadow-ray launch, and one
+ * blend launch per precision (FP32 SIMT, BF16 tensor core).  The whole
+ * sequence is captured once into a CUDA graph and replayed per update.  The
+ * result of every volume equals ddgi_update of that volume alone over all
+ * its probes.  Volumes with the atmospheric sky (ddgi_set_sky_mode) or a
+ * hysteresis ramp (ddgi_set_target_hysteresis) are not batched:
+ * ddgi_batch_update returns DDGI_ERR_UNSUPPORTED for them.
  *
  * ddgi_batch_create copies the volumes' acceleration structures into one
  * node/triangle/instance arena, so every volume needs a built scene at that

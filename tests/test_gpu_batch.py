@@ -172,3 +172,47 @@ def test_invalid_tuning_rejected(gpu_lib, volumes):
             b.set_tuning(**bad)
     b.close()
     ctxs[0].close()
+
+
+def test_ramping_volume_is_refused_until_the_ramp_is_off(gpu_lib, volumes, single_results):
+    """The batch blends with each grid's hysteresis, so a volume with a
+    hysteresis ramp (ddgi_set_target_hysteresis) is refused
+    (DDGI_ERR_UNSUPPORTED) instead of drifting from its own ddgi_update;
+    with the ramp off again the batch's result equals the single update."""
+    w = volumes[-1]
+    ctx = make_ctx(w)
+    b = Batch([ctx])
+    ctx.set_target_hysteresis(0.9)
+    with pytest.raises(DDGIError) as e:
+        b.update(orientations([w], 0))
+    assert e.value.status == 7
+    ctx.set_target_hysteresis(-1.0)
+    for k in range(2):
+        b.update(orientations([w], k))
+    b.synchronize()
+    assert_same(atlases(ctx), single_results[-1], "volume after its ramp was turned off")
+    b.close()
+    ctx.close()
+
+
+def test_reference_format_volumes_in_a_batch(gpu_lib):
+    """Volumes whose atlases are stored in the reference's image formats
+    (R11G11B10F colour, RG16F depth) next to FP32 and BF16 volumes: each
+    equal, bit for bit, to its own context updated alone."""
+    ws = [scenes.room_workload(81, n_boxes=60, resolution=(4, 3, 4), rays=64,
+                               precision=abi.PRECISION_REFERENCE_FORMAT),
+          scenes.room_workload(82, n_boxes=40, resolution=(3, 3, 3), rays=128,
+                               precision=abi.PRECISION_REFERENCE_FORMAT, color_res=6, depth_res=14),
+          scenes.room_workload(83, n_boxes=50, resolution=(3, 4, 3), rays=64, precision=abi.PRECISION_BF16),
+          scenes.room_workload(84, n_boxes=50, resolution=(4, 4, 3), rays=32)]
+    single = run_single(ws, 2)
+    ctxs = [make_ctx(w) for w in ws]
+    b = Batch(ctxs)
+    for k in range(2):
+        b.update(orientations(ws, k))
+    b.synchronize()
+    for v, (ctx, ref) in enumerate(zip(ctxs, single)):
+        assert_same(atlases(ctx), ref, "volume %d (%s)" % (v, ws[v].name))
+    b.close()
+    for c in ctxs:
+        c.close()

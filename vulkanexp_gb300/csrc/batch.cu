@@ -271,6 +271,11 @@ ddgi_status check_volumes(ddgi_batch* b) {
                          b->order[v]);
         if (c->dl.sky_mode != DDGI_SKY_CONSTANT)
             return bfail(b, DDGI_ERR_UNSUPPORTED, "volume %u: the atmospheric sky is not batched", b->order[v]);
+        // the batch blends with each grid's hysteresis; a volume whose
+        // hysteresis ramps (ddgi_set_target_hysteresis) would drift from
+        // its own ddgi_update, so it is refused rather than blended otherwise
+        if (c->ramp_on)
+            return bfail(b, DDGI_ERR_UNSUPPORTED, "volume %u: the hysteresis ramp is not batched", b->order[v]);
     }
     return DDGI_OK;
 }
