@@ -406,7 +406,9 @@ ddgi_status ddgi_set_materials(ddgi_ctx* ctx, const ddgi_material* materials, ui
  * atlas, with orientations K x 9, and records what the reverse pass needs:
  * every ray's closest hit and shadow result (the hit set is then held fixed)
  * and an atlas checkpoint every `checkpoint_every` updates.  The atlas ends
- * as after K ordinary updates. */
+ * as after K ordinary updates.  DDGI_ERR_UNSUPPORTED for a BF16 or
+ * reference-format context, the atmospheric sky or a hysteresis ramp
+ * (the reverse pass differentiates the grid's fixed hysteresis). */
 ddgi_status ddgi_forward_record(ddgi_ctx* ctx, uint32_t K, const float* orientations, uint32_t checkpoint_every,
                                 ddgi_stream stream);
 /* Reverse pass of the last ddgi_forward_record: given dL/d(colour atlas

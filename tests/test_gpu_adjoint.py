@@ -95,3 +95,39 @@ def test_adjoint_differentiation_workload_matches_fd(gpu_lib):
     w = scenes.workload(3)
     err = run_check(w, K=8, n_check=32, seed=1237)
     assert err.max() <= 1e-3
+
+
+def test_forward_record_refuses_what_the_adjoint_does_not_model(gpu_lib):
+    """The reverse pass differentiates the FP32 blend with the grid's fixed
+    hysteresis and a constant sky: recording is refused
+    (DDGI_ERR_UNSUPPORTED) while a hysteresis ramp is on, for the
+    atmospheric sky and for a BF16 context, and works again once the ramp is
+    off."""
+    from vulkanexp_gb300 import abi
+    from vulkanexp_gb300.ddgi import Context, DDGIError
+
+    w = scenes.room_workload(43, n_boxes=40, resolution=(3, 3, 3), rays=32)
+    orients = np.stack([w.orientation(k) for k in range(2)])
+    ctx = Context(w.grid)
+    ctx.build_scene(w.scene)
+    ctx.set_light(w.light)
+    ctx.set_target_hysteresis(0.9)
+    with pytest.raises(DDGIError) as e:
+        ctx.forward_record(orients, 1)
+    assert e.value.status == 7
+    ctx.set_target_hysteresis(-1.0)
+    ctx.forward_record(orients, 1)
+    ctx.set_sky_mode(abi.SKY_ATMOSPHERE)
+    with pytest.raises(DDGIError) as e:
+        ctx.forward_record(orients, 1)
+    assert e.value.status == 7
+    ctx.close()
+    g = w.grid.copy()
+    g.precision = abi.PRECISION_BF16
+    ctx = Context(g)
+    ctx.build_scene(w.scene)
+    ctx.set_light(w.light)
+    with pytest.raises(DDGIError) as e:
+        ctx.forward_record(orients, 1)
+    assert e.value.status == 7
+    ctx.close()

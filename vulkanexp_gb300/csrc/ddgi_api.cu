@@ -2185,6 +2185,9 @@ ddgi_status ddgi_forward_record(ddgi_ctx* ctx, uint32_t K, const float* orientat
         return fail(ctx, DDGI_ERR_UNSUPPORTED, "gradients need the FP32 form (unrounded atlas)");
     if (ctx->dl.sky_mode != DDGI_SKY_CONSTANT)
         return fail(ctx, DDGI_ERR_UNSUPPORTED, "gradients need the constant sky (a parameter)");
+    // the adjoint differentiates the blend with the grid's hysteresis
+    if (ctx->ramp_on)
+        return fail(ctx, DDGI_ERR_UNSUPPORTED, "gradients need a fixed hysteresis (no ddgi_set_target_hysteresis ramp)");
     if (!ctx->scene.built) return fail(ctx, DDGI_ERR_NO_SCENE, "no scene");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const uint32_t C = checkpoint_every, ncheck = (K + C - 1) / C;
