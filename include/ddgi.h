@@ -540,7 +540,8 @@ ddgi_status ddgi_get_trace_tuning(const ddgi_ctx* ctx, ddgi_trace_tuning* out);
 /* Times candidate tunings on updates of all probes with the given
  * orientation (`reps` timed updates each, coordinate descent), keeps the
  * fastest trace (primary + shading + shadow rays) and writes it to *chosen
- * (may be NULL).  The atlases, accumulators and probe states are restored
+ * (may be NULL).  The atlases, accumulators, probe states, the adaptive
+ * schedule's position and the hysteresis ramp's state are restored
  * afterwards.  Synchronous. */
 ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t reps, ddgi_stream stream,
                           ddgi_trace_tuning* chosen);

@@ -147,3 +147,24 @@ def test_ramp_rejects_bad_targets(gpu_lib):
         with pytest.raises(DDGIError):
             ctx.set_target_hysteresis(t)
     ctx.close()
+
+
+def test_autotune_keeps_the_ramp(gpu_lib):
+    """ddgi_autotune runs many trial updates; with the ramp on they step it,
+    so the ramp's state (and its pending start) is restored with the
+    atlases: afterwards the context ramps and blends exactly like a twin
+    that was never tuned."""
+    w = small_room(hysteresis=0.3)
+    tuned, twin = make_ctx(w), make_ctx(w)
+    for ctx in (tuned, twin):
+        ctx.set_target_hysteresis(0.9)
+    tuned.autotune(w.orientation(7), reps=1)
+    for k in range(6):
+        for ctx in (tuned, twin):
+            ctx.update(w.orientation(k))
+        assert tuned.hysteresis() == twin.hysteresis()
+    for kind in (abi.ATLAS_COLOR, abi.ATLAS_DEPTH):
+        a, b = tuned.get_atlas(kind), twin.get_atlas(kind)
+        assert (a.view(np.uint32) == b.view(np.uint32)).all()
+    tuned.close()
+    twin.close()

@@ -1697,8 +1697,12 @@ ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t re
     };
     std::vector<Saved> saved;
     const size_t cb = atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, ctx->fp16), db = atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, ctx->fp16);
-    std::vector<std::pair<void*, size_t>> parts = {
-        {ctx->color, cb}, {ctx->depth, db}, {ctx->states, sizeof(uint32_t) * probe_count_of(ctx->grid)}};
+    // the schedule and hysteresis-ramp words too: the trial updates step the
+    // ramp when it is on (its pending host-side commands are kept below)
+    std::vector<std::pair<void*, size_t>> parts = {{ctx->color, cb},
+                                                   {ctx->depth, db},
+                                                   {ctx->states, sizeof(uint32_t) * probe_count_of(ctx->grid)},
+                                                   {ctx->sched, 8 * sizeof(uint32_t)}};
     if (ctx->fp16) {
         parts.push_back({ctx->acc_color, atlas_bytes(ctx->dg, DDGI_ATLAS_COLOR, false)});
         parts.push_back({ctx->acc_depth, atlas_bytes(ctx->dg, DDGI_ATLAS_DEPTH, false)});
@@ -1718,6 +1722,7 @@ ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t re
         CK(cudaMemcpyAsync(c, pt.first, pt.second, cudaMemcpyDeviceToDevice, st), "autotune save");
     }
     const ddgi_trace_tuning start = ctx->tune;
+    const RampCmd ramp_cmd = ctx->ramp_cmd;
     const bool timing = ctx->timing;
     ctx->timing = true;
     auto measure = [&](const ddgi_trace_tuning& t, float* out) -> ddgi_status {
@@ -1778,6 +1783,7 @@ ddgi_status ddgi_autotune(ddgi_ctx* ctx, const float orientation[9], uint32_t re
     for (auto& x : saved) cudaMemcpyAsync(x.dst, x.copy, x.bytes, cudaMemcpyDeviceToDevice, st);
     cudaError_t e = cudaStreamSynchronize(st);
     release();
+    ctx->ramp_cmd = ramp_cmd;
     ctx->timing = timing;
     ctx->tune = err == DDGI_OK ? best : start;
     if (err != DDGI_OK) return err;
