@@ -197,3 +197,32 @@ def test_editor_saved_scene_fixture():
     assert (hits["instance"] != abi.MISS).all()
     assert set(hits["instance"].tolist()) >= {0, 2}
     o.close()
+
+
+def test_gltf_accessors_strided_and_normalised():
+    """Accessor reads: interleaved views (byteStride), byte offsets, and
+    normalised integer components (glTF 2.0: unsigned c / max, signed
+    max(c / max, -1)); plain integers stay integers."""
+    from vulkanexp_gb300.ingest import _accessor
+
+    # interleaved (u16 u, u16 v, pad, f32 x) records of 12 bytes, at offset 4
+    rec = np.zeros(3, dtype=[("u", "<u2"), ("v", "<u2"), ("pad", "<u4"), ("x", "<f4")])
+    rec["u"] = [0, 32767, 65535]
+    rec["v"] = [65535, 0, 1]
+    rec["x"] = [1.5, -2.0, 3.25]
+    blob = b"\0" * 4 + rec.tobytes()
+    s8 = np.array([-128, -127, 0, 127], np.int8).tobytes()
+    gl = {"bufferViews": [{"buffer": 0, "byteOffset": 4, "byteLength": rec.nbytes, "byteStride": 12},
+                          {"buffer": 1, "byteOffset": 0, "byteLength": 4}],
+          "accessors": [{"bufferView": 0, "componentType": 5123, "count": 3, "type": "VEC2", "normalized": True},
+                        {"bufferView": 0, "byteOffset": 8, "componentType": 5126, "count": 3, "type": "SCALAR"},
+                        {"bufferView": 0, "componentType": 5123, "count": 3, "type": "VEC2"},
+                        {"bufferView": 1, "componentType": 5120, "count": 4, "type": "SCALAR", "normalized": True}]}
+    bufs = [blob, s8]
+    uv = _accessor(gl, bufs, 0)
+    assert uv.dtype == np.float32
+    np.testing.assert_allclose(uv, [[0.0, 1.0], [32767 / 65535, 0.0], [1.0, 1 / 65535]], rtol=1e-7)
+    np.testing.assert_array_equal(_accessor(gl, bufs, 1)[:, 0], [1.5, -2.0, 3.25])
+    raw = _accessor(gl, bufs, 2)
+    assert raw.dtype == np.uint16 and raw.tolist() == [[0, 65535], [32767, 0], [65535, 1]]
+    np.testing.assert_allclose(_accessor(gl, bufs, 3)[:, 0], [-1.0, -1.0, 0.0, 1.0], rtol=1e-7)

@@ -264,6 +264,12 @@ def _accessor(gl, buffers, idx):
         cols = np.lib.stride_tricks.as_strided(raw[k * dt.itemsize:], shape=(count, dt.itemsize),
                                                strides=(stride, 1))
         out[:, k] = np.ascontiguousarray(cols).view(dt).reshape(count)
+    if a.get("normalized") and dt.kind in "iu":
+        # normalised integers (glTF 2.0 section 3.11): c / max, signed ones
+        # clamped at -1; the reference reads float attributes only
+        # (src/Scene.cpp:72-88, 229), so this widens what loads
+        top = float(np.iinfo(dt).max)
+        return np.maximum(out.astype(np.float64) / top, -1.0).astype(np.float32)
     return out
 
 
